@@ -1,0 +1,164 @@
+/*
+ * np_render.h -- C ABI of the GB300 Kerr null-geodesic renderer.
+ *
+ * This is the drop-in boundary for the reference renderer's hot path
+ * (`renderKernel` + `render_one`, render.cu:118-364 and render.cu:523-620).
+ * Everything crosses as plain pointers, sizes and a POD scene description;
+ * no C++ or torch types appear in any signature.
+ *
+ * Units.  With `units == NP_UNITS_RS` the scene follows render.cu exactly:
+ * `mass` is M, `r_cam` is in Schwarzschild radii (render.cu:21,131-135),
+ * and the camera angles / mass / radius pass through float exactly as the
+ * reference kernel arguments do (render.cu:118-123, 483-485).  With
+ * `units == NP_UNITS_M` every length is in units of M and all scene
+ * quantities stay double.
+ *
+ * Output layout (planar, structure of arrays, row-major, y = 0 is the top
+ * row as in render.cu:128,148-151):
+ *   rgb    float[3][height][width]  sum over this call's samples of the
+ *                                   per-sample linear radiance (render.cu:361-363)
+ *   rcross float[height][width]     first disk-crossing radius of sample 0
+ *                                   of this call (0 when sample 0 missed the disk)
+ *   inv3   float[3]                 max |H|, |dE/E|, |dL/L| (render.cu:233-244,
+ *                                   327-345); may be NULL
+ *
+ * Error handling: every entry point returns an np_status code; the message
+ * of the last failure on the calling thread is available from
+ * np_last_error().  Nothing aborts the process.
+ */
+#ifndef NP_RENDER_H
+#define NP_RENDER_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NP_ABI_VERSION 1
+
+typedef enum np_status {
+    NP_OK = 0,
+    NP_ERR_INVALID = -1,     /* bad argument (mirrors geokerr_stream.cu:163-165 "-1") */
+    NP_ERR_ALLOC = -2,       /* device allocation failed ("-2") */
+    NP_ERR_KERNEL = -3,      /* launch or execution failure ("-3") */
+    NP_ERR_NO_DEVICE = -4,   /* no CUDA device visible */
+    NP_ERR_TIMEOUT = -5      /* a bounded device wait gave up */
+} np_status;
+
+typedef enum np_units { NP_UNITS_RS = 0, NP_UNITS_M = 1 } np_units;
+typedef enum np_jitter { NP_JITTER_WANGHASH = 0, NP_JITTER_STRATIFIED = 1 } np_jitter;
+typedef enum np_camera { NP_CAMERA_STATIC = 0, NP_CAMERA_ZAMO = 1 } np_camera;
+typedef enum np_integrator { NP_INTEG_RK4 = 0, NP_INTEG_ADAPTIVE = 1 } np_integrator;
+typedef enum np_crossing { NP_CROSS_LINEAR = 0, NP_CROSS_HERMITE = 1 } np_crossing;
+typedef enum np_background { NP_BG_GRADIENT = 0, NP_BG_POINT = 1 } np_background;
+
+/* Arithmetic of the geodesic integration.
+ *   NP_PREC_FP64   the reference's FP64 Hamiltonian RK4 (render.cu:161-251),
+ *                  all eight phase-space components, compensated sums.
+ *   NP_PREC_MIXED  FP32 bulk integration of (r, theta, p_r, p_theta) with a
+ *                  compensated (hi+lo) state, FP64 steps near the horizon, at
+ *                  turning points and for near-critical impact parameters. */
+typedef enum np_precision { NP_PREC_FP64 = 0, NP_PREC_MIXED = 1 } np_precision;
+
+/* FP64 islands of NP_PREC_MIXED (bit mask, np_scene_t.islands). */
+#define NP_ISLAND_HORIZON 1   /* steps within 0.1 M of the outer horizon */
+#define NP_ISLAND_TURNING 2   /* steps across a radial or polar turning point */
+#define NP_ISLAND_CRITICAL 4  /* whole rays with |b - b_crit| < 1e-3 M */
+#define NP_ISLANDS_ALL 7
+
+typedef struct np_scene {
+    int32_t width, height;        /* render.cu:16-17 */
+    int32_t spp;                  /* samples traced by this call (render.cu:23) */
+    int32_t sample_offset;        /* first sample index (spp_done, render.cu:545) */
+    double mass;                  /* M (render.cu:20) */
+    double spin;                  /* a/M, |spin| < 1 (render.cu:29) */
+    double r_cam;                 /* camera radius (Rs or M, see units) */
+    double theta_deg;             /* camera polar angle (render.cu:19) */
+    double phi_deg;               /* camera azimuth (render.cu:27,632) */
+    double fov_y_deg;             /* vertical field of view (render.cu:18) */
+    int32_t units;                /* np_units */
+    int32_t camera;               /* np_camera; static falls back to ZAMO inside the ergosphere */
+    int32_t jitter;               /* np_jitter */
+    uint32_t seed;                /* seed of NP_JITTER_STRATIFIED */
+    int32_t integrator;           /* np_integrator */
+    int32_t max_steps;            /* step cap (MAX_INTEGRATION_STEPS, bh_common.h:203) */
+    double step_scale;            /* h = step_scale * clamp(r/M, 1, 100) (render.cu:185,207) */
+    double rtol, atol;            /* adaptive tolerances (bh_common.h:221,228) */
+    double escape_r;              /* absolute escape radius; <= 0 means r_cam + 10 Rs (render.cu:182) */
+    int32_t disk_on;              /* render.cu:43 */
+    int32_t disk_max_orders;      /* render.cu:45 */
+    double disk_rin, disk_rout;   /* absolute radii; <= 0 means 3 Rs / 20 Rs (render.cu:179-180) */
+    double emissivity_q;          /* j ~ r^-q (render.cu:67 uses q = 2) */
+    double disk_gain;             /* render.cu:44 */
+    int32_t crossing;             /* np_crossing; linear is render.cu:218-220 */
+    int32_t background;           /* np_background (render.cu:39) */
+    double bg_sigma_deg;          /* render.cu:40 */
+    double bg_brightness;         /* render.cu:41 */
+    int32_t check_invariants;     /* render.cu:32 */
+    int32_t islands;              /* NP_ISLAND_* mask of the mixed path */
+} np_scene_t;
+
+/* Per-call statistics, filled when the pointer is non-NULL. */
+typedef struct np_render_stats {
+    uint64_t rays;                /* rays traced */
+    uint64_t steps;               /* accepted integration steps */
+    uint64_t fp64_steps;          /* steps taken in FP64 by the mixed path */
+    uint64_t rhs_evals;           /* right-hand-side evaluations */
+    double kernel_ms;             /* device time of the render kernel */
+} np_render_stats_t;
+
+/* ABI version compiled into the library. */
+int np_abi_version(void);
+
+/* Message of the last failure on this thread ("" when none). */
+const char* np_last_error(void);
+
+/* Reference defaults of render.cu:15-46 (1280x720, M=10, r_cam=50 Rs, ...). */
+void np_scene_defaults(np_scene_t* scene);
+
+/* The 1280x720 a=0.9 benchmark scene: M=1, r_cam=50 M, theta=80 deg,
+ * fov 55 deg, 4 spp stratified from seed 0, disk from the prograde ISCO to
+ * 20 M with j ~ r^-3, 3 crossing orders, step cap 4096, escape at 1000 M. */
+void np_scene_benchmark(np_scene_t* scene);
+
+/* Prograde ISCO radius (Bardeen, Press & Teukolsky 1972) for mass M, spin a/M. */
+double np_isco_radius(double mass, double spin);
+
+/* Validates a scene the way render.cu:431-465 validates its flags. */
+int np_scene_validate(const np_scene_t* scene);
+
+/* Renders one pass into DEVICE buffers on `stream` (a cudaStream_t, NULL =
+ * legacy default stream).  When `accumulate` is non-zero the pass is added
+ * to rgb (progressive spp), otherwise rgb is overwritten.  rcross is
+ * written when non-NULL; inv3 is max-updated when non-NULL.  Returns after
+ * the launch; the caller synchronises the stream. */
+int np_render_device(const np_scene_t* scene, int precision,
+                     float* d_rgb, float* d_rcross, float* d_inv3,
+                     int accumulate, void* stream, np_render_stats_t* stats);
+
+/* Same pass with HOST buffers: the library copies to and from the device
+ * inside the call and returns when the results are in host memory. */
+int np_render_host(const np_scene_t* scene, int precision,
+                   float* h_rgb, float* h_rcross, float* h_inv3,
+                   np_render_stats_t* stats);
+
+/* Traces explicit rays and reports per-ray events; used for accuracy
+ * studies against the semi-analytic solver.  Ray i starts at pixel
+ * coordinates (px[i], py[i]) (continuous, 0..width, 0..height).  Outputs
+ * per ray (device pointers):
+ *   consts[4*i+0..3] = p_t, p_phi, Carter Q, sign(p_r) at the camera
+ *   cross[8*i + 2k], cross[8*i + 2k + 1] = r and phi of the k-th equatorial
+ *       crossing (k < 4), 0 when absent
+ *   status[i] = 0 escaped, 1 captured, 2 step cap; plus 16 * (crossings) */
+int np_trace_rays_device(const np_scene_t* scene, int precision, int n,
+                         const double* d_px, const double* d_py,
+                         double* d_consts, double* d_cross, int32_t* d_status,
+                         void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NP_RENDER_H */

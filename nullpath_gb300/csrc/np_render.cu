@@ -1,0 +1,590 @@
+// np_render.cu -- sm_103a Kerr renderer behind the C ABI of include/np_render.h.
+//
+// Kernels
+//   render_fp64_kernel   FP64 reference-form integrator (render.cu:161-251),
+//                        persistent, one ray per lane with per-lane refill.
+//   render_mixed_kernel  FP32/compensated Carter-form integrator with FP64
+//                        islands; near-critical rays are appended to a
+//                        deferred list and finished by render_fp64_kernel.
+//   resolve_kernel       sums the per-sample colours of a pass in sample
+//                        order into the planar image (progressive spp).
+//   trace_rays_kernel    explicit rays, per-ray crossing report.
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <cmath>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "np_common.cuh"
+#include "tracer_fp64.cuh"
+#include "tracer_mixed.cuh"
+
+using namespace np;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const char* fmt, ...) __attribute__((format(printf, 2, 3)));
+int fail(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return code;
+}
+
+#define NP_CU(expr, code)                                                          \
+    do {                                                                           \
+        cudaError_t e_ = (expr);                                                   \
+        if (e_ != cudaSuccess)                                                     \
+            return fail((code), "%s: %s", #expr, cudaGetErrorString(e_));          \
+    } while (0)
+
+constexpr int kBlock = 128;
+constexpr int kChunk = 64;
+
+// Device-side counters of one call.
+struct Counters {
+    unsigned long long work;        // next ray index (main pass)
+    unsigned long long work2;       // next deferred-list index
+    unsigned long long deferred;    // deferred-list length
+    unsigned long long rays, steps, fp64_steps, evals;
+};
+
+// ---------------------------------------------------------------------------
+// Scene preparation (host, FP64).
+
+void host_metric_cov(double M, double a, double r, double th,
+                     double& gtt, double& gtp, double& gpp, double& grr, double& ghh) {
+    double c = std::cos(th), s = std::sin(th), s2 = s * s;
+    double r2 = r * r, a2 = a * a;
+    double Sig = r2 + a2 * c * c;
+    double Del = r2 - 2.0 * M * r + a2;
+    double A = (r2 + a2) * (r2 + a2) - a2 * Del * s2;
+    gtt = -(1.0 - 2.0 * M * r / std::fmax(kEps, Sig));
+    gtp = -2.0 * M * a * r * s2 / std::fmax(kEps, Sig);
+    gpp = A * s2 / std::fmax(kEps, Sig);
+    grr = Sig / std::fmax(kEps, Del);
+    ghh = Sig;
+}
+
+// Builds the per-scene constants; camera tetrads follow bh_kerr.h:781-826
+// (static observer) and 910-967 (ZAMO), the static observer falling back to
+// the ZAMO inside the ergosphere (render.cu:163-170).
+int prepare_scene(const np_scene_t& sc, SceneDev& d) {
+    int v = np_scene_validate(&sc);
+    if (v != NP_OK) return v;
+    std::memset(&d, 0, sizeof(d));
+    d.W = sc.width; d.H = sc.height; d.spp = sc.spp; d.sample_offset = sc.sample_offset;
+    d.npix = (long long)sc.width * sc.height;
+    d.total = d.npix * sc.spp;
+    d.ref_units = sc.units == NP_UNITS_RS;
+    d.jitter = sc.jitter; d.seed = sc.seed;
+    d.strata = std::max(1, (int)std::floor(std::sqrt((double)std::max(1, sc.spp))));
+    d.integrator = sc.integrator; d.max_steps = sc.max_steps;
+    d.max_orders = std::max(1, sc.disk_max_orders);
+    d.crossing = sc.crossing; d.bg_mode = sc.background; d.disk_on = sc.disk_on;
+    d.check_inv = sc.check_invariants;
+    d.islands = sc.islands;
+    if (d.ref_units) {
+        float Mf = (float)sc.mass, Rsf = 2.0f * Mf;
+        float af = (float)sc.spin * Mf, rcf = (float)sc.r_cam * Rsf;
+        d.M = Mf; d.a = af; d.Rs = Rsf; d.r_cam = rcf;
+        d.th_cam = (float)sc.theta_deg * kPiF / 180.0f;
+        d.ph_cam = (float)sc.phi_deg * kPiF / 180.0f;
+        d.aspect_f = (float)sc.width / (float)sc.height;
+        float fov = (float)sc.fov_y_deg * kPiF / 180.0f;
+        d.tan_half_f = std::tan(0.5f * fov);
+        d.h_unit = (double)(float)sc.step_scale;
+        d.Rsf = Rsf;
+    } else {
+        d.M = sc.mass; d.a = sc.spin * sc.mass; d.Rs = 2.0 * sc.mass;
+        d.r_cam = sc.r_cam * sc.mass;
+        d.th_cam = sc.theta_deg * kPi / 180.0;
+        d.ph_cam = sc.phi_deg * kPi / 180.0;
+        d.aspect = (double)sc.width / (double)sc.height;
+        d.tan_half = std::tan(0.5 * sc.fov_y_deg * kPi / 180.0);
+        d.h_unit = sc.step_scale;
+        d.Rsf = (float)d.Rs;
+    }
+    double disc = std::fmax(0.0, d.M * d.M - d.a * d.a);
+    d.r_plus = d.M + std::sqrt(disc);
+    d.r_minus = d.M - std::sqrt(disc);
+    d.rin = sc.disk_rin > 0.0 ? sc.disk_rin : 3.0 * d.Rs;
+    d.rout = sc.disk_rout > 0.0 ? sc.disk_rout : 20.0 * d.Rs;
+    d.r_far = sc.escape_r > 0.0 ? sc.escape_r : d.r_cam + 10.0 * d.Rs;
+    d.q = sc.emissivity_q; d.qf = (float)sc.emissivity_q;
+    d.rtol = sc.rtol; d.atol = sc.atol;
+    d.gain = (float)sc.disk_gain;
+    d.bg_sigma_rad = (float)sc.bg_sigma_deg * kPiF / 180.0f;
+    d.bg_peak = (float)sc.bg_brightness;
+
+    const double M = d.M, a = d.a, r = d.r_cam, th = d.th_cam;
+    double gtt, gtp, gpp, grr, ghh;
+    host_metric_cov(M, a, r, th, gtt, gtp, gpp, grr, ghh);
+    d.gtt = gtt; d.gtp = gtp; d.gpp = gpp; d.grr = grr; d.ghh = ghh;
+    d.cos_cam = std::cos(th); d.sin_cam = std::sin(th);
+    bool zamo = (sc.camera == NP_CAMERA_ZAMO) || !(gtt < 0.0);
+    if (!zamo) {
+        double ut = 1.0 / std::sqrt(std::fmax(kEps, -gtt));
+        double er = 1.0 / std::sqrt(std::fmax(kEps, grr));
+        double eh = 1.0 / std::sqrt(std::fmax(kEps, ghh));
+        double ept, epp;
+        if (std::fabs(gtp) > kEps) {
+            double beta = -gtt / gtp;
+            // compensated |e_phi|^2 (bh_kerr.h:801-806)
+            double s = 0.0, c1 = 0.0, c2 = 0.0;
+            double terms[3] = {gtt, 2.0 * gtp * beta, gpp * beta * beta};
+            for (double x : terms) {
+                double t = s + x;
+                double e = (std::fabs(s) >= std::fabs(x)) ? (s - t) + x : (x - t) + s;
+                s = t;
+                double u = c1 + e;
+                double ee = (std::fabs(c1) >= std::fabs(e)) ? (c1 - u) + e : (e - u) + c1;
+                c1 = u; c2 += ee;
+            }
+            double n2 = s + c1 + c2;
+            double inv = 1.0 / std::sqrt(std::fmax(kEps, std::fabs(n2)));
+            ept = inv; epp = beta * inv;
+        } else {
+            ept = 0.0; epp = 1.0 / std::sqrt(std::fmax(kEps, gpp));
+        }
+        d.T0 = ut; d.T1 = ept; d.P0 = 0.0; d.P1 = epp; d.R1 = er; d.H1 = eh;
+    } else {
+        double c = std::cos(th), sn = std::sin(th);
+        double r2 = r * r, a2 = a * a;
+        double Sig = std::fmax(kEps, r2 + a2 * c * c);
+        double Del = r2 - 2.0 * M * r + a2;
+        double A = std::fmax(kEps, (r2 + a2) * (r2 + a2) - a2 * Del * sn * sn);
+        double alpha = std::sqrt(std::fmax(kEps, Del * Sig / A));
+        double omega = 2.0 * M * a * r / A;
+        d.T0 = 1.0 / std::fmax(kEps, alpha);
+        d.T1 = 0.0;
+        d.P0 = omega / std::fmax(kEps, alpha);
+        d.P1 = std::sqrt(std::fmax(kEps, Sig / A)) / std::fmax(kEps, std::fabs(sn));
+        d.R1 = std::sqrt(std::fmax(kEps, Del / Sig));
+        d.H1 = 1.0 / std::sqrt(Sig);
+    }
+    return NP_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Kernels.
+
+__device__ __forceinline__ void ray_coords(const SceneDev& s, long long item, long long& p, int& sl,
+                                           int& x, int& y, uint32_t& sid) {
+    p = item % s.npix;
+    sl = (int)(item / s.npix);
+    x = (int)(p % s.W);
+    y = (int)(p / s.W);
+    sid = (uint32_t)(s.sample_offset + sl);
+}
+
+__device__ __forceinline__ void write_sample(const SceneDev& s, float* srgb, float* rcross,
+                                             long long p, int sl, const float col[3], double first_r) {
+    float* base = srgb + (size_t)sl * 3 * s.npix;
+    base[p] = col[0];
+    base[s.npix + p] = col[1];
+    base[2 * s.npix + p] = col[2];
+    if (sl == 0 && rcross) rcross[p] = (float)first_r;
+}
+
+__device__ __forceinline__ void flush_counters(Counters* ctr, unsigned long long rays, unsigned long long steps,
+                                               unsigned long long f64, unsigned long long evals) {
+    for (int o = 16; o > 0; o >>= 1) {
+        rays += __shfl_down_sync(0xffffffffu, rays, o);
+        steps += __shfl_down_sync(0xffffffffu, steps, o);
+        f64 += __shfl_down_sync(0xffffffffu, f64, o);
+        evals += __shfl_down_sync(0xffffffffu, evals, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(&ctr->rays, rays);
+        atomicAdd(&ctr->steps, steps);
+        atomicAdd(&ctr->fp64_steps, f64);
+        atomicAdd(&ctr->evals, evals);
+    }
+}
+
+// FP64 reference-form tracer.  With `list` non-null the kernel traces the
+// rays named by list[0 .. ctr->deferred) (deferred near-critical rays of the
+// mixed pass); otherwise every ray index in [0, total).
+__global__ void __launch_bounds__(kBlock)
+render_fp64_kernel(const SceneDev s, float* __restrict__ srgb, float* __restrict__ rcross,
+                   float* __restrict__ inv3, Counters* __restrict__ ctr, const long long* __restrict__ list) {
+    const unsigned FULL = 0xffffffffu;
+    unsigned long long* counter = list ? &ctr->work2 : &ctr->work;
+    const long long total = list ? (long long)ctr->deferred : s.total;
+    WarpQueue q{0, 0};
+    bool drained = false;
+    RayFP64<false> R;
+    CamDir dir;
+    long long item = -1, p = 0;
+    int sl = 0;
+    bool have = false;
+    unsigned long long n_rays = 0, n_steps = 0, n_evals = 0;
+    while (true) {
+        unsigned need = __ballot_sync(FULL, !have);
+        if (need && !drained) {
+            long long idx = warp_take(q, need, counter, total, kChunk);
+            drained = q.base >= total;
+            if (!have && idx >= 0) {
+                item = list ? list[idx] : idx;
+                int x, y; uint32_t sid;
+                ray_coords(s, item, p, sl, x, y, sid);
+                dir = camera_dir(s, x, y, sid, false, 0.0, 0.0);
+                fp64_init(s, camera_momentum(s, dir), R);
+                have = true;
+                n_rays++;
+            }
+        }
+        if (!__any_sync(FULL, have)) break;
+        if (have) {
+            bool done = fp64_advance(s, R, inv3, n_evals);
+            n_steps++;
+            if (done) {
+                bool captured = R.status == 1;
+                if (s.check_inv && inv3 && !captured && !(R.orders > 0 && s.disk_on))
+                    invariants_ref(s, R.y, R.pt0, R.pph0, inv3);
+                float col[3];
+                sample_colour(s, captured, R.orders, R.disk, R.min_r, dir, col);
+                write_sample(s, srgb, rcross, p, sl, col, R.first_r);
+                have = false;
+            }
+        }
+    }
+    flush_counters(ctr, n_rays, n_steps, list ? n_steps : 0, n_evals);
+}
+
+// Mixed-precision tracer.
+__global__ void __launch_bounds__(kBlock)
+render_mixed_kernel(const SceneDev s, float* __restrict__ srgb, float* __restrict__ rcross,
+                    float* __restrict__ inv3, Counters* __restrict__ ctr, long long* __restrict__ defer_list) {
+    const unsigned FULL = 0xffffffffu;
+    WarpQueue q{0, 0};
+    bool drained = false;
+    RayMixed<false> R;
+    CamDir dir;
+    long long p = 0;
+    int sl = 0;
+    bool have = false;
+    unsigned long long n_rays = 0, n_steps = 0, n_f64 = 0, n_evals = 0;
+    const bool crit = (s.islands & kIslandCritical) != 0;
+    while (true) {
+        unsigned need = __ballot_sync(FULL, !have);
+        if (need && !drained) {
+            long long idx = warp_take(q, need, &ctr->work, s.total, kChunk);
+            drained = q.base >= s.total;
+            if (!have && idx >= 0) {
+                int x, y; uint32_t sid;
+                ray_coords(s, idx, p, sl, x, y, sid);
+                dir = camera_dir(s, x, y, sid, false, 0.0, 0.0);
+                Momentum m = camera_momentum(s, dir);
+                bool defer = false;
+                if (crit) {
+                    double E = -m.pt, L = m.pph;
+                    double Q = m.pth * m.pth + s.cos_cam * s.cos_cam *
+                               (L * L / (s.sin_cam * s.sin_cam) - s.a * s.a * E * E);
+                    defer = near_critical(E, L, Q, s.a, s.M, s.r_plus, kCriticalDb);
+                }
+                if (defer) {
+                    unsigned long long slot = atomicAdd(&ctr->deferred, 1ull);
+                    defer_list[slot] = idx;
+                } else {
+                    mixed_init(s, m, R);
+                    have = true;
+                    n_rays++;
+                    n_evals++;
+                }
+            }
+        }
+        if (!__any_sync(FULL, have)) {
+            if (drained) break;
+            continue;
+        }
+        if (have) {
+            bool done = mixed_advance(s, R, n_evals);
+            n_steps++;
+            if (done) {
+                bool captured = R.status == 1;
+                if (s.check_inv && inv3 && !captured && !(R.orders > 0 && s.disk_on))
+                    mixed_invariants(s, R, hl_d(R.r), hl_d(R.th), inv3);
+                float col[3];
+                sample_colour(s, captured, R.orders, R.disk, R.min_r, dir, col);
+                write_sample(s, srgb, rcross, p, sl, col, R.first_r);
+                n_f64 += R.fp64_steps;
+                have = false;
+            }
+        }
+    }
+    flush_counters(ctr, n_rays, n_steps, n_f64, n_evals);
+}
+
+// rgb[c][p] (+)= sum_s srgb[s][c][p], summed in sample order.
+__global__ void resolve_kernel(const float* __restrict__ srgb, float* __restrict__ rgb,
+                               long long npix, int spp, int accumulate) {
+    long long n = 3 * npix;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        float acc = 0.0f;
+        for (int sl = 0; sl < spp; ++sl) acc += srgb[(size_t)sl * n + i];
+        rgb[i] = accumulate ? rgb[i] + acc : acc;
+    }
+}
+
+// Explicit rays (positions in continuous pixel coordinates).
+__global__ void trace_rays_kernel(const SceneDev s, int precision, int n, const double* __restrict__ px,
+                                  const double* __restrict__ py, double* __restrict__ consts,
+                                  double* __restrict__ cross, int32_t* __restrict__ status) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    CamDir dir = camera_dir(s, 0, 0, 0, true, px[i], py[i]);
+    Momentum m = camera_momentum(s, dir);
+    double E = -m.pt, L = m.pph;
+    double Q = m.pth * m.pth + s.cos_cam * s.cos_cam * (L * L / (s.sin_cam * s.sin_cam) - s.a * s.a * E * E);
+    if (consts) {
+        consts[4 * i + 0] = m.pt; consts[4 * i + 1] = m.pph; consts[4 * i + 2] = Q;
+        consts[4 * i + 3] = m.pr >= 0.0 ? 1.0 : -1.0;
+    }
+    unsigned long long ev = 0;
+    double xr[4], xphi[4];
+    int ncross, st;
+    bool use64 = precision == NP_PREC_FP64 ||
+                 ((s.islands & kIslandCritical) && near_critical(E, L, Q, s.a, s.M, s.r_plus, kCriticalDb));
+    if (use64) {
+        RayFP64<true> R;
+        fp64_init(s, m, R);
+        while (!fp64_advance(s, R, nullptr, ev)) {}
+        for (int k = 0; k < 4; ++k) { xr[k] = R.xr[k]; xphi[k] = R.xphi[k]; }
+        ncross = R.crossings; st = R.status;
+    } else {
+        RayMixed<true> R;
+        mixed_init(s, m, R);
+        while (!mixed_advance(s, R, ev)) {}
+        for (int k = 0; k < 4; ++k) { xr[k] = R.xr[k]; xphi[k] = R.xphi[k]; }
+        ncross = R.crossings; st = R.status;
+    }
+    if (cross) for (int k = 0; k < 4; ++k) { cross[8 * i + 2 * k] = xr[k]; cross[8 * i + 2 * k + 1] = xphi[k]; }
+    if (status) status[i] = st + 16 * min(ncross, 15);
+}
+
+// ---------------------------------------------------------------------------
+// Per-(device, stream) scratch: per-sample colour planes, deferred list and
+// counters.  Grows on demand; calls on the same stream reuse it in order.
+struct Scratch {
+    int device = -1;
+    cudaStream_t stream = nullptr;
+    float* srgb = nullptr; size_t srgb_n = 0;
+    long long* list = nullptr; size_t list_n = 0;
+    Counters* ctr = nullptr;
+    Counters* h_ctr = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+std::mutex g_scratch_mu;
+std::vector<Scratch*> g_scratch;
+
+int get_scratch(cudaStream_t stream, size_t srgb_n, size_t list_n, Scratch** out) {
+    int dev = 0;
+    NP_CU(cudaGetDevice(&dev), NP_ERR_NO_DEVICE);
+    std::lock_guard<std::mutex> lk(g_scratch_mu);
+    Scratch* sc = nullptr;
+    for (Scratch* s : g_scratch)
+        if (s->device == dev && s->stream == stream) { sc = s; break; }
+    if (!sc) {
+        sc = new Scratch();
+        sc->device = dev; sc->stream = stream;
+        NP_CU(cudaMalloc(&sc->ctr, sizeof(Counters)), NP_ERR_ALLOC);
+        NP_CU(cudaMallocHost(&sc->h_ctr, sizeof(Counters)), NP_ERR_ALLOC);
+        NP_CU(cudaEventCreate(&sc->ev0), NP_ERR_KERNEL);
+        NP_CU(cudaEventCreate(&sc->ev1), NP_ERR_KERNEL);
+        g_scratch.push_back(sc);
+    }
+    if (sc->srgb_n < srgb_n) {
+        if (sc->srgb) { cudaStreamSynchronize(stream); cudaFree(sc->srgb); sc->srgb = nullptr; sc->srgb_n = 0; }
+        NP_CU(cudaMalloc(&sc->srgb, srgb_n * sizeof(float)), NP_ERR_ALLOC);
+        sc->srgb_n = srgb_n;
+    }
+    if (sc->list_n < list_n) {
+        if (sc->list) { cudaStreamSynchronize(stream); cudaFree(sc->list); sc->list = nullptr; sc->list_n = 0; }
+        NP_CU(cudaMalloc(&sc->list, list_n * sizeof(long long)), NP_ERR_ALLOC);
+        sc->list_n = list_n;
+    }
+    *out = sc;
+    return NP_OK;
+}
+
+int grid_for(const void* kernel) {
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kBlock, 0);
+    if (per_sm < 1) per_sm = 1;
+    return sms * per_sm;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// C ABI.
+
+extern "C" {
+
+int np_abi_version(void) { return NP_ABI_VERSION; }
+
+const char* np_last_error(void) { return g_last_error.c_str(); }
+
+void np_scene_defaults(np_scene_t* s) {
+    if (!s) return;
+    std::memset(s, 0, sizeof(*s));
+    s->width = 1280; s->height = 720; s->spp = 1; s->sample_offset = 0;
+    s->mass = 10.0; s->spin = 0.0; s->r_cam = 50.0;
+    s->theta_deg = 90.0; s->phi_deg = 0.0; s->fov_y_deg = 50.0;
+    s->units = NP_UNITS_RS; s->camera = NP_CAMERA_STATIC;
+    s->jitter = NP_JITTER_WANGHASH; s->seed = 0;
+    s->integrator = NP_INTEG_RK4; s->max_steps = 10000;
+    s->step_scale = 0.01; s->rtol = 1e-10; s->atol = 1e-12; s->escape_r = 0.0;
+    s->disk_on = 1; s->disk_max_orders = 1; s->disk_rin = 0.0; s->disk_rout = 0.0;
+    s->emissivity_q = 2.0; s->disk_gain = 1.0;
+    s->crossing = NP_CROSS_LINEAR; s->background = NP_BG_GRADIENT;
+    s->bg_sigma_deg = 1.0; s->bg_brightness = 3.0;
+    s->check_invariants = 0; s->islands = NP_ISLANDS_ALL;
+}
+
+double np_isco_radius(double mass, double spin) {
+    double a = spin;
+    double z1 = 1.0 + std::cbrt(1.0 - a * a) * (std::cbrt(1.0 + a) + std::cbrt(1.0 - a));
+    double z2 = std::sqrt(3.0 * a * a + z1 * z1);
+    double sg = a >= 0.0 ? 1.0 : -1.0;
+    return mass * (3.0 + z2 - sg * std::sqrt((3.0 - z1) * (3.0 + z1 + 2.0 * z2)));
+}
+
+void np_scene_benchmark(np_scene_t* s) {
+    if (!s) return;
+    np_scene_defaults(s);
+    s->width = 1280; s->height = 720; s->spp = 4;
+    s->mass = 1.0; s->spin = 0.9; s->r_cam = 50.0;
+    s->theta_deg = 80.0; s->fov_y_deg = 55.0;
+    s->units = NP_UNITS_M; s->jitter = NP_JITTER_STRATIFIED; s->seed = 0;
+    s->max_steps = 4096; s->rtol = 1e-7; s->escape_r = 1000.0;
+    s->disk_max_orders = 3; s->disk_rin = np_isco_radius(1.0, 0.9); s->disk_rout = 20.0;
+    s->emissivity_q = 3.0; s->crossing = NP_CROSS_HERMITE;
+}
+
+int np_scene_validate(const np_scene_t* s) {
+    if (!s) return fail(NP_ERR_INVALID, "scene is NULL");
+    if (s->width <= 0 || s->height <= 0) return fail(NP_ERR_INVALID, "Invalid image dimensions.");
+    if (s->spp <= 0) return fail(NP_ERR_INVALID, "Invalid samples per pixel.");
+    if (s->sample_offset < 0) return fail(NP_ERR_INVALID, "Invalid sample offset.");
+    if (!(s->mass > 0.0) || !(s->r_cam > 0.0)) return fail(NP_ERR_INVALID, "Invalid mass or camera radius.");
+    if (!(std::fabs(s->spin) < 1.0)) return fail(NP_ERR_INVALID, "Spin must satisfy |a/M| < 1.");
+    if (!(s->fov_y_deg > 0.0 && s->fov_y_deg < 179.0))
+        return fail(NP_ERR_INVALID, "Invalid FOV; expected (0, 179) degrees.");
+    if (s->max_steps <= 0) return fail(NP_ERR_INVALID, "Invalid step cap.");
+    if (!(s->step_scale > 0.0)) return fail(NP_ERR_INVALID, "Invalid step scale.");
+    if (s->units != NP_UNITS_RS && s->units != NP_UNITS_M) return fail(NP_ERR_INVALID, "Invalid units.");
+    if (s->integrator != NP_INTEG_RK4 && s->integrator != NP_INTEG_ADAPTIVE)
+        return fail(NP_ERR_INVALID, "Invalid integrator.");
+    if ((long long)s->width * s->height > (1ll << 40) / std::max(1, s->spp))
+        return fail(NP_ERR_INVALID, "Image too large.");
+    return NP_OK;
+}
+
+int np_render_device(const np_scene_t* scene, int precision, float* d_rgb, float* d_rcross, float* d_inv3,
+                     int accumulate, void* stream_v, np_render_stats_t* stats) {
+    if (!d_rgb) return fail(NP_ERR_INVALID, "rgb buffer is NULL");
+    if (precision != NP_PREC_FP64 && precision != NP_PREC_MIXED) return fail(NP_ERR_INVALID, "Invalid precision.");
+    SceneDev s;
+    int rc = prepare_scene(*scene, s);
+    if (rc != NP_OK) return rc;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) return fail(NP_ERR_NO_DEVICE, "No CUDA devices found.");
+    cudaStream_t st = (cudaStream_t)stream_v;
+    Scratch* sc = nullptr;
+    rc = get_scratch(st, (size_t)s.total * 3, precision == NP_PREC_MIXED ? (size_t)s.total : 1, &sc);
+    if (rc != NP_OK) return rc;
+    NP_CU(cudaMemsetAsync(sc->ctr, 0, sizeof(Counters), st), NP_ERR_KERNEL);
+    if (stats) NP_CU(cudaEventRecord(sc->ev0, st), NP_ERR_KERNEL);
+    if (precision == NP_PREC_FP64) {
+        render_fp64_kernel<<<grid_for((const void*)render_fp64_kernel), kBlock, 0, st>>>(
+            s, sc->srgb, d_rcross, d_inv3, sc->ctr, nullptr);
+    } else {
+        render_mixed_kernel<<<grid_for((const void*)render_mixed_kernel), kBlock, 0, st>>>(
+            s, sc->srgb, d_rcross, d_inv3, sc->ctr, sc->list);
+        render_fp64_kernel<<<grid_for((const void*)render_fp64_kernel), kBlock, 0, st>>>(
+            s, sc->srgb, d_rcross, d_inv3, sc->ctr, sc->list);
+    }
+    NP_CU(cudaGetLastError(), NP_ERR_KERNEL);
+    if (stats) NP_CU(cudaEventRecord(sc->ev1, st), NP_ERR_KERNEL);
+    {
+        long long n = 3 * s.npix;
+        int blocks = (int)std::min<long long>((n + 255) / 256, 152 * 16);
+        resolve_kernel<<<blocks, 256, 0, st>>>(sc->srgb, d_rgb, s.npix, s.spp, accumulate);
+        NP_CU(cudaGetLastError(), NP_ERR_KERNEL);
+    }
+    if (stats) {
+        NP_CU(cudaMemcpyAsync(sc->h_ctr, sc->ctr, sizeof(Counters), cudaMemcpyDeviceToHost, st), NP_ERR_KERNEL);
+        NP_CU(cudaStreamSynchronize(st), NP_ERR_KERNEL);
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, sc->ev0, sc->ev1);
+        stats->rays = sc->h_ctr->rays;
+        stats->steps = sc->h_ctr->steps;
+        stats->fp64_steps = sc->h_ctr->fp64_steps;
+        stats->rhs_evals = sc->h_ctr->evals;
+        stats->kernel_ms = ms;
+    }
+    return NP_OK;
+}
+
+int np_render_host(const np_scene_t* scene, int precision, float* h_rgb, float* h_rcross, float* h_inv3,
+                   np_render_stats_t* stats) {
+    if (!scene || !h_rgb) return fail(NP_ERR_INVALID, "NULL argument");
+    int rc = np_scene_validate(scene);
+    if (rc != NP_OK) return rc;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) return fail(NP_ERR_NO_DEVICE, "No CUDA devices found.");
+    size_t npix = (size_t)scene->width * scene->height;
+    float *d_rgb = nullptr, *d_rc = nullptr, *d_inv = nullptr;
+    NP_CU(cudaMalloc(&d_rgb, 3 * npix * sizeof(float)), NP_ERR_ALLOC);
+    if (h_rcross && cudaMalloc(&d_rc, npix * sizeof(float)) != cudaSuccess) {
+        cudaFree(d_rgb);
+        return fail(NP_ERR_ALLOC, "cudaMalloc rcross failed");
+    }
+    if (h_inv3) {
+        if (cudaMalloc(&d_inv, 3 * sizeof(float)) != cudaSuccess) {
+            cudaFree(d_rgb); cudaFree(d_rc);
+            return fail(NP_ERR_ALLOC, "cudaMalloc inv3 failed");
+        }
+        cudaMemcpy(d_inv, h_inv3, 3 * sizeof(float), cudaMemcpyHostToDevice);
+    }
+    cudaStream_t st = nullptr;
+    rc = np_render_device(scene, precision, d_rgb, d_rc, d_inv, 0, st, stats);
+    if (rc == NP_OK) {
+        cudaError_t e = cudaMemcpyAsync(h_rgb, d_rgb, 3 * npix * sizeof(float), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess && h_rcross) e = cudaMemcpyAsync(h_rcross, d_rc, npix * sizeof(float), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess && h_inv3) e = cudaMemcpyAsync(h_inv3, d_inv, 3 * sizeof(float), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) rc = fail(NP_ERR_KERNEL, "render: %s", cudaGetErrorString(e));
+    }
+    cudaFree(d_rgb); cudaFree(d_rc); cudaFree(d_inv);
+    return rc;
+}
+
+int np_trace_rays_device(const np_scene_t* scene, int precision, int n, const double* d_px, const double* d_py,
+                         double* d_consts, double* d_cross, int32_t* d_status, void* stream_v) {
+    if (n < 0 || (n > 0 && (!d_px || !d_py))) return fail(NP_ERR_INVALID, "bad ray arrays");
+    if (precision != NP_PREC_FP64 && precision != NP_PREC_MIXED) return fail(NP_ERR_INVALID, "Invalid precision.");
+    SceneDev s;
+    int rc = prepare_scene(*scene, s);
+    if (rc != NP_OK) return rc;
+    if (n == 0) return NP_OK;
+    cudaStream_t st = (cudaStream_t)stream_v;
+    trace_rays_kernel<<<(n + 127) / 128, 128, 0, st>>>(s, precision, n, d_px, d_py, d_consts, d_cross, d_status);
+    NP_CU(cudaGetLastError(), NP_ERR_KERNEL);
+    return NP_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,260 @@
+// tracer_fp64.cuh -- the reference renderer's FP64 Hamiltonian integrator
+// (render.cu:161-251) as a per-lane state machine for the persistent kernel.
+//
+// Formulation, floors and termination rules follow include/bh_kerr.h
+// (600-774 fixed RK4, 987-1105 adaptive step doubling); all eight phase-space
+// components are integrated and the stage combination uses the compensated
+// sum of bh_common.h:485-493.  This is the FP64 baseline form.
+#pragma once
+
+#include "np_common.cuh"
+
+namespace np {
+
+struct St8 { double t, r, th, ph, pt, pr, pth, pph; };
+
+__device__ __forceinline__ St8 axpy8(const St8& y, double h, const St8& k) {
+    return St8{y.t + h * k.t, y.r + h * k.r, y.th + h * k.th, y.ph + h * k.ph,
+               y.pt + h * k.pt, y.pr + h * k.pr, y.pth + h * k.pth, y.pph + h * k.pph};
+}
+
+__device__ __forceinline__ double r_plus_of(double M, double a) {
+    double d = M * M - a * a;
+    if (d < 0.0) d = 0.0;
+    return M + sqrt(d);
+}
+
+// Hamilton's equations with the analytic inverse-metric derivatives
+// (bh_kerr.h:600-727), fused into one routine that shares sin/cos.
+__device__ __forceinline__ void rhs_ref(const St8& y, double M, double a, double rp, St8& f) {
+    if (y.r <= rp + 1e-12 || y.r <= 1e-12) { f = St8{0, 0, 0, 0, 0, 0, 0, 0}; return; }
+    double s, c;
+    sincos(y.th, &s, &c);
+    const double r = y.r, r2 = r * r, a2 = a * a;
+    // inverse metric with floors (bh_kerr.h:600-617)
+    double s2f = fmax(kEps, s * s);
+    double Sgf = fmax(kEps, r2 + a2 * c * c);
+    double Del = r2 - 2.0 * M * r + a2;
+    double Af = (r2 + a2) * (r2 + a2) - a2 * Del * s2f;
+    double g_rr = fmax(kEps, Del) / Sgf;
+    double g_hh = 1.0 / Sgf;
+    double g_tt = -Af / fmax(kEps, Sgf * Del);
+    double g_tp = -2.0 * M * a * r / fmax(kEps, Sgf * Del);
+    double g_pp = (Del - a2 * s2f) / fmax(kEps, Sgf * Del * s2f);
+    // derivatives (bh_kerr.h:624-672)
+    double s2 = (s * s > 1e-30) ? s * s : 1e-30;
+    double B = r2 + a2;
+    double Sig = r2 + a2 * c * c;
+    double A = B * B - a2 * Del * s2;
+    double D = Sig * Del;
+    double D2 = D * D + 1e-48;
+    double ds2 = 2.0 * s * c;
+    double Sig_r = 2.0 * r, Sig_t = -2.0 * a2 * s * c;
+    double Del_r = 2.0 * (r - M);
+    double A_r = 4.0 * r * B - a2 * Del_r * s2;
+    double A_t = -a2 * Del * ds2;
+    double D_r = Sig_r * Del + Sig * Del_r;
+    double D_t = Sig_t * Del;
+    double inv_D2 = 1.0 / D2;
+    double tt_r = -(A_r * D - A * D_r) * inv_D2;
+    double tt_t = -(A_t * D - A * D_t) * inv_D2;
+    double Nn = 2.0 * M * a * r, Nn_r = 2.0 * M * a;
+    double tp_r = -(Nn_r * D - Nn * D_r) * inv_D2;
+    double tp_t = (Nn * D_t) * inv_D2;
+    double inv_S2 = 1.0 / (Sig * Sig);
+    double rr_r = (Del_r * Sig - Del * Sig_r) * inv_S2;
+    double rr_t = -(Del * Sig_t) * inv_S2;
+    double hh_r = -Sig_r * inv_S2;
+    double hh_t = -Sig_t * inv_S2;
+    double P = Del - a2 * s2, P_t = -a2 * ds2;
+    double Q = Del * Sig * s2 + 1e-48;
+    double Q_r = Del_r * Sig * s2 + Del * Sig_r * s2;
+    double Q_t = Del * Sig_t * s2 + Del * Sig * ds2;
+    double inv_Q2 = 1.0 / (Q * Q + 1e-48);
+    double pp_r = (Del_r * Q - P * Q_r) * inv_Q2;
+    double pp_t = (P_t * Q - P * Q_t) * inv_Q2;
+
+    f.t = g_tt * y.pt + g_tp * y.pph;
+    f.r = g_rr * y.pr;
+    f.th = g_hh * y.pth;
+    f.ph = g_tp * y.pt + g_pp * y.pph;
+    f.pt = 0.0;
+    f.pph = 0.0;
+    Klein<double> sr, st;
+    sr.add(tt_r * y.pt * y.pt); sr.add(2.0 * tp_r * y.pt * y.pph); sr.add(pp_r * y.pph * y.pph);
+    sr.add(rr_r * y.pr * y.pr); sr.add(hh_r * y.pth * y.pth);
+    st.add(tt_t * y.pt * y.pt); st.add(2.0 * tp_t * y.pt * y.pph); st.add(pp_t * y.pph * y.pph);
+    st.add(rr_t * y.pr * y.pr); st.add(hh_t * y.pth * y.pth);
+    f.pr = -0.5 * sr.value();
+    f.pth = -0.5 * st.value();
+}
+
+__device__ __forceinline__ double combine4(double k1, double k2, double k3, double k4) {
+    Klein<double> k; k.add(k1); k.add(2.0 * k2); k.add(2.0 * k3); k.add(k4);
+    return k.value();
+}
+
+// One RK4 step; k1 (= f(y)) is returned for the crossing interpolant.
+__device__ __forceinline__ void rk4_ref(const St8& y, double M, double a, double rp, double h, St8& out, St8& k1) {
+    St8 k2, k3, k4;
+    rhs_ref(y, M, a, rp, k1);
+    rhs_ref(axpy8(y, 0.5 * h, k1), M, a, rp, k2);
+    rhs_ref(axpy8(y, 0.5 * h, k2), M, a, rp, k3);
+    rhs_ref(axpy8(y, h, k3), M, a, rp, k4);
+    double h6 = h / 6.0;
+    out.t = y.t + h6 * combine4(k1.t, k2.t, k3.t, k4.t);
+    out.r = y.r + h6 * combine4(k1.r, k2.r, k3.r, k4.r);
+    out.th = y.th + h6 * combine4(k1.th, k2.th, k3.th, k4.th);
+    out.ph = y.ph + h6 * combine4(k1.ph, k2.ph, k3.ph, k4.ph);
+    out.pt = y.pt + h6 * combine4(k1.pt, k2.pt, k3.pt, k4.pt);
+    out.pr = y.pr + h6 * combine4(k1.pr, k2.pr, k3.pr, k4.pr);
+    out.pth = y.pth + h6 * combine4(k1.pth, k2.pth, k3.pth, k4.pth);
+    out.pph = y.pph + h6 * combine4(k1.pph, k2.pph, k3.pph, k4.pph);
+}
+
+// Step doubling (bh_kerr.h:1058-1105); returns the growth factor on
+// acceptance (y advanced), 0 on rejection (h shrunk).
+__device__ __forceinline__ double adaptive_ref(St8& y, double M, double a, double rp, double& h,
+                                               double rtol, double atol, St8& k1) {
+    St8 full, half1, half2, kd;
+    rk4_ref(y, M, a, rp, h, full, k1);
+    double h2 = 0.5 * h;
+    rk4_ref(y, M, a, rp, h2, half1, kd);
+    rk4_ref(half1, M, a, rp, h2, half2, kd);
+    auto alive = [&](const St8& z) { return z.r > rp + 1e-12 && z.th > 1e-9 && z.th < kPi - 1e-9; };
+    if (!(alive(full) && alive(half1) && alive(half2))) { h *= 0.5; return 0.0; }
+    auto nerr = [&](double u, double v) {
+        double sc = atol + rtol * fmax(fabs(u), fabs(v));
+        return fabs(u - v) / fmax(sc, 1e-30);
+    };
+    double e = fmax(fmax(nerr(full.r, half2.r), nerr(full.th, half2.th)),
+                    fmax(fmax(nerr(full.ph, half2.ph), nerr(full.pr, half2.pr)),
+                         fmax(nerr(full.pth, half2.pth), nerr(full.pph, half2.pph))));
+    if (e <= 1.0) {
+        y = half2;
+        return fmin(2.0, kSafety * pow(fmax(1e-12, e), -0.2));
+    }
+    h *= fmax(0.1, kSafety * pow(fmax(1e-12, e), -0.25));
+    return 0.0;
+}
+
+__device__ __forceinline__ void invariants_ref(const SceneDev& s, const St8& y, double pt0, double pph0, float* inv3) {
+    double sn, c;
+    sincos(y.th, &sn, &c);
+    double r2 = y.r * y.r, a2 = s.a * s.a;
+    double s2 = fmax(kEps, sn * sn);
+    double Sig = fmax(kEps, r2 + a2 * c * c);
+    double Del = r2 - 2.0 * s.M * y.r + a2;
+    double A = (r2 + a2) * (r2 + a2) - a2 * Del * s2;
+    double grr = fmax(kEps, Del) / Sig, ghh = 1.0 / Sig;
+    double gtt = -A / fmax(kEps, Sig * Del), gtp = -2.0 * s.M * s.a * y.r / fmax(kEps, Sig * Del);
+    double gpp = (Del - a2 * s2) / fmax(kEps, Sig * Del * s2);
+    double H = 0.5 * (gtt * y.pt * y.pt + 2.0 * gtp * y.pt * y.pph + gpp * y.pph * y.pph
+                      + grr * y.pr * y.pr + ghh * y.pth * y.pth);
+    atomic_max_nonneg(&inv3[0], (float)fabs(H));
+    atomic_max_nonneg(&inv3[1], (float)(fabs(y.pt - pt0) / fmax(1e-12, fabs(pt0))));
+    atomic_max_nonneg(&inv3[2], (float)(fabs(y.pph - pph0) / fmax(1e-12, fabs(pph0))));
+}
+
+// Per-lane ray of the FP64 tracer.  With REC the first four equatorial
+// crossings (any radius) are recorded for the per-ray report.
+template <bool REC>
+struct RayFP64 {
+    St8 y, prev;
+    double min_r, h_adapt, first_r, pt0, pph0;
+    double xr[REC ? 4 : 1], xphi[REC ? 4 : 1];
+    float disk[3];
+    int step, orders, crossings, status;   // status: 0 escaped, 1 captured, 2 step cap
+};
+
+template <bool REC>
+__device__ __forceinline__ void fp64_init(const SceneDev& s, const Momentum& m, RayFP64<REC>& R) {
+    R.y = St8{0.0, s.r_cam, s.th_cam, s.ph_cam, m.pt, m.pr, m.pth, m.pph};
+    R.prev = R.y;
+    R.min_r = s.r_cam;
+    R.h_adapt = 0.0;
+    R.first_r = 0.0;
+    R.pt0 = m.pt; R.pph0 = m.pph;
+    R.disk[0] = R.disk[1] = R.disk[2] = 0.0f;
+    R.step = 0; R.orders = 0; R.crossings = 0; R.status = 2;
+    if (REC) for (int k = 0; k < 4; ++k) { R.xr[k] = 0.0; R.xphi[k] = 0.0; }
+}
+
+// Advances the ray by one accepted step; returns true when it terminated.
+// `evals` counts right-hand-side evaluations.
+template <bool REC>
+__device__ __forceinline__ bool fp64_advance(const SceneDev& s, RayFP64<REC>& R, float* inv3, unsigned long long& evals) {
+    if (R.step >= s.max_steps) { R.status = 2; return true; }
+    const double M = s.M, a = s.a, rp = s.r_plus;
+    double scale = fmin(fmax(1.0, R.y.r / (0.5 * s.Rs)), 100.0);
+    bool ok = false;
+    double h_used = 0.0;
+    St8 k1;
+    if (s.integrator == NP_INTEG_ADAPTIVE) {
+        double hb = fmin(fmax(s.h_unit * scale, kHMin), kHMax);
+        double h = (R.h_adapt > 0.0) ? R.h_adapt : hb;
+        h = fmin(fmax(h, kHMin), kHMax);
+        for (int att = 0; att < 8; ++att) {
+            double ht = h;
+            double fac = adaptive_ref(R.y, M, a, rp, ht, s.rtol, s.atol, k1);
+            evals += 12;
+            if (fac > 0.0) {
+                ok = true; h_used = ht;
+                R.h_adapt = fmin(fmax(ht * fac, kHMin), kHMax);
+                break;
+            }
+            h = fmax(ht, kHMin);
+            if (h <= kHMin * 1.01) break;
+        }
+    } else {
+        h_used = s.h_unit * scale;
+        St8 out;
+        rk4_ref(R.y, M, a, rp, h_used, out, k1);
+        evals += 4;
+        R.y = out;
+        ok = R.y.r > rp + 1e-9 && R.y.th > 1e-9 && R.y.th < kPi - 1e-9;
+    }
+    R.step++;
+    if (!ok) { R.status = 1; return true; }
+    R.min_r = fmin(R.min_r, R.y.r);
+    const double hp = kPi * 0.5;
+    double dp = R.prev.th - hp, dc = R.y.th - hp;
+    bool sc = (dp > 0 && dc < 0) || (dp < 0 && dc > 0);
+    bool nz = (fabs(dp) < 1e-8 && fabs(dc) >= 1e-8) || (fabs(dc) < 1e-8 && fabs(dp) >= 1e-8);
+    if (sc || nz) {
+        double alpha = fabs(dp) / (fabs(dp) + fabs(dc) + 1e-30);
+        double rc, phc;
+        if (s.crossing == NP_CROSS_HERMITE && sc) {
+            St8 f1;
+            rhs_ref(R.y, M, a, rp, f1);
+            evals += 1;
+            double u = hermite_root(dp, dc, h_used * k1.th, h_used * f1.th, alpha);
+            rc = hermite_eval(R.prev.r, R.y.r, h_used * k1.r, h_used * f1.r, u);
+            phc = hermite_eval(R.prev.ph, R.y.ph, h_used * k1.ph, h_used * f1.ph, u);
+        } else {
+            rc = R.prev.r + alpha * (R.y.r - R.prev.r);
+            phc = R.prev.ph + alpha * (R.y.ph - R.prev.ph);
+        }
+        if (REC) {
+            if (R.crossings < 4) { R.xr[R.crossings] = rc; R.xphi[R.crossings] = phc; }
+        }
+        R.crossings++;
+        if (R.orders < s.max_orders && rc >= s.rin && rc <= s.rout) {
+            double pt = R.prev.pt + alpha * (R.y.pt - R.prev.pt);
+            double pph = R.prev.pph + alpha * (R.y.pph - R.prev.pph);
+            float g = (float)doppler_g(rc, pt, pph, M, a);
+            shade_disk((float)rc, g, s.qf, s.gain, R.disk);
+            if (R.orders == 0) R.first_r = rc;
+            R.orders++;
+            if (s.check_inv && inv3) {
+                St8 cr = R.y; cr.r = rc; cr.th = hp; cr.pt = pt; cr.pph = pph;
+                invariants_ref(s, cr, R.pt0, R.pph0, inv3);
+            }
+        }
+    }
+    R.prev = R.y;
+    if (R.y.r > s.r_far && R.step > 11) { R.status = 0; return true; }
+    return false;
+}
+
+}  // namespace np

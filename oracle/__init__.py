@@ -1,0 +1,117 @@
+"""ctypes access to the CPU oracle (test infrastructure only).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline legs import
+this package; the product library never calls it.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+_O = None
+_R = None
+
+
+def _scene_type():
+    from nullpath_gb300._abi import Scene
+    return Scene
+
+
+def load():
+    global _O
+    if _O is None:
+        p = os.path.join(HERE, "liboracle.so")
+        if not os.path.exists(p):
+            raise RuntimeError("oracle/liboracle.so not built; run `make -C oracle`")
+        lib = C.CDLL(p)
+        S = C.POINTER(_scene_type())
+        lib.npo_render.argtypes = [S, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
+        lib.npo_render.restype = C.c_int
+        lib.npo_trace_rays.argtypes = [S, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                       C.c_void_p, C.c_void_p, C.c_int]
+        lib.npo_trace_rays.restype = C.c_int
+        lib.npo_metric_inv.argtypes = [C.c_double] * 4 + [C.c_void_p]
+        lib.npo_metric_inv.restype = None
+        lib.npo_metric_inv_derivs.argtypes = [C.c_double] * 4 + [C.c_void_p, C.c_void_p]
+        lib.npo_metric_inv_derivs.restype = None
+        _O = lib
+    return _O
+
+
+def load_ref():
+    """The reference's own headers compiled here (oracle/_ref); None when absent."""
+    global _R
+    if _R is None:
+        p = os.path.join(HERE, "_ref", "libnpref.so")
+        if not os.path.exists(p):
+            return None
+        lib = C.CDLL(p)
+        S = C.POINTER(_scene_type())
+        lib.npref_render.argtypes = [S, C.c_int, C.c_int, C.c_void_p, C.c_void_p]
+        lib.npref_render.restype = C.c_int
+        lib.npref_metric_inv.argtypes = [C.c_double] * 4 + [C.c_void_p]
+        lib.npref_metric_inv_derivs.argtypes = [C.c_double] * 4 + [C.c_void_p, C.c_void_p]
+        _R = lib
+    return _R
+
+
+def _vp(a):
+    return a.ctypes.data_as(C.c_void_p) if a is not None else None
+
+
+def render(scene, y0=0, y1=None, threads=0, with_inv=False):
+    """Oracle render of rows [y0, y1): returns (rgb[3,H,W], rcross[H,W][, inv3])."""
+    lib = load()
+    H, W = scene.height, scene.width
+    y1 = H if y1 is None else y1
+    rgb = np.zeros((3, H, W), np.float32)
+    rc = np.zeros((H, W), np.float32)
+    inv = np.zeros(3, np.float32) if with_inv else None
+    rc_ = lib.npo_render(C.byref(scene), y0, y1, _vp(rgb), _vp(rc), _vp(inv), threads)
+    if rc_ != 0:
+        raise RuntimeError("oracle render failed: %d" % rc_)
+    return (rgb, rc, inv) if with_inv else (rgb, rc)
+
+
+def render_ref(scene, y0=0, y1=None):
+    lib = load_ref()
+    if lib is None:
+        return None
+    H, W = scene.height, scene.width
+    y1 = H if y1 is None else y1
+    rgb = np.zeros((3, H, W), np.float32)
+    rc = np.zeros((H, W), np.float32)
+    if lib.npref_render(C.byref(scene), y0, y1, _vp(rgb), _vp(rc)) != 0:
+        raise RuntimeError("reference render failed")
+    return rgb, rc
+
+
+def trace_rays(scene, px, py, threads=0):
+    lib = load()
+    px = np.ascontiguousarray(px, np.float64)
+    py = np.ascontiguousarray(py, np.float64)
+    n = px.size
+    consts = np.zeros((n, 4), np.float64)
+    cross = np.zeros((n, 4, 2), np.float64)
+    status = np.zeros(n, np.int32)
+    steps = np.zeros(n, np.int32)
+    if lib.npo_trace_rays(C.byref(scene), n, _vp(px), _vp(py), _vp(consts), _vp(cross), _vp(status),
+                          _vp(steps), threads) != 0:
+        raise RuntimeError("oracle trace failed")
+    return {"consts": consts, "cross": cross, "status": status, "steps": steps}
+
+
+def metric_inv(lib, M, a, r, th):
+    g = np.zeros(5)
+    fn = lib.npo_metric_inv if hasattr(lib, "npo_metric_inv") else lib.npref_metric_inv
+    fn(M, a, r, th, _vp(g))
+    return g
+
+
+def metric_inv_derivs(lib, M, a, r, th):
+    dr = np.zeros(5)
+    dt = np.zeros(5)
+    fn = lib.npo_metric_inv_derivs if hasattr(lib, "npo_metric_inv_derivs") else lib.npref_metric_inv_derivs
+    fn(M, a, r, th, _vp(dr), _vp(dt))
+    return dr, dt
