@@ -1,0 +1,271 @@
+"""Benchmark of the Kerr render path on the 1280x720, a = 0.9 scene.
+
+One step = one full frame: 1280 x 720 pixels x 4 stratified samples
+(3,686,400 rays), M = 1, observer at r = 50 M, theta = 80 deg, fov 55 deg,
+thin disk from the prograde ISCO to 20 M with j ~ r^-3, up to three crossing
+orders, step cap 4096, escape at 1000 M, traced by the mixed-precision path
+(FP32 bulk, FP64 islands).  Metric: rays per second.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+With N > 1 (launched by torch.distributed.run) every rank renders its own
+frame (independent seeds, weak scaling, no collective on the data path).
+`--impl reference` times the CPU FP64 restatement of the reference render
+path (oracle/, bit-identical to the reference headers in reference mode) on
+all host cores, on a bounded row sample of the same frame.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Kerr rays/s fwd & fwd+adjoint, 1280×720 a=0.9; error vs FP64 GEOKERR"
+WORKLOAD = "kerr_render_1280x720_a0.9_4spp"
+
+# Algorithmic work of one accepted step of the mixed tracer (FP32 Carter-form
+# RK4: four right-hand sides, three stage builds, compensated update), counted
+# from tracer_mixed.cuh with an FMA counted as two flops; reciprocals and
+# sincos are MUFU work and are not included.  nullpath_gb300/opcount.json
+# carries the itemised count.
+def _opcount():
+    with open(os.path.join(ROOT, "nullpath_gb300", "opcount.json")) as f:
+        return json.load(f)
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    return ws, rank
+
+
+def _clock_sampler(path):
+    cmd = ["nvidia-smi", "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+           "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+           "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+           "--format=csv,noheader,nounits", "-lms", "200"]
+    try:
+        f = open(path, "w")
+        return subprocess.Popen(cmd, stdout=f, stderr=subprocess.DEVNULL), f
+    except Exception:
+        return None, None
+
+
+def _clock_summary(path, gpu_index):
+    try:
+        rows = [l.strip().split(",") for l in open(path) if l.strip()]
+    except Exception:
+        return None
+    rows = [[c.strip() for c in r] for r in rows if len(r) >= 9]
+    rows = [r for r in rows if r[0] == str(gpu_index)] or rows
+    if not rows:
+        return None
+    sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+    mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+    names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+    reasons = sorted({n for r in rows for n, v in zip(names, r[5:9]) if v.lower() == "active"})
+    return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+            "reasons": reasons, "samples": len(rows)}
+
+
+def cpu_baseline(threads=None, rows_every=45):
+    """Oracle FP64 render of every `rows_every`-th row of the benchmark frame
+    on the host cores; returns (rays/s, cores, sample description)."""
+    import oracle
+    from nullpath_gb300._abi import benchmark_scene
+    sc = benchmark_scene()
+    threads = threads or os.cpu_count()
+    rows = list(range(0, sc.height, rows_every))
+    t0 = time.perf_counter()
+    for y in rows:
+        oracle.render(sc, y, y + 1, threads=threads)
+    dt = time.perf_counter() - t0
+    rays = len(rows) * sc.width * sc.spp
+    desc = "%d of %d rows (every %dth) x %d px x %d spp = %d rays, FP64 oracle, %.1f s" % (
+        len(rows), sc.height, rows_every, sc.width, sc.spp, rays, dt)
+    return rays / dt, threads, desc
+
+
+def run_reference(args):
+    ws, rank = _dist()
+    if rank != 0:
+        return
+    per_step = []
+    desc = None
+    cores = os.cpu_count()
+    for i in range(args.warmup + args.steps):
+        v, cores, desc = cpu_baseline(rows_every=90)
+        if i >= args.warmup:
+            per_step.append(v)
+    val = statistics.mean(per_step)
+    cpu = {"value": val, "unit": "rays/s", "cores": cores, "kind": "port",
+           "sample": desc + "; restatement bit-identical to the reference headers in reference mode"}
+    out = {"impl": "reference", "metric": METRIC, "value": val, "unit": "rays/s", "n_gpus": ws,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": WORKLOAD, "sample": desc, "device": "host cpu"},
+           "cpu_baseline": cpu,
+           "e2e": {"value": val, "unit": "rays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+    import nullpath_gb300 as npx
+
+    ws, rank = _dist()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if ws > 1:
+        dist.init_process_group("nccl")
+
+    def barrier():
+        if ws > 1:
+            dist.barrier()
+
+    lib = npx.load()
+    sc = npx.benchmark_scene(seed=rank)
+    H, W = sc.height, sc.width
+    rays_per_step = W * H * sc.spp
+    rgb = torch.zeros((3, H, W), dtype=torch.float32, device="cuda")
+    rc = torch.zeros((H, W), dtype=torch.float32, device="cuda")
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")   # 256 MiB > L2
+    stream = torch.cuda.current_stream()
+
+    for _ in range(args.warmup):
+        npx.render(sc, args.precision, rgb=rgb, rcross=rc)
+    torch.cuda.synchronize()
+
+    clock_path = os.path.join(ROOT, "gpurun_out", "bench_clocks_rank%d.csv" % rank)
+    os.makedirs(os.path.dirname(clock_path), exist_ok=True)
+    sampler, fh = _clock_sampler(clock_path)
+
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    stats = []
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        flush.fill_(float(i))          # evict L2 between timed steps (outside the events)
+        ev[i][0].record(stream)
+        _, _, st = npx.render(sc, args.precision, rgb=rgb, rcross=rc, stats=True)
+        ev[i][1].record(stream)
+        stats.append(st)
+    torch.cuda.synchronize()
+    barrier()
+    wall = time.perf_counter() - t0
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    ms = statistics.mean(step_ms)
+    if ws > 1:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+
+    # end-to-end through the host API: scene in, host image out (copies inside)
+    pinned_rgb = torch.empty((3, H, W), dtype=torch.float32).pin_memory()
+    pinned_rc = torch.empty((H, W), dtype=torch.float32).pin_memory()
+    import ctypes as C
+    e2e_ms = []
+    for i in range(args.steps + 1):
+        torch.cuda.synchronize()
+        s0 = time.perf_counter()
+        npx._lib.check(lib.np_render_host(C.byref(sc), npx.precision_code(args.precision),
+                                          C.c_void_p(pinned_rgb.data_ptr()), C.c_void_p(pinned_rc.data_ptr()),
+                                          None, None))
+        if i > 0:
+            e2e_ms.append((time.perf_counter() - s0) * 1e3)
+    e2e = statistics.mean(e2e_ms)
+    if ws > 1:
+        t = torch.tensor([e2e], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e = float(t.item())
+
+    if sampler is not None:
+        sampler.terminate()
+        fh.close()
+    clocks = _clock_summary(clock_path, local)
+
+    if rank == 0:
+        oc = _opcount()
+        st = stats[-1]
+        flop_step = oc["mixed_step_flops"] if args.precision == "mixed" else oc["fp64_step_flops"]
+        kern_ms = statistics.mean(s.kernel_ms for s in stats)
+        steps_main = st.steps - (st.fp64_steps if args.precision == "mixed" and st.deferred_rays else 0)
+        achieved = flop_step * steps_main / (kern_ms * 1e-3) / 1e12
+        peak = ctypes_peak(lib, 0 if args.precision == "mixed" else 1)
+        out = {
+            "metric": METRIC, "value": ws * rays_per_step / (ms * 1e-3), "unit": "rays/s",
+            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32+f64" if args.precision == "mixed" else "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "width": W, "height": H, "spp": sc.spp, "spin": sc.spin,
+                       "precision": args.precision, "rays_per_step": rays_per_step,
+                       "l2": "256 MiB buffer written between timed steps (outside the step events)",
+                       "parallelism": "replicas" if ws > 1 else "single"},
+            "steps_per_s": ws * st.steps / (ms * 1e-3),
+            "mean_steps_per_ray": st.steps / max(1, st.rays),
+            "fp64_island_steps_frac": st.fp64_steps / max(1, st.steps),
+            "deferred_rays": st.deferred_rays,
+            "kernel_ms": {"main": kern_ms, "deferred_fp64": statistics.mean(s.deferred_ms for s in stats)},
+            "roofline": {"bound": "fp32" if args.precision == "mixed" else "fp64", "achieved": achieved,
+                         "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
+                         "traffic": None,
+                         "peak_source": "measured in this run by np_measure_fma_peak (register FMA loop)"},
+            "e2e": {"value": ws * rays_per_step / (e2e * 1e-3), "unit": "rays/s", "h2d_bytes_per_step": C.sizeof(sc),
+                    "d2h_bytes_per_step": 4 * H * W * 4},
+            "gpu_launches": 3 * args.steps,
+            "clocks": clocks,
+            "wall_s": wall,
+        }
+        if args.fp64_frame and args.precision == "mixed":
+            _, _, s64 = npx.render(sc, "fp64", stats=True)
+            out["fp64_path"] = {"rays_per_s": rays_per_step / (s64.kernel_ms * 1e-3), "kernel_ms": s64.kernel_ms,
+                                "mean_steps_per_ray": s64.steps / max(1, s64.rays),
+                                "roofline": {"bound": "fp64", "achieved": oc["fp64_step_flops"] * s64.steps /
+                                             (s64.kernel_ms * 1e-3) / 1e12, "peak": ctypes_peak(lib, 1),
+                                             "unit": "TFLOP/s"}}
+            out["fp64_path"]["roofline"]["frac"] = out["fp64_path"]["roofline"]["achieved"] / \
+                out["fp64_path"]["roofline"]["peak"]
+            out["mixed_over_fp64"] = out["value"] / ws / out["fp64_path"]["rays_per_s"]
+        if args.cpu_baseline:
+            v, cores, desc = cpu_baseline()
+            out["cpu_baseline"] = {"value": v, "unit": "rays/s", "cores": cores, "kind": "port", "sample": desc}
+        print(json.dumps(out))
+    if ws > 1:
+        dist.destroy_process_group()
+
+
+def ctypes_peak(lib, which):
+    import ctypes as C
+    v = C.c_double(0.0)
+    if lib.np_measure_fma_peak(which, C.byref(v)) != 0:
+        return None
+    return v.value
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--no-fp64-frame", dest="fp64_frame", action="store_false")
+    ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        print("warning: fewer than 3 warm-up steps", file=sys.stderr)
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

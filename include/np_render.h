@@ -106,7 +106,9 @@ typedef struct np_render_stats {
     uint64_t steps;               /* accepted integration steps */
     uint64_t fp64_steps;          /* steps taken in FP64 by the mixed path */
     uint64_t rhs_evals;           /* right-hand-side evaluations */
-    double kernel_ms;             /* device time of the render kernel */
+    uint64_t deferred_rays;       /* near-critical rays finished by the FP64 tracer (mixed path) */
+    double kernel_ms;             /* device time of the main tracer kernel */
+    double deferred_ms;           /* device time of the deferred FP64 kernel (mixed path) */
 } np_render_stats_t;
 
 /* ABI version compiled into the library. */
@@ -156,6 +158,11 @@ int np_trace_rays_device(const np_scene_t* scene, int precision, int n,
                          const double* d_px, const double* d_py,
                          double* d_consts, double* d_cross, int32_t* d_status,
                          void* stream);
+
+/* Measures the sustained FMA throughput of this GPU's SIMT pipes with a
+ * register-resident FMA loop: which = 0 for FP32, 1 for FP64.  Writes
+ * TFLOP/s (an FMA counts as two flops).  Synchronous. */
+int np_measure_fma_peak(int which, double* tflops);
 
 #ifdef __cplusplus
 }

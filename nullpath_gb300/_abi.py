@@ -61,7 +61,8 @@ class RenderStats(C.Structure):
     """np_render_stats_t (include/np_render.h)."""
     _fields_ = [
         ("rays", C.c_uint64), ("steps", C.c_uint64), ("fp64_steps", C.c_uint64),
-        ("rhs_evals", C.c_uint64), ("kernel_ms", C.c_double),
+        ("rhs_evals", C.c_uint64), ("deferred_rays", C.c_uint64),
+        ("kernel_ms", C.c_double), ("deferred_ms", C.c_double),
     ]
 
 

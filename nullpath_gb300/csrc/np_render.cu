@@ -13,6 +13,7 @@
 #include <cstdio>
 #include <cstring>
 #include <cmath>
+#include <algorithm>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -372,6 +373,20 @@ __global__ void trace_rays_kernel(const SceneDev s, int precision, int n, const 
     if (status) status[i] = st + 16 * min(ncross, 15);
 }
 
+// Register-resident FMA throughput probe: 8 independent chains per thread.
+template <typename T>
+__global__ void fma_peak_kernel(T* out, int iters, T a, T b) {
+    T x[8];
+    for (int k = 0; k < 8; ++k) x[k] = (T)(threadIdx.x + k);
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) x[k] = x[k] * a + b;
+    }
+    T s = 0;
+    for (int k = 0; k < 8; ++k) s += x[k];
+    if (s == (T)-1.2345) out[0] = s;   // keeps the loop live; never true for these inputs
+}
+
 // ---------------------------------------------------------------------------
 // Per-(device, stream) scratch: per-sample colour planes, deferred list and
 // counters.  Grows on demand; calls on the same stream reuse it in order.
@@ -382,7 +397,7 @@ struct Scratch {
     long long* list = nullptr; size_t list_n = 0;
     Counters* ctr = nullptr;
     Counters* h_ctr = nullptr;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr;
 };
 std::mutex g_scratch_mu;
 std::vector<Scratch*> g_scratch;
@@ -401,6 +416,7 @@ int get_scratch(cudaStream_t stream, size_t srgb_n, size_t list_n, Scratch** out
         NP_CU(cudaMallocHost(&sc->h_ctr, sizeof(Counters)), NP_ERR_ALLOC);
         NP_CU(cudaEventCreate(&sc->ev0), NP_ERR_KERNEL);
         NP_CU(cudaEventCreate(&sc->ev1), NP_ERR_KERNEL);
+        NP_CU(cudaEventCreate(&sc->ev2), NP_ERR_KERNEL);
         g_scratch.push_back(sc);
     }
     if (sc->srgb_n < srgb_n) {
@@ -511,14 +527,18 @@ int np_render_device(const np_scene_t* scene, int precision, float* d_rgb, float
     if (precision == NP_PREC_FP64) {
         render_fp64_kernel<<<grid_for((const void*)render_fp64_kernel), kBlock, 0, st>>>(
             s, sc->srgb, d_rcross, d_inv3, sc->ctr, nullptr);
+        NP_CU(cudaGetLastError(), NP_ERR_KERNEL);
+        if (stats) NP_CU(cudaEventRecord(sc->ev1, st), NP_ERR_KERNEL);
     } else {
         render_mixed_kernel<<<grid_for((const void*)render_mixed_kernel), kBlock, 0, st>>>(
             s, sc->srgb, d_rcross, d_inv3, sc->ctr, sc->list);
+        NP_CU(cudaGetLastError(), NP_ERR_KERNEL);
+        if (stats) NP_CU(cudaEventRecord(sc->ev1, st), NP_ERR_KERNEL);
         render_fp64_kernel<<<grid_for((const void*)render_fp64_kernel), kBlock, 0, st>>>(
             s, sc->srgb, d_rcross, d_inv3, sc->ctr, sc->list);
+        NP_CU(cudaGetLastError(), NP_ERR_KERNEL);
     }
-    NP_CU(cudaGetLastError(), NP_ERR_KERNEL);
-    if (stats) NP_CU(cudaEventRecord(sc->ev1, st), NP_ERR_KERNEL);
+    if (stats) NP_CU(cudaEventRecord(sc->ev2, st), NP_ERR_KERNEL);
     {
         long long n = 3 * s.npix;
         int blocks = (int)std::min<long long>((n + 255) / 256, 152 * 16);
@@ -528,13 +548,16 @@ int np_render_device(const np_scene_t* scene, int precision, float* d_rgb, float
     if (stats) {
         NP_CU(cudaMemcpyAsync(sc->h_ctr, sc->ctr, sizeof(Counters), cudaMemcpyDeviceToHost, st), NP_ERR_KERNEL);
         NP_CU(cudaStreamSynchronize(st), NP_ERR_KERNEL);
-        float ms = 0.0f;
+        float ms = 0.0f, ms2 = 0.0f;
         cudaEventElapsedTime(&ms, sc->ev0, sc->ev1);
+        cudaEventElapsedTime(&ms2, sc->ev1, sc->ev2);
         stats->rays = sc->h_ctr->rays;
         stats->steps = sc->h_ctr->steps;
         stats->fp64_steps = sc->h_ctr->fp64_steps;
         stats->rhs_evals = sc->h_ctr->evals;
+        stats->deferred_rays = precision == NP_PREC_MIXED ? sc->h_ctr->deferred : 0;
         stats->kernel_ms = ms;
+        stats->deferred_ms = ms2;
     }
     return NP_OK;
 }
@@ -547,30 +570,30 @@ int np_render_host(const np_scene_t* scene, int precision, float* h_rgb, float* 
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) return fail(NP_ERR_NO_DEVICE, "No CUDA devices found.");
     size_t npix = (size_t)scene->width * scene->height;
-    float *d_rgb = nullptr, *d_rc = nullptr, *d_inv = nullptr;
-    NP_CU(cudaMalloc(&d_rgb, 3 * npix * sizeof(float)), NP_ERR_ALLOC);
-    if (h_rcross && cudaMalloc(&d_rc, npix * sizeof(float)) != cudaSuccess) {
-        cudaFree(d_rgb);
-        return fail(NP_ERR_ALLOC, "cudaMalloc rcross failed");
+    // device staging buffers, cached per host thread and grown on demand
+    thread_local float* d_buf = nullptr;
+    thread_local size_t d_cap = 0;
+    thread_local int d_dev = -1;
+    int dev = 0;
+    NP_CU(cudaGetDevice(&dev), NP_ERR_NO_DEVICE);
+    size_t need = 4 * npix + 4;
+    if (d_buf && (d_cap < need || d_dev != dev)) { cudaFree(d_buf); d_buf = nullptr; d_cap = 0; }
+    if (!d_buf) {
+        NP_CU(cudaMalloc(&d_buf, need * sizeof(float)), NP_ERR_ALLOC);
+        d_cap = need; d_dev = dev;
     }
-    if (h_inv3) {
-        if (cudaMalloc(&d_inv, 3 * sizeof(float)) != cudaSuccess) {
-            cudaFree(d_rgb); cudaFree(d_rc);
-            return fail(NP_ERR_ALLOC, "cudaMalloc inv3 failed");
-        }
-        cudaMemcpy(d_inv, h_inv3, 3 * sizeof(float), cudaMemcpyHostToDevice);
-    }
+    float* d_rgb = d_buf;
+    float* d_rc = h_rcross ? d_buf + 3 * npix : nullptr;
+    float* d_inv = h_inv3 ? d_buf + 4 * npix : nullptr;
     cudaStream_t st = nullptr;
+    if (h_inv3) NP_CU(cudaMemcpyAsync(d_inv, h_inv3, 3 * sizeof(float), cudaMemcpyHostToDevice, st), NP_ERR_KERNEL);
     rc = np_render_device(scene, precision, d_rgb, d_rc, d_inv, 0, st, stats);
-    if (rc == NP_OK) {
-        cudaError_t e = cudaMemcpyAsync(h_rgb, d_rgb, 3 * npix * sizeof(float), cudaMemcpyDeviceToHost, st);
-        if (e == cudaSuccess && h_rcross) e = cudaMemcpyAsync(h_rcross, d_rc, npix * sizeof(float), cudaMemcpyDeviceToHost, st);
-        if (e == cudaSuccess && h_inv3) e = cudaMemcpyAsync(h_inv3, d_inv, 3 * sizeof(float), cudaMemcpyDeviceToHost, st);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-        if (e != cudaSuccess) rc = fail(NP_ERR_KERNEL, "render: %s", cudaGetErrorString(e));
-    }
-    cudaFree(d_rgb); cudaFree(d_rc); cudaFree(d_inv);
-    return rc;
+    if (rc != NP_OK) return rc;
+    NP_CU(cudaMemcpyAsync(h_rgb, d_rgb, 3 * npix * sizeof(float), cudaMemcpyDeviceToHost, st), NP_ERR_KERNEL);
+    if (h_rcross) NP_CU(cudaMemcpyAsync(h_rcross, d_rc, npix * sizeof(float), cudaMemcpyDeviceToHost, st), NP_ERR_KERNEL);
+    if (h_inv3) NP_CU(cudaMemcpyAsync(h_inv3, d_inv, 3 * sizeof(float), cudaMemcpyDeviceToHost, st), NP_ERR_KERNEL);
+    NP_CU(cudaStreamSynchronize(st), NP_ERR_KERNEL);
+    return NP_OK;
 }
 
 int np_trace_rays_device(const np_scene_t* scene, int precision, int n, const double* d_px, const double* d_py,
@@ -584,6 +607,36 @@ int np_trace_rays_device(const np_scene_t* scene, int precision, int n, const do
     cudaStream_t st = (cudaStream_t)stream_v;
     trace_rays_kernel<<<(n + 127) / 128, 128, 0, st>>>(s, precision, n, d_px, d_py, d_consts, d_cross, d_status);
     NP_CU(cudaGetLastError(), NP_ERR_KERNEL);
+    return NP_OK;
+}
+
+int np_measure_fma_peak(int which, double* tflops) {
+    if (!tflops || (which != 0 && which != 1)) return fail(NP_ERR_INVALID, "bad arguments");
+    int dev = 0, sms = 0;
+    NP_CU(cudaGetDevice(&dev), NP_ERR_NO_DEVICE);
+    NP_CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), NP_ERR_NO_DEVICE);
+    void* out = nullptr;
+    NP_CU(cudaMalloc(&out, 16), NP_ERR_ALLOC);
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0); cudaEventCreate(&e1);
+    const int threads = 256, blocks = sms * 8;
+    const int iters = which == 0 ? 1 << 16 : 1 << 11;
+    double best = 0.0;
+    for (int rep = 0; rep < 4; ++rep) {
+        cudaEventRecord(e0);
+        if (which == 0) fma_peak_kernel<float><<<blocks, threads>>>((float*)out, iters, 0.999f, 0.001f);
+        else fma_peak_kernel<double><<<blocks, threads>>>((double*)out, iters, 0.999, 0.001);
+        cudaEventRecord(e1);
+        cudaError_t e = cudaEventSynchronize(e1);
+        if (e != cudaSuccess) { cudaFree(out); return fail(NP_ERR_KERNEL, "peak kernel: %s", cudaGetErrorString(e)); }
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        double flops = 2.0 * 8.0 * (double)iters * threads * blocks;
+        if (rep > 0) best = std::max(best, flops / (ms * 1e-3) / 1e12);
+    }
+    cudaEventDestroy(e0); cudaEventDestroy(e1);
+    cudaFree(out);
+    *tflops = best;
     return NP_OK;
 }
 

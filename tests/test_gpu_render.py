@@ -1,0 +1,153 @@
+"""GPU parity of the sm_103a render kernels against the CPU oracle and the
+reference golden vectors, through the C ABI (tolerances are stated per test).
+
+FP64 path: same algorithm as the reference (render.cu:161-251) in FP64; the
+GPU contracts multiply-adds and uses CUDA's sin/cos, so trajectories differ
+from the CPU by a few ulp and only near-critical rays can change outcome.
+Mixed path: FP32/compensated Carter-form integration with FP64 islands; its
+crossing radii agree with the FP64 oracle to the integrator's truncation
+level.
+"""
+import ast
+import os
+
+import numpy as np
+import pytest
+
+import nullpath_gb300 as npx
+import oracle
+from nullpath_gb300._abi import Scene, reference_defaults, benchmark_scene, NP_JITTER_WANGHASH
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def _scene_from(npz):
+    d = ast.literal_eval(str(npz["scene"][0]))
+    s = Scene()
+    for k, v in d.items():
+        setattr(s, k, v)
+    return s
+
+
+def _gold(prefix):
+    return sorted(f[:-4] for f in os.listdir(GOLD) if f.startswith(prefix) and f.endswith(".npz"))
+
+
+def _render_np(sc, prec):
+    import torch
+    rgb, rc = npx.render(sc, prec)
+    torch.cuda.synchronize()
+    return rgb.cpu().numpy(), rc.cpu().numpy()
+
+
+def _compare(rgb, rc, rgb_ref, rc_ref, rtol_rgb, r_tol, min_frac):
+    """Fraction of pixels whose colour matches; max crossing-radius error over
+    pixels that hit the disk in both."""
+    pix_ok = np.isclose(rgb, rgb_ref, rtol=rtol_rgb, atol=1e-7).all(axis=0)
+    both = (rc > 0) & (rc_ref > 0)
+    cls = ((rc > 0) == (rc_ref > 0)).mean()
+    rerr = np.abs(rc[both].astype(np.float64) - rc_ref[both])
+    assert pix_ok.mean() >= min_frac, ("colour", pix_ok.mean())
+    assert cls >= min_frac, ("classification", cls)
+    if both.any():
+        assert np.quantile(rerr, 0.99) <= r_tol, ("rcross p99", np.quantile(rerr, 0.99))
+    return pix_ok.mean(), cls, (rerr.max() if both.any() else 0.0)
+
+
+@pytest.mark.parametrize("name", _gold("ref_"))
+def test_fp64_matches_reference_golden(cuda, name):
+    z = np.load(os.path.join(GOLD, name + ".npz"))
+    sc = _scene_from(z)
+    rgb, rc = _render_np(sc, "fp64")
+    # float colours within 1e-5 relative on >= 98% of pixels; crossing radius p99 <= 1e-5 M
+    _compare(rgb, rc, z["rgb"], z["rcross"], 1e-5, 1e-5 * sc.mass * 20, 0.98)
+
+
+@pytest.mark.parametrize("name", _gold("bench_"))
+def test_fp64_matches_oracle_benchmark(cuda, name):
+    z = np.load(os.path.join(GOLD, name + ".npz"))
+    sc = _scene_from(z)
+    rgb, rc = _render_np(sc, "fp64")
+    _compare(rgb, rc, z["rgb"], z["rcross"], 1e-5, 1e-6, 0.98)
+
+
+@pytest.mark.parametrize("name", _gold("bench_"))
+def test_mixed_matches_oracle_benchmark(cuda, name):
+    z = np.load(os.path.join(GOLD, name + ".npz"))
+    sc = _scene_from(z)
+    rgb, rc = _render_np(sc, "mixed")
+    # colours within 1e-3 relative on >= 95% of pixels; crossing radius p99 <= 1e-4 M
+    _compare(rgb, rc, z["rgb"], z["rcross"], 1e-3, 1e-4, 0.95)
+
+
+def test_trace_rays_constants_and_crossings(cuda):
+    sc = benchmark_scene(width=64, height=36, spp=1)
+    rng = np.random.default_rng(3)
+    px = rng.uniform(0, 64, 512)
+    py = rng.uniform(0, 36, 512)
+    ref = oracle.trace_rays(sc, px, py)
+    for prec in ("fp64", "mixed"):
+        out = npx.trace_rays(sc, px, py, prec)
+        c = out["consts"].cpu().numpy()
+        assert np.allclose(c, ref["consts"], rtol=1e-13, atol=1e-13)
+        st = out["status"].cpu().numpy()
+        agree = (st % 16 == ref["status"] % 16).mean()
+        assert agree > 0.97, (prec, agree)
+        x = out["cross"].cpu().numpy()[:, 0, 0]
+        xr = ref["cross"][:, 0, 0]
+        both = (x > 0) & (xr > 0) & (np.abs(x - xr) < 1.0)
+        tol = 1e-7 if prec == "fp64" else 1e-4
+        assert np.quantile(np.abs(x[both] - xr[both]), 0.99) < tol, prec
+
+
+def test_progressive_accumulation(cuda):
+    import torch
+    sc = reference_defaults().replace(width=32, height=18, spin=0.7, theta_deg=75.0, fov_y_deg=50.0,
+                                      jitter=NP_JITTER_WANGHASH)
+    one, _ = npx.render(sc.replace(spp=4), "fp64")
+    acc, _ = npx.render(sc.replace(spp=2), "fp64")
+    npx.render(sc.replace(spp=2, sample_offset=2), "fp64", rgb=acc, accumulate=True)
+    torch.cuda.synchronize()
+    assert torch.allclose(one, acc, rtol=1e-6, atol=1e-7)
+
+
+def test_deterministic_and_host_api(cuda):
+    import torch
+    sc = benchmark_scene(width=40, height=24, spp=2)
+    a, ra = npx.render(sc, "mixed")
+    b, rb = npx.render(sc, "mixed")
+    torch.cuda.synchronize()
+    assert torch.equal(a, b) and torch.equal(ra, rb)
+    h_rgb, h_rc, st = npx.render_host(sc, "mixed")
+    assert np.array_equal(h_rgb, a.cpu().numpy()) and np.array_equal(h_rc, ra.cpu().numpy())
+    assert st.rays == 40 * 24 * 2 and st.steps > 0
+
+
+def test_invariants_reported(cuda):
+    sc = reference_defaults().replace(width=24, height=14, spin=0.9, theta_deg=80.0, check_invariants=1)
+    for prec in ("fp64", "mixed"):
+        rgb, rc, inv, st = npx.render_host(sc, prec, with_inv=True)
+        assert np.isfinite(inv).all() and (inv >= 0).all()
+        assert inv[0] < 1e-3, (prec, inv)
+
+
+def test_invalid_scene_raises(cuda):
+    with pytest.raises(npx.NullPathError):
+        npx.render(benchmark_scene(width=16, height=16).replace(spin=1.5), "mixed")
+
+
+def test_full_frame_mixed_vs_fp64(cuda):
+    """1280x720x4 benchmark frame: size-independent agreement of the two paths."""
+    import torch
+    sc = benchmark_scene()
+    m_rgb, m_rc = _render_np(sc, "mixed")
+    f_rgb, f_rc = _render_np(sc, "fp64")
+    assert np.isfinite(m_rgb).all() and (m_rgb >= 0).all()
+    cls = ((m_rc > 0) == (f_rc > 0)).mean()
+    assert cls > 0.995, cls
+    both = (m_rc > 0) & (f_rc > 0)
+    err = np.abs(m_rc[both].astype(np.float64) - f_rc[both])
+    assert np.quantile(err, 0.99) < 1e-4, np.quantile(err, 0.99)
+    close = np.isclose(m_rgb, f_rgb, rtol=1e-3, atol=1e-6).all(axis=0).mean()
+    assert close > 0.99, close
