@@ -196,7 +196,7 @@ def run_ours(args):
         st = stats[-1]
         flop_step = oc["mixed_step_flops"] if args.precision == "mixed" else oc["fp64_step_flops"]
         kern_ms = statistics.mean(s.kernel_ms for s in stats)
-        steps_main = st.steps - (st.fp64_steps if args.precision == "mixed" and st.deferred_rays else 0)
+        steps_main = st.steps - (st.fp64_steps if args.precision == "mixed" else 0)
         achieved = flop_step * steps_main / (kern_ms * 1e-3) / 1e12
         peak = ctypes_peak(lib, 0 if args.precision == "mixed" else 1)
         out = {
@@ -212,7 +212,7 @@ def run_ours(args):
             "mean_steps_per_ray": st.steps / max(1, st.rays),
             "fp64_island_steps_frac": st.fp64_steps / max(1, st.steps),
             "deferred_rays": st.deferred_rays,
-            "kernel_ms": {"main": kern_ms, "deferred_fp64": statistics.mean(s.deferred_ms for s in stats)},
+            "kernel_ms": {"tracer": kern_ms, "ray_init": statistics.mean(s.init_ms for s in stats)},
             "roofline": {"bound": "fp32" if args.precision == "mixed" else "fp64", "achieved": achieved,
                          "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
                          "traffic": None,

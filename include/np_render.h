@@ -106,9 +106,9 @@ typedef struct np_render_stats {
     uint64_t steps;               /* accepted integration steps */
     uint64_t fp64_steps;          /* steps taken in FP64 by the mixed path */
     uint64_t rhs_evals;           /* right-hand-side evaluations */
-    uint64_t deferred_rays;       /* near-critical rays finished by the FP64 tracer (mixed path) */
-    double kernel_ms;             /* device time of the main tracer kernel */
-    double deferred_ms;           /* device time of the deferred FP64 kernel (mixed path) */
+    uint64_t deferred_rays;       /* near-critical rays traced whole in FP64 (mixed path) */
+    double kernel_ms;             /* device time of the tracer kernel */
+    double init_ms;               /* device time of the ray-generation kernel (mixed path) */
 } np_render_stats_t;
 
 /* ABI version compiled into the library. */
@@ -158,6 +158,17 @@ int np_trace_rays_device(const np_scene_t* scene, int precision, int n,
                          const double* d_px, const double* d_py,
                          double* d_consts, double* d_cross, int32_t* d_status,
                          void* stream);
+
+/* Launch tunables of the mixed path (process-wide; the autotuner sets them).
+ *   NP_TUNE_ISLAND_BATCH  parked lanes of a warp that trigger a batched FP64
+ *                         island step (1..32, default 8)
+ *   NP_TUNE_MIN_BLOCKS    register cap of the tracer as resident 128-thread
+ *                         blocks per SM (3, 4, 5, 6 or 8; default 4)
+ *   NP_TUNE_CHUNK         ray indices a warp takes per atomic (default 64) */
+#define NP_TUNE_ISLAND_BATCH 1
+#define NP_TUNE_MIN_BLOCKS 2
+#define NP_TUNE_CHUNK 3
+int np_tune(int param, int value);
 
 /* Measures the sustained FMA throughput of this GPU's SIMT pipes with a
  * register-resident FMA loop: which = 0 for FP32, 1 for FP64.  Writes

@@ -43,6 +43,10 @@ struct SceneDev {
     double T0, T1, P0, P1, R1, H1;
     double gtt, gtp, gpp, grr, ghh;
     double cos_cam, sin_cam;
+    // FP32 copies for the mixed tracer's per-step path
+    float r_cam_hi, r_cam_lo, th_cam_hi, th_cam_lo, ph_cam_hi, ph_cam_lo;
+    float r_plus_f, r_band_f, pi_lim_f, rin_f, rout_f, r_far_f, h_unit_f, inv_M_f;
+    int island_batch;
 };
 
 // ---------------------------------------------------------------------------
@@ -218,20 +222,21 @@ __device__ __forceinline__ void shade_sky(float v, float out[3]) {
     out[0] = clamp01f(c0); out[1] = clamp01f(c1); out[2] = clamp01f(c2);
 }
 
-// Final colour of one sample (render.cu:312-359).
+// Final colour of one sample (render.cu:312-359); cam_y is the camera-frame
+// direction's y component (sky gradient), min_r the closest approach.
 __device__ __forceinline__ void sample_colour(const SceneDev& s, bool captured, int orders,
-                                              const float disk[3], double min_r, const CamDir& d, float col[3]) {
+                                              const float disk[3], float min_r, float cam_y, float col[3]) {
     if (captured || !(orders > 0 && s.disk_on)) {
         if (s.bg_mode == NP_BG_POINT) {
             float rph = 1.5f * s.Rsf;
             float w = fmaxf(0.02f * s.Rsf, 0.005f * s.Rsf + 0.02f * s.bg_sigma_rad * s.Rsf);
-            float dr = (float)min_r - rph;
+            float dr = min_r - rph;
             float I = s.bg_peak * expf(-0.5f * (dr / w) * (dr / w)) + (captured ? 0.0f : 0.02f);
             col[0] = col[1] = col[2] = I;
         } else if (captured) {
             col[0] = col[1] = col[2] = 0.0f;
         } else {
-            shade_sky(d.cam_y * 0.5f + 0.5f, col);
+            shade_sky(cam_y * 0.5f + 0.5f, col);
         }
     } else {
         col[0] = disk[0]; col[1] = disk[1]; col[2] = disk[2];

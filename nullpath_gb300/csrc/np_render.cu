@@ -49,6 +49,14 @@ int fail(int code, const char* fmt, ...) {
 constexpr int kBlock = 128;
 constexpr int kChunk = 64;
 
+// Tunables (set through np_tune; the autotuner searches them).
+struct Tuning {
+    int island_batch = 8;   // parked lanes that trigger a batched FP64 island step
+    int min_blocks = 4;     // register cap of the mixed tracer (blocks of 128 per SM)
+    int chunk = 64;         // ray indices a warp takes from the global counter at once
+};
+Tuning g_tune;
+
 // Device-side counters of one call.
 struct Counters {
     unsigned long long work;        // next ray index (main pass)
@@ -125,6 +133,17 @@ int prepare_scene(const np_scene_t& sc, SceneDev& d) {
     d.bg_sigma_rad = (float)sc.bg_sigma_deg * kPiF / 180.0f;
     d.bg_peak = (float)sc.bg_brightness;
 
+    {
+        HiLo v = d_hl(d.r_cam); d.r_cam_hi = v.hi; d.r_cam_lo = v.lo;
+        v = d_hl(d.th_cam); d.th_cam_hi = v.hi; d.th_cam_lo = v.lo;
+        v = d_hl(d.ph_cam); d.ph_cam_hi = v.hi; d.ph_cam_lo = v.lo;
+        d.r_plus_f = (float)d.r_plus;
+        d.r_band_f = (float)(d.r_plus + kHorizonBand * d.M);
+        d.pi_lim_f = 3.14159250f;              // largest float below pi - 1e-9
+        d.rin_f = (float)d.rin; d.rout_f = (float)d.rout; d.r_far_f = (float)d.r_far;
+        d.h_unit_f = (float)d.h_unit; d.inv_M_f = (float)(1.0 / d.M);
+        d.island_batch = g_tune.island_batch;
+    }
     const double M = d.M, a = d.a, r = d.r_cam, th = d.th_cam;
     double gtt, gtp, gpp, grr, ghh;
     host_metric_cov(M, a, r, th, gtt, gtp, gpp, grr, ghh);
@@ -252,7 +271,7 @@ render_fp64_kernel(const SceneDev s, float* __restrict__ srgb, float* __restrict
                 if (s.check_inv && inv3 && !captured && !(R.orders > 0 && s.disk_on))
                     invariants_ref(s, R.y, R.pt0, R.pph0, inv3);
                 float col[3];
-                sample_colour(s, captured, R.orders, R.disk, R.min_r, dir, col);
+                sample_colour(s, captured, R.orders, R.disk, (float)R.min_r, dir.cam_y, col);
                 write_sample(s, srgb, rcross, p, sl, col, R.first_r);
                 have = false;
             }
@@ -261,65 +280,150 @@ render_fp64_kernel(const SceneDev s, float* __restrict__ srgb, float* __restrict
     flush_counters(ctr, n_rays, n_steps, list ? n_steps : 0, n_evals);
 }
 
-// Mixed-precision tracer.
-__global__ void __launch_bounds__(kBlock)
-render_mixed_kernel(const SceneDev s, float* __restrict__ srgb, float* __restrict__ rcross,
-                    float* __restrict__ inv3, Counters* __restrict__ ctr, long long* __restrict__ defer_list) {
+// Per-ray initial data of the mixed path, structure of arrays:
+//   a[i] = (p_r hi, p_r lo, p_theta hi, p_theta lo), b[i] = (E hi, E lo, L hi, L lo),
+//   cy[i] = camera-frame y of the ray direction (sky colour), flag[i] = 1 for
+//   near-critical rays (deferred to the FP64 warps, listed in `list`).
+struct InitSoA {
+    float4* a;
+    float4* b;
+    float* cy;
+    unsigned char* flag;
+    long long* list;
+};
+
+// Camera rays of one pass, fully parallel (one ray per thread).  All FP64
+// work of ray generation happens here, with every lane of a warp active.
+__global__ void __launch_bounds__(256)
+ray_init_kernel(const SceneDev s, InitSoA soa, Counters* __restrict__ ctr) {
+    const bool crit = (s.islands & kIslandCritical) != 0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < s.total;
+         i += (long long)gridDim.x * blockDim.x) {
+        long long p; int sl, x, y; uint32_t sid;
+        ray_coords(s, i, p, sl, x, y, sid);
+        CamDir dir = camera_dir(s, x, y, sid, false, 0.0, 0.0);
+        Momentum m = camera_momentum(s, dir);
+        double E = -m.pt, L = m.pph;
+        bool defer = false;
+        if (crit) {
+            double Q = m.pth * m.pth + s.cos_cam * s.cos_cam * (L * L / (s.sin_cam * s.sin_cam) - s.a * s.a * E * E);
+            defer = near_critical(E, L, Q, s.a, s.M, s.r_plus, kCriticalDb);
+        }
+        HiLo pr = d_hl(m.pr), pth = d_hl(m.pth), Eh = d_hl(E), Lh = d_hl(L);
+        soa.a[i] = make_float4(pr.hi, pr.lo, pth.hi, pth.lo);
+        soa.b[i] = make_float4(Eh.hi, Eh.lo, Lh.hi, Lh.lo);
+        soa.cy[i] = dir.cam_y;
+        soa.flag[i] = defer ? 1 : 0;
+        if (defer) soa.list[atomicAdd(&ctr->deferred, 1ull)] = i;
+    }
+}
+
+__device__ __forceinline__ void load_ray(const InitSoA& soa, long long i, MRay<false>& R, float& cam_y) {
+    float4 a = soa.a[i], b = soa.b[i];
+    R.pr = HiLo{a.x, a.y}; R.pth = HiLo{a.z, a.w};
+    R.E = HiLo{b.x, b.y}; R.L = HiLo{b.z, b.w};
+    cam_y = soa.cy[i];
+}
+
+// Mixed-precision tracer.  Warp 0 of the first `nd` blocks first traces the
+// near-critical rays of `list` in FP64 (one block per SM, so their latency
+// overlaps the FP32 work of the rest of the grid); every warp then traces
+// FP32 rays from the shared counter, lanes refilling independently and
+// parked island steps executed in batches.
+template <int MINB>
+__global__ void __launch_bounds__(kBlock, MINB)
+render_mixed_kernel(const SceneDev s, const InitSoA soa, float* __restrict__ srgb, float* __restrict__ rcross,
+                    float* __restrict__ inv3, Counters* __restrict__ ctr, int chunk) {
     const unsigned FULL = 0xffffffffu;
+    const SpaceK k{(float)s.a, (float)(s.a * s.a), (float)s.M, (float)s.r_plus, (float)s.r_minus};
+    unsigned long long n_rays = 0, n_steps = 0, n_f64 = 0, n_evals = 0;
+
+    // ---- FP64 warps: near-critical rays
+    const long long D = (long long)ctr->deferred;
+    const int nd = D > 0 ? (int)min((long long)gridDim.x, (D + 3) / 4) : 0;
+    if ((threadIdx.x >> 5) == 0 && (int)blockIdx.x < nd) {
+        WarpQueue q{0, 0};
+        bool drained = false, have = false;
+        DRay<false> R;
+        long long item = 0, p = 0;
+        int sl = 0;
+        float cam_y = 0.0f;
+        while (true) {
+            unsigned need = __ballot_sync(FULL, !have);
+            if (need && !drained) {
+                long long idx = warp_take(q, need, &ctr->work2, D, 4);
+                drained = q.base >= D;
+                if (!have && idx >= 0) {
+                    item = soa.list[idx];
+                    int x, y; uint32_t sid;
+                    ray_coords(s, item, p, sl, x, y, sid);
+                    float4 a = soa.a[item], b = soa.b[item];
+                    cam_y = soa.cy[item];
+                    dray_start(R, s, (double)b.x + (double)b.y, (double)b.z + (double)b.w,
+                               (double)a.x + (double)a.y, (double)a.z + (double)a.w);
+                    have = true;
+                    n_rays++;
+                }
+            }
+            if (!__any_sync(FULL, have)) break;
+            if (have) {
+                bool done = dray_step(R, s);
+                n_steps++; n_f64++; n_evals += 4;
+                if (done) {
+                    float col[3];
+                    sample_colour(s, R.status == 1, R.orders, R.disk, (float)R.min_r, cam_y, col);
+                    write_sample(s, srgb, rcross, p, sl, col, R.first_r);
+                    have = false;
+                }
+            }
+        }
+    }
+
+    // ---- FP32 rays
     WarpQueue q{0, 0};
-    bool drained = false;
-    RayMixed<false> R;
-    CamDir dir;
+    bool drained = false, have = false;
+    MRay<false> R;
     long long p = 0;
     int sl = 0;
-    bool have = false;
-    unsigned long long n_rays = 0, n_steps = 0, n_f64 = 0, n_evals = 0;
-    const bool crit = (s.islands & kIslandCritical) != 0;
+    float cam_y = 0.0f;
+    const int T = s.island_batch;
     while (true) {
         unsigned need = __ballot_sync(FULL, !have);
         if (need && !drained) {
-            long long idx = warp_take(q, need, &ctr->work, s.total, kChunk);
+            long long idx = warp_take(q, need, &ctr->work, s.total, chunk);
             drained = q.base >= s.total;
-            if (!have && idx >= 0) {
+            if (!have && idx >= 0 && !soa.flag[idx]) {
                 int x, y; uint32_t sid;
                 ray_coords(s, idx, p, sl, x, y, sid);
-                dir = camera_dir(s, x, y, sid, false, 0.0, 0.0);
-                Momentum m = camera_momentum(s, dir);
-                bool defer = false;
-                if (crit) {
-                    double E = -m.pt, L = m.pph;
-                    double Q = m.pth * m.pth + s.cos_cam * s.cos_cam *
-                               (L * L / (s.sin_cam * s.sin_cam) - s.a * s.a * E * E);
-                    defer = near_critical(E, L, Q, s.a, s.M, s.r_plus, kCriticalDb);
-                }
-                if (defer) {
-                    unsigned long long slot = atomicAdd(&ctr->deferred, 1ull);
-                    defer_list[slot] = idx;
-                } else {
-                    mixed_init(s, m, R);
-                    have = true;
-                    n_rays++;
-                    n_evals++;
-                }
+                load_ray(soa, idx, R, cam_y);
+                mray_start(R, s, k);
+                have = true;
+                n_rays++;
+                n_evals++;
             }
         }
-        if (!__any_sync(FULL, have)) {
+        unsigned act = __ballot_sync(FULL, have && !R.pending);
+        unsigned pend = __ballot_sync(FULL, have && R.pending);
+        if (!(act | pend)) {
             if (drained) break;
             continue;
         }
-        if (have) {
-            bool done = mixed_advance(s, R, n_evals);
-            n_steps++;
-            if (done) {
-                bool captured = R.status == 1;
-                if (s.check_inv && inv3 && !captured && !(R.orders > 0 && s.disk_on))
-                    mixed_invariants(s, R, hl_d(R.r), hl_d(R.th), inv3);
-                float col[3];
-                sample_colour(s, captured, R.orders, R.disk, R.min_r, dir, col);
-                write_sample(s, srgb, rcross, p, sl, col, R.first_r);
-                n_f64 += R.fp64_steps;
-                have = false;
+        bool done = false;
+        if (pend && ((int)__popc(pend) >= T || !act)) {
+            if (have && R.pending) {
+                done = mray_island(R, s, k);
+                n_steps++; n_f64++; n_evals += 5;
             }
+        } else if (have && !R.pending) {
+            int r = mray_step32(R, s, k);
+            if (r != STEP_PARK) { n_steps++; n_evals += 4; }
+            done = r == STEP_DONE;
+        }
+        if (done) {
+            float col[3];
+            sample_colour(s, R.status == 1, R.orders, R.disk, R.min_r, cam_y, col);
+            write_sample(s, srgb, rcross, p, sl, col, R.first_r);
+            have = false;
         }
     }
     flush_counters(ctr, n_rays, n_steps, n_f64, n_evals);
@@ -337,7 +441,9 @@ __global__ void resolve_kernel(const float* __restrict__ srgb, float* __restrict
     }
 }
 
-// Explicit rays (positions in continuous pixel coordinates).
+// Explicit rays (positions in continuous pixel coordinates), one per thread.
+// The mixed path takes its island steps immediately (no batching) and
+// traces near-critical rays with the FP64 Carter tracer, as the renderer does.
 __global__ void trace_rays_kernel(const SceneDev s, int precision, int n, const double* __restrict__ px,
                                   const double* __restrict__ py, double* __restrict__ consts,
                                   double* __restrict__ cross, int32_t* __restrict__ status) {
@@ -352,24 +458,34 @@ __global__ void trace_rays_kernel(const SceneDev s, int precision, int n, const 
         consts[4 * i + 3] = m.pr >= 0.0 ? 1.0 : -1.0;
     }
     unsigned long long ev = 0;
-    double xr[4], xphi[4];
+    double xr[4] = {0, 0, 0, 0}, xphi[4] = {0, 0, 0, 0};
     int ncross, st;
-    bool use64 = precision == NP_PREC_FP64 ||
-                 ((s.islands & kIslandCritical) && near_critical(E, L, Q, s.a, s.M, s.r_plus, kCriticalDb));
-    if (use64) {
+    if (precision == NP_PREC_FP64) {
         RayFP64<true> R;
         fp64_init(s, m, R);
         while (!fp64_advance(s, R, nullptr, ev)) {}
-        for (int k = 0; k < 4; ++k) { xr[k] = R.xr[k]; xphi[k] = R.xphi[k]; }
+        for (int j = 0; j < 4; ++j) { xr[j] = R.xr[j]; xphi[j] = R.xphi[j]; }
+        ncross = R.crossings; st = R.status;
+    } else if ((s.islands & kIslandCritical) && near_critical(E, L, Q, s.a, s.M, s.r_plus, kCriticalDb)) {
+        DRay<true> R;
+        dray_start(R, s, E, L, m.pr, m.pth);
+        while (!dray_step(R, s)) {}
+        for (int j = 0; j < 4; ++j) { xr[j] = R.xr[j]; xphi[j] = R.xphi[j]; }
         ncross = R.crossings; st = R.status;
     } else {
-        RayMixed<true> R;
-        mixed_init(s, m, R);
-        while (!mixed_advance(s, R, ev)) {}
-        for (int k = 0; k < 4; ++k) { xr[k] = R.xr[k]; xphi[k] = R.xphi[k]; }
+        const SpaceK k{(float)s.a, (float)(s.a * s.a), (float)s.M, (float)s.r_plus, (float)s.r_minus};
+        MRay<true> R;
+        R.pr = d_hl(m.pr); R.pth = d_hl(m.pth); R.E = d_hl(E); R.L = d_hl(L);
+        mray_start(R, s, k);
+        while (true) {
+            int r = mray_step32(R, s, k);
+            if (r == STEP_PARK) r = mray_island(R, s, k) ? STEP_DONE : STEP_CONT;
+            if (r == STEP_DONE) break;
+        }
+        for (int j = 0; j < 4; ++j) { xr[j] = R.xr_d[j]; xphi[j] = R.xphi[j]; }
         ncross = R.crossings; st = R.status;
     }
-    if (cross) for (int k = 0; k < 4; ++k) { cross[8 * i + 2 * k] = xr[k]; cross[8 * i + 2 * k + 1] = xphi[k]; }
+    if (cross) for (int j = 0; j < 4; ++j) { cross[8 * i + 2 * j] = xr[j]; cross[8 * i + 2 * j + 1] = xphi[j]; }
     if (status) status[i] = st + 16 * min(ncross, 15);
 }
 
@@ -395,6 +511,8 @@ struct Scratch {
     cudaStream_t stream = nullptr;
     float* srgb = nullptr; size_t srgb_n = 0;
     long long* list = nullptr; size_t list_n = 0;
+    float4* soa_a = nullptr; float4* soa_b = nullptr; float* soa_cy = nullptr; unsigned char* soa_flag = nullptr;
+    size_t soa_n = 0;
     Counters* ctr = nullptr;
     Counters* h_ctr = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr;
@@ -429,6 +547,18 @@ int get_scratch(cudaStream_t stream, size_t srgb_n, size_t list_n, Scratch** out
         NP_CU(cudaMalloc(&sc->list, list_n * sizeof(long long)), NP_ERR_ALLOC);
         sc->list_n = list_n;
     }
+    if (sc->soa_n < list_n && list_n > 1) {
+        if (sc->soa_a) {
+            cudaStreamSynchronize(stream);
+            cudaFree(sc->soa_a); cudaFree(sc->soa_b); cudaFree(sc->soa_cy); cudaFree(sc->soa_flag);
+            sc->soa_a = nullptr; sc->soa_b = nullptr; sc->soa_cy = nullptr; sc->soa_flag = nullptr; sc->soa_n = 0;
+        }
+        NP_CU(cudaMalloc(&sc->soa_a, list_n * sizeof(float4)), NP_ERR_ALLOC);
+        NP_CU(cudaMalloc(&sc->soa_b, list_n * sizeof(float4)), NP_ERR_ALLOC);
+        NP_CU(cudaMalloc(&sc->soa_cy, list_n * sizeof(float)), NP_ERR_ALLOC);
+        NP_CU(cudaMalloc(&sc->soa_flag, list_n), NP_ERR_ALLOC);
+        sc->soa_n = list_n;
+    }
     *out = sc;
     return NP_OK;
 }
@@ -440,6 +570,26 @@ int grid_for(const void* kernel) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kBlock, 0);
     if (per_sm < 1) per_sm = 1;
     return sms * per_sm;
+}
+
+template <int MINB>
+void launch_mixed_t(const SceneDev& s, const InitSoA& soa, float* srgb, float* rc, float* inv3, Counters* ctr,
+                    int chunk, cudaStream_t st) {
+    render_mixed_kernel<MINB><<<grid_for((const void*)render_mixed_kernel<MINB>), kBlock, 0, st>>>(
+        s, soa, srgb, rc, inv3, ctr, chunk);
+}
+
+// Register-cap variants of the mixed tracer (blocks of 128 threads per SM
+// the compiler must fit: 3 -> 170 registers, 4 -> 128, 5 -> 102, 6 -> 85, 8 -> 64).
+void launch_mixed(int minb, const SceneDev& s, const InitSoA& soa, float* srgb, float* rc, float* inv3,
+                  Counters* ctr, int chunk, cudaStream_t st) {
+    switch (minb) {
+        case 3: launch_mixed_t<3>(s, soa, srgb, rc, inv3, ctr, chunk, st); break;
+        case 5: launch_mixed_t<5>(s, soa, srgb, rc, inv3, ctr, chunk, st); break;
+        case 6: launch_mixed_t<6>(s, soa, srgb, rc, inv3, ctr, chunk, st); break;
+        case 8: launch_mixed_t<8>(s, soa, srgb, rc, inv3, ctr, chunk, st); break;
+        default: launch_mixed_t<4>(s, soa, srgb, rc, inv3, ctr, chunk, st); break;
+    }
 }
 
 }  // namespace
@@ -530,12 +680,12 @@ int np_render_device(const np_scene_t* scene, int precision, float* d_rgb, float
         NP_CU(cudaGetLastError(), NP_ERR_KERNEL);
         if (stats) NP_CU(cudaEventRecord(sc->ev1, st), NP_ERR_KERNEL);
     } else {
-        render_mixed_kernel<<<grid_for((const void*)render_mixed_kernel), kBlock, 0, st>>>(
-            s, sc->srgb, d_rcross, d_inv3, sc->ctr, sc->list);
+        InitSoA soa{sc->soa_a, sc->soa_b, sc->soa_cy, sc->soa_flag, sc->list};
+        int ib = (int)std::min<long long>((s.total + 255) / 256, 152ll * 8);
+        ray_init_kernel<<<ib, 256, 0, st>>>(s, soa, sc->ctr);
         NP_CU(cudaGetLastError(), NP_ERR_KERNEL);
         if (stats) NP_CU(cudaEventRecord(sc->ev1, st), NP_ERR_KERNEL);
-        render_fp64_kernel<<<grid_for((const void*)render_fp64_kernel), kBlock, 0, st>>>(
-            s, sc->srgb, d_rcross, d_inv3, sc->ctr, sc->list);
+        launch_mixed(g_tune.min_blocks, s, soa, sc->srgb, d_rcross, d_inv3, sc->ctr, g_tune.chunk, st);
         NP_CU(cudaGetLastError(), NP_ERR_KERNEL);
     }
     if (stats) NP_CU(cudaEventRecord(sc->ev2, st), NP_ERR_KERNEL);
@@ -549,15 +699,19 @@ int np_render_device(const np_scene_t* scene, int precision, float* d_rgb, float
         NP_CU(cudaMemcpyAsync(sc->h_ctr, sc->ctr, sizeof(Counters), cudaMemcpyDeviceToHost, st), NP_ERR_KERNEL);
         NP_CU(cudaStreamSynchronize(st), NP_ERR_KERNEL);
         float ms = 0.0f, ms2 = 0.0f;
-        cudaEventElapsedTime(&ms, sc->ev0, sc->ev1);
-        cudaEventElapsedTime(&ms2, sc->ev1, sc->ev2);
+        if (precision == NP_PREC_FP64) {
+            cudaEventElapsedTime(&ms, sc->ev0, sc->ev1);
+        } else {   // ev0 -> ev1: ray init, ev1 -> ev2: tracer
+            cudaEventElapsedTime(&ms2, sc->ev0, sc->ev1);
+            cudaEventElapsedTime(&ms, sc->ev1, sc->ev2);
+        }
         stats->rays = sc->h_ctr->rays;
         stats->steps = sc->h_ctr->steps;
         stats->fp64_steps = sc->h_ctr->fp64_steps;
         stats->rhs_evals = sc->h_ctr->evals;
         stats->deferred_rays = precision == NP_PREC_MIXED ? sc->h_ctr->deferred : 0;
         stats->kernel_ms = ms;
-        stats->deferred_ms = ms2;
+        stats->init_ms = ms2;
     }
     return NP_OK;
 }
@@ -608,6 +762,26 @@ int np_trace_rays_device(const np_scene_t* scene, int precision, int n, const do
     trace_rays_kernel<<<(n + 127) / 128, 128, 0, st>>>(s, precision, n, d_px, d_py, d_consts, d_cross, d_status);
     NP_CU(cudaGetLastError(), NP_ERR_KERNEL);
     return NP_OK;
+}
+
+int np_tune(int param, int value) {
+    switch (param) {
+        case NP_TUNE_ISLAND_BATCH:
+            if (value < 1 || value > 32) return fail(NP_ERR_INVALID, "island batch must be in [1, 32]");
+            g_tune.island_batch = value;
+            return NP_OK;
+        case NP_TUNE_MIN_BLOCKS:
+            if (value != 3 && value != 4 && value != 5 && value != 6 && value != 8)
+                return fail(NP_ERR_INVALID, "min blocks must be one of 3, 4, 5, 6, 8");
+            g_tune.min_blocks = value;
+            return NP_OK;
+        case NP_TUNE_CHUNK:
+            if (value < 1 || value > 4096) return fail(NP_ERR_INVALID, "chunk must be in [1, 4096]");
+            g_tune.chunk = value;
+            return NP_OK;
+        default:
+            return fail(NP_ERR_INVALID, "unknown tuning parameter %d", param);
+    }
 }
 
 int np_measure_fma_peak(int which, double* tflops) {

@@ -7,46 +7,83 @@
 //               - 2 a E L + a^2 E^2 sin^2(theta),      P(r) = (r^2 + a^2) E - a L,
 //
 // whose analytic r- and theta-derivatives need three reciprocals and one
-// sincos per evaluation instead of the fifteen divisions of the contravariant
-// block form (bh_kerr.h:600-727).  p_t = -E and p_phi = L are conserved, so
-// only (r, theta, p_r, p_theta) are integrated (plus phi when requested).
+// sincos per evaluation instead of the divisions of the contravariant block
+// form (bh_kerr.h:600-727).  p_t = -E and p_phi = L are conserved, so only
+// (r, theta, p_r, p_theta) are integrated (plus phi for the per-ray report).
 //
-// Precision: right-hand sides in FP32; the state is kept as an unevaluated
+// Precision.  Right-hand sides are FP32; the state is an unevaluated
 // (hi, lo) FP32 pair and every RK4 increment is added with an error-free
-// two-sum, so rounding does not accumulate over thousands of steps.  Steps
-// within 0.1 M of the outer horizon and steps across a radial or polar
-// turning point are taken in FP64; rays whose impact parameter lies within
-// 1e-3 M of the critical curve are handed to the FP64 tracer whole.
+// two-sum, so rounding does not accumulate over thousands of steps.  FP64 is
+// used only where the scene's island mask asks for it:
+//   horizon   steps that start within 0.1 M of r_+;
+//   turning   steps across a sign change of p_r or p_theta (redone in FP64);
+//   critical  rays with |b - b_crit| < 1e-3 M (traced whole in FP64 by
+//             dedicated warps).
+// GB300 issues FP64 at 1/64 of the FP32 rate and a warp pays for an FP64
+// instruction whatever its active-lane count, so the per-step path holds no
+// FP64 instruction at all and island steps of different lanes are batched:
+// a lane that needs one parks until enough lanes of its warp are parked (or
+// none is left stepping) and the warp then takes all their FP64 steps at once.
 #pragma once
 
 #include "np_common.cuh"
-#include "tracer_fp64.cuh"
 
 namespace np {
 
-struct RayConst {
-    float E, L, a, a2, aL, a2E2, L2, twoaEL, M, rp, rm;
+__device__ __forceinline__ float rcp_approx(float x) {
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+struct HiLo { float hi, lo; };
+__host__ __device__ __forceinline__ double hl_d(const HiLo& v) { return (double)v.hi + (double)v.lo; }
+__host__ __device__ __forceinline__ HiLo d_hl(double x) { float h = (float)x; return HiLo{h, (float)(x - (double)h)}; }
+
+// Error-free a + b = s + e (Knuth two-sum), then renormalised into v.
+__device__ __forceinline__ void hl_add(HiLo& v, float d) {
+    float s = __fadd_rn(v.hi, d);
+    float bb = __fsub_rn(s, v.hi);
+    float e = __fadd_rn(__fsub_rn(v.hi, __fsub_rn(s, bb)), __fsub_rn(d, bb));
+    e = __fadd_rn(e, v.lo);
+    v.hi = __fadd_rn(s, e);
+    v.lo = __fsub_rn(e, __fsub_rn(v.hi, s));
+}
+
+// theta - pi/2 of a (hi, lo) angle, exact while |theta - pi/2| < pi/2.
+__device__ __forceinline__ float dtheta_eq(const HiLo& th) {
+    const float PI2_HI = 1.57079637050628662109375f;   // fl(pi/2)
+    const float PI2_LO = -4.37113900018624283e-8f;      // pi/2 - fl(pi/2)
+    return __fadd_rn(__fsub_rn(th.hi, PI2_HI), __fsub_rn(th.lo, PI2_LO));
+}
+
+// Constants of one ray (FP32) and of the spacetime.
+struct RayK {
+    float E, L, aL, a2E2, L2, twoaEL;
+};
+struct SpaceK {
+    float a, a2, M, rp, rm;
 };
 
 struct F5 { float r, th, pr, pth, ph; };
 
 // Carter-form Hamilton equations in FP32.
 template <bool PHI>
-__device__ __forceinline__ F5 rhs_carter_f(float r, float th, float pr, float pth, const RayConst& c) {
+__device__ __forceinline__ F5 rhs_f(float r, float th, float pr, float pth, const RayK& c, const SpaceK& k) {
     float sn, cs;
     sincosf(th, &sn, &cs);
     float s2 = fmaxf(sn * sn, 1e-30f);
-    float is2 = __frcp_rn(s2);
+    float is2 = rcp_approx(s2);
     float r2 = r * r;
-    float Sig = fmaf(c.a2, cs * cs, r2);
-    float iS = __frcp_rn(Sig);
-    float Del = (r - c.rp) * (r - c.rm);
-    float iD = __frcp_rn(Del);
-    float P = fmaf(r2 + c.a2, c.E, -c.aL);
+    float Sig = fmaf(k.a2, cs * cs, r2);
+    float iS = rcp_approx(Sig);
+    float Del = (r - k.rp) * (r - k.rm);
+    float iD = rcp_approx(Del);
+    float P = fmaf(r2 + k.a2, c.E, -c.aL);
     float PiD = P * iD;
     float W = fmaf(c.L2, is2, fmaf(c.a2E2, s2, -c.twoaEL));
     float F = fmaf(Del * pr, pr, fmaf(pth, pth, fmaf(-P, PiD, W)));
-    float Del_r = 2.0f * (r - c.M);
+    float Del_r = 2.0f * (r - k.M);
     float F_r = fmaf(Del_r, fmaf(pr, pr, PiD * PiD), -4.0f * r * c.E * PiD);
     float sc2 = 2.0f * sn * cs;
     float F_t = sc2 * fmaf(-c.L2 * is2, is2, c.a2E2);
@@ -54,17 +91,16 @@ __device__ __forceinline__ F5 rhs_carter_f(float r, float th, float pr, float pt
     d.r = Del * pr * iS;
     d.th = pth * iS;
     d.pr = -0.5f * iS * fmaf(-2.0f * r * iS, F, F_r);
-    d.pth = -0.5f * iS * fmaf(c.a2 * sc2 * iS, F, F_t);
-    d.ph = PHI ? iS * fmaf(c.a, PiD, fmaf(c.L, is2, -c.a * c.E)) : 0.0f;
+    d.pth = -0.5f * iS * fmaf(k.a2 * sc2 * iS, F, F_t);
+    d.ph = PHI ? iS * fmaf(k.a, PiD, fmaf(c.L, is2, -k.a * c.E)) : 0.0f;
     return d;
 }
 
 struct D5 { double r, th, pr, pth, ph; };
 
-// The same equations in FP64 (island steps); zero inside r_+ + 1e-12 as the
-// reference does (bh_kerr.h:684-690).
-__device__ __forceinline__ D5 rhs_carter_d(const D5& y, double E, double L, double a, double M,
-                                           double rp, double rm) {
+// The same equations in FP64 (island steps and near-critical rays); zero
+// inside r_+ + 1e-12 as the reference does (bh_kerr.h:684-690).
+__device__ __forceinline__ D5 rhs_d(const D5& y, double E, double L, double a, double M, double rp, double rm) {
     D5 d{0, 0, 0, 0, 0};
     if (y.r <= rp + 1e-12) return d;
     double sn, cs;
@@ -92,184 +128,305 @@ __device__ __forceinline__ D5 add5(const D5& y, double h, const D5& k) {
     return D5{y.r + h * k.r, y.th + h * k.th, y.pr + h * k.pr, y.pth + h * k.pth, y.ph + h * k.ph};
 }
 
-// Error-free transformation a + b = s + e (Knuth two-sum).
-__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
-    s = __fadd_rn(a, b);
-    float bb = __fsub_rn(s, a);
-    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+// One FP64 RK4 step of the Carter system.
+__device__ __forceinline__ D5 rk4_d(const D5& y, double h, double E, double L, double a, double M,
+                                    double rp, double rm, bool phi) {
+    D5 k1 = rhs_d(y, E, L, a, M, rp, rm);
+    D5 k2 = rhs_d(add5(y, 0.5 * h, k1), E, L, a, M, rp, rm);
+    D5 k3 = rhs_d(add5(y, 0.5 * h, k2), E, L, a, M, rp, rm);
+    D5 k4 = rhs_d(add5(y, h, k3), E, L, a, M, rp, rm);
+    double h6 = h * (1.0 / 6.0);
+    D5 o;
+    o.r = y.r + h6 * (k1.r + 2.0 * (k2.r + k3.r) + k4.r);
+    o.th = y.th + h6 * (k1.th + 2.0 * (k2.th + k3.th) + k4.th);
+    o.pr = y.pr + h6 * (k1.pr + 2.0 * (k2.pr + k3.pr) + k4.pr);
+    o.pth = y.pth + h6 * (k1.pth + 2.0 * (k2.pth + k3.pth) + k4.pth);
+    o.ph = phi ? y.ph + h6 * (k1.ph + 2.0 * (k2.ph + k3.ph) + k4.ph) : y.ph;
+    return o;
 }
 
-struct HiLo { float hi, lo; };
-__device__ __forceinline__ double hl_d(const HiLo& v) { return (double)v.hi + (double)v.lo; }
-__device__ __forceinline__ HiLo d_hl(double x) { float h = (float)x; return HiLo{h, (float)(x - (double)h)}; }
-__device__ __forceinline__ void hl_add(HiLo& v, float d) {
-    float s, e;
-    two_sum(v.hi, d, s, e);
-    e = __fadd_rn(e, v.lo);
-    v.hi = __fadd_rn(s, e);                  // renormalise (fast two-sum)
-    v.lo = __fsub_rn(e, __fsub_rn(v.hi, s));
+// Redshift g = E / (u^t (E - Omega L)) of a prograde Keplerian emitter on
+// the equator (the physics of bh_kerr.h:833-862, with k.u expanded), FP32.
+__device__ __forceinline__ float doppler_g_f(float r, float E, float L, float M, float a) {
+    float Ms = fmaxf(1e-12f, M);
+    float x = fmaxf(1.0f, r / Ms);
+    float Om = 1.0f / ((a / Ms + x * sqrtf(x)) * Ms);
+    float ir = 1.0f / r;
+    float gtt = -(1.0f - 2.0f * M * ir);
+    float gtp = -2.0f * M * a * ir;
+    float gpp = r * r + a * a + 2.0f * M * a * a * ir;
+    float den = -(gtt + Om * (2.0f * gtp + gpp * Om));
+    float ut = rsqrtf(fmaxf(den, 1e-24f));
+    float ku = ut * (E - Om * L);
+    float g = E / fmaxf(ku, 1e-18f);
+    return fmaxf(g, 0.0f);
 }
 
-// theta - pi/2 of a (hi, lo) angle, exact for |theta - pi/2| < pi/2.
-__device__ __forceinline__ float dtheta_eq(const HiLo& th) {
-    const float PI2_HI = 1.57079637050628662109375f;          // (float)(pi/2)
-    const float PI2_LO = -4.37113900018624283e-8f;             // pi/2 - PI2_HI
-    return __fadd_rn(__fsub_rn(th.hi, PI2_HI), __fsub_rn(th.lo, PI2_LO));
+// Root in [0, 1] of the cubic Hermite interpolant of d = theta - pi/2 over
+// one step (d0, d1 of opposite sign; slopes m0, m1 = h dtheta/dlambda),
+// safeguarded Newton from the linear estimate.
+__device__ __forceinline__ float hermite_root_f(float d0, float d1, float m0, float m1, float s_lin) {
+    float s = s_lin, lo = 0.0f, hi = 1.0f;
+#pragma unroll 1
+    for (int it = 0; it < 6; ++it) {
+        float s2 = s * s, s3 = s2 * s;
+        float h00 = 2.0f * s3 - 3.0f * s2 + 1.0f, h10 = s3 - 2.0f * s2 + s;
+        float h01 = 1.0f - h00, h11 = s3 - s2;
+        float p = h00 * d0 + h10 * m0 + h01 * d1 + h11 * m1;
+        float dh00 = 6.0f * (s2 - s);
+        float dp = dh00 * (d0 - d1) + (3.0f * s2 - 4.0f * s + 1.0f) * m0 + (3.0f * s2 - 2.0f * s) * m1;
+        if ((p > 0.0f) == (d0 > 0.0f)) lo = s; else hi = s;
+        float sn = (dp != 0.0f) ? s - p / dp : 0.5f * (lo + hi);
+        if (!(sn > lo && sn < hi)) sn = 0.5f * (lo + hi);
+        bool done = fabsf(sn - s) < 1e-7f;
+        s = sn;
+        if (done) break;
+    }
+    return s;
 }
 
-// Closeness of a ray to the critical curve: R(r) = P(r)^2 - Delta K has a
-// double root at the spherical photon orbit r_c exactly for critical rays.
-// r_c solves R'(r) = 0, i.e. the depressed cubic
+// Per-lane ray of the mixed tracer.
+template <bool PHI>
+struct MRay {
+    HiLo r, th, pr, pth, ph;
+    float k[5];                  // f(y) at the current state (first stage of the next step)
+    HiLo E, L;                   // conserved momenta (p_t = -E, p_phi = L)
+    RayK c;
+    float min_r, first_r, h_pend;
+    float disk[3];
+    int step, orders, crossings, status;
+    bool pending;                // parked for an FP64 island step of size h_pend
+    unsigned fp64_steps;
+    float xr[PHI ? 4 : 1], xphi[PHI ? 4 : 1];
+    double xr_d[PHI ? 4 : 1];
+};
+
+template <bool PHI>
+__device__ __forceinline__ void mray_consts(MRay<PHI>& R, float a) {
+    const float E = R.E.hi, L = R.L.hi;
+    R.c.E = E; R.c.L = L;
+    R.c.aL = a * L;
+    float aE = a * E;
+    R.c.a2E2 = aE * aE;
+    R.c.L2 = L * L;
+    R.c.twoaEL = 2.0f * aE * L;
+}
+
+template <bool PHI>
+__device__ __forceinline__ void mray_set_k(MRay<PHI>& R, const SpaceK& k) {
+    F5 f = rhs_f<PHI>(R.r.hi, R.th.hi, R.pr.hi, R.pth.hi, R.c, k);
+    R.k[0] = f.r; R.k[1] = f.th; R.k[2] = f.pr; R.k[3] = f.pth; R.k[4] = f.ph;
+}
+
+template <bool PHI>
+__device__ __forceinline__ void mray_start(MRay<PHI>& R, const SceneDev& s, const SpaceK& k) {
+    R.r = HiLo{s.r_cam_hi, s.r_cam_lo};
+    R.th = HiLo{s.th_cam_hi, s.th_cam_lo};
+    R.ph = HiLo{s.ph_cam_hi, s.ph_cam_lo};
+    R.min_r = s.r_cam_hi; R.first_r = 0.0f; R.h_pend = 0.0f;
+    R.disk[0] = R.disk[1] = R.disk[2] = 0.0f;
+    R.step = 0; R.orders = 0; R.crossings = 0; R.status = 2;
+    R.pending = false; R.fp64_steps = 0;
+    if (PHI) for (int i = 0; i < 4; ++i) { R.xr[i] = 0.0f; R.xphi[i] = 0.0f; R.xr_d[i] = 0.0; }
+    mray_consts(R, k.a);
+    mray_set_k(R, k);
+}
+
+// Common tail of a step (FP32 or island): termination, next k1, crossing,
+// escape.  (r0, th0, k0r, k0t, ph0, k0p) describe the start of the step.
+template <bool PHI>
+__device__ __forceinline__ bool mray_finish_step(MRay<PHI>& R, const SceneDev& s, const SpaceK& k, float h,
+                                                 const HiLo& r0, const HiLo& th0, float k0r, float k0t,
+                                                 const HiLo& ph0, float k0p) {
+    R.step++;
+    bool ok = R.r.hi > s.r_plus_f + 1e-6f * s.r_plus_f && R.th.hi > 1e-7f && R.th.hi < s.pi_lim_f;
+    if (!ok) { R.status = 1; return true; }
+    mray_set_k(R, k);
+    R.min_r = fminf(R.min_r, R.r.hi);
+    float dp = dtheta_eq(th0), dc = dtheta_eq(R.th);
+    bool sc = (dp > 0.0f && dc < 0.0f) || (dp < 0.0f && dc > 0.0f);
+    bool nz = (fabsf(dp) < 1e-8f && fabsf(dc) >= 1e-8f) || (fabsf(dc) < 1e-8f && fabsf(dp) >= 1e-8f);
+    if (sc || nz) {
+        float alpha = fabsf(dp) / (fabsf(dp) + fabsf(dc) + 1e-30f);
+        float u = alpha;
+        if (s.crossing == NP_CROSS_HERMITE && sc) u = hermite_root_f(dp, dc, h * k0t, h * R.k[1], alpha);
+        // r(u) = r0 + h01 (r1 - r0) + h10 m0 + h11 m1, with r1 - r0 formed from the pairs
+        float dr = (R.r.hi - r0.hi) + (R.r.lo - r0.lo);
+        float corr;
+        if (s.crossing == NP_CROSS_HERMITE && sc) {
+            float u2 = u * u, u3 = u2 * u;
+            corr = (3.0f * u2 - 2.0f * u3) * dr + (u3 - 2.0f * u2 + u) * (h * k0r) + (u3 - u2) * (h * R.k[0]);
+        } else {
+            corr = u * dr;
+        }
+        float rc_lo = r0.lo + corr;
+        float rc = r0.hi + rc_lo;
+        if (PHI && R.crossings < 4) {
+            float dph = (R.ph.hi - ph0.hi) + (R.ph.lo - ph0.lo);
+            float cph;
+            if (s.crossing == NP_CROSS_HERMITE && sc) {
+                float u2 = u * u, u3 = u2 * u;
+                cph = (3.0f * u2 - 2.0f * u3) * dph + (u3 - 2.0f * u2 + u) * (h * k0p) + (u3 - u2) * (h * R.k[4]);
+            } else {
+                cph = u * dph;
+            }
+            R.xr[R.crossings] = rc;
+            R.xr_d[R.crossings] = (double)r0.hi + (double)rc_lo;
+            R.xphi[R.crossings] = (float)((double)ph0.hi + (double)(ph0.lo + cph));
+        }
+        R.crossings++;
+        if (R.orders < s.max_orders && rc >= s.rin_f && rc <= s.rout_f) {
+            float g = doppler_g_f(rc, R.E.hi, R.L.hi, k.M, k.a);
+            shade_disk(rc, g, s.qf, s.gain, R.disk);
+            if (R.orders == 0) R.first_r = rc;
+            R.orders++;
+        }
+    }
+    if (R.r.hi > s.r_far_f && R.step > 11) { R.status = 0; return true; }
+    return false;
+}
+
+// Step size of render.cu:185,207 for the current radius (FP32).
+__device__ __forceinline__ float mray_h(const SceneDev& s, float r) {
+    return s.h_unit_f * fminf(fmaxf(1.0f, r * s.inv_M_f), 100.0f);
+}
+
+// Result of an FP32 attempt.
+enum { STEP_CONT = 0, STEP_DONE = 1, STEP_PARK = 2 };
+
+// One FP32 step, or parks the lane for an FP64 island step.
+template <bool PHI>
+__device__ __forceinline__ int mray_step32(MRay<PHI>& R, const SceneDev& s, const SpaceK& k) {
+    if (R.step >= s.max_steps) { R.status = 2; return STEP_DONE; }
+    const float h = mray_h(s, R.r.hi);
+    if ((s.islands & kIslandHorizon) && R.r.hi < s.r_band_f) {
+        R.pending = true; R.h_pend = h;
+        return STEP_PARK;
+    }
+    const HiLo r0 = R.r, th0 = R.th, pr0 = R.pr, pth0 = R.pth, ph0 = R.ph;
+    const float k0r = R.k[0], k0t = R.k[1], k0p = R.k[4];
+    const float hh = 0.5f * h;
+    F5 k2 = rhs_f<PHI>(R.r.hi + fmaf(hh, R.k[0], R.r.lo), R.th.hi + fmaf(hh, R.k[1], R.th.lo),
+                       R.pr.hi + fmaf(hh, R.k[2], R.pr.lo), R.pth.hi + fmaf(hh, R.k[3], R.pth.lo), R.c, k);
+    F5 k3 = rhs_f<PHI>(R.r.hi + fmaf(hh, k2.r, R.r.lo), R.th.hi + fmaf(hh, k2.th, R.th.lo),
+                       R.pr.hi + fmaf(hh, k2.pr, R.pr.lo), R.pth.hi + fmaf(hh, k2.pth, R.pth.lo), R.c, k);
+    F5 k4 = rhs_f<PHI>(R.r.hi + fmaf(h, k3.r, R.r.lo), R.th.hi + fmaf(h, k3.th, R.th.lo),
+                       R.pr.hi + fmaf(h, k3.pr, R.pr.lo), R.pth.hi + fmaf(h, k3.pth, R.pth.lo), R.c, k);
+    const float h6 = h * (1.0f / 6.0f);
+    hl_add(R.r, h6 * (R.k[0] + 2.0f * (k2.r + k3.r) + k4.r));
+    hl_add(R.th, h6 * (R.k[1] + 2.0f * (k2.th + k3.th) + k4.th));
+    hl_add(R.pr, h6 * (R.k[2] + 2.0f * (k2.pr + k3.pr) + k4.pr));
+    hl_add(R.pth, h6 * (R.k[3] + 2.0f * (k2.pth + k3.pth) + k4.pth));
+    if (PHI) hl_add(R.ph, h6 * (R.k[4] + 2.0f * (k2.ph + k3.ph) + k4.ph));
+    if (s.islands & kIslandTurning) {
+        bool turn = ((pr0.hi > 0.0f) != (R.pr.hi > 0.0f)) || ((pth0.hi > 0.0f) != (R.pth.hi > 0.0f));
+        if (turn) {
+            R.r = r0; R.th = th0; R.pr = pr0; R.pth = pth0; R.ph = ph0;
+            R.pending = true; R.h_pend = h;
+            return STEP_PARK;
+        }
+    }
+    return mray_finish_step(R, s, k, h, r0, th0, k0r, k0t, ph0, k0p) ? STEP_DONE : STEP_CONT;
+}
+
+// The parked FP64 step of size h_pend.
+template <bool PHI>
+__device__ __forceinline__ bool mray_island(MRay<PHI>& R, const SceneDev& s, const SpaceK& k) {
+    const HiLo r0 = R.r, th0 = R.th, ph0 = R.ph;
+    const float k0r = R.k[0], k0t = R.k[1], k0p = R.k[4];
+    const float h = R.h_pend;
+    D5 y{hl_d(R.r), hl_d(R.th), hl_d(R.pr), hl_d(R.pth), PHI ? hl_d(R.ph) : 0.0};
+    D5 o = rk4_d(y, (double)h, hl_d(R.E), hl_d(R.L), s.a, s.M, s.r_plus, s.r_minus, PHI);
+    R.r = d_hl(o.r); R.th = d_hl(o.th); R.pr = d_hl(o.pr); R.pth = d_hl(o.pth);
+    if (PHI) R.ph = d_hl(o.ph);
+    R.pending = false;
+    R.fp64_steps++;
+    return mray_finish_step(R, s, k, h, r0, th0, k0r, k0t, ph0, k0p);
+}
+
+// Closeness of a ray to the critical curve.  R(r) = P(r)^2 - Delta K
+// (K = Q + (L - aE)^2) has a double root at the spherical photon orbit r_c
+// exactly for critical rays; r_c solves R'(r) = 0, the depressed cubic
 //   4 E^2 r^3 + (4 a^2 E^2 - 4 a E L - 2 K) r + 2 M K = 0,
-// and near the critical curve R(r_c)/(E^2 r_c^4) ~ -(dR/db) db / r_c^4.  The
-// scale 0.385/M is that derivative for the Schwarzschild photon sphere, so
-// the test reads |b - b_crit| < db_thr.  Returns true when the ray is closer
-// than db_thr (in M).
+// and near the curve |R(r_c)| / (E^2 r_c^4) ~ |dR/db| |b - b_crit| / r_c^4.
+// The scale 0.385/M is that derivative for the Schwarzschild photon sphere,
+// so the test reads |b - b_crit| < db_thr (in M).
 __device__ __forceinline__ bool near_critical(double E, double L, double Q, double a, double M,
                                               double rp, double db_thr) {
     double K = Q + (L - a * E) * (L - a * E);
     double c3 = 4.0 * E * E;
     double c1 = 4.0 * a * a * E * E - 4.0 * a * E * L - 2.0 * K;
     double c0 = 2.0 * M * K;
-    // largest real root of c3 r^3 + c1 r + c0 by Newton from above
-    double r = fmax(3.0 * M, sqrt(fmax(0.0, -c1 / c3)) + 2.0 * M) + 4.0 * M;
-    for (int it = 0; it < 40; ++it) {
+    // largest real root by Newton from above (the cubic is convex there)
+    double r = sqrt(fmax(0.0, -c1 / c3)) + 4.0 * M;
+#pragma unroll 1
+    for (int it = 0; it < 30; ++it) {
         double f = (c3 * r * r + c1) * r + c0;
         double fp = 3.0 * c3 * r * r + c1;
         if (fp <= 0.0) break;
         double dr = f / fp;
         r -= dr;
-        if (fabs(dr) < 1e-13 * r) break;
+        if (fabs(dr) < 1e-12 * r) break;
     }
     if (!(r > rp)) return false;
     double r2 = r * r, a2 = a * a;
     double P = (r2 + a2) * E - a * L;
     double Del = r2 - 2.0 * M * r + a2;
     double R = P * P - Del * K;
-    double eps = fabs(R) / (E * E * r2 * r2);
-    return eps < 0.385 * db_thr / M;
+    return fabs(R) / (E * E * r2 * r2) < 0.385 * db_thr / M;
 }
 
-// Per-lane ray of the mixed tracer.  PHI integrates phi and records the
-// first four equatorial crossings for the per-ray report.
-template <bool PHI>
-struct RayMixed {
-    HiLo r, th, pr, pth, ph;
-    float k[5];                  // f(y) at the current state (first stage of the next step)
-    RayConst c;
-    double E, L;                 // conserved momenta in FP64
+// ---------------------------------------------------------------------------
+// FP64 Carter-form ray for near-critical rays (traced whole in FP64).  With
+// REC phi is integrated and the first four crossings are recorded.
+template <bool REC>
+struct DRay {
+    D5 y;
+    double E, L;
     double min_r, first_r;
-    double xr[PHI ? 4 : 1], xphi[PHI ? 4 : 1];
     float disk[3];
     int step, orders, crossings, status;
-    unsigned fp64_steps;
+    double xr[REC ? 4 : 1], xphi[REC ? 4 : 1];
 };
 
-template <bool PHI>
-__device__ __forceinline__ void mixed_set_k(RayMixed<PHI>& R) {
-    F5 f = rhs_carter_f<PHI>(R.r.hi, R.th.hi, R.pr.hi, R.pth.hi, R.c);
-    R.k[0] = f.r; R.k[1] = f.th; R.k[2] = f.pr; R.k[3] = f.pth; R.k[4] = f.ph;
-}
-
-template <bool PHI>
-__device__ __forceinline__ void mixed_init(const SceneDev& s, const Momentum& m, RayMixed<PHI>& R) {
-    R.E = -m.pt; R.L = m.pph;
-    R.c.E = (float)R.E; R.c.L = (float)R.L; R.c.a = (float)s.a; R.c.a2 = (float)(s.a * s.a);
-    R.c.aL = (float)(s.a * R.L); R.c.a2E2 = (float)(s.a * s.a * R.E * R.E);
-    R.c.L2 = (float)(R.L * R.L); R.c.twoaEL = (float)(2.0 * s.a * R.E * R.L);
-    R.c.M = (float)s.M; R.c.rp = (float)s.r_plus; R.c.rm = (float)s.r_minus;
-    R.r = d_hl(s.r_cam); R.th = d_hl(s.th_cam); R.pr = d_hl(m.pr); R.pth = d_hl(m.pth); R.ph = d_hl(s.ph_cam);
+template <bool REC>
+__device__ __forceinline__ void dray_start(DRay<REC>& R, const SceneDev& s, double E, double L, double pr, double pth) {
+    R.y = D5{s.r_cam, s.th_cam, pr, pth, s.ph_cam};
+    R.E = E; R.L = L;
     R.min_r = s.r_cam; R.first_r = 0.0;
     R.disk[0] = R.disk[1] = R.disk[2] = 0.0f;
-    R.step = 0; R.orders = 0; R.crossings = 0; R.status = 2; R.fp64_steps = 0;
-    if (PHI) for (int k = 0; k < 4; ++k) { R.xr[k] = 0.0; R.xphi[k] = 0.0; }
-    mixed_set_k(R);
+    R.step = 0; R.orders = 0; R.crossings = 0; R.status = 2;
+    if (REC) for (int i = 0; i < 4; ++i) { R.xr[i] = 0.0; R.xphi[i] = 0.0; }
 }
 
-// One FP64 RK4 step from (hi, lo) state; returns false when the ray fell
-// through the horizon or reached a pole (bh_kerr.h:770-773).
-template <bool PHI>
-__device__ __forceinline__ bool mixed_step_fp64(const SceneDev& s, RayMixed<PHI>& R, double h) {
-    D5 y{hl_d(R.r), hl_d(R.th), hl_d(R.pr), hl_d(R.pth), PHI ? hl_d(R.ph) : 0.0};
-    const double E = R.E, L = R.L, a = s.a, M = s.M, rp = s.r_plus, rm = s.r_minus;
-    D5 k1 = rhs_carter_d(y, E, L, a, M, rp, rm);
-    D5 k2 = rhs_carter_d(add5(y, 0.5 * h, k1), E, L, a, M, rp, rm);
-    D5 k3 = rhs_carter_d(add5(y, 0.5 * h, k2), E, L, a, M, rp, rm);
-    D5 k4 = rhs_carter_d(add5(y, h, k3), E, L, a, M, rp, rm);
-    double h6 = h / 6.0;
-    y.r += h6 * (k1.r + 2.0 * k2.r + 2.0 * k3.r + k4.r);
-    y.th += h6 * (k1.th + 2.0 * k2.th + 2.0 * k3.th + k4.th);
-    y.pr += h6 * (k1.pr + 2.0 * k2.pr + 2.0 * k3.pr + k4.pr);
-    y.pth += h6 * (k1.pth + 2.0 * k2.pth + 2.0 * k3.pth + k4.pth);
-    if (PHI) y.ph += h6 * (k1.ph + 2.0 * k2.ph + 2.0 * k3.ph + k4.ph);
-    R.r = d_hl(y.r); R.th = d_hl(y.th); R.pr = d_hl(y.pr); R.pth = d_hl(y.pth);
-    if (PHI) R.ph = d_hl(y.ph);
-    R.fp64_steps++;
-    return y.r > rp + 1e-9 && y.th > 1e-9 && y.th < kPi - 1e-9;
-}
-
-// Advances one step; returns true when the ray terminated.
-template <bool PHI>
-__device__ __forceinline__ bool mixed_advance(const SceneDev& s, RayMixed<PHI>& R, unsigned long long& evals) {
+// One FP64 step with the same step law, crossing rule and shading.
+template <bool REC>
+__device__ __forceinline__ bool dray_step(DRay<REC>& R, const SceneDev& s) {
     if (R.step >= s.max_steps) { R.status = 2; return true; }
-    const float rf = R.r.hi;
-    const double h = s.h_unit * fmin(fmax(1.0, (double)rf / s.M), 100.0);
-    // start of step (for crossings and island redo)
-    const HiLo r0 = R.r, th0 = R.th, pr0 = R.pr, pth0 = R.pth, ph0 = R.ph;
-    const float k0r = R.k[0], k0t = R.k[1], k0p = R.k[4];
-    bool ok;
-    if ((s.islands & kIslandHorizon) && (double)rf < s.r_plus + kHorizonBand) {
-        ok = mixed_step_fp64(s, R, h);
-        evals += 4;
-    } else {
-        const float hf = (float)h, hh = 0.5f * hf;
-        F5 k2 = rhs_carter_f<PHI>(R.r.hi + fmaf(hh, R.k[0], R.r.lo), R.th.hi + fmaf(hh, R.k[1], R.th.lo),
-                                  R.pr.hi + fmaf(hh, R.k[2], R.pr.lo), R.pth.hi + fmaf(hh, R.k[3], R.pth.lo), R.c);
-        F5 k3 = rhs_carter_f<PHI>(R.r.hi + fmaf(hh, k2.r, R.r.lo), R.th.hi + fmaf(hh, k2.th, R.th.lo),
-                                  R.pr.hi + fmaf(hh, k2.pr, R.pr.lo), R.pth.hi + fmaf(hh, k2.pth, R.pth.lo), R.c);
-        F5 k4 = rhs_carter_f<PHI>(R.r.hi + fmaf(hf, k3.r, R.r.lo), R.th.hi + fmaf(hf, k3.th, R.th.lo),
-                                  R.pr.hi + fmaf(hf, k3.pr, R.pr.lo), R.pth.hi + fmaf(hf, k3.pth, R.pth.lo), R.c);
-        const float h6 = (float)(h / 6.0);
-        hl_add(R.r, h6 * (R.k[0] + 2.0f * (k2.r + k3.r) + k4.r));
-        hl_add(R.th, h6 * (R.k[1] + 2.0f * (k2.th + k3.th) + k4.th));
-        hl_add(R.pr, h6 * (R.k[2] + 2.0f * (k2.pr + k3.pr) + k4.pr));
-        hl_add(R.pth, h6 * (R.k[3] + 2.0f * (k2.pth + k3.pth) + k4.pth));
-        if (PHI) hl_add(R.ph, h6 * (R.k[4] + 2.0f * (k2.ph + k3.ph) + k4.ph));
-        evals += 3;
-        bool turn = ((pr0.hi > 0.0f) != (R.pr.hi > 0.0f)) || ((pth0.hi > 0.0f) != (R.pth.hi > 0.0f));
-        if ((s.islands & kIslandTurning) && turn) {
-            R.r = r0; R.th = th0; R.pr = pr0; R.pth = pth0; R.ph = ph0;
-            ok = mixed_step_fp64(s, R, h);
-            evals += 4;
-        } else {
-            ok = (double)R.r.hi > s.r_plus + 1e-9 && R.th.hi > 1e-9f && (double)R.th.hi < kPi - 1e-9;
-        }
-    }
+    const double h = s.h_unit * fmin(fmax(1.0, R.y.r / s.M), 100.0);
+    const D5 y0 = R.y;
+    D5 f0 = rhs_d(y0, R.E, R.L, s.a, s.M, s.r_plus, s.r_minus);
+    R.y = rk4_d(y0, h, R.E, R.L, s.a, s.M, s.r_plus, s.r_minus, REC);
     R.step++;
+    bool ok = R.y.r > s.r_plus + 1e-9 && R.y.th > 1e-9 && R.y.th < kPi - 1e-9;
     if (!ok) { R.status = 1; return true; }
-    mixed_set_k(R);
-    evals += 1;
-    double rn = hl_d(R.r);
-    R.min_r = fmin(R.min_r, rn);
-    float dp = dtheta_eq(th0), dc = dtheta_eq(R.th);
-    bool sc = (dp > 0.0f && dc < 0.0f) || (dp < 0.0f && dc > 0.0f);
-    bool nz = (fabsf(dp) < 1e-8f && fabsf(dc) >= 1e-8f) || (fabsf(dc) < 1e-8f && fabsf(dp) >= 1e-8f);
+    R.min_r = fmin(R.min_r, R.y.r);
+    double dp = y0.th - kPi * 0.5, dc = R.y.th - kPi * 0.5;
+    bool sc = (dp > 0 && dc < 0) || (dp < 0 && dc > 0);
+    bool nz = (fabs(dp) < 1e-8 && fabs(dc) >= 1e-8) || (fabs(dc) < 1e-8 && fabs(dp) >= 1e-8);
     if (sc || nz) {
-        double d0 = dp, d1 = dc;
-        double alpha = fabs(d0) / (fabs(d0) + fabs(d1) + 1e-30);
-        double r_0 = hl_d(r0);
-        double rc, phc = 0.0;
+        double alpha = fabs(dp) / (fabs(dp) + fabs(dc) + 1e-30);
+        double rc, phc;
         if (s.crossing == NP_CROSS_HERMITE && sc) {
-            double u = hermite_root(d0, d1, h * (double)k0t, h * (double)R.k[1], alpha);
-            rc = hermite_eval(r_0, rn, h * (double)k0r, h * (double)R.k[0], u);
-            if (PHI) phc = hermite_eval(hl_d(ph0), hl_d(R.ph), h * (double)k0p, h * (double)R.k[4], u);
+            D5 f1 = rhs_d(R.y, R.E, R.L, s.a, s.M, s.r_plus, s.r_minus);
+            double u = hermite_root(dp, dc, h * f0.th, h * f1.th, alpha);
+            rc = hermite_eval(y0.r, R.y.r, h * f0.r, h * f1.r, u);
+            phc = hermite_eval(y0.ph, R.y.ph, h * f0.ph, h * f1.ph, u);
         } else {
-            rc = r_0 + alpha * (rn - r_0);
-            if (PHI) phc = hl_d(ph0) + alpha * (hl_d(R.ph) - hl_d(ph0));
+            rc = y0.r + alpha * (R.y.r - y0.r);
+            phc = y0.ph + alpha * (R.y.ph - y0.ph);
         }
-        if (PHI) {
-            if (R.crossings < 4) { R.xr[R.crossings] = rc; R.xphi[R.crossings] = phc; }
-        }
+        if (REC && R.crossings < 4) { R.xr[R.crossings] = rc; R.xphi[R.crossings] = phc; }
         R.crossings++;
         if (R.orders < s.max_orders && rc >= s.rin && rc <= s.rout) {
             float g = (float)doppler_g(rc, -R.E, R.L, s.M, s.a);
@@ -278,24 +435,8 @@ __device__ __forceinline__ bool mixed_advance(const SceneDev& s, RayMixed<PHI>& 
             R.orders++;
         }
     }
-    if (rn > s.r_far && R.step > 11) { R.status = 0; return true; }
+    if (R.y.r > s.r_far && R.step > 11) { R.status = 0; return true; }
     return false;
-}
-
-// |H| at the current state, for the invariant report (E and L are exact).
-template <bool PHI>
-__device__ __forceinline__ void mixed_invariants(const SceneDev& s, const RayMixed<PHI>& R, double r, double th, float* inv3) {
-    double sn, cs;
-    sincos(th, &sn, &cs);
-    double s2 = fmax(sn * sn, 1e-30), a = s.a, a2 = a * a, E = R.E, L = R.L;
-    double Sig = r * r + a2 * cs * cs;
-    double Del = (r - s.r_plus) * (r - s.r_minus);
-    double P = (r * r + a2) * E - a * L;
-    double pr = hl_d(R.pr), pth = hl_d(R.pth);
-    double F = Del * pr * pr + pth * pth - P * P / Del + L * L / s2 - 2.0 * a * E * L + a2 * E * E * s2;
-    atomic_max_nonneg(&inv3[0], (float)fabs(0.5 * F / Sig));
-    atomic_max_nonneg(&inv3[1], 0.0f);
-    atomic_max_nonneg(&inv3[2], 0.0f);
 }
 
 }  // namespace np

@@ -69,7 +69,8 @@ def test_fp64_matches_oracle_benchmark(cuda, name):
     z = np.load(os.path.join(GOLD, name + ".npz"))
     sc = _scene_from(z)
     rgb, rc = _render_np(sc, "fp64")
-    _compare(rgb, rc, z["rgb"], z["rcross"], 1e-5, 1e-6, 0.98)
+    # crossing radius p99 <= 1e-5 M (a few float32 ulp of the stored radius)
+    _compare(rgb, rc, z["rgb"], z["rcross"], 1e-5, 1e-5, 0.98)
 
 
 @pytest.mark.parametrize("name", _gold("bench_"))
@@ -97,8 +98,10 @@ def test_trace_rays_constants_and_crossings(cuda):
         x = out["cross"].cpu().numpy()[:, 0, 0]
         xr = ref["cross"][:, 0, 0]
         both = (x > 0) & (xr > 0) & (np.abs(x - xr) < 1.0)
-        tol = 1e-7 if prec == "fp64" else 1e-4
-        assert np.quantile(np.abs(x[both] - xr[both]), 0.99) < tol, prec
+        rel = np.abs(x[both] - xr[both]) / xr[both]
+        # relative crossing-radius agreement (p99): 1e-6 FP64, 1e-5 mixed
+        tol = 1e-6 if prec == "fp64" else 1e-5
+        assert np.quantile(rel, 0.99) < tol, (prec, np.quantile(rel, 0.99))
 
 
 def test_progressive_accumulation(cuda):
