@@ -159,6 +159,30 @@ int np_trace_rays_device(const np_scene_t* scene, int precision, int n,
                          double* d_consts, double* d_cross, int32_t* d_status,
                          void* stream);
 
+/* Largest pass (width * height * spp rays) np_render_device_noalloc accepts. */
+#define NP_NOALLOC_MAX_RAYS 262144
+
+/* No counterpart in the reference: an entry point for callers that cannot
+ * allocate device memory.  Some hosts own the whole GPU through their own
+ * allocator (an engine or framework that reserves device memory up front)
+ * or forbid allocation inside their frame loop; for them this renders one
+ * pass like np_render_device but uses, instead of library-allocated scratch,
+ * a fixed scratch array compiled into the library (about 15 MB, held on
+ * every GPU that loads the library until the process exits).  Limits and
+ * rules:
+ *   - at most NP_NOALLOC_MAX_RAYS rays per call; larger passes are rejected
+ *     with NP_ERR_INVALID (split the samples over several calls with
+ *     sample_offset and accumulate = 1);
+ *   - the first call on each device looks up the array's device address;
+ *     make that first call before any stream capture;
+ *   - every call shares the one array, so calls whose work overlaps on the
+ *     GPU (different streams, or different host threads) race; serialise
+ *     them;
+ *   - no statistics are returned and nothing is allocated or freed.
+ * Buffers are device pointers as for np_render_device. */
+int np_render_device_noalloc(const np_scene_t* scene, int precision,
+                             float* d_rgb, float* d_rcross, int accumulate, void* stream);
+
 /* Launch tunables of the mixed path (process-wide; the autotuner sets them).
  *   NP_TUNE_ISLAND_BATCH  parked lanes of a warp that trigger a batched FP64
  *                         island step (1..32, default 8)

@@ -815,3 +815,79 @@ int np_measure_fma_peak(int which, double* tflops) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free render pass.  Its scratch (counters, per-sample colours,
+// ray-generation arrays, deferred list) lives in one file-scope device array
+// sized for NP_NOALLOC_MAX_RAYS rays; each device's copy is looked up once
+// with cudaGetSymbolAddress and reused.  Calls share the array.
+
+namespace {
+
+constexpr size_t na_align(size_t x) { return (x + 255) & ~(size_t)255; }
+constexpr size_t kNaRays = NP_NOALLOC_MAX_RAYS;
+constexpr size_t kNaCtr = 0;
+constexpr size_t kNaSrgb = kNaCtr + na_align(sizeof(Counters));
+constexpr size_t kNaA = kNaSrgb + na_align(3 * kNaRays * sizeof(float));
+constexpr size_t kNaB = kNaA + na_align(kNaRays * sizeof(float4));
+constexpr size_t kNaCy = kNaB + na_align(kNaRays * sizeof(float4));
+constexpr size_t kNaFlag = kNaCy + na_align(kNaRays * sizeof(float));
+constexpr size_t kNaList = kNaFlag + na_align(kNaRays);
+constexpr size_t kNaBytes = kNaList + na_align(kNaRays * sizeof(long long));
+
+__device__ __align__(256) unsigned char g_na_scratch[kNaBytes];
+
+constexpr int kNaMaxDevices = 64;
+unsigned char* g_na_ptr[kNaMaxDevices] = {};
+std::mutex g_na_mu;
+
+}  // namespace
+
+extern "C" int np_render_device_noalloc(const np_scene_t* scene, int precision, float* d_rgb, float* d_rcross,
+                                        int accumulate, void* stream_v) {
+    if (!scene || !d_rgb) return fail(NP_ERR_INVALID, "scene or rgb buffer is NULL");
+    if (precision != NP_PREC_FP64 && precision != NP_PREC_MIXED) return fail(NP_ERR_INVALID, "Invalid precision.");
+    SceneDev s;
+    int rc = prepare_scene(*scene, s);
+    if (rc != NP_OK) return rc;
+    if (s.total > (long long)kNaRays)
+        return fail(NP_ERR_INVALID, "pass of %lld rays exceeds NP_NOALLOC_MAX_RAYS (%lld); split the samples "
+                    "over several calls", s.total, (long long)kNaRays);
+    int dev = 0;
+    NP_CU(cudaGetDevice(&dev), NP_ERR_NO_DEVICE);
+    if (dev < 0 || dev >= kNaMaxDevices) return fail(NP_ERR_INVALID, "device index %d out of range", dev);
+    unsigned char* base = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(g_na_mu);
+        if (!g_na_ptr[dev]) {
+            void* p = nullptr;
+            cudaError_t e = cudaGetSymbolAddress(&p, g_na_scratch);
+            if (e != cudaSuccess || !p)
+                return fail(NP_ERR_NO_DEVICE, "cudaGetSymbolAddress of the scratch array failed: %s",
+                            cudaGetErrorString(e));
+            g_na_ptr[dev] = (unsigned char*)p;
+        }
+        base = g_na_ptr[dev];
+    }
+    cudaStream_t st = (cudaStream_t)stream_v;
+    Counters* ctr = (Counters*)(base + kNaCtr);
+    float* srgb = (float*)(base + kNaSrgb);
+    NP_CU(cudaMemsetAsync(ctr, 0, sizeof(Counters), st), NP_ERR_KERNEL);
+    if (precision == NP_PREC_FP64) {
+        render_fp64_kernel<<<grid_for((const void*)render_fp64_kernel), kBlock, 0, st>>>(
+            s, srgb, d_rcross, nullptr, ctr, nullptr);
+    } else {
+        InitSoA soa{(float4*)(base + kNaA), (float4*)(base + kNaB), (float*)(base + kNaCy),
+                    (unsigned char*)(base + kNaFlag), (long long*)(base + kNaList)};
+        int ib = (int)std::min<long long>((s.total + 255) / 256, 152ll * 8);
+        ray_init_kernel<<<ib, 256, 0, st>>>(s, soa, ctr);
+        NP_CU(cudaGetLastError(), NP_ERR_KERNEL);
+        launch_mixed(g_tune.min_blocks, s, soa, srgb, d_rcross, nullptr, ctr, g_tune.chunk, st);
+    }
+    NP_CU(cudaGetLastError(), NP_ERR_KERNEL);
+    long long n = 3 * s.npix;
+    int blocks = (int)std::min<long long>((n + 255) / 256, 152 * 16);
+    resolve_kernel<<<blocks, 256, 0, st>>>(srgb, d_rgb, s.npix, s.spp, accumulate);
+    NP_CU(cudaGetLastError(), NP_ERR_KERNEL);
+    return NP_OK;
+}
