@@ -1,0 +1,102 @@
+/*
+ * geokerr_c_api.h -- C ABI of the GB300 GEOKERR-equivalent Mino-time solver.
+ *
+ * Drop-in for the reference's geokerr_port C interfaces:
+ *   geokerr_eval_lambda, geokerr_estimate_periods, geokerr_phi_omega
+ *       Fortran ISO_C_BINDING entry points, geokerr_port/reference/
+ *       geokerr_eval_lambda.f90:57-70, 205-210, 299-306 (C prototypes used
+ *       by the reference at geokerr_port/validation/gkval_adapters.c:33-44);
+ *   geokerr_stream_cuda, geokerr_complete_stream_cuda
+ *       CUDA host wrappers, geokerr_port/cuda/geokerr_stream.cu:158-161 and
+ *       geokerr_port/cuda/geokerr_complete.cu:446-449;
+ *   compute_geokerr_complete_cuda
+ *       geokerr_port/cuda/geokerr_complete.cu:356-363.
+ * Same names, argument order and meaning, host pointers, synchronous; the
+ * work runs on the current CUDA device.  Units M = E = 1, u = 1/r,
+ * mu = cos(theta), Lz = L/E, Q2 = Q/E^2.
+ *
+ * The batched entry points (np_geokerr_*) take device pointers, run one
+ * geodesic per GPU thread and return np_status codes (include/np_render.h).
+ */
+#ifndef GEOKERR_C_API_H
+#define GEOKERR_C_API_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Samples one null geodesic at S affine parameters lam0 + k dlam
+ * (geokerr_eval_lambda.f90:57-203): GEOKERR's NUP = S points uniform in u
+ * (OFFSET 0.5, in to the radial turning point and back), linearly resampled
+ * in affine lambda; u, mu at k = 0 are forced to the inputs; tpmi/tpri are
+ * the 0-based grid indices of the first mu / u turning points or -1;
+ * info = 0 ok, 1 if S <= 0, 2 if the geodesic could not be sampled. */
+void geokerr_eval_lambda(double u0, double mu0, double uf, double a, double Lz, double Q2, double t0,
+                         double lam0, double dlam, int S,
+                         double* u, double* mu, double* t, double* phi, double* affine,
+                         int* tpmi, int* tpri, int* info);
+
+/* Radial and polar periods in affine lambda from turning-point spacing on a
+ * 4096-point sampling (geokerr_eval_lambda.f90:205-297); -1 when not found. */
+void geokerr_estimate_periods(double u0, double mu0, double a, double Lz, double Q2,
+                              double* Tr, double* Ttheta, int* info);
+
+/* d phi / d lambda (Mino) at (u0, mu0) (geokerr_eval_lambda.f90:299-306). */
+double geokerr_phi_omega(double u0, double mu0, double a, double Lz, double Q2);
+
+/* Exact Mino-time samples lambda_k = lam0 + k dlam (k < S) of the geodesic
+ * leaving u0 towards uf (du/dlambda sign from uf - u0, dmu/dlambda sign -1
+ * for mu0 > 0): u, mu, t, phi and lambda itself in h_affine.  Returns 0,
+ * -1 bad argument, -2 allocation failure, -3 kernel failure
+ * (geokerr_stream.cu:163-180). */
+int geokerr_stream_cuda(double u0, double uf, double mu0, double a, double L, double Q2,
+                        double lam0, double dlam, int S,
+                        double* h_u, double* h_mu, double* h_t, double* h_phi, double* h_affine);
+
+/* geokerr_eval_lambda on the GPU (the gkval harness's CUDA solver,
+ * gkval_adapters.c:675-682); t0 = 0.  Return codes as geokerr_stream_cuda. */
+int geokerr_complete_stream_cuda(double u0, double uf, double mu0, double a, double L, double Q2,
+                                 double lam0, double dlam, int S,
+                                 double* h_u, double* h_mu, double* h_t, double* h_phi, double* h_affine);
+
+/* Per ray i < n: Mino time lambda from u0 to uf (through the radial turning
+ * point when uf lies beyond it, GEOMU semantics), mu at uf, a case number
+ * (1 turning point on the way in, 2 turning point on the way out, 3 no
+ * turning point) and a validity flag. */
+void compute_geokerr_complete_cuda(const double* h_u0, const double* h_uf, const double* h_mu0,
+                                   const double* h_a, const double* h_l, const double* h_q2,
+                                   const int* h_su, const int* h_sm,
+                                   double* h_lambda_results, double* h_muf_results,
+                                   int* h_ncase_results, char* h_valid_results, int n_cases);
+
+/* Batched GEOKERR sampler (geokerr_original.f:357-605 with USEGEOR false,
+ * PHIT true, NPTS = 0): ray i uses u0[i], uf[i], mu0[i], l[i], q2[i],
+ * su[i], sm[i] and the common spin a, TPR flag, nup and offset; outputs are
+ * [n][nup] device arrays (u, mu, delta t, delta phi, affine lambda, mu and
+ * u turning counts) and npts[i] = points written (0 when the ray could not
+ * be sampled).  Device pointers; returns np_status. */
+int np_geokerr_points_device(int n, double a, const double* u0, const double* uf, const double* mu0,
+                             const double* l, const double* q2, const double* su, const double* sm,
+                             int tpr, int nup, double offset,
+                             double* u, double* mu, double* dt, double* dphi, double* lam,
+                             int32_t* tpm, int32_t* tprv, int32_t* npts, void* stream);
+
+/* Batched geokerr_eval_lambda: ray i with u0[i], mu0[i], uf[i], Lz[i],
+ * Q2[i], t0[i], lam0[i], dlam[i] and common a and S; outputs [n][S]
+ * device arrays plus tpmi[n], tpri[n], info[n].  `work` is caller scratch
+ * of at least np_geokerr_eval_lambda_work_bytes(n, S) bytes, or NULL to let
+ * the library allocate it.  Returns np_status. */
+int np_geokerr_eval_lambda_device(int n, double a, const double* u0, const double* mu0, const double* uf,
+                                  const double* Lz, const double* Q2, const double* t0,
+                                  const double* lam0, const double* dlam, int S,
+                                  double* u, double* mu, double* t, double* phi, double* affine,
+                                  int32_t* tpmi, int32_t* tpri, int32_t* info, void* work, void* stream);
+size_t np_geokerr_eval_lambda_work_bytes(int n, int S);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GEOKERR_C_API_H */

@@ -1,0 +1,675 @@
+// geokerr.cu -- GEOKERR-equivalent Mino-time geodesic solver on sm_103a, behind
+// the C ABI of include/geokerr_c_api.h.
+//
+// One geodesic per thread, FP64 throughout (this is one of the FP64 islands
+// of the design: the whole solver is short and must hold 1e-12).  The
+// equations, in Mino time l with M = E = 1, u = 1/r, mu = cos(theta):
+//   u''  = U'(u)/2,  U(u) = 1 + A2 u^2 + A3 u^3 + A4 u^4
+//          A2 = a^2 - q2 - l^2, A3 = 2((a - l)^2 + q2), A4 = -a^2 q2
+//   mu'' = M'(mu)/2, M(mu) = Q0 + B2 mu^2 + B4 mu^4 (GEOKERR's polar potential,
+//          with its rule that a mu0 outside the polar roots becomes the
+//          turning point, geokerr_original.f:1121-1170)
+//   t'   = (r^2 + a^2)(r^2 + a^2 - a l)/Delta + a l - a^2 (1 - mu^2)
+//   phi' = a (r^2 + a^2 - a l)/Delta + l/(1 - mu^2) - a
+//   lambda_affine' = r^2 + a^2 mu^2
+// are advanced by order-24 Taylor series whose coefficients come from the
+// recurrences of the polynomial right-hand sides and of series division
+// (Jorba & Zou 2005).  A step is a fixed fraction of the smallest radius of
+// convergence, so every step is exact to rounding and sample points are found
+// by Newton iteration on the step's series.  The sampling logic is GEOKERR's
+// (geokerr_original.f:357-605): NUP points uniform in u from U0, offset by
+// OFFSET steps, in to the radial turning point UB and back out.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <algorithm>
+
+#include <cuda_runtime.h>
+
+#include "geokerr_c_api.h"
+#include "np_render.h"
+
+namespace {
+
+thread_local std::string g_gk_error;
+
+int gk_fail(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_gk_error = buf;
+    return code;
+}
+
+constexpr int P = 24;
+
+struct Par {
+    double a, l, A2, A3, A4, Q0, B2, B4, uplus;
+};
+
+// Constants of the motion and GEOKERR's polar potential (roots of M in mu^2
+// by the stable quadratic formula; a violated root moves to mu0^2).  a^2 mneg
+// is carried instead of mneg so that a = 0 needs no special case.
+__host__ __device__ Par make_par(double a, double l, double q2, double mu0) {
+    Par p;
+    p.a = a; p.l = l;
+    p.A2 = a * a - q2 - l * l;
+    p.A3 = 2.0 * ((a - l) * (a - l) + q2);
+    p.A4 = -a * a * q2;
+    p.uplus = 1.0 / (1.0 + sqrt(1.0 - a * a));
+    const double a2 = a * a, b = a2 - (q2 + l * l);
+    const double yy = -0.5 * (b + (b >= 0.0 ? 1.0 : -1.0) * sqrt(b * b + 4.0 * q2 * a2));
+    double mpos, a2mneg;
+    if (b < 0.0) { a2mneg = -yy; mpos = q2 / yy; }
+    else { a2mneg = a2 * q2 / yy; mpos = -yy / a2; }
+    if (mpos > 1.0) mpos = 1.0;
+    if (a2mneg < 0.0 || a2 == 0.0) {
+        if (sqrt(mpos) < mu0) mpos = mu0 * mu0;
+    } else {
+        if (a2mneg > a2 * mu0 * mu0) a2mneg = a2 * mu0 * mu0;
+        if (mu0 * mu0 > mpos) mpos = mu0 * mu0;
+    }
+    p.B4 = -a2;
+    p.B2 = a2 * mpos + a2mneg;
+    p.Q0 = -mpos * a2mneg;
+    return p;
+}
+
+__device__ __forceinline__ double Uof(const Par& p, double u) { return 1.0 + u * u * (p.A2 + u * (p.A3 + u * p.A4)); }
+__device__ __forceinline__ double Mof(const Par& p, double m) { double m2 = m * m; return p.Q0 + m2 * (p.B2 + m2 * p.B4); }
+
+struct St { double u, du, m, dm, t, ph, lam; };
+struct Ser { double u[P + 1], m[P + 1], t[P + 1], ph[P + 1], lam[P + 1]; };
+
+// Taylor coefficients of one step; `acc` adds the t, phi, lambda series.
+__device__ void taylor(const Par& p, const St& s, Ser& c, bool acc) {
+    double U2[P + 1], M2[P + 1];
+    c.u[0] = s.u; c.u[1] = s.du;
+    c.m[0] = s.m; c.m[1] = s.dm;
+    {
+        double U3[P + 1], M3[P + 1];
+        for (int k = 0; k <= P; ++k) {
+            double su2 = 0.0, sm2 = 0.0;
+            for (int j = 0; j <= k; ++j) { su2 = fma(c.u[j], c.u[k - j], su2); sm2 = fma(c.m[j], c.m[k - j], sm2); }
+            U2[k] = su2; M2[k] = sm2;
+            double su3 = 0.0, sm3 = 0.0;
+            for (int j = 0; j <= k; ++j) { su3 = fma(U2[j], c.u[k - j], su3); sm3 = fma(M2[j], c.m[k - j], sm3); }
+            U3[k] = su3; M3[k] = sm3;
+            if (k + 2 <= P) {
+                const double inv = 1.0 / ((k + 1.0) * (k + 2.0));
+                c.u[k + 2] = (p.A2 * c.u[k] + 1.5 * p.A3 * U2[k] + 2.0 * p.A4 * U3[k]) * inv;
+                c.m[k + 2] = (p.B2 * c.m[k] + 2.0 * p.B4 * M3[k]) * inv;
+            }
+        }
+    }
+    if (!acc) return;
+    const double a = p.a, l = p.l, a2 = a * a;
+    double Du[P + 1], Sm[P + 1], Dt[P + 1], phr[P + 1], phm[P + 1], tr[P + 1], iu2[P + 1];
+    for (int k = 0; k <= P; ++k) {
+        double d0 = (k == 0) ? 1.0 : 0.0;
+        Du[k] = d0 - 2.0 * c.u[k] + a2 * U2[k];
+        Sm[k] = d0 - M2[k];
+        double sd = 0.0;
+        for (int j = 0; j <= k; ++j) sd = fma(U2[j], Du[k - j], sd);
+        Dt[k] = sd;
+    }
+    for (int k = 0; k <= P; ++k) {
+        double d0 = (k == 0) ? 1.0 : 0.0;
+        double u4 = 0.0;
+        for (int j = 0; j <= k; ++j) u4 = fma(U2[j], U2[k - j], u4);
+        double x = a * (d0 + (a2 - a * l) * U2[k]);
+        double y = d0 * l;
+        double z = d0 + (2.0 * a2 - a * l) * U2[k] + a2 * (a2 - a * l) * u4;
+        double w = d0;
+        for (int j = 0; j < k; ++j) {
+            x = fma(-phr[j], Du[k - j], x);
+            y = fma(-phm[j], Sm[k - j], y);
+            z = fma(-tr[j], Dt[k - j], z);
+            w = fma(-iu2[j], U2[k - j], w);
+        }
+        phr[k] = x / Du[0];
+        phm[k] = y / Sm[0];
+        tr[k] = z / Dt[0];
+        iu2[k] = w / U2[0];
+    }
+    c.t[0] = s.t; c.ph[0] = s.ph; c.lam[0] = s.lam;
+    for (int k = 0; k < P; ++k) {
+        const double inv = 1.0 / (k + 1.0);
+        c.t[k + 1] = (tr[k] + (k == 0 ? a * l - a2 : 0.0) + a2 * M2[k]) * inv;
+        c.ph[k + 1] = (phr[k] + phm[k] - (k == 0 ? a : 0.0)) * inv;
+        c.lam[k + 1] = (iu2[k] + a2 * M2[k]) * inv;
+    }
+}
+
+__device__ __forceinline__ double hv(const double* c, double h) {
+    double v = c[P];
+    for (int k = P - 1; k >= 0; --k) v = fma(v, h, c[k]);
+    return v;
+}
+__device__ __forceinline__ double hd(const double* c, double h) {
+    double v = P * c[P];
+    for (int k = P - 1; k >= 1; --k) v = fma(v, h, k * c[k]);
+    return v;
+}
+__device__ __forceinline__ double hdd(const double* c, double h) {
+    double v = P * (P - 1.0) * c[P];
+    for (int k = P - 1; k >= 2; --k) v = fma(v, h, k * (k - 1.0) * c[k]);
+    return v;
+}
+
+__device__ __forceinline__ double radius(const double* x) {
+    double r = 1e300;
+    for (int k = P - 1; k <= P; ++k)
+        if (x[k] != 0.0 && x[k - 8] != 0.0) r = fmin(r, pow(fabs(x[k - 8] / x[k]), 0.125));
+    return r;
+}
+
+// 0.2 x the smallest radius of convergence (truncation ~0.2^24 of the series
+// scale), capped so a step holds at most one radial and one polar turning point.
+__device__ double step_size(const Par& p, const Ser& c, const St& s, bool acc) {
+    double R = fmin(radius(c.u), radius(c.m));
+    if (acc) R = fmin(R, fmin(radius(c.t), fmin(radius(c.ph), radius(c.lam))));
+    double wu = sqrt(fabs(p.A2) + 3.0 * fabs(p.A3) * fabs(s.u) + 6.0 * fabs(p.A4) * s.u * s.u + 1e-30);
+    double wm = sqrt(fabs(p.B2) + 6.0 * fabs(p.B4) * s.m * s.m + 1e-30);
+    return fmin(0.2 * R, 0.5 / fmax(wu, wm));
+}
+
+__device__ St advance(const Ser& c, double h, bool acc) {
+    St s;
+    s.u = hv(c.u, h); s.du = hd(c.u, h);
+    s.m = hv(c.m, h); s.dm = hd(c.m, h);
+    if (acc) { s.t = hv(c.t, h); s.ph = hv(c.ph, h); s.lam = hv(c.lam, h); }
+    else { s.t = s.ph = s.lam = 0.0; }
+    return s;
+}
+
+// Root in [lo, hi] of series(s) - target (or of its derivative when `deriv`),
+// the end values bracketing it; safeguarded Newton, at most 100 iterations.
+__device__ double solve(const double* c, double target, double lo, double hi, bool deriv) {
+    double glo = (deriv ? hd(c, lo) : hv(c, lo)) - target;
+    if (glo == 0.0) return lo;
+    double ghi = (deriv ? hd(c, hi) : hv(c, hi)) - target;
+    double x = (ghi != glo) ? lo + (hi - lo) * glo / (glo - ghi) : 0.5 * (lo + hi);
+    for (int it = 0; it < 100; ++it) {
+        double gx = (deriv ? hd(c, x) : hv(c, x)) - target;
+        if (gx == 0.0) return x;
+        if ((gx > 0) == (glo > 0)) { lo = x; glo = gx; } else { hi = x; }
+        double d = deriv ? hdd(c, x) : hd(c, x);
+        double xn = (d != 0.0) ? x - gx / d : 0.5 * (lo + hi);
+        if (!(xn > lo && xn < hi)) xn = 0.5 * (lo + hi);
+        if (fabs(xn - x) <= 1e-16 * fmax(1.0, fabs(x))) { x = xn; break; }
+        x = xn;
+    }
+    return x;
+}
+
+constexpr int kMaxSteps = 200000;
+
+// First radial turning point in the direction su before the horizon / u = 0.
+__device__ bool find_turning(const Par& p, const St& s0, double su, double& ub) {
+    St s = s0;
+    ub = su > 0 ? p.uplus : 0.0;
+    Ser c;
+    for (int it = 0; it < kMaxSteps; ++it) {
+        taylor(p, s, c, false);
+        double h = step_size(p, c, s, false);
+        St e = advance(c, h, false);
+        bool past = su > 0 ? (e.u >= p.uplus) : (e.u <= 0.0);
+        if ((e.du > 0) != (s.du > 0) && e.du != 0.0 && !past) {
+            ub = hv(c.u, solve(c.u, 0.0, 0.0, h, true));
+            return true;
+        }
+        if (past) return false;
+        s = e;
+    }
+    return false;
+}
+
+struct PointOut {
+    double *u, *mu, *dt, *dphi, *lam;
+    int32_t *tpm, *tpr;
+    long long stride;   // element offset of this ray's first point
+};
+
+// GEOKERR sampler; returns the number of points written (0 on failure).
+__device__ int sample_points(const Par& p, double u0, double uf, double mu0, double su, double sm, int tpr_in,
+                             int nup, double offset, const PointOut& o) {
+    const double Uu0 = Uof(p, u0), Mm0 = Mof(p, mu0);
+    if (!(Uu0 >= 0.0) || !(Mm0 >= -1e-14) || nup <= 0) return 0;
+    const St s0{u0, su * sqrt(fmax(0.0, Uu0)), mu0, sm * sqrt(fmax(0.0, Mm0)), 0.0, 0.0, 0.0};
+    double ub;
+    int tpr = tpr_in;
+    if (!find_turning(p, s0, su, ub)) tpr = 0;
+    double UF = uf;
+    if (tpr == 1 && ((su > 0 && UF > ub) || (su < 0 && UF < ub))) UF = ub;
+    if (tpr == 1 && UF == ub) UF = u0;
+    double du = ((ub - u0) >= 0 ? 1.0 : -1.0) * su * ((ub - u0) + (2.0 * tpr - 1.0) * (ub - UF)) / (double)nup;
+    int kmax = (du == 0.0) ? 0 : min((int)((ub - u0) / du + offset), nup);
+    if (kmax <= 0 && tpr == 0) return 0;
+    const int last = tpr == 1 ? nup : min(kmax, nup);
+    St s = s0;
+    int next = 0, tp_mu = 0, tp_r = 0;
+    Ser c;
+    for (int it = 0; it < 2 * kMaxSteps && next < last; ++it) {
+        taylor(p, s, c, true);
+        double h = step_size(p, c, s, true);
+        St e = advance(c, h, true);
+        double s_r = -1.0, s_m = -1.0;
+        if ((e.du > 0) != (s.du > 0) && e.du != 0.0 && s.du != 0.0) s_r = solve(c.u, 0.0, 0.0, h, true);
+        if ((e.dm > 0) != (s.dm > 0) && e.dm != 0.0 && s.dm != 0.0) s_m = solve(c.m, 0.0, 0.0, h, true);
+        while (next < last) {
+            const int k = next + 1;
+            const bool branch2 = k > kmax;
+            const double ut = branch2 ? 2.0 * ub - (u0 + (k - offset) * du) : u0 + (k - offset) * du;
+            double lo = 0.0, hi = h;
+            if (s_r >= 0.0) { if (branch2) lo = s_r; else hi = s_r; }
+            else if (branch2 != (tp_r == 1)) break;
+            double ga = hv(c.u, lo) - ut, gb = hv(c.u, hi) - ut;
+            if ((ga > 0) == (gb > 0) && ga != 0.0 && gb != 0.0) break;
+            double x = solve(c.u, ut, lo, hi, false);
+            const long long i = o.stride + next;
+            o.u[i] = ut;
+            o.mu[i] = hv(c.m, x);
+            o.dt[i] = hv(c.t, x);
+            o.dphi[i] = hv(c.ph, x);
+            o.lam[i] = hv(c.lam, x);
+            o.tpm[i] = tp_mu + ((s_m >= 0.0 && x > s_m) ? 1 : 0);
+            o.tpr[i] = branch2 ? 1 : 0;
+            next++;
+        }
+        if (s_m >= 0.0) tp_mu++;
+        if (s_r >= 0.0) tp_r = 1;
+        bool past = su > 0 ? (e.u >= p.uplus) : (e.u <= 0.0);
+        if (past) break;
+        s = e;
+    }
+    return next == last ? last : 0;
+}
+
+__global__ void geokerr_points_kernel(int n, double a, const double* __restrict__ u0, const double* __restrict__ uf,
+                                      const double* __restrict__ mu0, const double* __restrict__ l,
+                                      const double* __restrict__ q2, const double* __restrict__ su,
+                                      const double* __restrict__ sm, int tpr, int nup, double offset,
+                                      double* u, double* mu, double* dt, double* dphi, double* lam,
+                                      int32_t* tpm, int32_t* tprv, int32_t* npts) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    Par p = make_par(a, l[i], q2[i], mu0[i]);
+    PointOut o{u, mu, dt, dphi, lam, tpm, tprv, (long long)i * nup};
+    int w = sample_points(p, u0[i], uf[i], mu0[i], su[i], sm[i], tpr, nup, offset, o);
+    if (npts) npts[i] = w;
+}
+
+// eval_lambda, step 1: GEOKERR points with the conventions of
+// geokerr_eval_lambda.f90:102-118 (SU from uf - u0, SM = -1 for mu0 > 0,
+// TPR = 1, OFFSET = 0.5, NUP = S).
+__global__ void eval_points_kernel(int n, double a, const double* __restrict__ u0, const double* __restrict__ mu0,
+                                   const double* __restrict__ uf, const double* __restrict__ Lz,
+                                   const double* __restrict__ Q2, int S, double* w_u, double* w_mu, double* w_dt,
+                                   double* w_dphi, double* w_lam, int32_t* w_tpm, int32_t* w_tpr, int32_t* w_n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double su = (uf[i] - u0[i]) >= 0.0 ? 1.0 : -1.0;
+    const double sm = mu0[i] <= 0.0 ? 1.0 : -1.0;
+    Par p = make_par(a, Lz[i], Q2[i], mu0[i]);
+    PointOut o{w_u, w_mu, w_dt, w_dphi, w_lam, w_tpm, w_tpr, (long long)i * S};
+    w_n[i] = sample_points(p, u0[i], uf[i], mu0[i], su, sm, 1, S, 0.5, o);
+}
+
+// eval_lambda, step 2: linear resampling onto lam0 + k dlam
+// (geokerr_eval_lambda.f90:125-199).
+__global__ void eval_resample_kernel(int n, int S, const double* __restrict__ u0, const double* __restrict__ mu0,
+                                     const double* __restrict__ t0, const double* __restrict__ lam0,
+                                     const double* __restrict__ dlam, const double* w_u, const double* w_mu,
+                                     const double* w_dt, const double* w_dphi, const double* w_lam,
+                                     const int32_t* w_tpm, const int32_t* w_tpr, const int32_t* w_n,
+                                     double* u, double* mu, double* t, double* phi, double* affine,
+                                     int32_t* tpmi, int32_t* tpri, int32_t* info) {
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    const long long b = (long long)r * S;
+    if (w_n[r] != S) {
+        for (int i = 0; i < S; ++i) {
+            u[b + i] = mu[b + i] = t[b + i] = phi[b + i] = affine[b + i] = nan("");
+        }
+        tpmi[r] = -1; tpri[r] = -1; info[r] = 2;
+        return;
+    }
+    const double* L = w_lam + b;
+    const double base = L[0];
+    int j = 0;
+    for (int i = 0; i < S; ++i) {
+        const double lamk = lam0[r] + dlam[r] * (double)i;
+        affine[b + i] = lamk;
+        while (j < S - 1 && (L[j + 1] - base) < lamk - 1.0e-30) j++;
+        double uu, mm, tt, pp;
+        if (lamk <= L[0] - base) {
+            uu = w_u[b]; mm = w_mu[b]; tt = t0[r] + w_dt[b]; pp = w_dphi[b];
+        } else if (lamk >= L[S - 1] - base) {
+            uu = w_u[b + S - 1]; mm = w_mu[b + S - 1]; tt = t0[r] + w_dt[b + S - 1]; pp = w_dphi[b + S - 1];
+        } else {
+            const double x0 = L[j] - base, x1 = L[j + 1] - base;
+            const double w = (x1 <= x0 + 1.0e-30) ? 0.0 : (lamk - x0) / (x1 - x0);
+            uu = (1.0 - w) * w_u[b + j] + w * w_u[b + j + 1];
+            mm = (1.0 - w) * w_mu[b + j] + w * w_mu[b + j + 1];
+            tt = t0[r] + ((1.0 - w) * w_dt[b + j] + w * w_dt[b + j + 1]);
+            pp = (1.0 - w) * w_dphi[b + j] + w * w_dphi[b + j + 1];
+        }
+        if (i == 0) { uu = u0[r]; mm = mu0[r]; }
+        u[b + i] = uu; mu[b + i] = mm; t[b + i] = tt; phi[b + i] = pp;
+    }
+    int tm = -1, tr = -1;
+    for (int jj = 0; jj < S && (tm < 0 || tr < 0); ++jj) {
+        if (tm < 0 && w_tpm[b + jj] > 0)
+            for (int i = 0; i < S; ++i) if (affine[b + i] >= L[jj] - base) { tm = i; break; }
+        if (tr < 0 && w_tpr[b + jj] > 0)
+            for (int i = 0; i < S; ++i) if (affine[b + i] >= L[jj] - base) { tr = i; break; }
+    }
+    tpmi[r] = tm; tpri[r] = tr; info[r] = 0;
+}
+
+// Exact samples at uniform Mino time (geokerr_stream_cuda).  Samples past
+// the horizon or past u = 0 repeat the last state reached.
+__global__ void stream_kernel(double u0, double uf, double mu0, double a, double L, double Q2, double lam0,
+                              double dlam, int S, double* u, double* mu, double* t, double* phi, double* aff) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    const double su = (uf - u0) >= 0.0 ? 1.0 : -1.0;
+    const double sm = mu0 <= 0.0 ? 1.0 : -1.0;
+    Par p = make_par(a, L, Q2, mu0);
+    St s{u0, su * sqrt(fmax(0.0, Uof(p, u0))), mu0, sm * sqrt(fmax(0.0, Mof(p, mu0))), 0.0, 0.0, 0.0};
+    double lam_a = 0.0;
+    int k = 0;
+    Ser c;
+    while (k < S && lam0 + k * dlam < 0.0) {   // before the start: the start state
+        u[k] = u0; mu[k] = mu0; t[k] = 0.0; phi[k] = 0.0; aff[k] = lam0 + k * dlam; ++k;
+    }
+    for (int it = 0; it < 2 * kMaxSteps && k < S; ++it) {
+        taylor(p, s, c, true);
+        double h = step_size(p, c, s, true);
+        while (k < S) {
+            double lk = lam0 + k * dlam;
+            if (lk > lam_a + h) break;
+            double x = lk - lam_a;
+            u[k] = hv(c.u, x); mu[k] = hv(c.m, x); t[k] = hv(c.t, x); phi[k] = hv(c.ph, x); aff[k] = lk;
+            ++k;
+        }
+        St e = advance(c, h, true);
+        if (e.u >= p.uplus || e.u <= 0.0 || !isfinite(e.t)) {
+            double uu = k > 0 ? u[k - 1] : u0, mm = k > 0 ? mu[k - 1] : mu0;
+            double tt = k > 0 ? t[k - 1] : 0.0, pp = k > 0 ? phi[k - 1] : 0.0;
+            for (; k < S; ++k) { u[k] = uu; mu[k] = mm; t[k] = tt; phi[k] = pp; aff[k] = lam0 + k * dlam; }
+            break;
+        }
+        s = e;
+        lam_a += h;
+    }
+    if (S > 0) { u[0] = u0; mu[0] = mu0; }   // exact seeding of sample 0 (geokerr_stream.cu:86-89)
+}
+
+// Mino time from u0 to the first arrival at uf and mu there; ncase 1 when
+// uf is reached before a radial turning point, 2 after it, 3 when the ray
+// has no turning point (it falls in or escapes).
+__global__ void complete_kernel(int n, const double* __restrict__ u0, const double* __restrict__ uf,
+                                const double* __restrict__ mu0, const double* __restrict__ a,
+                                const double* __restrict__ l, const double* __restrict__ q2,
+                                const int* __restrict__ su_in, const int* __restrict__ sm_in,
+                                double* lam_out, double* muf_out, int* ncase, char* valid) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    lam_out[i] = nan(""); muf_out[i] = nan(""); ncase[i] = 0; valid[i] = 0;
+    if (!(fabs(a[i]) < 1.0)) return;
+    const double su = su_in[i] >= 0 ? 1.0 : -1.0, sm = sm_in[i] >= 0 ? 1.0 : -1.0;
+    Par p = make_par(a[i], l[i], q2[i], mu0[i]);
+    const double Uu0 = Uof(p, u0[i]);
+    if (!(Uu0 >= 0.0)) return;
+    St s{u0[i], su * sqrt(fmax(0.0, Uu0)), mu0[i], sm * sqrt(fmax(0.0, Mof(p, mu0[i]))), 0.0, 0.0, 0.0};
+    double ub;
+    const bool has_tp = find_turning(p, s, su, ub);
+    const double target = uf[i];
+    double lam_a = 0.0;
+    bool passed = false;
+    Ser c;
+    for (int it = 0; it < kMaxSteps; ++it) {
+        taylor(p, s, c, false);
+        double h = step_size(p, c, s, false);
+        St e = advance(c, h, false);
+        double s_r = -1.0;
+        if ((e.du > 0) != (s.du > 0) && e.du != 0.0 && s.du != 0.0) s_r = solve(c.u, 0.0, 0.0, h, true);
+        double seg_lo[2] = {0.0, s_r}, seg_hi[2] = {s_r >= 0.0 ? s_r : h, h};
+        for (int g = 0; g < (s_r >= 0.0 ? 2 : 1); ++g) {
+            double ga = hv(c.u, seg_lo[g]) - target, gb = hv(c.u, seg_hi[g]) - target;
+            if (ga == 0.0 || gb == 0.0 || (ga > 0) != (gb > 0)) {
+                double x = solve(c.u, target, seg_lo[g], seg_hi[g], false);
+                lam_out[i] = lam_a + x;
+                muf_out[i] = hv(c.m, x);
+                ncase[i] = has_tp ? ((passed || g == 1) ? 2 : 1) : 3;
+                valid[i] = 1;
+                return;
+            }
+        }
+        if (s_r >= 0.0) passed = true;
+        if (e.u >= p.uplus || e.u <= 0.0) return;
+        s = e;
+        lam_a += h;
+    }
+}
+
+int grid(int n, int b) { return (n + b - 1) / b; }
+
+}  // namespace
+
+extern "C" {
+
+int np_geokerr_points_device(int n, double a, const double* u0, const double* uf, const double* mu0,
+                             const double* l, const double* q2, const double* su, const double* sm,
+                             int tpr, int nup, double offset, double* u, double* mu, double* dt, double* dphi,
+                             double* lam, int32_t* tpm, int32_t* tprv, int32_t* npts, void* stream) {
+    if (n < 0 || nup <= 0) return gk_fail(NP_ERR_INVALID, "bad sizes");
+    if (n == 0) return NP_OK;
+    if (!(fabs(a) < 1.0)) return gk_fail(NP_ERR_INVALID, "spin must satisfy |a| < 1");
+    geokerr_points_kernel<<<grid(n, 64), 64, 0, (cudaStream_t)stream>>>(n, a, u0, uf, mu0, l, q2, su, sm, tpr, nup,
+                                                                        offset, u, mu, dt, dphi, lam, tpm, tprv, npts);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? NP_OK : gk_fail(NP_ERR_KERNEL, "%s", cudaGetErrorString(e));
+}
+
+size_t np_geokerr_eval_lambda_work_bytes(int n, int S) {
+    if (n <= 0 || S <= 0) return 0;
+    return (size_t)n * S * (5 * sizeof(double) + 2 * sizeof(int32_t)) + (size_t)n * sizeof(int32_t) + 256;
+}
+
+int np_geokerr_eval_lambda_device(int n, double a, const double* u0, const double* mu0, const double* uf,
+                                  const double* Lz, const double* Q2, const double* t0, const double* lam0,
+                                  const double* dlam, int S, double* u, double* mu, double* t, double* phi,
+                                  double* affine, int32_t* tpmi, int32_t* tpri, int32_t* info, void* work,
+                                  void* stream) {
+    if (n < 0 || S <= 0) return gk_fail(NP_ERR_INVALID, "bad sizes");
+    if (n == 0) return NP_OK;
+    if (!(fabs(a) < 1.0)) return gk_fail(NP_ERR_INVALID, "spin must satisfy |a| < 1");
+    cudaStream_t st = (cudaStream_t)stream;
+    void* w = work;
+    bool own = false;
+    if (!w) {
+        if (cudaMalloc(&w, np_geokerr_eval_lambda_work_bytes(n, S)) != cudaSuccess)
+            return gk_fail(NP_ERR_ALLOC, "cudaMalloc of %zu bytes failed", np_geokerr_eval_lambda_work_bytes(n, S));
+        own = true;
+    }
+    const size_t m = (size_t)n * S;
+    double* wd = (double*)w;
+    double *w_u = wd, *w_mu = wd + m, *w_dt = wd + 2 * m, *w_dphi = wd + 3 * m, *w_lam = wd + 4 * m;
+    int32_t* wi = (int32_t*)(wd + 5 * m);
+    int32_t *w_tpm = wi, *w_tpr = wi + m, *w_n = wi + 2 * m;
+    eval_points_kernel<<<grid(n, 64), 64, 0, st>>>(n, a, u0, mu0, uf, Lz, Q2, S, w_u, w_mu, w_dt, w_dphi, w_lam,
+                                                  w_tpm, w_tpr, w_n);
+    eval_resample_kernel<<<grid(n, 64), 64, 0, st>>>(n, S, u0, mu0, t0, lam0, dlam, w_u, w_mu, w_dt, w_dphi, w_lam,
+                                                    w_tpm, w_tpr, w_n, u, mu, t, phi, affine, tpmi, tpri, info);
+    cudaError_t e = cudaGetLastError();
+    if (own) {
+        cudaError_t e2 = cudaStreamSynchronize(st);
+        cudaFree(w);
+        if (e == cudaSuccess) e = e2;
+    }
+    return e == cudaSuccess ? NP_OK : gk_fail(NP_ERR_KERNEL, "%s", cudaGetErrorString(e));
+}
+
+void geokerr_eval_lambda(double u0, double mu0, double uf, double a, double Lz, double Q2, double t0,
+                         double lam0, double dlam, int S, double* u, double* mu, double* t, double* phi,
+                         double* affine, int* tpmi, int* tpri, int* info) {
+    if (info) *info = 0;
+    if (S <= 0) { if (info) *info = 1; return; }
+    // one device block: 8 scalars in, 5 x S doubles + 3 ints out, work after
+    const size_t outb = 5 * (size_t)S * sizeof(double) + 3 * sizeof(int32_t);
+    const size_t inb = 8 * sizeof(double);
+    const size_t wb = np_geokerr_eval_lambda_work_bytes(1, S);
+    char* d = nullptr;
+    if (cudaMalloc(&d, inb + outb + wb + 512) != cudaSuccess) { if (info) *info = 3; return; }
+    double hin[8] = {u0, mu0, uf, Lz, Q2, t0, lam0, dlam};
+    double* din = (double*)d;
+    cudaMemcpy(din, hin, inb, cudaMemcpyHostToDevice);
+    double* dout = (double*)(d + 256);
+    int32_t* di = (int32_t*)(dout + 5 * (size_t)S);
+    void* dw = (void*)(((uintptr_t)(di + 3) + 255) & ~(uintptr_t)255);
+    int rc = np_geokerr_eval_lambda_device(1, a, din, din + 1, din + 2, din + 3, din + 4, din + 5, din + 6, din + 7,
+                                           S, dout, dout + S, dout + 2 * S, dout + 3 * S, dout + 4 * S,
+                                           di, di + 1, di + 2, dw, nullptr);
+    int32_t hi[3] = {-1, -1, 3};
+    if (rc == NP_OK && cudaDeviceSynchronize() == cudaSuccess) {
+        cudaMemcpy(u, dout, S * sizeof(double), cudaMemcpyDeviceToHost);
+        cudaMemcpy(mu, dout + S, S * sizeof(double), cudaMemcpyDeviceToHost);
+        cudaMemcpy(t, dout + 2 * S, S * sizeof(double), cudaMemcpyDeviceToHost);
+        cudaMemcpy(phi, dout + 3 * S, S * sizeof(double), cudaMemcpyDeviceToHost);
+        cudaMemcpy(affine, dout + 4 * S, S * sizeof(double), cudaMemcpyDeviceToHost);
+        cudaMemcpy(hi, di, 3 * sizeof(int32_t), cudaMemcpyDeviceToHost);
+    }
+    cudaFree(d);
+    if (tpmi) *tpmi = hi[0];
+    if (tpri) *tpri = hi[1];
+    if (info) *info = hi[2];
+}
+
+void geokerr_estimate_periods(double u0, double mu0, double a, double Lz, double Q2, double* Tr, double* Ttheta,
+                              int* info) {
+    const int nup = 4096;
+    if (Tr) *Tr = -1.0;
+    if (Ttheta) *Ttheta = -1.0;
+    if (info) *info = 0;
+    const size_t m = nup;
+    char* d = nullptr;
+    const size_t bytes = 8 * sizeof(double) + m * (5 * sizeof(double) + 2 * sizeof(int32_t)) + 1024;
+    if (cudaMalloc(&d, bytes) != cudaSuccess) { if (info) *info = 3; return; }
+    const double sm = mu0 <= 0.0 ? 1.0 : -1.0;
+    double hin[8] = {u0, u0, mu0, Lz, Q2, 1.0, sm, 0.0};
+    double* din = (double*)d;
+    cudaMemcpy(din, hin, sizeof(hin), cudaMemcpyHostToDevice);
+    double* dp = din + 8;
+    int32_t* di = (int32_t*)(dp + 5 * m);
+    int rc = np_geokerr_points_device(1, a, din, din + 1, din + 2, din + 3, din + 4, din + 5, din + 6, 1, nup, 0.5,
+                                      dp, dp + m, dp + 2 * m, dp + 3 * m, dp + 4 * m, di, di + m, di + 2 * m, nullptr);
+    if (rc == NP_OK && cudaDeviceSynchronize() == cudaSuccess) {
+        double* lam = new double[m];
+        int32_t* tpm = new int32_t[m];
+        int32_t* tpr = new int32_t[m];
+        int32_t n = 0;
+        cudaMemcpy(lam, dp + 4 * m, m * sizeof(double), cudaMemcpyDeviceToHost);
+        cudaMemcpy(tpm, di, m * sizeof(int32_t), cudaMemcpyDeviceToHost);
+        cudaMemcpy(tpr, di + m, m * sizeof(int32_t), cudaMemcpyDeviceToHost);
+        cudaMemcpy(&n, di + 2 * m, sizeof(int32_t), cudaMemcpyDeviceToHost);
+        if (n > 0) {
+            const double base = lam[0];
+            int m1 = -1, m2 = -1, r1 = -1, r2 = -1, pm = 0, pr = 0;
+            for (int j = 0; j < n; ++j) {
+                if (m1 < 0 && pm < 1 && tpm[j] >= 1) m1 = j;
+                if (m2 < 0 && pm < 2 && tpm[j] >= 2) m2 = j;
+                if (r1 < 0 && pr < 1 && tpr[j] >= 1) r1 = j;
+                if (r2 < 0 && pr < 2 && tpr[j] >= 2) r2 = j;
+                pm = std::max(pm, (int)tpm[j]); pr = std::max(pr, (int)tpr[j]);
+                if (m2 >= 0 && r2 >= 0) break;
+            }
+            if (Tr && r1 >= 0 && r2 >= 0) *Tr = 2.0 * std::max(1e-18, (lam[r2] - base) - (lam[r1] - base));
+            if (Ttheta && m1 >= 0 && m2 >= 0) *Ttheta = 2.0 * std::max(1e-18, (lam[m2] - base) - (lam[m1] - base));
+        }
+        delete[] lam; delete[] tpm; delete[] tpr;
+    } else if (info) {
+        *info = 3;
+    }
+    cudaFree(d);
+}
+
+double geokerr_phi_omega(double u0, double mu0, double a, double Lz, double Q2) {
+    (void)Q2;
+    double r = std::max(1e-12, 1.0 / std::max(1e-12, u0));
+    double Delta = std::max(1e-30, r * r - 2.0 * r + a * a);
+    double sin2 = std::max(1e-30, 1.0 - mu0 * mu0);
+    return a * (((r * r + a * a) - a * Lz) / Delta) + Lz / sin2 - a;
+}
+
+int geokerr_stream_cuda(double u0, double uf, double mu0, double a, double L, double Q2, double lam0, double dlam,
+                        int S, double* h_u, double* h_mu, double* h_t, double* h_phi, double* h_affine) {
+    if (S <= 0 || !h_u || !h_mu || !h_t || !h_phi || !h_affine || !(fabs(a) < 1.0)) return -1;
+    double* d = nullptr;
+    if (cudaMalloc(&d, 5 * (size_t)S * sizeof(double)) != cudaSuccess) return -2;
+    stream_kernel<<<1, 1>>>(u0, uf, mu0, a, L, Q2, lam0, dlam, S, d, d + S, d + 2 * S, d + 3 * S, d + 4 * S);
+    if (cudaDeviceSynchronize() != cudaSuccess) { cudaFree(d); return -3; }
+    cudaMemcpy(h_u, d, S * sizeof(double), cudaMemcpyDeviceToHost);
+    cudaMemcpy(h_mu, d + S, S * sizeof(double), cudaMemcpyDeviceToHost);
+    cudaMemcpy(h_t, d + 2 * S, S * sizeof(double), cudaMemcpyDeviceToHost);
+    cudaMemcpy(h_phi, d + 3 * S, S * sizeof(double), cudaMemcpyDeviceToHost);
+    cudaMemcpy(h_affine, d + 4 * S, S * sizeof(double), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    return 0;
+}
+
+int geokerr_complete_stream_cuda(double u0, double uf, double mu0, double a, double L, double Q2, double lam0,
+                                 double dlam, int S, double* h_u, double* h_mu, double* h_t, double* h_phi,
+                                 double* h_affine) {
+    if (S <= 0 || !h_u || !h_mu || !h_t || !h_phi || !h_affine || !(fabs(a) < 1.0)) return -1;
+    int tpmi = -1, tpri = -1, info = 0;
+    geokerr_eval_lambda(u0, mu0, uf, a, L, Q2, 0.0, lam0, dlam, S, h_u, h_mu, h_t, h_phi, h_affine, &tpmi, &tpri,
+                        &info);
+    if (info == 3) return -2;
+    return info == 0 ? 0 : -3;
+}
+
+void compute_geokerr_complete_cuda(const double* h_u0, const double* h_uf, const double* h_mu0, const double* h_a,
+                                   const double* h_l, const double* h_q2, const int* h_su, const int* h_sm,
+                                   double* h_lambda_results, double* h_muf_results, int* h_ncase_results,
+                                   char* h_valid_results, int n_cases) {
+    if (n_cases <= 0) return;
+    const size_t n = n_cases;
+    const size_t bytes = n * (8 * sizeof(double) + 3 * sizeof(int) + 1) + 1024;
+    char* d = nullptr;
+    if (cudaMalloc(&d, bytes) != cudaSuccess) {
+        for (size_t i = 0; i < n; ++i) h_valid_results[i] = 0;
+        return;
+    }
+    double* dd = (double*)d;
+    double *du0 = dd, *duf = dd + n, *dmu0 = dd + 2 * n, *da = dd + 3 * n, *dl = dd + 4 * n, *dq2 = dd + 5 * n;
+    double *dlam = dd + 6 * n, *dmuf = dd + 7 * n;
+    int* di = (int*)(dd + 8 * n);
+    int *dsu = di, *dsm = di + n, *dnc = di + 2 * n;
+    char* dv = (char*)(di + 3 * n);
+    cudaMemcpy(du0, h_u0, n * sizeof(double), cudaMemcpyHostToDevice);
+    cudaMemcpy(duf, h_uf, n * sizeof(double), cudaMemcpyHostToDevice);
+    cudaMemcpy(dmu0, h_mu0, n * sizeof(double), cudaMemcpyHostToDevice);
+    cudaMemcpy(da, h_a, n * sizeof(double), cudaMemcpyHostToDevice);
+    cudaMemcpy(dl, h_l, n * sizeof(double), cudaMemcpyHostToDevice);
+    cudaMemcpy(dq2, h_q2, n * sizeof(double), cudaMemcpyHostToDevice);
+    cudaMemcpy(dsu, h_su, n * sizeof(int), cudaMemcpyHostToDevice);
+    cudaMemcpy(dsm, h_sm, n * sizeof(int), cudaMemcpyHostToDevice);
+    complete_kernel<<<grid(n_cases, 64), 64>>>(n_cases, du0, duf, dmu0, da, dl, dq2, dsu, dsm, dlam, dmuf, dnc, dv);
+    if (cudaDeviceSynchronize() == cudaSuccess) {
+        cudaMemcpy(h_lambda_results, dlam, n * sizeof(double), cudaMemcpyDeviceToHost);
+        cudaMemcpy(h_muf_results, dmuf, n * sizeof(double), cudaMemcpyDeviceToHost);
+        cudaMemcpy(h_ncase_results, dnc, n * sizeof(int), cudaMemcpyDeviceToHost);
+        cudaMemcpy(h_valid_results, dv, n, cudaMemcpyDeviceToHost);
+    } else {
+        for (size_t i = 0; i < n; ++i) h_valid_results[i] = 0;
+    }
+    cudaFree(d);
+}
+
+}  // extern "C"

@@ -1,0 +1,121 @@
+"""Python entry points of the GEOKERR-equivalent solver (include/geokerr_c_api.h).
+
+The f90-compatible functions take and return host numpy arrays; the batched
+functions take torch CUDA tensors and run one geodesic per GPU thread.
+"""
+import ctypes as C
+
+import numpy as np
+
+from ._lib import load, check
+
+D, I, V = C.c_double, C.c_int, C.c_void_p
+_PROTOS = {
+    "geokerr_eval_lambda": (None, [D] * 9 + [I] + [V] * 5 + [C.POINTER(I)] * 3),
+    "geokerr_estimate_periods": (None, [D] * 5 + [C.POINTER(D), C.POINTER(D), C.POINTER(I)]),
+    "geokerr_phi_omega": (D, [D] * 5),
+    "geokerr_stream_cuda": (I, [D] * 8 + [I] + [V] * 5),
+    "geokerr_complete_stream_cuda": (I, [D] * 8 + [I] + [V] * 5),
+    "compute_geokerr_complete_cuda": (None, [V] * 12 + [I]),
+    "np_geokerr_points_device": (I, [I, D] + [V] * 7 + [I, I, D] + [V] * 8 + [V]),
+    "np_geokerr_eval_lambda_device": (I, [I, D] + [V] * 8 + [I] + [V] * 8 + [V, V]),
+    "np_geokerr_eval_lambda_work_bytes": (C.c_size_t, [I, I]),
+}
+
+
+def _lib():
+    lib = load()
+    if not getattr(lib, "_gk_ready", False):
+        for name, (res, args) in _PROTOS.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        lib._gk_ready = True
+    return lib
+
+
+def _vp(a):
+    return a.ctypes.data_as(V)
+
+
+def eval_lambda(u0, mu0, uf, a, Lz, Q2, t0, lam0, dlam, S):
+    """geokerr_eval_lambda on the GPU; returns a dict of numpy arrays."""
+    lib = _lib()
+    arrs = [np.zeros(S) for _ in range(5)]
+    tpmi, tpri, info = I(), I(), I()
+    lib.geokerr_eval_lambda(u0, mu0, uf, a, Lz, Q2, t0, lam0, dlam, S, *[_vp(x) for x in arrs],
+                            C.byref(tpmi), C.byref(tpri), C.byref(info))
+    return dict(u=arrs[0], mu=arrs[1], t=arrs[2], phi=arrs[3], affine=arrs[4],
+                tpmi=tpmi.value, tpri=tpri.value, info=info.value)
+
+
+def estimate_periods(u0, mu0, a, Lz, Q2):
+    lib = _lib()
+    tr, tt, info = D(), D(), I()
+    lib.geokerr_estimate_periods(u0, mu0, a, Lz, Q2, C.byref(tr), C.byref(tt), C.byref(info))
+    return tr.value, tt.value, info.value
+
+
+def phi_omega(u0, mu0, a, Lz, Q2):
+    return _lib().geokerr_phi_omega(u0, mu0, a, Lz, Q2)
+
+
+def stream(u0, uf, mu0, a, L, Q2, lam0, dlam, S, complete=False):
+    lib = _lib()
+    arrs = [np.zeros(S) for _ in range(5)]
+    fn = lib.geokerr_complete_stream_cuda if complete else lib.geokerr_stream_cuda
+    rc = fn(u0, uf, mu0, a, L, Q2, lam0, dlam, S, *[_vp(x) for x in arrs])
+    return rc, dict(u=arrs[0], mu=arrs[1], t=arrs[2], phi=arrs[3], affine=arrs[4])
+
+
+def complete(u0, uf, mu0, a, l, q2, su, sm):
+    lib = _lib()
+    n = len(u0)
+    f = lambda x: np.ascontiguousarray(x, np.float64)
+    i = lambda x: np.ascontiguousarray(x, np.int32)
+    ins = [f(u0), f(uf), f(mu0), f(a), f(l), f(q2), i(su), i(sm)]
+    lam, muf = np.zeros(n), np.zeros(n)
+    nc, valid = np.zeros(n, np.int32), np.zeros(n, np.int8)
+    lib.compute_geokerr_complete_cuda(*[_vp(x) for x in ins], _vp(lam), _vp(muf), _vp(nc), _vp(valid), n)
+    return lam, muf, nc, valid
+
+
+def _t(x):
+    return C.c_void_p(x.data_ptr()) if x is not None else None
+
+
+def points(a, u0, uf, mu0, l, q2, su, sm, tpr=1, nup=32, offset=0.5):
+    """Batched GEOKERR sampler on CUDA tensors; returns a dict of [n, nup] tensors."""
+    import torch
+    lib = _lib()
+    dev = torch.device("cuda")
+    cv = lambda x: torch.as_tensor(x, dtype=torch.float64, device=dev).contiguous()
+    ins = [cv(x) for x in (u0, uf, mu0, l, q2, su, sm)]
+    n = ins[0].numel()
+    out = {k: torch.zeros((n, nup), dtype=torch.float64, device=dev) for k in ("u", "mu", "dt", "dphi", "lam")}
+    out["tpm"] = torch.zeros((n, nup), dtype=torch.int32, device=dev)
+    out["tpr"] = torch.zeros((n, nup), dtype=torch.int32, device=dev)
+    out["n"] = torch.zeros(n, dtype=torch.int32, device=dev)
+    check(lib.np_geokerr_points_device(n, a, *[_t(x) for x in ins], tpr, nup, offset,
+                                       *[_t(out[k]) for k in ("u", "mu", "dt", "dphi", "lam", "tpm", "tpr", "n")],
+                                       C.c_void_p(torch.cuda.current_stream().cuda_stream)))
+    return out
+
+
+def eval_lambda_batch(a, u0, mu0, uf, Lz, Q2, t0, lam0, dlam, S):
+    """Batched geokerr_eval_lambda on CUDA tensors."""
+    import torch
+    lib = _lib()
+    dev = torch.device("cuda")
+    cv = lambda x: torch.as_tensor(x, dtype=torch.float64, device=dev).contiguous()
+    ins = [cv(x) for x in (u0, mu0, uf, Lz, Q2, t0, lam0, dlam)]
+    n = ins[0].numel()
+    out = {k: torch.zeros((n, S), dtype=torch.float64, device=dev) for k in ("u", "mu", "t", "phi", "affine")}
+    for k in ("tpmi", "tpri", "info"):
+        out[k] = torch.zeros(n, dtype=torch.int32, device=dev)
+    work = torch.empty(lib.np_geokerr_eval_lambda_work_bytes(n, S), dtype=torch.uint8, device=dev)
+    check(lib.np_geokerr_eval_lambda_device(n, a, *[_t(x) for x in ins], S,
+                                            *[_t(out[k]) for k in ("u", "mu", "t", "phi", "affine", "tpmi", "tpri",
+                                                                   "info")],
+                                            _t(work), C.c_void_p(torch.cuda.current_stream().cuda_stream)))
+    return out

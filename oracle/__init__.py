@@ -115,3 +115,81 @@ def metric_inv_derivs(lib, M, a, r, th):
     fn = lib.npo_metric_inv_derivs if hasattr(lib, "npo_metric_inv_derivs") else lib.npref_metric_inv_derivs
     fn(M, a, r, th, _vp(dr), _vp(dt))
     return dr, dt
+
+
+# ---------------------------------------------------------------------------
+# GEOKERR restatement (geokerr_oracle.cpp)
+
+def _geo_protos(lib):
+    if getattr(lib, "_geo_ready", False):
+        return
+    D, I, V = C.c_double, C.c_int, C.c_void_p
+    lib.npo_geokerr.argtypes = [D] * 8 + [I, I, D] + [V] * 7
+    lib.npo_geokerr.restype = I
+    lib.npo_geokerr_eval_lambda.argtypes = [D] * 9 + [I] + [V] * 5 + [C.POINTER(I)] * 3
+    lib.npo_geokerr_eval_lambda.restype = None
+    lib.npo_geokerr_estimate_periods.argtypes = [D] * 5 + [C.POINTER(D), C.POINTER(D), C.POINTER(I)]
+    lib.npo_geokerr_estimate_periods.restype = None
+    lib.npo_geokerr_phi_omega.argtypes = [D] * 5
+    lib.npo_geokerr_phi_omega.restype = D
+    lib.npo_geokerr_stream.argtypes = [D] * 8 + [I] + [V] * 5
+    lib.npo_geokerr_stream.restype = I
+    lib._geo_ready = True
+
+
+def geokerr_points(u0, uf, mu0, a, l, q2, su, sm, tpr=1, nup=32, offset=0.5):
+    """GEOKERR sampler: dict of u, mu, dt, dphi, lam, tpm, tpr arrays and n."""
+    lib = load()
+    _geo_protos(lib)
+    out = {k: np.zeros(nup) for k in ("u", "mu", "dt", "dphi", "lam")}
+    out["tpm"] = np.zeros(nup, np.int32)
+    out["tpr"] = np.zeros(nup, np.int32)
+    n = lib.npo_geokerr(u0, uf, mu0, a, l, q2, su, sm, tpr, nup, offset,
+                        *[_vp(out[k]) for k in ("u", "mu", "dt", "dphi", "lam", "tpm", "tpr")])
+    out["n"] = n
+    return out
+
+
+def geokerr_eval_lambda(u0, mu0, uf, a, Lz, Q2, t0, lam0, dlam, S):
+    lib = load()
+    _geo_protos(lib)
+    arrs = [np.zeros(S) for _ in range(5)]
+    tpmi, tpri, info = C.c_int(), C.c_int(), C.c_int()
+    lib.npo_geokerr_eval_lambda(u0, mu0, uf, a, Lz, Q2, t0, lam0, dlam, S, *[_vp(x) for x in arrs],
+                                C.byref(tpmi), C.byref(tpri), C.byref(info))
+    return dict(u=arrs[0], mu=arrs[1], t=arrs[2], phi=arrs[3], affine=arrs[4],
+                tpmi=tpmi.value, tpri=tpri.value, info=info.value)
+
+
+def geokerr_estimate_periods(u0, mu0, a, Lz, Q2):
+    lib = load()
+    _geo_protos(lib)
+    tr, tt, info = C.c_double(), C.c_double(), C.c_int()
+    lib.npo_geokerr_estimate_periods(u0, mu0, a, Lz, Q2, C.byref(tr), C.byref(tt), C.byref(info))
+    return tr.value, tt.value, info.value
+
+
+def geokerr_stream(u0, uf, mu0, a, L, Q2, lam0, dlam, S):
+    lib = load()
+    _geo_protos(lib)
+    arrs = [np.zeros(S) for _ in range(5)]
+    rc = lib.npo_geokerr_stream(u0, uf, mu0, a, L, Q2, lam0, dlam, S, *[_vp(x) for x in arrs])
+    return rc, dict(u=arrs[0], mu=arrs[1], t=arrs[2], phi=arrs[3], affine=arrs[4])
+
+
+def geokerr_camera_grid(a, mu0, n_alpha, n_beta, a1=-12.0, a2=12.0, b1=-12.0, b2=12.0, input_limit=1e-5):
+    """Constants of GEOKERR's standard rectangular camera grid
+    (geokerr_original.f:255-290): cell-centred alpha, beta; l, q2, su, sm."""
+    i = np.arange(n_alpha)
+    j = np.arange(n_beta)
+    al = a1 + (a2 - a1) * (i + 0.5) / n_alpha
+    be = b1 + (b2 - b1) * (j + 0.5) / n_beta
+    AL, BE = np.meshgrid(al, be, indexing="ij")
+    AL, BE = AL.ravel(), BE.ravel()
+    l = -AL * np.sqrt(1.0 - mu0 * mu0)
+    q2 = BE * BE - (a * a - AL * AL) * mu0 * mu0
+    q2 = np.where(np.abs(q2) < input_limit ** 2, 0.0, q2)
+    l = np.where(np.abs(l) < input_limit, 0.0, l)
+    sm = np.where((BE > 0) & (mu0 < 1.0), 1.0, -1.0)
+    su = np.ones_like(l)
+    return dict(alpha=AL, beta=BE, l=l, q2=q2, su=su, sm=sm)

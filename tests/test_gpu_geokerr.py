@@ -1,0 +1,98 @@
+"""GPU GEOKERR-equivalent solver against the CPU restatement (1e-12 relative,
+the bar of the GEOKERR grid configuration) and against the reference's golden
+vector (GEOKERR's own noise level), through the C ABI."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(HERE, "golden"))
+import geokerr_golden as gg  # noqa: E402
+import oracle  # noqa: E402
+from nullpath_gb300 import geokerr as gk  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+
+def _rel(x, y):
+    return np.max(np.abs(x - y) / np.maximum(np.abs(y), 1e-300))
+
+
+def test_eval_lambda_golden_and_oracle(cuda):
+    g = gg.read_cache()
+    args = (g["u0"], g["mu0"], g["uf"], g["a"], g["Lz"], g["Q2"], g["t0"], g["lam0"], g["dlam"], g["S"])
+    out = gk.eval_lambda(*args)
+    ref = oracle.geokerr_eval_lambda(*args)
+    assert out["info"] == 0 and (out["tpmi"], out["tpri"]) == (g["tpmi"], g["tpri"])
+    assert np.array_equal(out["affine"], g["affine"])
+    assert _rel(out["u"], g["u"]) < 2e-12 and _rel(out["mu"], g["mu"]) < 1e-13
+    assert np.max(np.abs(out["t"] - g["t"])) < 2e-11 and np.max(np.abs(out["phi"] - g["phi"])) < 1e-11
+    for k in ("u", "mu", "t", "phi"):
+        assert _rel(out[k], ref[k]) < 1e-12, k      # GPU vs CPU restatement
+
+
+def test_grid_points_match_oracle(cuda):
+    """GEOKERR standard camera grid (a=0.9, r_o=1e6 M, i=60 deg, [-12,12]^2, 32 points)."""
+    a, mu0, u0 = 0.9, 0.5, 1e-6
+    uplus = 1.0 / (1.0 + np.sqrt(1.0 - a * a))
+    g = oracle.geokerr_camera_grid(a, mu0, 16, 16)
+    n = g["l"].size
+    out = gk.points(a, np.full(n, u0), np.full(n, uplus), np.full(n, mu0), g["l"], g["q2"], g["su"], g["sm"],
+                    tpr=1, nup=32, offset=0.5)
+    got = {k: v.cpu().numpy() for k, v in out.items()}
+    assert (got["n"] == 32).all()
+    for i in range(n):
+        ref = oracle.geokerr_points(u0, uplus, mu0, a, g["l"][i], g["q2"][i], 1.0, g["sm"][i], 1, 32, 0.5)
+        assert ref["n"] == 32
+        for k in ("u", "mu", "dt", "dphi", "lam"):
+            assert _rel(got[k][i], ref[k]) < 1e-12, (i, k)
+        assert np.array_equal(got["tpm"][i], ref["tpm"]) and np.array_equal(got["tpr"][i], ref["tpr"])
+
+
+def test_eval_lambda_batch_matches_single(cuda):
+    rng = np.random.default_rng(5)
+    n, S = 24, 64
+    u0 = rng.uniform(0.02, 0.1, n)
+    mu0 = rng.uniform(-0.9, 0.9, n)
+    uf = rng.uniform(0.001, 0.01, n)
+    Lz = rng.uniform(-4, 4, n)
+    Q2 = rng.uniform(0.5, 20, n)
+    t0 = np.zeros(n)
+    lam0 = np.zeros(n)
+    dlam = np.full(n, 0.05)
+    out = gk.eval_lambda_batch(0.7, u0, mu0, uf, Lz, Q2, t0, lam0, dlam, S)
+    got = {k: v.cpu().numpy() for k, v in out.items()}
+    for i in range(n):
+        ref = oracle.geokerr_eval_lambda(u0[i], mu0[i], uf[i], 0.7, Lz[i], Q2[i], 0.0, 0.0, 0.05, S)
+        assert got["info"][i] == ref["info"]
+        if ref["info"] != 0:
+            continue
+        for k in ("u", "mu", "t", "phi"):
+            assert _rel(got[k][i], ref[k]) < 1e-12, (i, k)
+        assert (got["tpmi"][i], got["tpri"][i]) == (ref["tpmi"], ref["tpri"])
+
+
+def test_stream_and_complete(cuda):
+    rc, s = gk.stream(0.1, 0.01, 0.3, 0.5, 2.0, 4.0, 0.0, 0.01, 30)
+    rc2, r = oracle.geokerr_stream(0.1, 0.01, 0.3, 0.5, 2.0, 4.0, 0.0, 0.01, 30)
+    assert rc == 0 and rc2 == 0
+    for k in ("u", "mu", "t", "phi"):
+        assert _rel(s[k][1:], r[k][1:]) < 1e-12, k
+    # complete: Mino time to uf reproduces uf when streamed there
+    lam, muf, nc, valid = gk.complete([0.1], [0.05], [0.3], [0.5], [2.0], [4.0], [-1], [-1])
+    assert valid[0] == 1 and nc[0] == 3
+    rc, s = gk.stream(0.1, 0.01, 0.3, 0.5, 2.0, 4.0, float(lam[0]), 0.0, 2)
+    assert abs(s["u"][1] - 0.05) < 1e-12 and abs(s["mu"][1] - muf[0]) < 1e-12
+    rc, c = gk.stream(0.1, 0.01, 0.8, 0.5, 2.0, 4.0, 0.0, 0.0014652014652014652, 50, complete=True)
+    ref = oracle.geokerr_eval_lambda(0.1, 0.8, 0.01, 0.5, 2.0, 4.0, 0.0, 0.0, 0.0014652014652014652, 50)
+    assert rc == 0 and _rel(c["u"], ref["u"]) < 1e-12
+
+
+def test_estimate_periods_and_phi_omega(cuda):
+    assert gk.estimate_periods(0.1, 0.3, 0.5, 2.0, 4.0) == pytest.approx(
+        oracle.geokerr_estimate_periods(0.1, 0.3, 0.5, 2.0, 4.0), rel=1e-12)
+    lib = oracle.load()
+    oracle._geo_protos(lib)
+    assert gk.phi_omega(0.1, 0.8, 0.5, 2.0, 4.0) == lib.npo_geokerr_phi_omega(0.1, 0.8, 0.5, 2.0, 4.0)
