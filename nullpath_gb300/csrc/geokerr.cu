@@ -79,36 +79,57 @@ __host__ __device__ Par make_par(double a, double l, double q2, double mu0) {
     return p;
 }
 
-__device__ __forceinline__ double Uof(const Par& p, double u) { return 1.0 + u * u * (p.A2 + u * (p.A3 + u * p.A4)); }
-__device__ __forceinline__ double Mof(const Par& p, double m) { double m2 = m * m; return p.Q0 + m2 * (p.B2 + m2 * p.B4); }
+__host__ __device__ __forceinline__ double Uof(const Par& p, double u) { return 1.0 + u * u * (p.A2 + u * (p.A3 + u * p.A4)); }
+__host__ __device__ __forceinline__ double Mof(const Par& p, double m) { double m2 = m * m; return p.Q0 + m2 * (p.B2 + m2 * p.B4); }
+
+// Potentials at the start point, with rounding below zero (a start on a
+// turning point, as GEOMU's moved polar root makes it) clamped to zero;
+// returns false when the start is genuinely forbidden.
+__host__ __device__ __forceinline__ bool start_potentials(const Par& p, double u0, double mu0, double& U0, double& M0) {
+    U0 = Uof(p, u0);
+    M0 = Mof(p, mu0);
+    const double m2 = mu0 * mu0, u2 = u0 * u0;
+    const double su = 1.0 + u2 * (fabs(p.A2) + fabs(u0) * (fabs(p.A3) + fabs(u0) * fabs(p.A4)));
+    const double sm = fabs(p.Q0) + m2 * (fabs(p.B2) + m2 * fabs(p.B4));
+    if (!(U0 >= -1e-12 * su) || !(M0 >= -1e-12 * sm)) return false;
+    U0 = fmax(U0, 0.0);
+    M0 = fmax(M0, 0.0);
+    return true;
+}
 
 struct St { double u, du, m, dm, t, ph, lam; };
-struct Ser { double u[P + 1], m[P + 1], t[P + 1], ph[P + 1], lam[P + 1]; };
+// Series of one step plus the scratch series of the recurrences; one object
+// per thread, owned by the kernel frame (no callee-local arrays).
+struct Ser {
+    double u[P + 1], m[P + 1], t[P + 1], ph[P + 1], lam[P + 1];
+    double U2[P + 1], M2[P + 1], U3[P + 1], M3[P + 1];
+    double Du[P + 1], Sm[P + 1], Dt[P + 1], phr[P + 1], phm[P + 1], tr[P + 1], iu2[P + 1];
+};
 
 // Taylor coefficients of one step; `acc` adds the t, phi, lambda series.
-__device__ void taylor(const Par& p, const St& s, Ser& c, bool acc) {
-    double U2[P + 1], M2[P + 1];
+__host__ __device__ __forceinline__ void taylor(const Par& p, const St& s, Ser& c, bool acc) {
+    double* U2 = c.U2;
+    double* M2 = c.M2;
+    double* U3 = c.U3;
+    double* M3 = c.M3;
     c.u[0] = s.u; c.u[1] = s.du;
     c.m[0] = s.m; c.m[1] = s.dm;
-    {
-        double U3[P + 1], M3[P + 1];
-        for (int k = 0; k <= P; ++k) {
-            double su2 = 0.0, sm2 = 0.0;
-            for (int j = 0; j <= k; ++j) { su2 = fma(c.u[j], c.u[k - j], su2); sm2 = fma(c.m[j], c.m[k - j], sm2); }
-            U2[k] = su2; M2[k] = sm2;
-            double su3 = 0.0, sm3 = 0.0;
-            for (int j = 0; j <= k; ++j) { su3 = fma(U2[j], c.u[k - j], su3); sm3 = fma(M2[j], c.m[k - j], sm3); }
-            U3[k] = su3; M3[k] = sm3;
-            if (k + 2 <= P) {
-                const double inv = 1.0 / ((k + 1.0) * (k + 2.0));
-                c.u[k + 2] = (p.A2 * c.u[k] + 1.5 * p.A3 * U2[k] + 2.0 * p.A4 * U3[k]) * inv;
-                c.m[k + 2] = (p.B2 * c.m[k] + 2.0 * p.B4 * M3[k]) * inv;
-            }
+    for (int k = 0; k <= P; ++k) {
+        double su2 = 0.0, sm2 = 0.0;
+        for (int j = 0; j <= k; ++j) { su2 = fma(c.u[j], c.u[k - j], su2); sm2 = fma(c.m[j], c.m[k - j], sm2); }
+        U2[k] = su2; M2[k] = sm2;
+        double su3 = 0.0, sm3 = 0.0;
+        for (int j = 0; j <= k; ++j) { su3 = fma(U2[j], c.u[k - j], su3); sm3 = fma(M2[j], c.m[k - j], sm3); }
+        U3[k] = su3; M3[k] = sm3;
+        if (k + 2 <= P) {
+            const double inv = 1.0 / ((k + 1.0) * (k + 2.0));
+            c.u[k + 2] = (p.A2 * c.u[k] + 1.5 * p.A3 * U2[k] + 2.0 * p.A4 * U3[k]) * inv;
+            c.m[k + 2] = (p.B2 * c.m[k] + 2.0 * p.B4 * M3[k]) * inv;
         }
     }
     if (!acc) return;
     const double a = p.a, l = p.l, a2 = a * a;
-    double Du[P + 1], Sm[P + 1], Dt[P + 1], phr[P + 1], phm[P + 1], tr[P + 1], iu2[P + 1];
+    double *Du = c.Du, *Sm = c.Sm, *Dt = c.Dt, *phr = c.phr, *phm = c.phm, *tr = c.tr, *iu2 = c.iu2;
     for (int k = 0; k <= P; ++k) {
         double d0 = (k == 0) ? 1.0 : 0.0;
         Du[k] = d0 - 2.0 * c.u[k] + a2 * U2[k];
@@ -145,23 +166,23 @@ __device__ void taylor(const Par& p, const St& s, Ser& c, bool acc) {
     }
 }
 
-__device__ __forceinline__ double hv(const double* c, double h) {
+__host__ __device__ __forceinline__ double hv(const double* c, double h) {
     double v = c[P];
     for (int k = P - 1; k >= 0; --k) v = fma(v, h, c[k]);
     return v;
 }
-__device__ __forceinline__ double hd(const double* c, double h) {
+__host__ __device__ __forceinline__ double hd(const double* c, double h) {
     double v = P * c[P];
     for (int k = P - 1; k >= 1; --k) v = fma(v, h, k * c[k]);
     return v;
 }
-__device__ __forceinline__ double hdd(const double* c, double h) {
+__host__ __device__ __forceinline__ double hdd(const double* c, double h) {
     double v = P * (P - 1.0) * c[P];
     for (int k = P - 1; k >= 2; --k) v = fma(v, h, k * (k - 1.0) * c[k]);
     return v;
 }
 
-__device__ __forceinline__ double radius(const double* x) {
+__host__ __device__ __forceinline__ double radius(const double* x) {
     double r = 1e300;
     for (int k = P - 1; k <= P; ++k)
         if (x[k] != 0.0 && x[k - 8] != 0.0) r = fmin(r, pow(fabs(x[k - 8] / x[k]), 0.125));
@@ -170,7 +191,7 @@ __device__ __forceinline__ double radius(const double* x) {
 
 // 0.2 x the smallest radius of convergence (truncation ~0.2^24 of the series
 // scale), capped so a step holds at most one radial and one polar turning point.
-__device__ double step_size(const Par& p, const Ser& c, const St& s, bool acc) {
+__host__ __device__ double step_size(const Par& p, const Ser& c, const St& s, bool acc) {
     double R = fmin(radius(c.u), radius(c.m));
     if (acc) R = fmin(R, fmin(radius(c.t), fmin(radius(c.ph), radius(c.lam))));
     double wu = sqrt(fabs(p.A2) + 3.0 * fabs(p.A3) * fabs(s.u) + 6.0 * fabs(p.A4) * s.u * s.u + 1e-30);
@@ -178,7 +199,7 @@ __device__ double step_size(const Par& p, const Ser& c, const St& s, bool acc) {
     return fmin(0.2 * R, 0.5 / fmax(wu, wm));
 }
 
-__device__ St advance(const Ser& c, double h, bool acc) {
+__host__ __device__ St advance(const Ser& c, double h, bool acc) {
     St s;
     s.u = hv(c.u, h); s.du = hd(c.u, h);
     s.m = hv(c.m, h); s.dm = hd(c.m, h);
@@ -189,7 +210,7 @@ __device__ St advance(const Ser& c, double h, bool acc) {
 
 // Root in [lo, hi] of series(s) - target (or of its derivative when `deriv`),
 // the end values bracketing it; safeguarded Newton, at most 100 iterations.
-__device__ double solve(const double* c, double target, double lo, double hi, bool deriv) {
+__host__ __device__ double solve(const double* c, double target, double lo, double hi, bool deriv) {
     double glo = (deriv ? hd(c, lo) : hv(c, lo)) - target;
     if (glo == 0.0) return lo;
     double ghi = (deriv ? hd(c, hi) : hv(c, hi)) - target;
@@ -210,7 +231,7 @@ __device__ double solve(const double* c, double target, double lo, double hi, bo
 constexpr int kMaxSteps = 200000;
 
 // First radial turning point in the direction su before the horizon / u = 0.
-__device__ bool find_turning(const Par& p, const St& s0, double su, double& ub) {
+__host__ __device__ bool find_turning(const Par& p, const St& s0, double su, double& ub) {
     St s = s0;
     ub = su > 0 ? p.uplus : 0.0;
     Ser c;
@@ -236,11 +257,11 @@ struct PointOut {
 };
 
 // GEOKERR sampler; returns the number of points written (0 on failure).
-__device__ int sample_points(const Par& p, double u0, double uf, double mu0, double su, double sm, int tpr_in,
+__host__ __device__ int sample_points(const Par& p, double u0, double uf, double mu0, double su, double sm, int tpr_in,
                              int nup, double offset, const PointOut& o) {
-    const double Uu0 = Uof(p, u0), Mm0 = Mof(p, mu0);
-    if (!(Uu0 >= 0.0) || !(Mm0 >= -1e-14) || nup <= 0) return 0;
-    const St s0{u0, su * sqrt(fmax(0.0, Uu0)), mu0, sm * sqrt(fmax(0.0, Mm0)), 0.0, 0.0, 0.0};
+    double Uu0, Mm0;
+    if (nup <= 0 || !start_potentials(p, u0, mu0, Uu0, Mm0)) return 0;
+    const St s0{u0, su * sqrt(Uu0), mu0, sm * sqrt(Mm0), 0.0, 0.0, 0.0};
     double ub;
     int tpr = tpr_in;
     if (!find_turning(p, s0, su, ub)) tpr = 0;
@@ -380,7 +401,9 @@ __global__ void stream_kernel(double u0, double uf, double mu0, double a, double
     const double su = (uf - u0) >= 0.0 ? 1.0 : -1.0;
     const double sm = mu0 <= 0.0 ? 1.0 : -1.0;
     Par p = make_par(a, L, Q2, mu0);
-    St s{u0, su * sqrt(fmax(0.0, Uof(p, u0))), mu0, sm * sqrt(fmax(0.0, Mof(p, mu0))), 0.0, 0.0, 0.0};
+    double U0, M0;
+    start_potentials(p, u0, mu0, U0, M0);
+    St s{u0, su * sqrt(U0), mu0, sm * sqrt(M0), 0.0, 0.0, 0.0};
     double lam_a = 0.0;
     int k = 0;
     Ser c;
@@ -424,9 +447,9 @@ __global__ void complete_kernel(int n, const double* __restrict__ u0, const doub
     if (!(fabs(a[i]) < 1.0)) return;
     const double su = su_in[i] >= 0 ? 1.0 : -1.0, sm = sm_in[i] >= 0 ? 1.0 : -1.0;
     Par p = make_par(a[i], l[i], q2[i], mu0[i]);
-    const double Uu0 = Uof(p, u0[i]);
-    if (!(Uu0 >= 0.0)) return;
-    St s{u0[i], su * sqrt(fmax(0.0, Uu0)), mu0[i], sm * sqrt(fmax(0.0, Mof(p, mu0[i]))), 0.0, 0.0, 0.0};
+    double U0, M0;
+    if (!start_potentials(p, u0[i], mu0[i], U0, M0)) return;
+    St s{u0[i], su * sqrt(U0), mu0[i], sm * sqrt(M0), 0.0, 0.0, 0.0};
     double ub;
     const bool has_tp = find_turning(p, s, su, ub);
     const double target = uf[i];

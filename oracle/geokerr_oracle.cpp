@@ -92,6 +92,20 @@ static inline double Mfun(const Params& p, double m) {
     return p.Q0 + m2 * (p.B2 + m2 * p.B4);
 }
 
+// Potentials at the start, rounding below zero (a start on a turning point)
+// clamped to zero; false when the start is forbidden.
+static bool start_potentials(const Params& p, double u0, double mu0, double& U0, double& M0) {
+    U0 = Ufun(p, u0);
+    M0 = Mfun(p, mu0);
+    const double m2 = mu0 * mu0, u2 = u0 * u0;
+    const double su = 1.0 + u2 * (std::fabs(p.A2) + std::fabs(u0) * (std::fabs(p.A3) + std::fabs(u0) * std::fabs(p.A4)));
+    const double sm = std::fabs(p.Q0) + m2 * (std::fabs(p.B2) + m2 * std::fabs(p.B4));
+    if (!(U0 >= -1e-12 * su) || !(M0 >= -1e-12 * sm)) return false;
+    U0 = std::max(U0, 0.0);
+    M0 = std::max(M0, 0.0);
+    return true;
+}
+
 // State at the start of a step.
 struct State { double u, du, m, dm, t, ph, lam; };
 
@@ -243,9 +257,9 @@ static int geokerr(double u0, double uf, double mu0, double a, double l, double 
     Params p = make_params(a, l, q2, mu0);
     out.u.assign(nup, 0.0); out.mu.assign(nup, 0.0); out.dt.assign(nup, 0.0);
     out.dphi.assign(nup, 0.0); out.lam.assign(nup, 0.0); out.tpm.assign(nup, 0); out.tpr.assign(nup, 0);
-    const double Uu0 = Ufun(p, u0), Mm0 = Mfun(p, mu0);
-    if (!(Uu0 >= 0.0) || !(Mm0 >= -1e-14)) return 0;
-    State s0{u0, su * std::sqrt(std::max(0.0, Uu0)), mu0, sm * std::sqrt(std::max(0.0, Mm0)), 0.0, 0.0, 0.0};
+    double Uu0, Mm0;
+    if (!start_potentials(p, u0, mu0, Uu0, Mm0)) return 0;
+    State s0{u0, su * std::sqrt(Uu0), mu0, sm * std::sqrt(Mm0), 0.0, 0.0, 0.0};
 
     // Pass 1: find the radial turning point in the direction su before the
     // horizon (su > 0) or before u = 0 (su < 0).
@@ -435,7 +449,9 @@ int npo_geokerr_stream(double u0, double uf, double mu0, double a, double L, dou
     const double su = (uf - u0) >= 0.0 ? 1.0 : -1.0;
     const double sm = mu0 <= 0.0 ? 1.0 : -1.0;
     Params p = make_params(a, L, Q2, mu0);
-    State s{u0, su * std::sqrt(std::max(0.0, Ufun(p, u0))), mu0, sm * std::sqrt(std::max(0.0, Mfun(p, mu0))), 0, 0, 0};
+    double U0, M0;
+    start_potentials(p, u0, mu0, U0, M0);
+    State s{u0, su * std::sqrt(U0), mu0, sm * std::sqrt(M0), 0, 0, 0};
     double lam_a = 0.0;
     int k = 0;
     while (k < S && lam0 + k * dlam < 0.0) { u[k] = u0; mu[k] = mu0; t[k] = 0; phi[k] = 0; aff[k] = lam0 + k * dlam; ++k; }
