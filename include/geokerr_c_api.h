@@ -95,6 +95,16 @@ int np_geokerr_eval_lambda_device(int n, double a, const double* u0, const doubl
                                   int32_t* tpmi, int32_t* tpri, int32_t* info, void* work, void* stream);
 size_t np_geokerr_eval_lambda_work_bytes(int n, int S);
 
+/* Equatorial crossings (mu = 0; GEOR with muf = 0, geokerr_original.f:2672)
+ * of rays leaving (u0[i], mu0[i]) with constants l[i], q2[i] and initial
+ * signs su[i] (du/dlambda), sm[i] (dmu/dlambda): the first K crossings' u
+ * and phi (phi measured from the start) in xu[n][K], xphi[n][K], their count
+ * in nx[i] (-1 when the start is forbidden).  A ray ends at the horizon, at
+ * u <= u_end or after K crossings.  Device pointers; returns np_status. */
+int np_geokerr_equator_crossings_device(int n, double a, const double* u0, const double* mu0, const double* l,
+                                        const double* q2, const double* su, const double* sm, double u_end, int K,
+                                        double* xu, double* xphi, int32_t* nx, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

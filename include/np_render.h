@@ -150,7 +150,7 @@ int np_render_host(const np_scene_t* scene, int precision,
  * studies against the semi-analytic solver.  Ray i starts at pixel
  * coordinates (px[i], py[i]) (continuous, 0..width, 0..height).  Outputs
  * per ray (device pointers):
- *   consts[4*i+0..3] = p_t, p_phi, Carter Q, sign(p_r) at the camera
+ *   consts[4*i+0..3] = p_t, p_phi, p_r, p_theta at the camera
  *   cross[8*i + 2k], cross[8*i + 2k + 1] = r and phi of the k-th equatorial
  *       crossing (k < 4), 0 when absent
  *   status[i] = 0 escaped, 1 captured, 2 step cap; plus 16 * (crossings) */

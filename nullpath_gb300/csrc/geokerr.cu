@@ -481,6 +481,44 @@ __global__ void complete_kernel(int n, const double* __restrict__ u0, const doub
     }
 }
 
+// Equatorial crossings (mu = 0, GEOR with muf = 0) of rays leaving u0:
+// for each ray the first K crossings' u and phi, and their count.  A ray
+// ends at the horizon, at u <= u_end (escape) or after K crossings.
+__global__ void crossings_kernel(int n, double a, const double* __restrict__ u0, const double* __restrict__ mu0,
+                                 const double* __restrict__ l, const double* __restrict__ q2,
+                                 const double* __restrict__ su, const double* __restrict__ sm, double u_end, int K,
+                                 double* xu, double* xphi, int32_t* nx) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    for (int k = 0; k < K; ++k) { xu[(long long)i * K + k] = 0.0; xphi[(long long)i * K + k] = 0.0; }
+    nx[i] = 0;
+    Par p = make_par(a, l[i], q2[i], mu0[i]);
+    double U0, M0;
+    if (!start_potentials(p, u0[i], mu0[i], U0, M0)) { nx[i] = -1; return; }
+    St s{u0[i], su[i] * sqrt(U0), mu0[i], sm[i] * sqrt(M0), 0.0, 0.0, 0.0};
+    int found = 0;
+    Ser c;
+    for (int it = 0; it < kMaxSteps && found < K; ++it) {
+        taylor(p, s, c, true);
+        double h = step_size(p, c, s, true);
+        St e = advance(c, h, true);
+        // mu = 0 crossings inside the step (at most one: the step holds at most
+        // one polar turning point and |mu| < mu_+ keeps the sign changes apart)
+        if ((s.m > 0.0) != (e.m > 0.0) && s.m != 0.0) {
+            double x = solve(c.m, 0.0, 0.0, h, false);
+            double ux = hv(c.u, x);
+            if (ux > u_end && ux < p.uplus) {
+                xu[(long long)i * K + found] = ux;
+                xphi[(long long)i * K + found] = hv(c.ph, x);
+                ++found;
+            }
+        }
+        if (e.u >= p.uplus || e.u <= u_end || !isfinite(e.ph)) break;
+        s = e;
+    }
+    nx[i] = found;
+}
+
 int grid(int n, int b) { return (n + b - 1) / b; }
 
 }  // namespace
@@ -496,6 +534,18 @@ int np_geokerr_points_device(int n, double a, const double* u0, const double* uf
     if (!(fabs(a) < 1.0)) return gk_fail(NP_ERR_INVALID, "spin must satisfy |a| < 1");
     geokerr_points_kernel<<<grid(n, 64), 64, 0, (cudaStream_t)stream>>>(n, a, u0, uf, mu0, l, q2, su, sm, tpr, nup,
                                                                         offset, u, mu, dt, dphi, lam, tpm, tprv, npts);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? NP_OK : gk_fail(NP_ERR_KERNEL, "%s", cudaGetErrorString(e));
+}
+
+int np_geokerr_equator_crossings_device(int n, double a, const double* u0, const double* mu0, const double* l,
+                                        const double* q2, const double* su, const double* sm, double u_end, int K,
+                                        double* xu, double* xphi, int32_t* nx, void* stream) {
+    if (n < 0 || K <= 0) return gk_fail(NP_ERR_INVALID, "bad sizes");
+    if (n == 0) return NP_OK;
+    if (!(fabs(a) < 1.0)) return gk_fail(NP_ERR_INVALID, "spin must satisfy |a| < 1");
+    crossings_kernel<<<grid(n, 64), 64, 0, (cudaStream_t)stream>>>(n, a, u0, mu0, l, q2, su, sm, u_end, K, xu, xphi,
+                                                                   nx);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? NP_OK : gk_fail(NP_ERR_KERNEL, "%s", cudaGetErrorString(e));
 }

@@ -454,8 +454,7 @@ __global__ void trace_rays_kernel(const SceneDev s, int precision, int n, const 
     double E = -m.pt, L = m.pph;
     double Q = m.pth * m.pth + s.cos_cam * s.cos_cam * (L * L / (s.sin_cam * s.sin_cam) - s.a * s.a * E * E);
     if (consts) {
-        consts[4 * i + 0] = m.pt; consts[4 * i + 1] = m.pph; consts[4 * i + 2] = Q;
-        consts[4 * i + 3] = m.pr >= 0.0 ? 1.0 : -1.0;
+        consts[4 * i + 0] = m.pt; consts[4 * i + 1] = m.pph; consts[4 * i + 2] = m.pr; consts[4 * i + 3] = m.pth;
     }
     unsigned long long ev = 0;
     double xr[4] = {0, 0, 0, 0}, xphi[4] = {0, 0, 0, 0};

@@ -20,6 +20,7 @@ _PROTOS = {
     "np_geokerr_points_device": (I, [I, D] + [V] * 7 + [I, I, D] + [V] * 8 + [V]),
     "np_geokerr_eval_lambda_device": (I, [I, D] + [V] * 8 + [I] + [V] * 8 + [V, V]),
     "np_geokerr_eval_lambda_work_bytes": (C.c_size_t, [I, I]),
+    "np_geokerr_equator_crossings_device": (I, [I, D] + [V] * 6 + [D, I] + [V] * 3 + [V]),
 }
 
 
@@ -119,3 +120,42 @@ def eval_lambda_batch(a, u0, mu0, uf, Lz, Q2, t0, lam0, dlam, S):
                                                                    "info")],
                                             _t(work), C.c_void_p(torch.cuda.current_stream().cuda_stream)))
     return out
+
+
+def equator_crossings(a, u0, mu0, l, q2, su, sm, u_end=1e-3, K=4):
+    """First K equatorial crossings (u, phi) per ray on CUDA tensors."""
+    import torch
+    lib = _lib()
+    dev = torch.device("cuda")
+    cv = lambda x: torch.as_tensor(x, dtype=torch.float64, device=dev).contiguous()
+    ins = [cv(x) for x in (u0, mu0, l, q2, su, sm)]
+    n = ins[0].numel()
+    xu = torch.zeros((n, K), dtype=torch.float64, device=dev)
+    xphi = torch.zeros((n, K), dtype=torch.float64, device=dev)
+    nx = torch.zeros(n, dtype=torch.int32, device=dev)
+    check(lib.np_geokerr_equator_crossings_device(n, a, *[_t(x) for x in ins], u_end, K, _t(xu), _t(xphi), _t(nx),
+                                                  C.c_void_p(torch.cuda.current_stream().cuda_stream)))
+    return xu, xphi, nx
+
+
+def render_ray_constants(consts, scene):
+    """GEOKERR inputs (u0, mu0, l, q2, su, sm) of render rays from their camera
+    momenta (p_t, p_phi, p_r, p_theta) as returned by trace_rays: E = -p_t,
+    l = p_phi/(E M), q2 = Q/(E M)^2 with Carter's Q = p_theta^2 +
+    cos^2(theta) (L^2/sin^2(theta) - a^2 E^2); su = +1 for ingoing rays
+    (p_r < 0) and sm = -sign(p_theta), since mu = cos(theta)."""
+    import math
+    c = np.asarray(consts)
+    E, L, pr, pth = -c[:, 0], c[:, 1], c[:, 2], c[:, 3]
+    M = scene.mass
+    lunit = M if scene.units == 1 else 2.0 * M
+    r_cam = scene.r_cam * lunit
+    th = math.radians(scene.theta_deg)
+    a = scene.spin * M
+    Q = pth * pth + math.cos(th) ** 2 * (L * L / math.sin(th) ** 2 - a * a * E * E)
+    n = len(E)
+    u0 = np.full(n, M / r_cam)
+    mu0 = np.full(n, math.cos(th))
+    su = np.where(pr < 0, 1.0, -1.0)
+    sm = np.where(pth > 0, -1.0, 1.0)
+    return u0, mu0, L / (E * M), Q / (E * E * M * M), su, sm

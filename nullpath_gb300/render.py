@@ -69,7 +69,7 @@ def render_host(scene, precision="mixed", with_inv=False):
 
 def trace_rays(scene, px, py, precision="mixed"):
     """Traces rays through continuous image positions (px, py); returns a dict
-    of CUDA tensors: consts[n,4] (p_t, p_phi, Q, sign p_r), cross[n,4,2]
+    of CUDA tensors: consts[n,4] (p_t, p_phi, p_r, p_theta), cross[n,4,2]
     (r, phi of the first four equatorial crossings), status[n]."""
     import torch
     lib = load()

@@ -134,6 +134,8 @@ def _geo_protos(lib):
     lib.npo_geokerr_phi_omega.restype = D
     lib.npo_geokerr_stream.argtypes = [D] * 8 + [I] + [V] * 5
     lib.npo_geokerr_stream.restype = I
+    lib.npo_geokerr_crossings.argtypes = [D] * 8 + [I, V, V]
+    lib.npo_geokerr_crossings.restype = I
     lib._geo_ready = True
 
 
@@ -193,3 +195,11 @@ def geokerr_camera_grid(a, mu0, n_alpha, n_beta, a1=-12.0, a2=12.0, b1=-12.0, b2
     sm = np.where((BE > 0) & (mu0 < 1.0), 1.0, -1.0)
     su = np.ones_like(l)
     return dict(alpha=AL, beta=BE, l=l, q2=q2, su=su, sm=sm)
+
+
+def geokerr_crossings(u0, mu0, a, l, q2, su, sm, u_end=1e-3, K=4):
+    lib = load()
+    _geo_protos(lib)
+    xu, xphi = np.zeros(K), np.zeros(K)
+    n = lib.npo_geokerr_crossings(u0, mu0, a, l, q2, su, sm, u_end, K, _vp(xu), _vp(xphi))
+    return n, xu, xphi

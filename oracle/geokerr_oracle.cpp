@@ -480,6 +480,34 @@ int npo_geokerr_stream(double u0, double uf, double mu0, double a, double L, dou
     return 0;
 }
 
+// First K equatorial crossings (mu = 0; GEOR with muf = 0) of a ray leaving
+// (u0, mu0): u and phi of each, count returned (-1 when the start is
+// forbidden).  The ray ends at the horizon, at u <= u_end or after K crossings.
+int npo_geokerr_crossings(double u0, double mu0, double a, double l, double q2, double su, double sm, double u_end,
+                          int K, double* xu, double* xphi) {
+    using namespace geo;
+    for (int k = 0; k < K; ++k) { xu[k] = 0.0; xphi[k] = 0.0; }
+    Params p = make_params(a, l, q2, mu0);
+    double U0, M0;
+    if (!start_potentials(p, u0, mu0, U0, M0)) return -1;
+    State s{u0, su * std::sqrt(U0), mu0, sm * std::sqrt(M0), 0, 0, 0};
+    int found = 0;
+    for (int it = 0; it < 200000 && found < K; ++it) {
+        Series c;
+        taylor(p, s, c);
+        double h = step_size(p, c, s, true);
+        State e = advance(c, h);
+        if ((s.m > 0.0) != (e.m > 0.0) && s.m != 0.0) {
+            double x = solve(c.m, 0.0, 0.0, h, false);
+            double ux = horner(c.u, x);
+            if (ux > u_end && ux < p.uplus) { xu[found] = ux; xphi[found] = horner(c.ph, x); ++found; }
+        }
+        if (e.u >= p.uplus || e.u <= u_end || !std::isfinite(e.ph)) break;
+        s = e;
+    }
+    return found;
+}
+
 // geokerr_phi_omega (geokerr_eval_lambda.f90:299-306): dphi/dlambda at u0.
 double npo_geokerr_phi_omega(double u0, double mu0, double a, double Lz, double Q2) {
     (void)Q2;

@@ -712,10 +712,11 @@ int npo_trace_rays(const np_scene_t* sc, int n, const double* px, const double* 
                               : camera_static(f.M, f.a, f.r_cam, f.th_cam, f.ph_cam, d.nr, d.nth, d.nph);
             double E = -y0.pt, L = y0.pph;
             double Q = y0.pth * y0.pth + c * c * (L * L / (sn * sn) - f.a * f.a * E * E);
+            (void)Q;
             consts[4 * i + 0] = y0.pt;
             consts[4 * i + 1] = y0.pph;
-            consts[4 * i + 2] = Q;
-            consts[4 * i + 3] = (y0.pr >= 0.0) ? 1.0 : -1.0;
+            consts[4 * i + 2] = y0.pr;
+            consts[4 * i + 3] = y0.pth;
         }
         if (cross) for (int k = 0; k < 4; ++k) { cross[8 * i + 2 * k] = o.xr[k]; cross[8 * i + 2 * k + 1] = o.xphi[k]; }
         if (status) status[i] = o.status + 16 * std::min(o.crossings, 15);

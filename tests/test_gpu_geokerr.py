@@ -99,3 +99,22 @@ def test_estimate_periods_and_phi_omega(cuda):
     oracle._geo_protos(lib)
     assert gk.phi_omega(0.1, 0.8, 0.5, 2.0, 4.0) == pytest.approx(lib.npo_geokerr_phi_omega(0.1, 0.8, 0.5, 2.0, 4.0),
                                                                rel=1e-14)   # host FMA contraction may differ
+
+
+def test_equator_crossings_match_oracle(cuda):
+    rng = np.random.default_rng(11)
+    n = 64
+    a = 0.9
+    u0 = np.full(n, 0.02)
+    mu0 = rng.uniform(-0.6, 0.6, n)
+    l = rng.uniform(-6, 6, n)
+    q2 = rng.uniform(1, 40, n)
+    su = np.ones(n)
+    sm = np.where(rng.uniform(size=n) > 0.5, 1.0, -1.0)
+    xu, xphi, nx = gk.equator_crossings(a, u0, mu0, l, q2, su, sm, 1e-3, 4)
+    xu, xphi, nx = xu.cpu().numpy(), xphi.cpu().numpy(), nx.cpu().numpy()
+    for i in range(n):
+        k, ru, rphi = oracle.geokerr_crossings(u0[i], mu0[i], a, l[i], q2[i], su[i], sm[i], 1e-3, 4)
+        assert nx[i] == k, i
+        if k > 0:
+            assert _rel(xu[i, :k], ru[:k]) < 1e-12 and _rel(xphi[i, :k], rphi[:k]) < 1e-12, i

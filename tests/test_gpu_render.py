@@ -90,7 +90,7 @@ def test_trace_rays_constants_and_crossings(cuda):
     ref = oracle.trace_rays(sc, px, py)
     for prec in ("fp64", "mixed"):
         out = npx.trace_rays(sc, px, py, prec)
-        c = out["consts"].cpu().numpy()
+        c = out["consts"].cpu().numpy()       # p_t, p_phi, p_r, p_theta at the camera
         assert np.allclose(c, ref["consts"], rtol=1e-13, atol=1e-13)
         st = out["status"].cpu().numpy()
         agree = (st % 16 == ref["status"] % 16).mean()
