@@ -91,6 +91,48 @@ def cpu_baseline(threads=None, rows_every=45):
     return rays / dt, threads, desc
 
 
+def geokerr_grid_leg(n_side=128, nup=32, cpu_sample=1024):
+    """GEOKERR standard grid: a=0.9, r_o=1e6 M, i=60 deg, [-12,12]^2 alpha/beta,
+    n_side^2 geodesics x nup points on the GPU; the CPU restatement times a
+    bounded sample on all host cores and is the parity reference (max
+    normwise relative difference over the sample)."""
+    import numpy as np
+    import torch
+    from concurrent.futures import ThreadPoolExecutor
+    import oracle
+    from nullpath_gb300 import geokerr as gk
+    a, mu0, u0 = 0.9, 0.5, 1e-6
+    uplus = 1.0 / (1.0 + np.sqrt(1.0 - a * a))
+    g = oracle.geokerr_camera_grid(a, mu0, n_side, n_side)
+    n = g["l"].size
+    args = (a, np.full(n, u0), np.full(n, uplus), np.full(n, mu0), g["l"], g["q2"], g["su"], g["sm"])
+    gk.points(*args, tpr=1, nup=nup)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    out = gk.points(*args, tpr=1, nup=nup)
+    e1.record()
+    torch.cuda.synchronize()
+    gpu_ms = e0.elapsed_time(e1)
+    got = {k: v.cpu().numpy() for k, v in out.items()}
+    idx = np.linspace(0, n - 1, cpu_sample).astype(int)
+
+    def one(i):
+        return oracle.geokerr_points(u0, uplus, mu0, a, g["l"][i], g["q2"][i], 1.0, g["sm"][i], 1, nup, 0.5)
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=os.cpu_count()) as ex:
+        refs = list(ex.map(one, idx))
+    cpu_s = time.perf_counter() - t0
+    worst = 0.0
+    for i, ref in zip(idx, refs):
+        for k in ("u", "mu", "dt", "dphi", "lam"):
+            worst = max(worst, float(np.max(np.abs(got[k][i] - ref[k])) / max(np.max(np.abs(ref[k])), 1e-300)))
+    return {"geodesics": n, "points_per_geodesic": nup, "gpu_ms": gpu_ms,
+            "gpu_geodesics_per_s": n / (gpu_ms * 1e-3),
+            "cpu_geodesics_per_s": len(idx) / cpu_s, "cpu_cores": os.cpu_count(), "cpu_sample": len(idx),
+            "max_rel_diff_gpu_vs_cpu": worst, "all_sampled": bool((got["n"] == nup).all())}
+
+
 def run_reference(args):
     ws, rank = _dist()
     if rank != 0:
@@ -233,6 +275,23 @@ def run_ours(args):
             out["fp64_path"]["roofline"]["frac"] = out["fp64_path"]["roofline"]["achieved"] / \
                 out["fp64_path"]["roofline"]["peak"]
             out["mixed_over_fp64"] = out["value"] / ws / out["fp64_path"]["rays_per_s"]
+        if args.accuracy:
+            from nullpath_gb300 import accuracy
+            acc = {"reference_step_law": accuracy.crossing_error(sc, n=20000, precision=args.precision, seed=1)}
+            fine = sc.replace(step_scale=0.0025)
+            _, _, sf = npx.render(fine, args.precision, rgb=rgb, rcross=rc, stats=True)
+            _, _, sf = npx.render(fine, args.precision, rgb=rgb, rcross=rc, stats=True)
+            acc["step_0.0025"] = accuracy.crossing_error(fine, n=20000, precision=args.precision, seed=1)
+            acc["step_0.0025"]["rays_per_s"] = rays_per_step / ((sf.kernel_ms + sf.init_ms) * 1e-3)
+            from nullpath_gb300._abi import NP_INTEG_ADAPTIVE
+            adap = sc.replace(integrator=NP_INTEG_ADAPTIVE, rtol=1e-7)
+            _, _, sa = npx.render(adap, args.precision, rgb=rgb, rcross=rc, stats=True)
+            _, _, sa = npx.render(adap, args.precision, rgb=rgb, rcross=rc, stats=True)
+            acc["adaptive_rtol_1e-7"] = accuracy.crossing_error(adap, n=20000, precision=args.precision, seed=1)
+            acc["adaptive_rtol_1e-7"]["rays_per_s"] = rays_per_step / ((sa.kernel_ms + sa.init_ms) * 1e-3)
+            acc["adaptive_rtol_1e-7"]["mean_steps_per_ray"] = sa.steps / max(1, sa.rays)
+            out["error_vs_geokerr"] = acc
+            out["geokerr_grid"] = geokerr_grid_leg()
         if args.cpu_baseline:
             v, cores, desc = cpu_baseline()
             out["cpu_baseline"] = {"value": v, "unit": "rays/s", "cores": cores, "kind": "port", "sample": desc}
@@ -258,6 +317,7 @@ def main():
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--no-fp64-frame", dest="fp64_frame", action="store_false")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--no-accuracy", dest="accuracy", action="store_false")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)

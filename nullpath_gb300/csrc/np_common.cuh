@@ -46,6 +46,8 @@ struct SceneDev {
     // FP32 copies for the mixed tracer's per-step path
     float r_cam_hi, r_cam_lo, th_cam_hi, th_cam_lo, ph_cam_hi, ph_cam_lo;
     float r_plus_f, r_band_f, pi_lim_f, rin_f, rout_f, r_far_f, h_unit_f, inv_M_f;
+    float hmin_f, hmax_f, rtol_f, atol_f;
+    double hmin, hmax;         // adaptive step bounds (hmax scales with r in units of M)
     int island_batch;
 };
 

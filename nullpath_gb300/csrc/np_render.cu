@@ -142,6 +142,10 @@ int prepare_scene(const np_scene_t& sc, SceneDev& d) {
         d.pi_lim_f = 3.14159250f;              // largest float below pi - 1e-9
         d.rin_f = (float)d.rin; d.rout_f = (float)d.rout; d.r_far_f = (float)d.r_far;
         d.h_unit_f = (float)d.h_unit; d.inv_M_f = (float)(1.0 / d.M);
+        if (d.ref_units) { d.hmin = kHMin; d.hmax = kHMax; }
+        else { d.hmin = kHMin * d.M; d.hmax = 10.0 * d.h_unit; }
+        d.hmin_f = (float)d.hmin; d.hmax_f = (float)d.hmax;
+        d.rtol_f = (float)d.rtol; d.atol_f = (float)d.atol;
         d.island_batch = g_tune.island_batch;
     }
     const double M = d.M, a = d.a, r = d.r_cam, th = d.th_cam;
@@ -415,8 +419,8 @@ render_mixed_kernel(const SceneDev s, const InitSoA soa, float* __restrict__ srg
                 n_steps++; n_f64++; n_evals += 5;
             }
         } else if (have && !R.pending) {
-            int r = mray_step32(R, s, k);
-            if (r != STEP_PARK) { n_steps++; n_evals += 4; }
+            int r = s.integrator == NP_INTEG_ADAPTIVE ? mray_step32_adaptive(R, s, k) : mray_step32(R, s, k);
+            if (r != STEP_PARK) { n_steps++; n_evals += s.integrator == NP_INTEG_ADAPTIVE ? 11 : 4; }
             done = r == STEP_DONE;
         }
         if (done) {
@@ -477,7 +481,7 @@ __global__ void trace_rays_kernel(const SceneDev s, int precision, int n, const 
         R.pr = d_hl(m.pr); R.pth = d_hl(m.pth); R.E = d_hl(E); R.L = d_hl(L);
         mray_start(R, s, k);
         while (true) {
-            int r = mray_step32(R, s, k);
+            int r = s.integrator == NP_INTEG_ADAPTIVE ? mray_step32_adaptive(R, s, k) : mray_step32(R, s, k);
             if (r == STEP_PARK) r = mray_island(R, s, k) ? STEP_DONE : STEP_CONT;
             if (r == STEP_DONE) break;
         }

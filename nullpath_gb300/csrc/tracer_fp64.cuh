@@ -191,20 +191,24 @@ __device__ __forceinline__ bool fp64_advance(const SceneDev& s, RayFP64<REC>& R,
     double h_used = 0.0;
     St8 k1;
     if (s.integrator == NP_INTEG_ADAPTIVE) {
-        double hb = fmin(fmax(s.h_unit * scale, kHMin), kHMax);
+        // bounds: BH_RK_HMIN/HMAX (bh_common.h:245,253) for reference scenes;
+        // hmax scaled like the fixed step law for scenes in units of M
+        const double hmin = s.hmin, hmax = s.ref_units ? s.hmax : s.hmax * scale;
+        double hb = fmin(fmax(s.h_unit * scale, hmin), hmax);
         double h = (R.h_adapt > 0.0) ? R.h_adapt : hb;
-        h = fmin(fmax(h, kHMin), kHMax);
+        h = fmin(fmax(h, hmin), hmax);
         for (int att = 0; att < 8; ++att) {
             double ht = h;
             double fac = adaptive_ref(R.y, M, a, rp, ht, s.rtol, s.atol, k1);
             evals += 12;
             if (fac > 0.0) {
                 ok = true; h_used = ht;
-                R.h_adapt = fmin(fmax(ht * fac, kHMin), kHMax);
+                double sc2 = fmin(fmax(1.0, R.y.r / (0.5 * s.Rs)), 100.0);
+                R.h_adapt = fmin(fmax(ht * fac, hmin), s.ref_units ? s.hmax : s.hmax * sc2);
                 break;
             }
-            h = fmax(ht, kHMin);
-            if (h <= kHMin * 1.01) break;
+            h = fmax(ht, hmin);
+            if (h <= hmin * 1.01) break;
         }
     } else {
         h_used = s.h_unit * scale;

@@ -192,10 +192,11 @@ struct MRay {
     float k[5];                  // f(y) at the current state (first stage of the next step)
     HiLo E, L;                   // conserved momenta (p_t = -E, p_phi = L)
     RayK c;
-    float min_r, first_r, h_pend;
+    float min_r, first_r, h_pend, h_adapt;
     float disk[3];
     int step, orders, crossings, status;
     bool pending;                // parked for an FP64 island step of size h_pend
+    bool pend_halves;            // the island step is two half steps (adaptive mode)
     unsigned fp64_steps;
     float xr[PHI ? 4 : 1], xphi[PHI ? 4 : 1];
     double xr_d[PHI ? 4 : 1];
@@ -223,7 +224,7 @@ __device__ __forceinline__ void mray_start(MRay<PHI>& R, const SceneDev& s, cons
     R.r = HiLo{s.r_cam_hi, s.r_cam_lo};
     R.th = HiLo{s.th_cam_hi, s.th_cam_lo};
     R.ph = HiLo{s.ph_cam_hi, s.ph_cam_lo};
-    R.min_r = s.r_cam_hi; R.first_r = 0.0f; R.h_pend = 0.0f;
+    R.min_r = s.r_cam_hi; R.first_r = 0.0f; R.h_pend = 0.0f; R.h_adapt = 0.0f; R.pend_halves = false;
     R.disk[0] = R.disk[1] = R.disk[2] = 0.0f;
     R.step = 0; R.orders = 0; R.crossings = 0; R.status = 2;
     R.pending = false; R.fp64_steps = 0;
@@ -290,6 +291,11 @@ __device__ __forceinline__ bool mray_finish_step(MRay<PHI>& R, const SceneDev& s
 __device__ __forceinline__ float mray_h(const SceneDev& s, float r) {
     return s.h_unit_f * fminf(fmaxf(1.0f, r * s.inv_M_f), 100.0f);
 }
+// Largest adaptive step: BH_RK_HMAX (bh_common.h:253) for reference scenes,
+// 10 x the fixed step law for scenes in units of M.
+__device__ __forceinline__ float mray_hmax(const SceneDev& s, float r) {
+    return s.ref_units ? s.hmax_f : s.hmax_f * fminf(fmaxf(1.0f, r * s.inv_M_f), 100.0f);
+}
 
 // Result of an FP32 attempt.
 enum { STEP_CONT = 0, STEP_DONE = 1, STEP_PARK = 2 };
@@ -336,7 +342,14 @@ __device__ __forceinline__ bool mray_island(MRay<PHI>& R, const SceneDev& s, con
     const float k0r = R.k[0], k0t = R.k[1], k0p = R.k[4];
     const float h = R.h_pend;
     D5 y{hl_d(R.r), hl_d(R.th), hl_d(R.pr), hl_d(R.pth), PHI ? hl_d(R.ph) : 0.0};
-    D5 o = rk4_d(y, (double)h, hl_d(R.E), hl_d(R.L), s.a, s.M, s.r_plus, s.r_minus, PHI);
+    const double E = hl_d(R.E), L = hl_d(R.L);
+    D5 o;
+    if (R.pend_halves) {
+        o = rk4_d(y, 0.5 * (double)h, E, L, s.a, s.M, s.r_plus, s.r_minus, PHI);
+        o = rk4_d(o, 0.5 * (double)h, E, L, s.a, s.M, s.r_plus, s.r_minus, PHI);
+    } else {
+        o = rk4_d(y, (double)h, E, L, s.a, s.M, s.r_plus, s.r_minus, PHI);
+    }
     R.r = d_hl(o.r); R.th = d_hl(o.th); R.pr = d_hl(o.pr); R.pth = d_hl(o.pth);
     if (PHI) R.ph = d_hl(o.ph);
     R.pending = false;
@@ -374,6 +387,102 @@ __device__ __forceinline__ bool near_critical(double E, double L, double Q, doub
     double Del = r2 - 2.0 * M * r + a2;
     double R = P * P - Del * K;
     return fabs(R) / (E * E * r2 * r2) < 0.385 * db_thr / M;
+}
+
+// RK4 increments d = h/6 (k1 + 2 k2 + 2 k3 + k4) of (r, theta, p_r, p_theta[, phi])
+// from a (hi, lo) state whose first stage k1 is known.
+template <bool PHI>
+__device__ __forceinline__ void rk4_incr(const HiLo& r, const HiLo& th, const HiLo& pr, const HiLo& pth,
+                                         const float k1[5], float h, const RayK& c, const SpaceK& k, float d[5]) {
+    const float hh = 0.5f * h;
+    F5 k2 = rhs_f<PHI>(r.hi + fmaf(hh, k1[0], r.lo), th.hi + fmaf(hh, k1[1], th.lo),
+                       pr.hi + fmaf(hh, k1[2], pr.lo), pth.hi + fmaf(hh, k1[3], pth.lo), c, k);
+    F5 k3 = rhs_f<PHI>(r.hi + fmaf(hh, k2.r, r.lo), th.hi + fmaf(hh, k2.th, th.lo),
+                       pr.hi + fmaf(hh, k2.pr, pr.lo), pth.hi + fmaf(hh, k2.pth, pth.lo), c, k);
+    F5 k4 = rhs_f<PHI>(r.hi + fmaf(h, k3.r, r.lo), th.hi + fmaf(h, k3.th, th.lo),
+                       pr.hi + fmaf(h, k3.pr, pr.lo), pth.hi + fmaf(h, k3.pth, pth.lo), c, k);
+    const float h6 = h * (1.0f / 6.0f);
+    d[0] = h6 * (k1[0] + 2.0f * (k2.r + k3.r) + k4.r);
+    d[1] = h6 * (k1[1] + 2.0f * (k2.th + k3.th) + k4.th);
+    d[2] = h6 * (k1[2] + 2.0f * (k2.pr + k3.pr) + k4.pr);
+    d[3] = h6 * (k1[3] + 2.0f * (k2.pth + k3.pth) + k4.pth);
+    d[4] = PHI ? h6 * (k1[4] + 2.0f * (k2.ph + k3.ph) + k4.ph) : 0.0f;
+}
+
+__device__ __forceinline__ bool mray_alive(const SceneDev& s, float r, float th) {
+    return r > s.r_plus_f + 1e-6f * s.r_plus_f && th > 1e-7f && th < s.pi_lim_f;
+}
+
+// One accepted adaptive step (step doubling with the error norm and step
+// factors of bh_kerr.h:1058-1105 and the retry loop of render.cu:187-205),
+// or a park for an FP64 island.  The error is measured on the compensated
+// increments, |d_full - (d_half1 + d_half2)| / (atol + rtol max|y|) over
+// r, theta, p_r, p_theta, so FP32 rounding of the state does not enter it.
+template <bool PHI>
+__device__ __forceinline__ int mray_step32_adaptive(MRay<PHI>& R, const SceneDev& s, const SpaceK& k) {
+    if (R.step >= s.max_steps) { R.status = 2; return STEP_DONE; }
+    const float hb = fminf(fmaxf(mray_h(s, R.r.hi), s.hmin_f), mray_hmax(s, R.r.hi));
+    if ((s.islands & kIslandHorizon) && R.r.hi < s.r_band_f) {
+        R.pending = true; R.pend_halves = false; R.h_pend = hb;
+        return STEP_PARK;
+    }
+    float h = (R.h_adapt > 0.0f) ? R.h_adapt : hb;
+    h = fminf(fmaxf(h, s.hmin_f), mray_hmax(s, R.r.hi));
+    const HiLo r0 = R.r, th0 = R.th, pr0 = R.pr, pth0 = R.pth, ph0 = R.ph;
+    const float k0r = R.k[0], k0t = R.k[1], k0p = R.k[4];
+    const float rtol = s.rtol_f, atol = s.atol_f;
+#pragma unroll 1
+    for (int att = 0; att < 8; ++att) {
+        float dF[5], dA[5], dB[5];
+        rk4_incr<PHI>(r0, th0, pr0, pth0, R.k, h, R.c, k, dF);
+        rk4_incr<PHI>(r0, th0, pr0, pth0, R.k, 0.5f * h, R.c, k, dA);
+        HiLo r1 = r0, t1 = th0, p1 = pr0, q1 = pth0;
+        hl_add(r1, dA[0]); hl_add(t1, dA[1]); hl_add(p1, dA[2]); hl_add(q1, dA[3]);
+        F5 f1 = rhs_f<PHI>(r1.hi, t1.hi, p1.hi, q1.hi, R.c, k);
+        float k1b[5] = {f1.r, f1.th, f1.pr, f1.pth, f1.ph};
+        rk4_incr<PHI>(r1, t1, p1, q1, k1b, 0.5f * h, R.c, k, dB);
+        const float rF = r0.hi + dF[0], tF = th0.hi + dF[1];
+        const float r2 = r1.hi + dB[0], t2 = t1.hi + dB[1];
+        bool alive = mray_alive(s, rF, tF) && mray_alive(s, r1.hi, t1.hi) && mray_alive(s, r2, t2);
+        if (!alive) {
+            h *= 0.5f;
+        } else {
+            float e = 0.0f;
+            const float y0v[4] = {r0.hi, th0.hi, pr0.hi, pth0.hi};
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                float full = dF[i], half = dA[i] + dB[i];
+                float sc = atol + rtol * fmaxf(fabsf(y0v[i] + full), fabsf(y0v[i] + half));
+                // never ask for less than the FP32 rounding of the increments
+                // themselves (~8 ulp), or a tight rtol rejects every step
+                sc = fmaxf(sc, 5e-7f * (fabsf(full) + fabsf(dA[i]) + fabsf(dB[i])));
+                e = fmaxf(e, fabsf(full - half) / fmaxf(sc, 1e-30f));
+            }
+            if (e <= 1.0f) {
+                // accept the two half steps
+                R.r = r1; R.th = t1; R.pr = p1; R.pth = q1;
+                hl_add(R.r, dB[0]); hl_add(R.th, dB[1]); hl_add(R.pr, dB[2]); hl_add(R.pth, dB[3]);
+                if (PHI) { hl_add(R.ph, dA[4]); hl_add(R.ph, dB[4]); }
+                float fac = fminf(2.0f, 0.9f * __powf(fmaxf(1e-12f, e), -0.2f));
+                R.h_adapt = fminf(fmaxf(h * fac, s.hmin_f), mray_hmax(s, R.r.hi));
+                if (s.islands & kIslandTurning) {
+                    bool turn = ((pr0.hi > 0.0f) != (R.pr.hi > 0.0f)) || ((pth0.hi > 0.0f) != (R.pth.hi > 0.0f));
+                    if (turn) {
+                        R.r = r0; R.th = th0; R.pr = pr0; R.pth = pth0; R.ph = ph0;
+                        R.pending = true; R.pend_halves = true; R.h_pend = h;
+                        return STEP_PARK;
+                    }
+                }
+                return mray_finish_step(R, s, k, h, r0, th0, k0r, k0t, ph0, k0p) ? STEP_DONE : STEP_CONT;
+            }
+            h *= fmaxf(0.1f, 0.9f * __powf(fmaxf(1e-12f, e), -0.25f));
+        }
+        h = fmaxf(h, s.hmin_f);
+        if (h <= s.hmin_f * 1.01f) break;
+    }
+    R.step++;
+    R.status = 1;                 // no acceptable step: the reference counts the ray as captured
+    return STEP_DONE;
 }
 
 // ---------------------------------------------------------------------------

@@ -537,19 +537,24 @@ static void trace(const Frame& f, const Dir& d, bool track_inv, RayOut& o) {
         double h_used = 0.0;
         State k1{};
         if (f.integrator == NP_INTEG_ADAPTIVE) {
-            double hb = std::fmin(std::fmax(f.h_unit * scale, kHMin), kHMax);
+            // BH_RK_HMIN/HMAX for reference scenes; in units of M the largest
+            // step is 10 x the fixed step law at the current radius
+            const double hmin = f.ref_units ? kHMin : kHMin * f.M;
+            const double hmax = f.ref_units ? kHMax : 10.0 * f.h_unit * scale;
+            double hb = std::fmin(std::fmax(f.h_unit * scale, hmin), hmax);
             double h = (h_adapt > 0.0) ? h_adapt : hb;
-            h = std::fmin(std::fmax(h, kHMin), kHMax);
+            h = std::fmin(std::fmax(h, hmin), hmax);
             for (int att = 0; att < 8; ++att) {
                 double ht = h;
                 double fac = adaptive_step(y, f.M, f.a, ht, f.rtol, f.atol, &k1);
                 if (fac > 0.0) {
                     ok = true; h_used = ht;
-                    h_adapt = std::fmin(std::fmax(ht * fac, kHMin), kHMax);
+                    double sc2 = std::fmin(std::fmax(1.0, y.r / (0.5 * f.Rs)), 100.0);
+                    h_adapt = std::fmin(std::fmax(ht * fac, hmin), f.ref_units ? kHMax : 10.0 * f.h_unit * sc2);
                     break;
                 }
-                h = std::fmax(ht, kHMin);
-                if (h <= kHMin * 1.01) break;
+                h = std::fmax(ht, hmin);
+                if (h <= hmin * 1.01) break;
             }
         } else {
             h_used = f.h_unit * scale;
