@@ -159,6 +159,39 @@ int np_trace_rays_device(const np_scene_t* scene, int precision, int n,
                          double* d_consts, double* d_cross, int32_t* d_status,
                          void* stream);
 
+/* ------------------------------------------------------------------------
+ * Differentiable render (adjoint).  The image is the mean over samples of
+ * the scene's colours; gradients are taken with respect to (spin a/M,
+ * camera inclination theta in radians, disk gain, emissivity index q) by a
+ * reverse sweep through the RK4 steps with checkpoints every K steps.  The
+ * scene must use lengths in M, fixed-step RK4, Hermite crossings and the
+ * gradient sky.  Event changes (disk edges, capture, escape) are not
+ * differentiated. */
+typedef struct np_adjoint np_adjoint_t;
+
+typedef struct np_adjoint_stats {
+    double forward_ms;                 /* device time of the forward pass */
+    double backward_ms;                /* device time of the reverse sweep */
+    uint64_t workspace_bytes;          /* device bytes held by the handle */
+    uint64_t checkpoint_bytes_per_ray; /* checkpoint storage per ray */
+} np_adjoint_stats_t;
+
+np_adjoint_t* np_adjoint_create(void);
+void np_adjoint_destroy(np_adjoint_t* handle);
+
+/* Forward pass: renders the mean image d_img [3][H][W] and keeps the
+ * checkpoints in the handle.  d_sample_rgb [spp][3][H][W] and d_sample_sig
+ * [spp][H][W] (status + 4 * disk hits per sample) are written when non-NULL.
+ * precision: NP_PREC_MIXED integrates in FP32, NP_PREC_FP64 in FP64. */
+int np_adjoint_forward(np_adjoint_t* handle, const np_scene_t* scene, int precision, int K, float* d_img,
+                       float* d_sample_rgb, int32_t* d_sample_sig, void* stream, np_adjoint_stats_t* stats);
+
+/* Reverse sweep for the upstream gradient d_grad_img = dLoss/d_img
+ * [3][H][W]; writes dLoss/d(spin, theta_rad, gain, q) to h_grad4 (host).
+ * Synchronises the stream. */
+int np_adjoint_backward(np_adjoint_t* handle, const float* d_grad_img, double* h_grad4, void* stream,
+                        np_adjoint_stats_t* stats);
+
 /* Largest pass (width * height * spp rays) np_render_device_noalloc accepts. */
 #define NP_NOALLOC_MAX_RAYS 262144
 

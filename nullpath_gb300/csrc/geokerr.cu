@@ -31,6 +31,8 @@
 #include "geokerr_c_api.h"
 #include "np_render.h"
 
+void np_record_error(const char* msg);
+
 namespace {
 
 thread_local std::string g_gk_error;
@@ -42,6 +44,7 @@ int gk_fail(int code, const char* fmt, ...) {
     vsnprintf(buf, sizeof(buf), fmt, ap);
     va_end(ap);
     g_gk_error = buf;
+    np_record_error(buf);
     return code;
 }
 

@@ -7,6 +7,9 @@
 
 #include "np_render.h"
 
+// Records the message np_last_error() returns (thread-local, np_render.cu).
+void np_record_error(const char* msg);
+
 namespace np {
 
 constexpr double kPi = 3.141592653589793238462643383279502884;

@@ -39,6 +39,12 @@ int fail(int code, const char* fmt, ...) {
     return code;
 }
 
+}  // namespace
+
+void np_record_error(const char* msg) { g_last_error = msg ? msg : ""; }
+
+namespace {
+
 #define NP_CU(expr, code)                                                          \
     do {                                                                           \
         cudaError_t e_ = (expr);                                                   \

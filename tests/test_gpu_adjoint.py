@@ -1,0 +1,62 @@
+"""Adjoint of the differentiable render against central finite differences
+(FP64, h = 1e-4, event structure held fixed) on the target/current pair of the
+differentiable-render configuration: target (a=0.7, theta=60 deg, gain=1,
+q=3), current (0.5, 50 deg, 0.8, 2.5), L2 loss, seed 2 (smaller image)."""
+import math
+
+import numpy as np
+import pytest
+
+import nullpath_gb300 as npx
+from nullpath_gb300 import diff
+
+pytestmark = pytest.mark.gpu
+
+
+def _scene(w=48, h=48, spp=2):
+    return npx.benchmark_scene(width=w, height=h, spp=spp, spin=0.5, seed=2)
+
+
+def _setup(prec, w=48, h=48, spp=2):
+    import torch
+    sc = _scene(w, h, spp)
+    target = diff.Adjoint().forward(diff.scene_with(sc, 0.7, math.radians(60.0), 1.0, 3.0), "fp64", 16)
+    params = torch.tensor([0.5, math.radians(50.0), 0.8, 2.5], dtype=torch.float64, requires_grad=True)
+    return sc, target, params
+
+
+@pytest.mark.parametrize("K", [16, 64, 256])
+def test_fp64_adjoint_matches_fd(cuda, K):
+    import torch
+    sc, target, params = _setup("fp64")
+    img = diff.render_diff(params, sc, "fp64", K)
+    loss = ((img.double() - target.double()) ** 2).sum()
+    loss.backward()
+    g = params.grad.numpy()
+    fd = diff.fd_gradient(sc, params.detach().numpy(), target, h=1e-4, precision="fp64")
+    rel = np.abs(g - fd) / np.maximum(np.abs(fd), 1e-12)
+    # 1e-3 relative per component (the differentiable-render acceptance bar)
+    assert (rel < 1e-3).all(), (K, g, fd, rel)
+
+
+def test_checkpoint_interval_does_not_change_gradient(cuda):
+    import torch
+    sc, target, _ = _setup("fp64")
+    grads = []
+    for K in (16, 64, 256):
+        params = torch.tensor([0.5, math.radians(50.0), 0.8, 2.5], dtype=torch.float64, requires_grad=True)
+        loss = ((diff.render_diff(params, sc, "fp64", K).double() - target.double()) ** 2).sum()
+        loss.backward()
+        grads.append(params.grad.numpy())
+    assert np.array_equal(grads[0], grads[1]) and np.array_equal(grads[0], grads[2])
+
+
+def test_fp32_adjoint_close_to_fd(cuda):
+    import torch
+    sc, target, params = _setup("mixed")
+    loss = ((diff.render_diff(params, sc, "mixed", 16).double() - target.double()) ** 2).sum()
+    loss.backward()
+    g = params.grad.numpy()
+    fd = diff.fd_gradient(sc, params.detach().numpy(), target, h=1e-4, precision="fp64")
+    rel = np.abs(g - fd) / np.maximum(np.abs(fd), 1e-12)
+    assert (rel < 2e-2).all(), (g, fd, rel)
