@@ -133,6 +133,46 @@ def geokerr_grid_leg(n_side=128, nup=32, cpu_sample=1024):
             "max_rel_diff_gpu_vs_cpu": worst, "all_sampled": bool((got["n"] == nup).all())}
 
 
+def adjoint_leg(Ks=(16, 64, 256)):
+    """Differentiable render, 256x256x4 from seed 2: target (0.7, 60 deg, 1, 3),
+    current (0.5, 50 deg, 0.8, 2.5), L2 loss.  FP32 adjoint per K (forward +
+    reverse sweep timed with CUDA events), forward-only mixed render of the same
+    scene for the cost ratio, and the gradient error against the event-masked
+    central FP64 FD (h = 1e-4)."""
+    import math
+    import numpy as np
+    import torch
+    import nullpath_gb300 as npx
+    from nullpath_gb300 import diff
+    sc = npx.benchmark_scene(width=256, height=256, spp=4, spin=0.5, seed=2)
+    rays = 256 * 256 * 4
+    p = [0.5, math.radians(50.0), 0.8, 2.5]
+    target = diff.Adjoint().forward(diff.scene_with(sc, 0.7, math.radians(60.0), 1.0, 3.0), "fp64", 16)
+    cur = diff.scene_with(sc, *p)
+    for _ in range(2):
+        npx.render(cur, "mixed")
+    _, _, fst = npx.render(cur, "mixed", stats=True)
+    fwd_ms = fst.kernel_ms + fst.init_ms
+    out = {"rays": rays, "forward_only_ms": fwd_ms, "forward_only_rays_per_s": rays / (fwd_ms * 1e-3), "K": {}}
+    fd = diff.fd_gradient(sc, np.array(p), target, h=1e-4, precision="fp64")
+    out["fd_gradient"] = fd.tolist()
+    for K in Ks:
+        adj = diff.Adjoint()
+        st = diff.AdjointStats()
+        for rep in range(2):
+            img = adj.forward(cur, "mixed", K, stats=st)
+            g = adj.backward(2.0 * (img - target), stats=st)
+        tot = st.forward_ms + st.backward_ms
+        rel = np.abs(g - fd) / np.maximum(np.abs(fd), 1e-12)
+        out["K"][str(K)] = {"forward_ms": st.forward_ms, "backward_ms": st.backward_ms,
+                            "fwd_adj_rays_per_s": rays / (tot * 1e-3), "cost_vs_forward": tot / fwd_ms,
+                            "workspace_bytes": int(st.workspace_bytes),
+                            "checkpoint_bytes_per_ray": int(st.checkpoint_bytes_per_ray),
+                            "gradient": g.tolist(), "max_rel_err_vs_fd": float(rel.max())}
+        adj.close()
+    return out
+
+
 def run_reference(args):
     ws, rank = _dist()
     if rank != 0:
@@ -292,6 +332,7 @@ def run_ours(args):
             acc["adaptive_rtol_1e-7"]["mean_steps_per_ray"] = sa.steps / max(1, sa.rays)
             out["error_vs_geokerr"] = acc
             out["geokerr_grid"] = geokerr_grid_leg()
+            out["adjoint_256x256x4"] = adjoint_leg()
         if args.cpu_baseline:
             v, cores, desc = cpu_baseline()
             out["cpu_baseline"] = {"value": v, "unit": "rays/s", "cores": cores, "kind": "port", "sample": desc}

@@ -48,7 +48,9 @@ def test_checkpoint_interval_does_not_change_gradient(cuda):
         loss = ((diff.render_diff(params, sc, "fp64", K).double() - target.double()) ** 2).sum()
         loss.backward()
         grads.append(params.grad.numpy())
-    assert np.array_equal(grads[0], grads[1]) and np.array_equal(grads[0], grads[2])
+    # the segment recomputation is a separate call site whose multiply-add
+    # contraction may round differently from the forward loop: 1e-9 relative
+    assert np.allclose(grads[0], grads[1], rtol=1e-9, atol=0) and np.allclose(grads[0], grads[2], rtol=1e-9, atol=0)
 
 
 def test_fp32_adjoint_close_to_fd(cuda):
