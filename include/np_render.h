@@ -187,10 +187,11 @@ int np_adjoint_forward(np_adjoint_t* handle, const np_scene_t* scene, int precis
                        float* d_sample_rgb, int32_t* d_sample_sig, void* stream, np_adjoint_stats_t* stats);
 
 /* Reverse sweep for the upstream gradient d_grad_img = dLoss/d_img
- * [3][H][W]; writes dLoss/d(spin, theta_rad, gain, q) to h_grad4 (host).
- * Synchronises the stream. */
-int np_adjoint_backward(np_adjoint_t* handle, const float* d_grad_img, double* h_grad4, void* stream,
-                        np_adjoint_stats_t* stats);
+ * [3][H][W]; writes dLoss/d(spin, theta_rad, gain, q) to h_grad4 (host) and,
+ * when d_sample_grad is non-NULL, each sample's contribution to it
+ * ([spp][H][W][4], device).  Synchronises the stream. */
+int np_adjoint_backward(np_adjoint_t* handle, const float* d_grad_img, double* h_grad4, double* d_sample_grad,
+                        void* stream, np_adjoint_stats_t* stats);
 
 /* Largest pass (width * height * spp rays) np_render_device_noalloc accepts. */
 #define NP_NOALLOC_MAX_RAYS 262144

@@ -758,8 +758,8 @@ int np_adjoint_forward(np_adjoint_t* h, const np_scene_t* scene, int precision, 
     return NP_OK;
 }
 
-int np_adjoint_backward(np_adjoint_t* h, const float* d_grad_img, double* h_grad4, void* stream_v,
-                        np_adjoint_stats_t* stats) {
+int np_adjoint_backward(np_adjoint_t* h, const float* d_grad_img, double* h_grad4, double* d_sample_grad,
+                        void* stream_v, np_adjoint_stats_t* stats) {
     if (!h || !d_grad_img || !h_grad4) return adj_fail(NP_ERR_INVALID, "NULL argument");
     if (!h->have_forward) return adj_fail(NP_ERR_INVALID, "np_adjoint_forward must run first");
     cudaStream_t st = (cudaStream_t)stream_v;
@@ -777,6 +777,10 @@ int np_adjoint_backward(np_adjoint_t* h, const float* d_grad_img, double* h_grad
     const size_t n = (size_t)s.total;
     double* hg = (double*)malloc(n * 4 * sizeof(double));
     if (!hg) return adj_fail(NP_ERR_ALLOC, "host allocation failed");
+    if (d_sample_grad) {
+        e = cudaMemcpyAsync(d_sample_grad, h->b.grad, n * 4 * sizeof(double), cudaMemcpyDeviceToDevice, st);
+        if (e != cudaSuccess) { free(hg); return adj_fail(NP_ERR_KERNEL, "%s", cudaGetErrorString(e)); }
+    }
     e = cudaMemcpyAsync(hg, h->b.grad, n * 4 * sizeof(double), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) { free(hg); return adj_fail(NP_ERR_KERNEL, "%s", cudaGetErrorString(e)); }

@@ -25,6 +25,57 @@ def _setup(prec, w=48, h=48, spp=2):
     return sc, target, params
 
 
+def test_per_sample_adjoint_matches_complex_step(cuda):
+    """FP64 per-sample gradients against the complex-step derivative of the
+    same discrete map (oracle/adjoint_cs.py) on 24 random disk samples.  The
+    oracle skips samples whose own complex step and central difference at
+    1e-7 disagree (maps that change faster than rounding can follow)."""
+    import torch
+    from oracle import adjoint_cs as cs
+    sc = diff.scene_with(_scene(64, 64, 2), 0.5, math.radians(50.0), 0.8, 2.5)
+    d = cs.scene_dict(sc)
+    adj = diff.Adjoint()
+    _, _, sig = adj.forward(sc, "fp64", 16, samples=True)
+    ps = torch.zeros((2, 64, 64, 4), dtype=torch.float64, device="cuda")
+    adj.backward(torch.ones((3, 64, 64), dtype=torch.float32, device="cuda"), per_sample=ps)
+    adj.close()
+    sig = sig.flatten().cpu().numpy()
+    ps = ps.reshape(-1, 4).cpu().numpy()
+    hits = np.flatnonzero(((sig & 3) != 1) & (sig >= 4))
+    rng = np.random.default_rng(7)
+    checked = 0
+    for idx in rng.permutation(hits)[:40]:
+        ref_sig, g = cs.sample_gradient(d, int(idx))
+        assert ref_sig == sig[idx]
+        y, x = divmod(int(idx) % 4096, 64)
+        sl = int(idx) // 4096
+        h = 1e-7
+        th0 = math.radians(50.0)
+        fp = cs.trace(d, 0.5, th0 + h, 2.5, x, y, sl)[3]
+        fm = cs.trace(d, 0.5, th0 - h, 2.5, x, y, sl)[3]
+        fd_t = (fp - fm) / (2 * h) * 0.8 * 2.2 / 2
+        if abs(fd_t - g[1]) > 1e-4 * abs(g[1]) + 1e-12:
+            continue
+        assert np.allclose(ps[idx], g, rtol=1e-6, atol=1e-12), (int(idx), ps[idx], g)
+        checked += 1
+        if checked == 24:
+            break
+    assert checked >= 20
+
+
+def test_gradient_check_at_scale(cuda):
+    """128x128x4: FP64 and FP32 adjoints against the event-masked FD over the
+    FD-resolved samples (1e-3 relative for FP64, 1e-2 for FP32)."""
+    sc, target, params = _setup("fp64", 128, 128, 4)
+    p = params.detach().numpy()
+    fd = diff.fd_gradient(sc, p, target, precision="fp64", per_sample=True)
+    r64 = diff.gradient_check(sc, p, target, precision="fp64", K=64, fd=fd)
+    assert max(r64["rel_err_resolved"]) < 1e-3, r64
+    assert max(r64["excluded_sample_frac"]) < 0.01, r64
+    r32 = diff.gradient_check(sc, p, target, precision="mixed", K=64, fd=fd)
+    assert max(r32["rel_err_resolved"]) < 1e-2, r32
+
+
 @pytest.mark.parametrize("K", [16, 64, 256])
 def test_fp64_adjoint_matches_fd(cuda, K):
     import torch
