@@ -11,7 +11,7 @@ from ._abi import (Scene, RenderStats, isco_radius, reference_defaults, benchmar
                    NP_JITTER_WANGHASH, NP_JITTER_STRATIFIED, NP_CAMERA_STATIC, NP_CAMERA_ZAMO,
                    NP_INTEG_RK4, NP_INTEG_ADAPTIVE, NP_CROSS_LINEAR, NP_CROSS_HERMITE,
                    NP_BG_GRADIENT, NP_BG_POINT, NP_ISLAND_HORIZON, NP_ISLAND_TURNING,
-                   NP_ISLAND_CRITICAL, NP_ISLANDS_ALL)
+                   NP_ISLAND_CRITICAL, NP_ISLANDS_ALL, NP_ISLANDS_DEFAULT)
 from ._lib import load, lib_path, NullPathError
 from .render import render, render_host, trace_rays, precision_code
 

@@ -21,6 +21,7 @@ NP_BG_GRADIENT, NP_BG_POINT = 0, 1
 NP_PREC_FP64, NP_PREC_MIXED = 0, 1
 NP_ISLAND_HORIZON, NP_ISLAND_TURNING, NP_ISLAND_CRITICAL = 1, 2, 4
 NP_ISLANDS_ALL = 7
+NP_ISLANDS_DEFAULT = NP_ISLAND_HORIZON | NP_ISLAND_CRITICAL
 
 
 class Scene(C.Structure):
@@ -86,7 +87,7 @@ def reference_defaults():
                  disk_on=1, disk_max_orders=1, disk_rin=0.0, disk_rout=0.0,
                  emissivity_q=2.0, disk_gain=1.0, crossing=NP_CROSS_LINEAR,
                  background=NP_BG_GRADIENT, bg_sigma_deg=1.0, bg_brightness=3.0,
-                 check_invariants=0, islands=NP_ISLANDS_ALL)
+                 check_invariants=0, islands=NP_ISLANDS_DEFAULT)
 
 
 def benchmark_scene(width=1280, height=720, spp=4, spin=0.9, seed=0):
@@ -101,4 +102,4 @@ def benchmark_scene(width=1280, height=720, spp=4, spin=0.9, seed=0):
                  disk_on=1, disk_max_orders=3, disk_rin=isco_radius(1.0, spin), disk_rout=20.0,
                  emissivity_q=3.0, disk_gain=1.0, crossing=NP_CROSS_HERMITE,
                  background=NP_BG_GRADIENT, bg_sigma_deg=1.0, bg_brightness=3.0,
-                 check_invariants=0, islands=NP_ISLANDS_ALL)
+                 check_invariants=0, islands=NP_ISLANDS_DEFAULT)

@@ -106,6 +106,9 @@ int prepare_scene(const np_scene_t& sc, SceneDev& d) {
     d.crossing = sc.crossing; d.bg_mode = sc.background; d.disk_on = sc.disk_on;
     d.check_inv = sc.check_invariants;
     d.islands = sc.islands;
+    // Step doubling at a tight rtol works at the FP32 precision floor where p_r
+    // or p_theta changes sign; its turning-point steps are always FP64.
+    if (sc.integrator == NP_INTEG_ADAPTIVE) d.islands |= NP_ISLAND_TURNING;
     if (d.ref_units) {
         float Mf = (float)sc.mass, Rsf = 2.0f * Mf;
         float af = (float)sc.spin * Mf, rcf = (float)sc.r_cam * Rsf;
@@ -626,7 +629,7 @@ void np_scene_defaults(np_scene_t* s) {
     s->emissivity_q = 2.0; s->disk_gain = 1.0;
     s->crossing = NP_CROSS_LINEAR; s->background = NP_BG_GRADIENT;
     s->bg_sigma_deg = 1.0; s->bg_brightness = 3.0;
-    s->check_invariants = 0; s->islands = NP_ISLANDS_ALL;
+    s->check_invariants = 0; s->islands = NP_ISLANDS_DEFAULT;
 }
 
 double np_isco_radius(double mass, double spin) {

@@ -128,10 +128,9 @@ __device__ __forceinline__ D5 add5(const D5& y, double h, const D5& k) {
     return D5{y.r + h * k.r, y.th + h * k.th, y.pr + h * k.pr, y.pth + h * k.pth, y.ph + h * k.ph};
 }
 
-// One FP64 RK4 step of the Carter system.
-__device__ __forceinline__ D5 rk4_d(const D5& y, double h, double E, double L, double a, double M,
-                                    double rp, double rm, bool phi) {
-    D5 k1 = rhs_d(y, E, L, a, M, rp, rm);
+// One FP64 RK4 step of the Carter system whose first stage k1 = f(y) is known.
+__device__ __forceinline__ D5 rk4_d_k1(const D5& y, const D5& k1, double h, double E, double L, double a,
+                                       double M, double rp, double rm, bool phi) {
     D5 k2 = rhs_d(add5(y, 0.5 * h, k1), E, L, a, M, rp, rm);
     D5 k3 = rhs_d(add5(y, 0.5 * h, k2), E, L, a, M, rp, rm);
     D5 k4 = rhs_d(add5(y, h, k3), E, L, a, M, rp, rm);
@@ -143,6 +142,11 @@ __device__ __forceinline__ D5 rk4_d(const D5& y, double h, double E, double L, d
     o.pth = y.pth + h6 * (k1.pth + 2.0 * (k2.pth + k3.pth) + k4.pth);
     o.ph = phi ? y.ph + h6 * (k1.ph + 2.0 * (k2.ph + k3.ph) + k4.ph) : y.ph;
     return o;
+}
+
+__device__ __forceinline__ D5 rk4_d(const D5& y, double h, double E, double L, double a, double M,
+                                    double rp, double rm, bool phi) {
+    return rk4_d_k1(y, rhs_d(y, E, L, a, M, rp, rm), h, E, L, a, M, rp, rm, phi);
 }
 
 // Redshift g = E / (u^t (E - Omega L)) of a prograde Keplerian emitter on
@@ -490,7 +494,7 @@ __device__ __forceinline__ int mray_step32_adaptive(MRay<PHI>& R, const SceneDev
 // REC phi is integrated and the first four crossings are recorded.
 template <bool REC>
 struct DRay {
-    D5 y;
+    D5 y, f;                     // state and f(state), the first stage of the next step
     double E, L;
     double min_r, first_r;
     float disk[3];
@@ -502,6 +506,7 @@ template <bool REC>
 __device__ __forceinline__ void dray_start(DRay<REC>& R, const SceneDev& s, double E, double L, double pr, double pth) {
     R.y = D5{s.r_cam, s.th_cam, pr, pth, s.ph_cam};
     R.E = E; R.L = L;
+    R.f = rhs_d(R.y, E, L, s.a, s.M, s.r_plus, s.r_minus);
     R.min_r = s.r_cam; R.first_r = 0.0;
     R.disk[0] = R.disk[1] = R.disk[2] = 0.0f;
     R.step = 0; R.orders = 0; R.crossings = 0; R.status = 2;
@@ -513,12 +518,13 @@ template <bool REC>
 __device__ __forceinline__ bool dray_step(DRay<REC>& R, const SceneDev& s) {
     if (R.step >= s.max_steps) { R.status = 2; return true; }
     const double h = s.h_unit * fmin(fmax(1.0, R.y.r / s.M), 100.0);
-    const D5 y0 = R.y;
-    D5 f0 = rhs_d(y0, R.E, R.L, s.a, s.M, s.r_plus, s.r_minus);
-    R.y = rk4_d(y0, h, R.E, R.L, s.a, s.M, s.r_plus, s.r_minus, REC);
+    const D5 y0 = R.y, f0 = R.f;
+    R.y = rk4_d_k1(y0, f0, h, R.E, R.L, s.a, s.M, s.r_plus, s.r_minus, REC);
     R.step++;
     bool ok = R.y.r > s.r_plus + 1e-9 && R.y.th > 1e-9 && R.y.th < kPi - 1e-9;
     if (!ok) { R.status = 1; return true; }
+    R.f = rhs_d(R.y, R.E, R.L, s.a, s.M, s.r_plus, s.r_minus);
+    const D5& f1 = R.f;
     R.min_r = fmin(R.min_r, R.y.r);
     double dp = y0.th - kPi * 0.5, dc = R.y.th - kPi * 0.5;
     bool sc = (dp > 0 && dc < 0) || (dp < 0 && dc > 0);
@@ -527,7 +533,6 @@ __device__ __forceinline__ bool dray_step(DRay<REC>& R, const SceneDev& s) {
         double alpha = fabs(dp) / (fabs(dp) + fabs(dc) + 1e-30);
         double rc, phc;
         if (s.crossing == NP_CROSS_HERMITE && sc) {
-            D5 f1 = rhs_d(R.y, R.E, R.L, s.a, s.M, s.r_plus, s.r_minus);
             double u = hermite_root(dp, dc, h * f0.th, h * f1.th, alpha);
             rc = hermite_eval(y0.r, R.y.r, h * f0.r, h * f1.r, u);
             phc = hermite_eval(y0.ph, R.y.ph, h * f0.ph, h * f1.ph, u);
