@@ -214,7 +214,9 @@ def run_ours(args):
             dist.barrier()
 
     lib = npx.load()
-    sc = npx.benchmark_scene(seed=rank)
+    # FP64 within 0.1 M of the horizon, at turning points and for near-critical
+    # impact parameters: every island of the mixed path
+    sc = npx.benchmark_scene(seed=rank).replace(islands=npx.NP_ISLANDS_ALL)
     H, W = sc.height, sc.width
     rays_per_step = W * H * sc.spp
     rgb = torch.zeros((3, H, W), dtype=torch.float32, device="cuda")
@@ -290,6 +292,7 @@ def run_ours(args):
             "dtype": "f32+f64" if args.precision == "mixed" else "f64", "data": "synthetic",
             "config": {"workload": WORKLOAD, "width": W, "height": H, "spp": sc.spp, "spin": sc.spin,
                        "precision": args.precision, "rays_per_step": rays_per_step,
+                       "fp64_islands": "horizon band 0.1 M, radial/polar turning points, |b-b_crit| < 1e-3 M",
                        "l2": "256 MiB buffer written between timed steps (outside the step events)",
                        "parallelism": "replicas" if ws > 1 else "single"},
             "steps_per_s": ws * st.steps / (ms * 1e-3),
@@ -307,6 +310,16 @@ def run_ours(args):
             "clocks": clocks,
             "wall_s": wall,
         }
+        if args.precision == "mixed":
+            # the library's default island mask (horizon and near-critical)
+            dsc = sc.replace(islands=npx.NP_ISLANDS_DEFAULT)
+            dms = []
+            for i in range(3):
+                flush.fill_(float(i))
+                _, _, sd = npx.render(dsc, "mixed", rgb=rgb, rcross=rc, stats=True)
+                dms.append(sd.kernel_ms + sd.init_ms)
+            out["default_islands"] = {"islands": "horizon band + near-critical", "rays_per_s":
+                                      rays_per_step / (min(dms) * 1e-3), "kernel_ms": min(dms)}
         if args.fp64_frame and args.precision == "mixed":
             _, _, s64 = npx.render(sc, "fp64", stats=True)
             out["fp64_path"] = {"rays_per_s": rays_per_step / (s64.kernel_ms * 1e-3), "kernel_ms": s64.kernel_ms,

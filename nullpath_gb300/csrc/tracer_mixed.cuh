@@ -98,17 +98,20 @@ __device__ __forceinline__ F5 rhs_f(float r, float th, float pr, float pth, cons
 
 struct D5 { double r, th, pr, pth, ph; };
 
-// The same equations in FP64 (island steps and near-critical rays); zero
-// inside r_+ + 1e-12 as the reference does (bh_kerr.h:684-690).
-__device__ __forceinline__ D5 rhs_d(const D5& y, double E, double L, double a, double M, double rp, double rm) {
+// The same equations in FP64 (island steps and near-critical rays), given
+// sin and cos of theta; zero inside r_+ + 1e-12 as the reference does
+// (bh_kerr.h:684-690).  GB300 issues FP64 at 1/64 of the FP32 rate, so the
+// three reciprocals share one division.
+__device__ __forceinline__ D5 rhs_dsc(const D5& y, double sn, double cs, double E, double L, double a, double M,
+                                      double rp, double rm) {
     D5 d{0, 0, 0, 0, 0};
     if (y.r <= rp + 1e-12) return d;
-    double sn, cs;
-    sincos(y.th, &sn, &cs);
-    double s2 = fmax(sn * sn, 1e-30), is2 = 1.0 / s2;
+    double s2 = fmax(sn * sn, 1e-30);
     double r = y.r, r2 = r * r, a2 = a * a;
-    double Sig = r2 + a2 * cs * cs, iS = 1.0 / Sig;
-    double Del = (r - rp) * (r - rm), iD = 1.0 / Del;
+    double Sig = r2 + a2 * cs * cs;
+    double Del = (r - rp) * (r - rm);
+    double SD = Sig * Del, inv = 1.0 / (s2 * SD);
+    double is2 = SD * inv, iS = s2 * Del * inv, iD = s2 * Sig * inv;
     double P = (r2 + a2) * E - a * L, PiD = P * iD;
     double W = L * L * is2 + a2 * E * E * s2 - 2.0 * a * E * L;
     double F = Del * y.pr * y.pr + y.pth * y.pth - P * PiD + W;
@@ -124,16 +127,47 @@ __device__ __forceinline__ D5 rhs_d(const D5& y, double E, double L, double a, d
     return d;
 }
 
+__device__ __forceinline__ D5 rhs_d(const D5& y, double E, double L, double a, double M, double rp, double rm) {
+    double sn, cs;
+    sincos(y.th, &sn, &cs);
+    return rhs_dsc(y, sn, cs, E, L, a, M, rp, rm);
+}
+
+// sin and cos of theta0 + d from those of theta0.  An RK4 stage moves theta
+// by a small angle d; sin d and cos d come from their Taylor series through
+// d^13 and d^12 (truncation below 1e-18 for |d| <= 1/4) and the angle-
+// addition formulas, about half the FP64 instructions of sincos.  Larger d
+// falls back to sincos.
+__device__ __forceinline__ void stage_sincos_d(double th0, double sn0, double cs0, double d, double& sn, double& cs) {
+    if (fabs(d) <= 0.25) {
+        const double z = d * d;
+        const double sd = d * (1.0 + z * (-1.0 / 6.0 + z * (1.0 / 120.0 + z * (-1.0 / 5040.0 + z * (1.0 / 362880.0 +
+                              z * (-1.0 / 39916800.0 + z * (1.0 / 6227020800.0)))))));
+        const double cd = 1.0 + z * (-0.5 + z * (1.0 / 24.0 + z * (-1.0 / 720.0 + z * (1.0 / 40320.0 +
+                              z * (-1.0 / 3628800.0 + z * (1.0 / 479001600.0))))));
+        sn = sn0 * cd + cs0 * sd;
+        cs = cs0 * cd - sn0 * sd;
+    } else {
+        sincos(th0 + d, &sn, &cs);
+    }
+}
+
 __device__ __forceinline__ D5 add5(const D5& y, double h, const D5& k) {
     return D5{y.r + h * k.r, y.th + h * k.th, y.pr + h * k.pr, y.pth + h * k.pth, y.ph + h * k.ph};
 }
 
-// One FP64 RK4 step of the Carter system whose first stage k1 = f(y) is known.
-__device__ __forceinline__ D5 rk4_d_k1(const D5& y, const D5& k1, double h, double E, double L, double a,
-                                       double M, double rp, double rm, bool phi) {
-    D5 k2 = rhs_d(add5(y, 0.5 * h, k1), E, L, a, M, rp, rm);
-    D5 k3 = rhs_d(add5(y, 0.5 * h, k2), E, L, a, M, rp, rm);
-    D5 k4 = rhs_d(add5(y, h, k3), E, L, a, M, rp, rm);
+// One FP64 RK4 step of the Carter system whose first stage k1 = f(y) is
+// known, with sin/cos of y.th.
+__device__ __forceinline__ D5 rk4_d_k1(const D5& y, double sn0, double cs0, const D5& k1, double h, double E,
+                                       double L, double a, double M, double rp, double rm, bool phi) {
+    double sn, cs;
+    const double hh = 0.5 * h;
+    stage_sincos_d(y.th, sn0, cs0, hh * k1.th, sn, cs);
+    D5 k2 = rhs_dsc(add5(y, hh, k1), sn, cs, E, L, a, M, rp, rm);
+    stage_sincos_d(y.th, sn0, cs0, hh * k2.th, sn, cs);
+    D5 k3 = rhs_dsc(add5(y, hh, k2), sn, cs, E, L, a, M, rp, rm);
+    stage_sincos_d(y.th, sn0, cs0, h * k3.th, sn, cs);
+    D5 k4 = rhs_dsc(add5(y, h, k3), sn, cs, E, L, a, M, rp, rm);
     double h6 = h * (1.0 / 6.0);
     D5 o;
     o.r = y.r + h6 * (k1.r + 2.0 * (k2.r + k3.r) + k4.r);
@@ -146,7 +180,9 @@ __device__ __forceinline__ D5 rk4_d_k1(const D5& y, const D5& k1, double h, doub
 
 __device__ __forceinline__ D5 rk4_d(const D5& y, double h, double E, double L, double a, double M,
                                     double rp, double rm, bool phi) {
-    return rk4_d_k1(y, rhs_d(y, E, L, a, M, rp, rm), h, E, L, a, M, rp, rm, phi);
+    double sn, cs;
+    sincos(y.th, &sn, &cs);
+    return rk4_d_k1(y, sn, cs, rhs_dsc(y, sn, cs, E, L, a, M, rp, rm), h, E, L, a, M, rp, rm, phi);
 }
 
 // Redshift g = E / (u^t (E - Omega L)) of a prograde Keplerian emitter on
@@ -495,6 +531,7 @@ __device__ __forceinline__ int mray_step32_adaptive(MRay<PHI>& R, const SceneDev
 template <bool REC>
 struct DRay {
     D5 y, f;                     // state and f(state), the first stage of the next step
+    double sn, cs;               // sin and cos of y.th
     double E, L;
     double min_r, first_r;
     float disk[3];
@@ -506,7 +543,8 @@ template <bool REC>
 __device__ __forceinline__ void dray_start(DRay<REC>& R, const SceneDev& s, double E, double L, double pr, double pth) {
     R.y = D5{s.r_cam, s.th_cam, pr, pth, s.ph_cam};
     R.E = E; R.L = L;
-    R.f = rhs_d(R.y, E, L, s.a, s.M, s.r_plus, s.r_minus);
+    sincos(R.y.th, &R.sn, &R.cs);
+    R.f = rhs_dsc(R.y, R.sn, R.cs, E, L, s.a, s.M, s.r_plus, s.r_minus);
     R.min_r = s.r_cam; R.first_r = 0.0;
     R.disk[0] = R.disk[1] = R.disk[2] = 0.0f;
     R.step = 0; R.orders = 0; R.crossings = 0; R.status = 2;
@@ -519,11 +557,12 @@ __device__ __forceinline__ bool dray_step(DRay<REC>& R, const SceneDev& s) {
     if (R.step >= s.max_steps) { R.status = 2; return true; }
     const double h = s.h_unit * fmin(fmax(1.0, R.y.r / s.M), 100.0);
     const D5 y0 = R.y, f0 = R.f;
-    R.y = rk4_d_k1(y0, f0, h, R.E, R.L, s.a, s.M, s.r_plus, s.r_minus, REC);
+    R.y = rk4_d_k1(y0, R.sn, R.cs, f0, h, R.E, R.L, s.a, s.M, s.r_plus, s.r_minus, REC);
     R.step++;
     bool ok = R.y.r > s.r_plus + 1e-9 && R.y.th > 1e-9 && R.y.th < kPi - 1e-9;
     if (!ok) { R.status = 1; return true; }
-    R.f = rhs_d(R.y, R.E, R.L, s.a, s.M, s.r_plus, s.r_minus);
+    sincos(R.y.th, &R.sn, &R.cs);
+    R.f = rhs_dsc(R.y, R.sn, R.cs, R.E, R.L, s.a, s.M, s.r_plus, s.r_minus);
     const D5& f1 = R.f;
     R.min_r = fmin(R.min_r, R.y.r);
     double dp = y0.th - kPi * 0.5, dc = R.y.th - kPi * 0.5;
