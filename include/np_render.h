@@ -239,6 +239,50 @@ int np_tune(int param, int value);
  * TFLOP/s (an FMA counts as two flops).  Synchronous. */
 int np_measure_fma_peak(int which, double* tflops);
 
+/* ------------------------------------------------------------------------
+ * Batched scenes (no counterpart in the reference, whose renderer takes one
+ * scene per process): n scenes of any size, spin, inclination, spp and disk
+ * orders traced by one persistent launch of the mixed path over one device
+ * ray queue; the pass (counter reset, ray generation, tracing, resolve) is
+ * captured into a CUDA graph on the first np_batch_run with use_graph = 1
+ * and replayed afterwards.  Only NP_PREC_MIXED is accepted.  Outputs stay in
+ * the batch: np_batch_scene_output returns device pointers to scene i's
+ * planar [3][H][W] image and [H][W] first-crossing radii. */
+typedef struct np_batch np_batch_t;
+
+typedef struct np_batch_stats {
+    int32_t scenes;
+    uint64_t rays, steps, fp64_steps, deferred_rays;
+    double total_ms;            /* CUDA-event time of the whole pass */
+    double scene_ms_p50, scene_ms_p99, scene_ms_max;   /* scene completion after ray generation starts */
+    int32_t block, min_blocks, chunk, island_batch;    /* launch setting used */
+} np_batch_stats_t;
+
+typedef struct np_batch_tune {
+    int32_t shape, block, min_blocks, chunk, island_batch, trials;
+    double best_ms;
+} np_batch_tune_t;
+
+/* NULL on failure (np_last_error). `stream` is the CUDA stream of the batch. */
+np_batch_t* np_batch_create(const np_scene_t* scenes, int n, int precision, void* stream);
+void np_batch_destroy(np_batch_t* b);
+/* One pass; with stats non-NULL the call waits for the pass and fills them. */
+int np_batch_run(np_batch_t* b, int use_graph, np_batch_stats_t* stats);
+int np_batch_scene_output(np_batch_t* b, int i, float** d_rgb, float** d_rcross);
+/* Copies scene i's image and radii of the last pass into caller device
+ * buffers (ordered on the batch stream; either pointer may be NULL). */
+int np_batch_copy_output(np_batch_t* b, int i, float* d_rgb, float* d_rcross);
+/* Per-scene completion times (ms after ray generation started) of the last pass. */
+int np_batch_scene_latency(np_batch_t* b, double* ms);
+/* Launch setting of later passes: shape index (np_batch_shape gives its
+ * threads per block and resident blocks per SM), rays a warp takes from the
+ * queue at once, and parked lanes that trigger a batched FP64 island step. */
+int np_batch_set_tuning(int shape, int chunk, int island_batch);
+int np_batch_shape(int shape, int* block, int* min_blocks);
+/* Coordinate-descent autotuner over shape, chunk and island batch on batch b
+ * (typically a sub-batch of the production scenes); installs the best. */
+int np_batch_autotune(np_batch_t* b, np_batch_tune_t* out);
+
 #ifdef __cplusplus
 }
 #endif

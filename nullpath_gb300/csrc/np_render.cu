@@ -307,28 +307,37 @@ struct InitSoA {
 
 // Camera rays of one pass, fully parallel (one ray per thread).  All FP64
 // work of ray generation happens here, with every lane of a warp active.
+// Initial data of ray `li` of scene s, stored at index gi of the arrays;
+// near-critical rays go to the deferred list (at most list_cap entries).
+__device__ __forceinline__ void init_one(const SceneDev& s, long long li, long long gi, const InitSoA& soa,
+                                         Counters* __restrict__ ctr, unsigned long long list_cap) {
+    long long p; int sl, x, y; uint32_t sid;
+    ray_coords(s, li, p, sl, x, y, sid);
+    CamDir dir = camera_dir(s, x, y, sid, false, 0.0, 0.0);
+    Momentum m = camera_momentum(s, dir);
+    double E = -m.pt, L = m.pph;
+    bool defer = false;
+    if (s.islands & kIslandCritical) {
+        double Q = m.pth * m.pth + s.cos_cam * s.cos_cam * (L * L / (s.sin_cam * s.sin_cam) - s.a * s.a * E * E);
+        defer = near_critical(E, L, Q, s.a, s.M, s.r_plus, kCriticalDb);
+    }
+    HiLo pr = d_hl(m.pr), pth = d_hl(m.pth), Eh = d_hl(E), Lh = d_hl(L);
+    soa.a[gi] = make_float4(pr.hi, pr.lo, pth.hi, pth.lo);
+    soa.b[gi] = make_float4(Eh.hi, Eh.lo, Lh.hi, Lh.lo);
+    soa.cy[gi] = dir.cam_y;
+    if (defer) {
+        unsigned long long slot = atomicAdd(&ctr->deferred, 1ull);
+        if (slot < list_cap) soa.list[slot] = gi;
+        else defer = false;         // list full: the ray stays on the FP32 path
+    }
+    soa.flag[gi] = defer ? 1 : 0;
+}
+
 __global__ void __launch_bounds__(256)
 ray_init_kernel(const SceneDev s, InitSoA soa, Counters* __restrict__ ctr) {
-    const bool crit = (s.islands & kIslandCritical) != 0;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < s.total;
-         i += (long long)gridDim.x * blockDim.x) {
-        long long p; int sl, x, y; uint32_t sid;
-        ray_coords(s, i, p, sl, x, y, sid);
-        CamDir dir = camera_dir(s, x, y, sid, false, 0.0, 0.0);
-        Momentum m = camera_momentum(s, dir);
-        double E = -m.pt, L = m.pph;
-        bool defer = false;
-        if (crit) {
-            double Q = m.pth * m.pth + s.cos_cam * s.cos_cam * (L * L / (s.sin_cam * s.sin_cam) - s.a * s.a * E * E);
-            defer = near_critical(E, L, Q, s.a, s.M, s.r_plus, kCriticalDb);
-        }
-        HiLo pr = d_hl(m.pr), pth = d_hl(m.pth), Eh = d_hl(E), Lh = d_hl(L);
-        soa.a[i] = make_float4(pr.hi, pr.lo, pth.hi, pth.lo);
-        soa.b[i] = make_float4(Eh.hi, Eh.lo, Lh.hi, Lh.lo);
-        soa.cy[i] = dir.cam_y;
-        soa.flag[i] = defer ? 1 : 0;
-        if (defer) soa.list[atomicAdd(&ctr->deferred, 1ull)] = i;
-    }
+         i += (long long)gridDim.x * blockDim.x)
+        init_one(s, i, i, soa, ctr, (unsigned long long)s.total);
 }
 
 __device__ __forceinline__ void load_ray(const InitSoA& soa, long long i, MRay<false>& R, float& cam_y) {
@@ -903,3 +912,552 @@ extern "C" int np_render_device_noalloc(const np_scene_t* scene, int precision, 
     NP_CU(cudaGetLastError(), NP_ERR_KERNEL);
     return NP_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Batched scenes: many scenes of uneven size, spin, inclination, spp and disk
+// orders traced by one persistent launch of the mixed path over a single
+// device-side ray queue.  Ray index i belongs to the scene s with
+// ray_off[s] <= i < ray_off[s + 1]; lanes of one warp may hold rays of
+// different scenes, so each lane keeps a pointer to its scene's constants
+// (a few hundred bytes per scene, read through L1).  The sequence
+// (counter reset, ray generation, tracing, resolve) is captured once into a
+// CUDA graph and replayed.
+
+namespace {
+
+struct BatchDev {
+    const SceneDev* __restrict__ scenes;
+    const long long* __restrict__ ray_off;    // [n + 1]
+    const long long* __restrict__ pix_off;    // [n + 1]
+    int n;
+    long long total, total_pix;
+    unsigned long long list_cap;
+    float* srgb;                   // scene s at 3 ray_off[s]: [spp][3][npix]
+    float* rgb;                    // scene s at 3 pix_off[s]: [3][npix]
+    float* rcross;                 // scene s at pix_off[s]
+    unsigned* done;                // finished rays per scene
+    unsigned long long* t_done;    // %globaltimer when a scene's last ray finished
+    unsigned long long* t_start;   // %globaltimer at the start of ray generation
+    InitSoA soa;
+    Counters* ctr;
+};
+
+// Largest s in [0, n) with off[s] <= i.
+__device__ __forceinline__ int find_seg(const long long* __restrict__ off, int n, long long i) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (off[mid] <= i) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ void batch_write(const BatchDev& B, int sc, const SceneDev& S, long long p, int sl,
+                                            const float col[3], double first_r) {
+    write_sample(S, B.srgb + 3 * B.ray_off[sc], B.rcross + B.pix_off[sc], p, sl, col, first_r);
+    unsigned d = atomicAdd(&B.done[sc], 1u) + 1u;
+    if ((long long)d == S.total) B.t_done[sc] = global_ns();
+}
+
+__global__ void __launch_bounds__(256) batch_init_kernel(const BatchDev B) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) *B.t_start = global_ns();
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < B.total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int sc = find_seg(B.ray_off, B.n, i);
+        init_one(B.scenes[sc], i - B.ray_off[sc], i, B.soa, B.ctr, B.list_cap);
+    }
+}
+
+template <int BLOCK, int MINB>
+__global__ void __launch_bounds__(BLOCK, MINB) batch_mixed_kernel(const BatchDev B, int chunk, int T) {
+    const unsigned FULL = 0xffffffffu;
+    Counters* ctr = B.ctr;
+    const InitSoA& soa = B.soa;
+    unsigned long long n_rays = 0, n_steps = 0, n_f64 = 0, n_evals = 0;
+
+    // ---- FP64 warps: near-critical rays of every scene
+    const long long D = (long long)min(ctr->deferred, B.list_cap);
+    const int nd = D > 0 ? (int)min((long long)gridDim.x, (D + 3) / 4) : 0;
+    if ((threadIdx.x >> 5) == 0 && (int)blockIdx.x < nd) {
+        WarpQueue q{0, 0};
+        bool drained = false, have = false;
+        DRay<false> R;
+        const SceneDev* sp = B.scenes;
+        int sc = 0;
+        long long p = 0;
+        int sl = 0;
+        float cam_y = 0.0f;
+        while (true) {
+            unsigned need = __ballot_sync(FULL, !have);
+            if (need && !drained) {
+                long long idx = warp_take(q, need, &ctr->work2, D, 4);
+                drained = q.base >= D;
+                if (!have && idx >= 0) {
+                    const long long item = soa.list[idx];
+                    sc = find_seg(B.ray_off, B.n, item);
+                    sp = B.scenes + sc;
+                    int x, y; uint32_t sid;
+                    ray_coords(*sp, item - B.ray_off[sc], p, sl, x, y, sid);
+                    float4 a = soa.a[item], b = soa.b[item];
+                    cam_y = soa.cy[item];
+                    dray_start(R, *sp, (double)b.x + (double)b.y, (double)b.z + (double)b.w,
+                               (double)a.x + (double)a.y, (double)a.z + (double)a.w);
+                    have = true;
+                    n_rays++;
+                }
+            }
+            if (!__any_sync(FULL, have)) break;
+            if (have) {
+                bool done = dray_step(R, *sp);
+                n_steps++; n_f64++; n_evals += 4;
+                if (done) {
+                    float col[3];
+                    sample_colour(*sp, R.status == 1, R.orders, R.disk, (float)R.min_r, cam_y, col);
+                    batch_write(B, sc, *sp, p, sl, col, R.first_r);
+                    have = false;
+                }
+            }
+        }
+    }
+
+    // ---- FP32 rays (the loop of render_mixed_kernel with a per-lane scene)
+    WarpQueue q{0, 0};
+    bool drained = false, have = false;
+    MRay<false> R;
+    const SceneDev* sp = B.scenes;
+    SpaceK k{0.0f, 0.0f, 1.0f, 1.0f, 0.0f};
+    int sc = 0;
+    long long p = 0;
+    int sl = 0;
+    float cam_y = 0.0f;
+    while (true) {
+        unsigned need = __ballot_sync(FULL, !have);
+        if (need && !drained) {
+            long long idx = warp_take(q, need, &ctr->work, B.total, chunk);
+            drained = q.base >= B.total;
+            if (!have && idx >= 0 && !soa.flag[idx]) {
+                sc = find_seg(B.ray_off, B.n, idx);
+                sp = B.scenes + sc;
+                const SceneDev& S = *sp;
+                k = SpaceK{(float)S.a, (float)(S.a * S.a), (float)S.M, (float)S.r_plus, (float)S.r_minus};
+                int x, y; uint32_t sid;
+                ray_coords(S, idx - B.ray_off[sc], p, sl, x, y, sid);
+                load_ray(soa, idx, R, cam_y);
+                mray_start(R, S, k);
+                have = true;
+                n_rays++;
+                n_evals++;
+            }
+        }
+        unsigned act = __ballot_sync(FULL, have && !R.pending);
+        unsigned pend = __ballot_sync(FULL, have && R.pending);
+        if (!(act | pend)) {
+            if (drained) break;
+            continue;
+        }
+        bool done = false;
+        const SceneDev& S = *sp;
+        if (pend && ((int)__popc(pend) >= T || !act)) {
+            if (have && R.pending) {
+                done = mray_island(R, S, k);
+                n_steps++; n_f64++; n_evals += 5;
+            }
+        } else if (have && !R.pending) {
+            int r = S.integrator == NP_INTEG_ADAPTIVE ? mray_step32_adaptive(R, S, k) : mray_step32(R, S, k);
+            if (r != STEP_PARK) { n_steps++; n_evals += S.integrator == NP_INTEG_ADAPTIVE ? 11 : 4; }
+            done = r == STEP_DONE;
+        }
+        if (done) {
+            float col[3];
+            sample_colour(S, R.status == 1, R.orders, R.disk, R.min_r, cam_y, col);
+            batch_write(B, sc, S, p, sl, col, R.first_r);
+            have = false;
+        }
+    }
+    flush_counters(ctr, n_rays, n_steps, n_f64, n_evals);
+}
+
+__global__ void batch_resolve_kernel(const BatchDev B) {
+    for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < B.total_pix;
+         j += (long long)gridDim.x * blockDim.x) {
+        const int sc = find_seg(B.pix_off, B.n, j);
+        const SceneDev& S = B.scenes[sc];
+        const long long p = j - B.pix_off[sc];
+        const float* src = B.srgb + 3 * B.ray_off[sc];
+        float* dst = B.rgb + 3 * B.pix_off[sc];
+        for (int c = 0; c < 3; ++c) {
+            float acc = 0.0f;
+            for (int s = 0; s < S.spp; ++s) acc += src[((size_t)s * 3 + c) * S.npix + p];
+            dst[(size_t)c * S.npix + p] = acc;
+        }
+    }
+}
+
+// Launch-shape variants the autotuner chooses from: threads per block and
+// the blocks per SM the register allocation must allow.
+struct BatchShape { int block, minb; };
+constexpr BatchShape kBatchShapes[] = {{128, 4}, {64, 8}, {256, 2}, {128, 3}, {128, 5}};
+constexpr int kNumBatchShapes = sizeof(kBatchShapes) / sizeof(kBatchShapes[0]);
+
+struct BatchTune { int shape = 0, chunk = 64, island_batch = 8; };
+BatchTune g_btune;
+int g_btune_epoch = 0;
+
+// Persistent grid of each shape: SMs x resident blocks (queried once per
+// batch, before any graph capture).
+template <int BLOCK, int MINB>
+int batch_grid_t(int sms) {
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_mixed_kernel<BLOCK, MINB>, BLOCK, 0);
+    return sms * std::max(1, per_sm);
+}
+
+int batch_grid(int shape, int sms) {
+    switch (shape) {
+        case 1: return batch_grid_t<64, 8>(sms);
+        case 2: return batch_grid_t<256, 2>(sms);
+        case 3: return batch_grid_t<128, 3>(sms);
+        case 4: return batch_grid_t<128, 5>(sms);
+        default: return batch_grid_t<128, 4>(sms);
+    }
+}
+
+void batch_launch(const BatchDev& B, const BatchTune& t, int grid, cudaStream_t st) {
+    switch (t.shape) {
+        case 1: batch_mixed_kernel<64, 8><<<grid, 64, 0, st>>>(B, t.chunk, t.island_batch); break;
+        case 2: batch_mixed_kernel<256, 2><<<grid, 256, 0, st>>>(B, t.chunk, t.island_batch); break;
+        case 3: batch_mixed_kernel<128, 3><<<grid, 128, 0, st>>>(B, t.chunk, t.island_batch); break;
+        case 4: batch_mixed_kernel<128, 5><<<grid, 128, 0, st>>>(B, t.chunk, t.island_batch); break;
+        default: batch_mixed_kernel<128, 4><<<grid, 128, 0, st>>>(B, t.chunk, t.island_batch); break;
+    }
+}
+
+}  // namespace
+
+struct np_batch {
+    int device = -1;
+    int n = 0;
+    cudaStream_t stream = nullptr;
+    std::vector<long long> ray_off, pix_off;     // in queue order
+    std::vector<long long> npix;                 // by caller index
+    std::vector<int> pos;                        // caller index -> queue position
+    BatchDev B{};
+    void* mem = nullptr;
+    Counters* h_ctr = nullptr;
+    unsigned long long* h_times = nullptr;     // [n + 1]: t_done[0..n), t_start
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaGraphExec_t graph = nullptr;
+    int graph_epoch = -1;
+    BatchTune graph_tune{};
+    int grid[8] = {};
+};
+
+namespace {
+
+void batch_free(np_batch* b) {
+    if (!b) return;
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    if (b->mem) cudaFree(b->mem);
+    if (b->h_ctr) cudaFreeHost(b->h_ctr);
+    if (b->h_times) cudaFreeHost(b->h_times);
+    if (b->e0) cudaEventDestroy(b->e0);
+    if (b->e1) cudaEventDestroy(b->e1);
+    delete b;
+}
+
+// Enqueues one batch pass (no host synchronisation).
+int batch_enqueue(np_batch* b, const BatchTune& t, cudaStream_t st) {
+    const BatchDev& B = b->B;
+    NP_CU(cudaMemsetAsync(B.ctr, 0, sizeof(Counters), st), NP_ERR_KERNEL);
+    NP_CU(cudaMemsetAsync(B.done, 0, (size_t)b->n * sizeof(unsigned), st), NP_ERR_KERNEL);
+    const int ib = (int)std::min<long long>((B.total + 255) / 256, 152ll * 8);
+    batch_init_kernel<<<ib, 256, 0, st>>>(B);
+    NP_CU(cudaGetLastError(), NP_ERR_KERNEL);
+    batch_launch(B, t, b->grid[t.shape], st);
+    NP_CU(cudaGetLastError(), NP_ERR_KERNEL);
+    const int rb = (int)std::min<long long>((B.total_pix + 255) / 256, 152ll * 16);
+    batch_resolve_kernel<<<rb, 256, 0, st>>>(B);
+    NP_CU(cudaGetLastError(), NP_ERR_KERNEL);
+    return NP_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+np_batch_t* np_batch_create(const np_scene_t* scenes, int n, int precision, void* stream) {
+    if (!scenes || n < 1) { fail(NP_ERR_INVALID, "scenes is NULL or n < 1"); return nullptr; }
+    if (precision != NP_PREC_MIXED) {
+        fail(NP_ERR_INVALID, "batched scenes run the mixed-precision path");
+        return nullptr;
+    }
+    std::vector<SceneDev> byidx((size_t)n), devs((size_t)n);
+    np_batch* b = new np_batch();
+    b->n = n;
+    b->stream = (cudaStream_t)stream;
+    b->ray_off.assign((size_t)n + 1, 0);
+    b->pix_off.assign((size_t)n + 1, 0);
+    for (int i = 0; i < n; ++i) {
+        int rc = prepare_scene(scenes[i], byidx[(size_t)i]);
+        if (rc != NP_OK) {
+            std::string msg = g_last_error;
+            batch_free(b);
+            fail(rc, "scene %d: %s", i, msg.c_str());
+            return nullptr;
+        }
+        b->npix.push_back(byidx[(size_t)i].npix);
+    }
+    // Queue order: fewest rays first (shortest job first), which minimises
+    // the mean scene completion time of a FIFO ray queue; ties keep caller order.
+    std::vector<int> order((size_t)n);
+    for (int i = 0; i < n; ++i) order[(size_t)i] = i;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int x, int y) { return byidx[(size_t)x].total < byidx[(size_t)y].total; });
+    b->pos.assign((size_t)n, 0);
+    for (int q = 0; q < n; ++q) {
+        const SceneDev& d = byidx[(size_t)order[(size_t)q]];
+        devs[(size_t)q] = d;
+        b->pos[(size_t)order[(size_t)q]] = q;
+        b->ray_off[(size_t)q + 1] = b->ray_off[(size_t)q] + d.total;
+        b->pix_off[(size_t)q + 1] = b->pix_off[(size_t)q] + d.npix;
+    }
+    const long long total = b->ray_off[(size_t)n], total_pix = b->pix_off[(size_t)n];
+    const unsigned long long list_cap = (unsigned long long)std::max<long long>(1024, total / 64);
+    auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    size_t off = 0;
+    const size_t o_scenes = off; off += al(sizeof(SceneDev) * (size_t)n);
+    const size_t o_roff = off; off += al(sizeof(long long) * ((size_t)n + 1));
+    const size_t o_poff = off; off += al(sizeof(long long) * ((size_t)n + 1));
+    const size_t o_srgb = off; off += al(sizeof(float) * 3 * (size_t)total);
+    const size_t o_rgb = off; off += al(sizeof(float) * 3 * (size_t)total_pix);
+    const size_t o_rc = off; off += al(sizeof(float) * (size_t)total_pix);
+    const size_t o_done = off; off += al(sizeof(unsigned) * (size_t)n);
+    const size_t o_tdone = off; off += al(sizeof(unsigned long long) * ((size_t)n + 1));
+    const size_t o_a = off; off += al(sizeof(float4) * (size_t)total);
+    const size_t o_b = off; off += al(sizeof(float4) * (size_t)total);
+    const size_t o_cy = off; off += al(sizeof(float) * (size_t)total);
+    const size_t o_flag = off; off += al((size_t)total);
+    const size_t o_list = off; off += al(sizeof(long long) * (size_t)list_cap);
+    const size_t o_ctr = off; off += al(sizeof(Counters));
+    if (cudaGetDevice(&b->device) != cudaSuccess || cudaMalloc(&b->mem, off) != cudaSuccess ||
+        cudaMallocHost(&b->h_ctr, sizeof(Counters)) != cudaSuccess ||
+        cudaMallocHost(&b->h_times, sizeof(unsigned long long) * ((size_t)n + 1)) != cudaSuccess ||
+        cudaEventCreate(&b->e0) != cudaSuccess || cudaEventCreate(&b->e1) != cudaSuccess) {
+        cudaGetLastError();
+        batch_free(b);
+        fail(NP_ERR_ALLOC, "device allocation of %zu bytes for %d scenes failed", off, n);
+        return nullptr;
+    }
+    unsigned char* m = (unsigned char*)b->mem;
+    BatchDev& B = b->B;
+    B.scenes = (const SceneDev*)(m + o_scenes);
+    B.ray_off = (const long long*)(m + o_roff);
+    B.pix_off = (const long long*)(m + o_poff);
+    B.n = n; B.total = total; B.total_pix = total_pix; B.list_cap = list_cap;
+    B.srgb = (float*)(m + o_srgb); B.rgb = (float*)(m + o_rgb); B.rcross = (float*)(m + o_rc);
+    B.done = (unsigned*)(m + o_done);
+    B.t_done = (unsigned long long*)(m + o_tdone);
+    B.t_start = B.t_done + n;
+    B.soa = InitSoA{(float4*)(m + o_a), (float4*)(m + o_b), (float*)(m + o_cy), (unsigned char*)(m + o_flag),
+                    (long long*)(m + o_list)};
+    B.ctr = (Counters*)(m + o_ctr);
+    if (cudaMemcpy((void*)B.scenes, devs.data(), sizeof(SceneDev) * (size_t)n, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy((void*)B.ray_off, b->ray_off.data(), sizeof(long long) * ((size_t)n + 1),
+                   cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy((void*)B.pix_off, b->pix_off.data(), sizeof(long long) * ((size_t)n + 1),
+                   cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemset(B.rcross, 0, sizeof(float) * (size_t)total_pix) != cudaSuccess) {
+        cudaGetLastError();
+        batch_free(b);
+        fail(NP_ERR_KERNEL, "upload of the scene table failed");
+        return nullptr;
+    }
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
+    for (int i = 0; i < kNumBatchShapes; ++i) b->grid[i] = batch_grid(i, std::max(1, sms));
+    return b;
+}
+
+void np_batch_destroy(np_batch_t* b) {
+    if (b) cudaStreamSynchronize(b->stream);
+    batch_free(b);
+}
+
+int np_batch_run(np_batch_t* b, int use_graph, np_batch_stats_t* stats) {
+    if (!b) return fail(NP_ERR_INVALID, "batch is NULL");
+    int dev = 0;
+    NP_CU(cudaGetDevice(&dev), NP_ERR_NO_DEVICE);
+    if (dev != b->device) return fail(NP_ERR_INVALID, "batch was created on device %d, current is %d", b->device, dev);
+    cudaStream_t st = b->stream;
+    const BatchTune t = g_btune;
+    NP_CU(cudaEventRecord(b->e0, st), NP_ERR_KERNEL);
+    if (use_graph) {
+        if (!b->graph || b->graph_epoch != g_btune_epoch) {
+            if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
+            cudaStream_t cap = nullptr;
+            NP_CU(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking), NP_ERR_KERNEL);
+            cudaGraph_t g = nullptr;
+            cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+            int rc = e == cudaSuccess ? batch_enqueue(b, t, cap) : NP_ERR_KERNEL;
+            cudaError_t e2 = cudaStreamEndCapture(cap, &g);
+            cudaStreamDestroy(cap);
+            if (e != cudaSuccess || rc != NP_OK || e2 != cudaSuccess || !g) {
+                if (g) cudaGraphDestroy(g);
+                cudaGetLastError();
+                return fail(NP_ERR_KERNEL, "capture of the batch graph failed");
+            }
+            e = cudaGraphInstantiate(&b->graph, g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess) { b->graph = nullptr; return fail(NP_ERR_KERNEL, "graph instantiation: %s", cudaGetErrorString(e)); }
+            b->graph_epoch = g_btune_epoch;
+            b->graph_tune = t;
+        }
+        NP_CU(cudaGraphLaunch(b->graph, st), NP_ERR_KERNEL);
+    } else {
+        int rc = batch_enqueue(b, t, st);
+        if (rc != NP_OK) return rc;
+    }
+    NP_CU(cudaEventRecord(b->e1, st), NP_ERR_KERNEL);
+    if (stats) {
+        NP_CU(cudaMemcpyAsync(b->h_ctr, b->B.ctr, sizeof(Counters), cudaMemcpyDeviceToHost, st), NP_ERR_KERNEL);
+        NP_CU(cudaMemcpyAsync(b->h_times, b->B.t_done, sizeof(unsigned long long) * ((size_t)b->n + 1),
+                              cudaMemcpyDeviceToHost, st), NP_ERR_KERNEL);
+        NP_CU(cudaStreamSynchronize(st), NP_ERR_KERNEL);
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, b->e0, b->e1);
+        std::vector<double> lat((size_t)b->n);
+        const unsigned long long t0 = b->h_times[b->n];
+        for (int i = 0; i < b->n; ++i) lat[(size_t)i] = (double)(b->h_times[i] - t0) * 1e-6;
+        std::vector<double> sorted = lat;
+        std::sort(sorted.begin(), sorted.end());
+        auto q = [&](double f) { return sorted[(size_t)std::min<double>((double)b->n - 1, std::floor(f * (b->n - 1) + 0.5))]; };
+        stats->scenes = b->n;
+        stats->rays = b->h_ctr->rays;
+        stats->steps = b->h_ctr->steps;
+        stats->fp64_steps = b->h_ctr->fp64_steps;
+        stats->deferred_rays = std::min<unsigned long long>(b->h_ctr->deferred, b->B.list_cap);
+        stats->total_ms = ms;
+        stats->scene_ms_p50 = q(0.5);
+        stats->scene_ms_p99 = q(0.99);
+        stats->scene_ms_max = sorted.back();
+        stats->block = kBatchShapes[t.shape].block;
+        stats->min_blocks = kBatchShapes[t.shape].minb;
+        stats->chunk = t.chunk;
+        stats->island_batch = t.island_batch;
+    }
+    return NP_OK;
+}
+
+int np_batch_scene_output(np_batch_t* b, int i, float** d_rgb, float** d_rcross) {
+    if (!b || i < 0 || i >= b->n) return fail(NP_ERR_INVALID, "bad batch or scene index");
+    const long long po = b->pix_off[(size_t)b->pos[(size_t)i]];
+    if (d_rgb) *d_rgb = b->B.rgb + 3 * po;
+    if (d_rcross) *d_rcross = b->B.rcross + po;
+    return NP_OK;
+}
+
+int np_batch_copy_output(np_batch_t* b, int i, float* d_rgb, float* d_rcross) {
+    if (!b || i < 0 || i >= b->n) return fail(NP_ERR_INVALID, "bad batch or scene index");
+    const size_t np_ = (size_t)b->npix[(size_t)i];
+    const long long po = b->pix_off[(size_t)b->pos[(size_t)i]];
+    if (d_rgb)
+        NP_CU(cudaMemcpyAsync(d_rgb, b->B.rgb + 3 * po, 3 * np_ * sizeof(float), cudaMemcpyDeviceToDevice,
+                              b->stream), NP_ERR_KERNEL);
+    if (d_rcross)
+        NP_CU(cudaMemcpyAsync(d_rcross, b->B.rcross + po, np_ * sizeof(float), cudaMemcpyDeviceToDevice,
+                              b->stream), NP_ERR_KERNEL);
+    return NP_OK;
+}
+
+int np_batch_scene_latency(np_batch_t* b, double* ms) {
+    if (!b || !ms) return fail(NP_ERR_INVALID, "NULL argument");
+    NP_CU(cudaStreamSynchronize(b->stream), NP_ERR_KERNEL);
+    NP_CU(cudaMemcpy(b->h_times, b->B.t_done, sizeof(unsigned long long) * ((size_t)b->n + 1), cudaMemcpyDeviceToHost),
+          NP_ERR_KERNEL);
+    for (int i = 0; i < b->n; ++i) ms[i] = (double)(b->h_times[b->pos[(size_t)i]] - b->h_times[b->n]) * 1e-6;
+    return NP_OK;
+}
+
+int np_batch_set_tuning(int shape, int chunk, int island_batch) {
+    if (shape < 0 || shape >= kNumBatchShapes) return fail(NP_ERR_INVALID, "shape must be in [0, %d)", kNumBatchShapes);
+    if (chunk < 1 || chunk > 4096) return fail(NP_ERR_INVALID, "chunk must be in [1, 4096]");
+    if (island_batch < 1 || island_batch > 32) return fail(NP_ERR_INVALID, "island batch must be in [1, 32]");
+    g_btune.shape = shape; g_btune.chunk = chunk; g_btune.island_batch = island_batch;
+    ++g_btune_epoch;
+    return NP_OK;
+}
+
+int np_batch_shape(int shape, int* block, int* min_blocks) {
+    if (shape < 0 || shape >= kNumBatchShapes) return fail(NP_ERR_INVALID, "shape must be in [0, %d)", kNumBatchShapes);
+    if (block) *block = kBatchShapes[shape].block;
+    if (min_blocks) *min_blocks = kBatchShapes[shape].minb;
+    return NP_OK;
+}
+
+// Coordinate descent over launch shape, queue chunk and island batch on the
+// given (sub-)batch: each trial is one timed pass after one untimed pass of
+// the first trial; the best setting is installed and returned.
+int np_batch_autotune(np_batch_t* b, np_batch_tune_t* out) {
+    if (!b) return fail(NP_ERR_INVALID, "batch is NULL");
+    BatchTune best = g_btune;
+    auto trial = [&](const BatchTune& t, double& ms) -> int {
+        BatchTune saved = g_btune;
+        g_btune = t;
+        np_batch_stats_t s{};
+        int rc = np_batch_run(b, 0, &s);
+        g_btune = saved;
+        ms = s.total_ms;
+        return rc;
+    };
+    double best_ms = 0.0;
+    int rc = trial(best, best_ms);                  // warm-up
+    if (rc != NP_OK) return rc;
+    rc = trial(best, best_ms);
+    if (rc != NP_OK) return rc;
+    int trials = 2;
+    for (int s = 0; s < kNumBatchShapes; ++s) {
+        if (s == best.shape) continue;
+        BatchTune t = best; t.shape = s;
+        double ms; if ((rc = trial(t, ms)) != NP_OK) return rc;
+        ++trials;
+        if (ms < best_ms) { best_ms = ms; best = t; }
+    }
+    const int chunks[] = {16, 32, 64, 128, 256};
+    const BatchTune base_c = best;
+    for (int c : chunks) {
+        if (c == base_c.chunk) continue;
+        BatchTune t = base_c; t.chunk = c;
+        double ms; if ((rc = trial(t, ms)) != NP_OK) return rc;
+        ++trials;
+        if (ms < best_ms) { best_ms = ms; best = t; }
+    }
+    const int batches[] = {4, 8, 12, 16};
+    const BatchTune base_i = best;
+    for (int ib : batches) {
+        if (ib == base_i.island_batch) continue;
+        BatchTune t = base_i; t.island_batch = ib;
+        double ms; if ((rc = trial(t, ms)) != NP_OK) return rc;
+        ++trials;
+        if (ms < best_ms) { best_ms = ms; best = t; }
+    }
+    g_btune = best;
+    ++g_btune_epoch;
+    if (out) {
+        out->shape = best.shape;
+        out->block = kBatchShapes[best.shape].block;
+        out->min_blocks = kBatchShapes[best.shape].minb;
+        out->chunk = best.chunk;
+        out->island_batch = best.island_batch;
+        out->best_ms = best_ms;
+        out->trials = trials;
+    }
+    return NP_OK;
+}
+
+}  // extern "C"

@@ -81,3 +81,37 @@ def test_render_host_without_gpu_fails_cleanly(built):
         pytest.skip("GPU present")
     with pytest.raises(npx.NullPathError):
         npx.render_host(npx.benchmark_scene(width=8, height=8, spp=1))
+
+
+def test_batch_struct_layouts(built, tmp_path):
+    from nullpath_gb300.batch import BatchStats, BatchTune
+    prog = ['#include <stdio.h>', '#include <stddef.h>', '#include "np_render.h"', 'int main(void){',
+            'printf("%zu %zu\\n", sizeof(np_batch_stats_t), sizeof(np_batch_tune_t));']
+    for f, _ in BatchStats._fields_:
+        prog.append('printf("%%zu\\n", offsetof(np_batch_stats_t, %s));' % f)
+    for f, _ in BatchTune._fields_:
+        prog.append('printf("%%zu\\n", offsetof(np_batch_tune_t, %s));' % f)
+    prog.append("return 0;}")
+    src = tmp_path / "blayout.c"
+    src.write_text("\n".join(prog))
+    exe = tmp_path / "blayout"
+    subprocess.run(["gcc", "-I" + INC, str(src), "-o", str(exe)], check=True)
+    out = [int(v) for v in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()]
+    assert out[0] == C.sizeof(BatchStats) and out[1] == C.sizeof(BatchTune)
+    offs = out[2:]
+    for (f, _), off in zip(BatchStats._fields_, offs[:len(BatchStats._fields_)]):
+        assert getattr(BatchStats, f).offset == off, f
+    for (f, _), off in zip(BatchTune._fields_, offs[len(BatchStats._fields_):]):
+        assert getattr(BatchTune, f).offset == off, f
+
+
+def test_uneven_scene_draws():
+    from nullpath_gb300.batch import uneven_scenes, RESOLUTIONS
+    a = uneven_scenes(256, seed=1)
+    b = uneven_scenes(256, seed=1)
+    assert [(s.width, s.spp, s.spin, s.theta_deg, s.disk_max_orders) for s in a] == \
+           [(s.width, s.spp, s.spin, s.theta_deg, s.disk_max_orders) for s in b]
+    assert all(s.width == s.height and s.width in RESOLUTIONS for s in a)
+    assert all(1 <= s.spp <= 8 and 1 <= s.disk_max_orders <= 3 for s in a)
+    assert all(0.0 <= s.spin <= 0.998 and 5.0 <= s.theta_deg <= 85.0 for s in a)
+    assert {s.width for s in a} == set(RESOLUTIONS)

@@ -1,0 +1,73 @@
+"""Batched uneven scenes (one persistent launch, CUDA graph) against the
+single-scene renderer: every ray runs the same arithmetic, so each scene of
+the batch matches its own render bit for bit."""
+import numpy as np
+import pytest
+
+import nullpath_gb300 as npx
+from nullpath_gb300 import batch
+
+pytestmark = pytest.mark.gpu
+
+
+def _small_scenes(n=10):
+    # the uneven workload's draws at an eighth of the resolution
+    out = []
+    for sc in batch.uneven_scenes(n, seed=1):
+        r = max(8, sc.width // 8)
+        out.append(sc.replace(width=r, height=r))
+    return out
+
+
+def test_batch_matches_single_scene_renders(cuda):
+    import torch
+    scenes = _small_scenes()
+    b = batch.Batch(scenes)
+    st = b.run(graph=False, stats=True)
+    assert st.rays == sum(s.width * s.height * s.spp for s in scenes)
+    for i, sc in enumerate(scenes):
+        rgb, rc = b.image(i)
+        ref_rgb, ref_rc = npx.render(sc, "mixed")
+        torch.cuda.synchronize()
+        assert torch.equal(rgb, ref_rgb), i
+        assert torch.equal(rc, ref_rc), i
+    b.close()
+
+
+def test_graph_replay_and_tuning_are_deterministic(cuda):
+    import torch
+    scenes = _small_scenes(8)
+    b = batch.Batch(scenes)
+    b.run(graph=False)
+    ref = [b.image(i) for i in range(len(scenes))]
+    for shape, chunk, ib in ((0, 64, 8), (1, 16, 4), (2, 256, 16), (3, 32, 12)):
+        batch.set_tuning(shape, chunk, ib)
+        for _ in range(2):
+            st = b.run(graph=True, stats=True)
+            assert (st.chunk, st.island_batch) == (chunk, ib)
+            for i in range(len(scenes)):
+                rgb, rc = b.image(i)
+                assert torch.equal(rgb, ref[i][0]) and torch.equal(rc, ref[i][1]), (shape, i)
+    batch.set_tuning()
+    lat = b.latency_ms()
+    assert (lat > 0).all() and lat.max() <= st.total_ms + 1e-3
+    assert st.scene_ms_p50 <= st.scene_ms_p99 <= st.scene_ms_max
+    b.close()
+
+
+def test_autotuner_installs_a_valid_setting(cuda):
+    b = batch.Batch(_small_scenes(6))
+    t = batch.autotune(b)
+    assert t["trials"] >= 10 and t["best_ms"] > 0
+    assert t["block"] in (64, 128, 256) and t["chunk"] in (16, 32, 64, 128, 256)
+    st = b.run(graph=True, stats=True)
+    assert (st.block, st.chunk, st.island_batch) == (t["block"], t["chunk"], t["island_batch"])
+    batch.set_tuning()
+    b.close()
+
+
+def test_batch_rejects_bad_scene(cuda):
+    scenes = _small_scenes(3)
+    scenes[1] = scenes[1].replace(spin=1.2)
+    with pytest.raises(npx.NullPathError):
+        batch.Batch(scenes)
