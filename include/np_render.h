@@ -283,6 +283,22 @@ int np_batch_shape(int shape, int* block, int* min_blocks);
  * (typically a sub-batch of the production scenes); installs the best. */
 int np_batch_autotune(np_batch_t* b, np_batch_tune_t* out);
 
+/* ------------------------------------------------------------------------
+ * The physics-header API (include/np_kerr.h, the reference's bh_kerr.h
+ * names) driven from C: ray i starts at a static observer (zamo = 0; a ZAMO
+ * when 1) at cam[6i..6i+2] = (r, theta, phi) with local direction
+ * cam[6i+3..6i+5] = (n_r, n_theta, n_phi) (init_ray_from_camera_general_d /
+ * init_ray_from_camera_zamo_d, bh_kerr.h:781-826, 910-967) and takes up to
+ * `steps` integrateGeodesicKerrD steps of h = h_scale r (bh_kerr.h:734-774),
+ * stopping when a step returns false.  states[8i..8i+7] = (t, r, theta, phi,
+ * p_t, p_r, p_theta, p_phi); alive[i] = the last step's result.  The device
+ * entry takes device pointers and is ordered on `stream`; the host entry runs
+ * the same header code on the CPU. */
+int np_kerr_integrate_device(int n, double M, double a, const double* d_cam, int steps, double h_scale, int zamo,
+                             double* d_states, int* d_alive, void* stream);
+int np_kerr_integrate_host(int n, double M, double a, const double* cam, int steps, double h_scale, int zamo,
+                           double* states, int* alive);
+
 #ifdef __cplusplus
 }
 #endif
