@@ -299,6 +299,24 @@ int np_kerr_integrate_device(int n, double M, double a, const double* d_cam, int
 int np_kerr_integrate_host(int n, double M, double a, const double* cam, int steps, double h_scale, int zamo,
                            double* states, int* alive);
 
+/* ------------------------------------------------------------------------
+ * Progressive frames (render.cu:523-620 with the accumulation and output
+ * mapping on the device): passes of scene.spp samples add their colour sums
+ * into a device buffer (sample offsets continue across passes), and
+ * np_frame_tonemap maps sum / spp to interleaved 8-bit RGB with exposure
+ * 2^EV, optional Reinhard x/(1+x), display gamma (none when gamma is 1 or
+ * <= 0 means 1) and truncation of 255 x, exactly as the reference's host
+ * loop.  np_frame_read returns the mean colour [3][H][W], the first-crossing
+ * radius of sample 0 and the invariant maxima (when the scene asks for them). */
+typedef struct np_frame np_frame_t;
+np_frame_t* np_frame_create(int width, int height, void* stream);
+void np_frame_destroy(np_frame_t* f);
+int np_frame_reset(np_frame_t* f);
+int np_frame_add_pass(np_frame_t* f, const np_scene_t* scene, int precision, np_render_stats_t* stats);
+int np_frame_spp(const np_frame_t* f);
+int np_frame_tonemap(np_frame_t* f, float exposure_ev, float gamma, int reinhard, unsigned char* h_rgb8);
+int np_frame_read(np_frame_t* f, float* h_rgb_mean, float* h_rcross, float* h_inv3);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1461,3 +1461,139 @@ int np_batch_autotune(np_batch_t* b, np_batch_tune_t* out) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Progressive frames: per-pixel colour sums accumulated on the device over
+// passes of `samples` spp, then exposure, optional Reinhard tone map, display
+// gamma and 8-bit quantisation on the device (render.cu:523-620).
+
+namespace {
+
+// sum[c][p] / spp -> interleaved 8-bit RGB, with the reference's output
+// mapping: scale 2^EV, x / (1 + x) when tonemap, x^(1/gamma) unless gamma is
+// 1, clamp to [0, 1], truncation of 255 x (render.cu:577-601).
+__global__ void tonemap_kernel(const float* __restrict__ sum, long long npix, float inv_spp, float scale, int reinhard,
+                               float gamma, unsigned char* __restrict__ out) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < npix;
+         i += (long long)gridDim.x * blockDim.x) {
+        for (int c = 0; c < 3; ++c) {
+            float v = sum[(size_t)c * npix + i] * inv_spp;
+            v *= scale;
+            if (reinhard) v = v / (1.0f + v);
+            if (fabsf(gamma - 1.0f) > 1e-6f) v = powf(fmaxf(v, 0.0f), 1.0f / fmaxf(1e-6f, gamma));
+            v = fminf(fmaxf(v, 0.0f), 1.0f);
+            out[3 * i + c] = (unsigned char)(255.0f * v);
+        }
+    }
+}
+
+__global__ void scale_kernel(const float* __restrict__ in, float* __restrict__ out, long long n, float s) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        out[i] = in[i] * s;
+}
+
+}  // namespace
+
+struct np_frame {
+    int device = -1;
+    int W = 0, H = 0;
+    int spp_done = 0;
+    cudaStream_t stream = nullptr;
+    float* d_sum = nullptr;        // [3][H][W] colour sums
+    float* d_rc = nullptr;         // [H][W] first-crossing radius of sample 0
+    float* d_inv = nullptr;        // [3] invariant maxima
+    unsigned char* d_u8 = nullptr;
+    float* d_tmp = nullptr;
+};
+
+extern "C" {
+
+np_frame_t* np_frame_create(int width, int height, void* stream) {
+    if (width <= 0 || height <= 0) { fail(NP_ERR_INVALID, "Invalid image dimensions."); return nullptr; }
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) {
+        cudaGetLastError();
+        fail(NP_ERR_NO_DEVICE, "No CUDA devices found.");
+        return nullptr;
+    }
+    np_frame* f = new np_frame();
+    f->W = width; f->H = height; f->stream = (cudaStream_t)stream;
+    const size_t np_ = (size_t)width * height;
+    if (cudaGetDevice(&f->device) != cudaSuccess || cudaMalloc(&f->d_sum, 3 * np_ * sizeof(float)) != cudaSuccess ||
+        cudaMalloc(&f->d_rc, np_ * sizeof(float)) != cudaSuccess || cudaMalloc(&f->d_inv, 4 * sizeof(float)) != cudaSuccess ||
+        cudaMalloc(&f->d_u8, 3 * np_) != cudaSuccess || cudaMalloc(&f->d_tmp, 3 * np_ * sizeof(float)) != cudaSuccess) {
+        cudaGetLastError();
+        np_frame_destroy(f);
+        fail(NP_ERR_ALLOC, "device allocation for a %dx%d frame failed", width, height);
+        return nullptr;
+    }
+    np_frame_reset(f);
+    return f;
+}
+
+void np_frame_destroy(np_frame_t* f) {
+    if (!f) return;
+    cudaStreamSynchronize(f->stream);
+    cudaFree(f->d_sum); cudaFree(f->d_rc); cudaFree(f->d_inv); cudaFree(f->d_u8); cudaFree(f->d_tmp);
+    delete f;
+}
+
+int np_frame_reset(np_frame_t* f) {
+    if (!f) return fail(NP_ERR_INVALID, "frame is NULL");
+    const size_t np_ = (size_t)f->W * f->H;
+    NP_CU(cudaMemsetAsync(f->d_sum, 0, 3 * np_ * sizeof(float), f->stream), NP_ERR_KERNEL);
+    NP_CU(cudaMemsetAsync(f->d_rc, 0, np_ * sizeof(float), f->stream), NP_ERR_KERNEL);
+    NP_CU(cudaMemsetAsync(f->d_inv, 0, 4 * sizeof(float), f->stream), NP_ERR_KERNEL);
+    f->spp_done = 0;
+    return NP_OK;
+}
+
+int np_frame_add_pass(np_frame_t* f, const np_scene_t* scene, int precision, np_render_stats_t* stats) {
+    if (!f || !scene) return fail(NP_ERR_INVALID, "NULL argument");
+    if (scene->width != f->W || scene->height != f->H) return fail(NP_ERR_INVALID, "scene size differs from the frame");
+    np_scene_t s = *scene;
+    s.sample_offset = scene->sample_offset + f->spp_done;
+    int rc = np_render_device(&s, precision, f->d_sum, f->spp_done == 0 ? f->d_rc : nullptr,
+                              scene->check_invariants ? f->d_inv : nullptr, f->spp_done > 0 ? 1 : 0, f->stream, stats);
+    if (rc != NP_OK) return rc;
+    f->spp_done += scene->spp;
+    return NP_OK;
+}
+
+int np_frame_spp(const np_frame_t* f) { return f ? f->spp_done : 0; }
+
+int np_frame_tonemap(np_frame_t* f, float exposure_ev, float gamma, int reinhard, unsigned char* h_rgb8) {
+    if (!f || !h_rgb8) return fail(NP_ERR_INVALID, "NULL argument");
+    if (f->spp_done <= 0) return fail(NP_ERR_INVALID, "no pass rendered");
+    const long long np_ = (long long)f->W * f->H;
+    const float g = gamma <= 0.0f ? 1.0f : gamma;
+    const int blocks = (int)std::min<long long>((np_ + 255) / 256, 152ll * 16);
+    tonemap_kernel<<<blocks, 256, 0, f->stream>>>(f->d_sum, np_, 1.0f / (float)f->spp_done, powf(2.0f, exposure_ev),
+                                                  reinhard ? 1 : 0, g, f->d_u8);
+    NP_CU(cudaGetLastError(), NP_ERR_KERNEL);
+    NP_CU(cudaMemcpyAsync(h_rgb8, f->d_u8, 3 * (size_t)np_, cudaMemcpyDeviceToHost, f->stream), NP_ERR_KERNEL);
+    NP_CU(cudaStreamSynchronize(f->stream), NP_ERR_KERNEL);
+    return NP_OK;
+}
+
+int np_frame_read(np_frame_t* f, float* h_rgb_mean, float* h_rcross, float* h_inv3) {
+    if (!f) return fail(NP_ERR_INVALID, "frame is NULL");
+    if (f->spp_done <= 0) return fail(NP_ERR_INVALID, "no pass rendered");
+    const long long np_ = (long long)f->W * f->H;
+    if (h_rgb_mean) {
+        const int blocks = (int)std::min<long long>((3 * np_ + 255) / 256, 152ll * 16);
+        scale_kernel<<<blocks, 256, 0, f->stream>>>(f->d_sum, f->d_tmp, 3 * np_, 1.0f / (float)f->spp_done);
+        NP_CU(cudaGetLastError(), NP_ERR_KERNEL);
+        NP_CU(cudaMemcpyAsync(h_rgb_mean, f->d_tmp, 3 * (size_t)np_ * sizeof(float), cudaMemcpyDeviceToHost, f->stream),
+              NP_ERR_KERNEL);
+    }
+    if (h_rcross)
+        NP_CU(cudaMemcpyAsync(h_rcross, f->d_rc, (size_t)np_ * sizeof(float), cudaMemcpyDeviceToHost, f->stream),
+              NP_ERR_KERNEL);
+    if (h_inv3)
+        NP_CU(cudaMemcpyAsync(h_inv3, f->d_inv, 3 * sizeof(float), cudaMemcpyDeviceToHost, f->stream), NP_ERR_KERNEL);
+    NP_CU(cudaStreamSynchronize(f->stream), NP_ERR_KERNEL);
+    return NP_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,282 @@
+// render_cli.cpp -- the `render` command-line tool over the C ABI
+// (include/np_render.h), a drop-in for the reference's render binary.
+//
+// Flags, defaults, validation messages, exit codes and console lines follow
+// render.cu:15-46 (defaults), 397-423 (flags), 431-474 (validation and
+// --mode), 523-620 (passes, checkpoints, tone mapping, PPM) and 606-619
+// (frames).  Extensions (no counterpart in the reference):
+//   --units M|Rs        unit of --rcam (disk edges and escape radius are absolute)
+//   --seed N            stratified sub-pixel jitter from seed N (implies --stratified)
+//   --stratified        stratified jitter instead of the wanghash pattern
+//   --disk-rin isco|R   inner disk edge (isco = prograde ISCO of --mass, --spin)
+//   --disk-rout R       outer disk edge
+//   --emissivity-q Q    disk emissivity index (j ~ r^-Q)
+//   --escape-r R        escape radius
+//   --max-steps N       step cap per ray
+//   --precision fp64|mixed
+//   --integrator rk4|adaptive, --rtol X, --atol X
+//   --crossing linear|hermite
+//   --islands N         FP64 island mask of the mixed path (NP_ISLAND_*)
+//   --benchmark         the 1280x720, a=0.9 benchmark scene (other flags may follow)
+//   --out-raw FILE      float32 mean RGB [3][H][W] and first-crossing radius [H][W]
+//   --json FILE         a sidecar with the scene, passes and timings
+#include <cctype>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "np_render.h"
+
+namespace {
+
+struct Cli {
+    np_scene_t scene;
+    const char* out_path = "render.ppm";
+    int samples = 1;
+    int tile_h = 128;
+    int frames = 1;
+    float turns = 1.0f;
+    float phi0_deg = 0.0f;
+    const char* out_pat = "frame_%05d.ppm";
+    int spp_total = 0;
+    int checkpoint_every = 0;
+    const char* mode = "balanced";
+    float exposure_ev = 0.0f;
+    float gamma = 2.2f;
+    const char* tonemap = "none";
+    const char* bg = "gradient";
+    int precision = NP_PREC_FP64;
+    const char* out_raw = nullptr;
+    const char* json = nullptr;
+    bool rin_isco = false;
+    bool integrator_set = false;
+};
+
+std::string lower(const char* s) {
+    std::string o(s ? s : "");
+    for (char& c : o) c = (char)std::tolower((unsigned char)c);
+    return o;
+}
+
+// One %d-like conversion and otherwise only %% (render.cu:375-389).
+bool valid_pattern(const char* pat) {
+    if (!pat) return false;
+    int n = 0;
+    for (const char* p = pat; *p; ++p) {
+        if (*p != '%') continue;
+        ++p;
+        if (!*p) return false;
+        if (*p == '%') continue;
+        if (*p == '-') ++p;
+        while (*p >= '0' && *p <= '9') ++p;
+        if (*p != 'd') return false;
+        ++n;
+    }
+    return n == 1;
+}
+
+bool write_ppm(const char* path, int w, int h, const std::vector<unsigned char>& rgb) {
+    FILE* f = std::fopen(path, "wb");
+    if (!f) return false;
+    std::fprintf(f, "P6\n%d %d\n255\n", w, h);
+    size_t n = std::fwrite(rgb.data(), 1, rgb.size(), f);
+    std::fclose(f);
+    return n == rgb.size();
+}
+
+bool write_raw(const char* path, int w, int h, int spp, const std::vector<float>& rgb, const std::vector<float>& rc) {
+    FILE* f = std::fopen(path, "wb");
+    if (!f) return false;
+    const unsigned hdr[5] = {0x5752504eu /* "NPRW" */, 1u, (unsigned)w, (unsigned)h, (unsigned)spp};
+    bool ok = std::fwrite(hdr, sizeof(hdr), 1, f) == 1 && std::fwrite(rgb.data(), sizeof(float), rgb.size(), f) == rgb.size() &&
+              std::fwrite(rc.data(), sizeof(float), rc.size(), f) == rc.size();
+    std::fclose(f);
+    return ok;
+}
+
+void parse(int argc, char** argv, Cli& c) {
+    np_scene_t& s = c.scene;
+    for (int i = 1; i < argc; ++i) {
+        std::string a(argv[i]);
+        auto has = [&]() { return i + 1 < argc; };
+        auto f = [&](double& v) { if (has()) v = std::strtod(argv[++i], nullptr); };
+        auto fl = [&](float& v) { if (has()) v = std::strtof(argv[++i], nullptr); };
+        auto n = [&](int& v) { if (has()) v = std::atoi(argv[++i]); };
+        auto str = [&](const char*& v) { if (has()) v = argv[++i]; };
+        if (a == "--w" || a == "-w") n(s.width);
+        else if (a == "--h" || a == "-h") n(s.height);
+        else if (a == "--fov") f(s.fov_y_deg);
+        else if (a == "--theta") f(s.theta_deg);
+        else if (a == "--mass") f(s.mass);
+        else if (a == "--rcam") f(s.r_cam);
+        else if (a == "--out") str(c.out_path);
+        else if (a == "--samples" || a == "-s") n(c.samples);
+        else if (a == "--spp-total") n(c.spp_total);
+        else if (a == "--checkpoint-every") n(c.checkpoint_every);
+        else if (a == "--spin") f(s.spin);
+        else if (a == "--check-invariants") s.check_invariants = 1;
+        else if (a == "--tile") n(c.tile_h);
+        else if (a == "--frames") n(c.frames);
+        else if (a == "--turns") fl(c.turns);
+        else if (a == "--phi0") fl(c.phi0_deg);
+        else if (a == "--outpat") str(c.out_pat);
+        else if (a == "--mode" && has()) c.mode = argv[++i];
+        else if (a == "--exposure") fl(c.exposure_ev);
+        else if (a == "--gamma") fl(c.gamma);
+        else if (a == "--tonemap" && has()) c.tonemap = argv[++i];
+        else if (a == "--bg" && has()) c.bg = argv[++i];
+        else if (a == "--bg-sigma") f(s.bg_sigma_deg);
+        else if (a == "--bg-bright") f(s.bg_brightness);
+        else if (a == "--no-disk") s.disk_on = 0;
+        else if (a == "--disk-gain") f(s.disk_gain);
+        else if (a == "--disk-max-orders") n(s.disk_max_orders);
+        // extensions
+        else if (a == "--benchmark") np_scene_benchmark(&s);
+        else if (a == "--units" && has()) { std::string u = lower(argv[++i]); s.units = u == "m" ? NP_UNITS_M : NP_UNITS_RS; }
+        else if (a == "--seed") { int v = 0; n(v); s.seed = (uint32_t)v; s.jitter = NP_JITTER_STRATIFIED; }
+        else if (a == "--stratified") s.jitter = NP_JITTER_STRATIFIED;
+        else if (a == "--disk-rin" && has()) {
+            std::string v = lower(argv[++i]);
+            if (v == "isco") c.rin_isco = true;
+            else { c.rin_isco = false; s.disk_rin = std::strtod(v.c_str(), nullptr); }
+        }
+        else if (a == "--disk-rout") f(s.disk_rout);
+        else if (a == "--emissivity-q") f(s.emissivity_q);
+        else if (a == "--escape-r") f(s.escape_r);
+        else if (a == "--max-steps") n(s.max_steps);
+        else if (a == "--precision" && has()) c.precision = lower(argv[++i]) == "mixed" ? NP_PREC_MIXED : NP_PREC_FP64;
+        else if (a == "--integrator" && has()) {
+            s.integrator = lower(argv[++i]) == "adaptive" ? NP_INTEG_ADAPTIVE : NP_INTEG_RK4;
+            c.integrator_set = true;
+        }
+        else if (a == "--rtol") f(s.rtol);
+        else if (a == "--atol") f(s.atol);
+        else if (a == "--crossing" && has()) s.crossing = lower(argv[++i]) == "hermite" ? NP_CROSS_HERMITE : NP_CROSS_LINEAR;
+        else if (a == "--islands") n(s.islands);
+        else if (a == "--out-raw") str(c.out_raw);
+        else if (a == "--json") str(c.json);
+    }
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+    Cli c;
+    np_scene_defaults(&c.scene);
+    parse(argc, argv, c);
+    np_scene_t& s = c.scene;
+
+    if (s.width <= 0 || s.height <= 0) { std::fprintf(stderr, "Invalid image dimensions.\n"); return 1; }
+    if (c.tile_h <= 0) { std::fprintf(stderr, "Invalid tile height.\n"); return 1; }
+    if (c.samples <= 0) { std::fprintf(stderr, "Invalid samples per pixel.\n"); return 1; }
+    if (c.spp_total < 0) { std::fprintf(stderr, "Invalid total spp.\n"); return 1; }
+    if (c.frames <= 0) { std::fprintf(stderr, "Invalid frame count.\n"); return 1; }
+    if (s.mass <= 0.0 || s.r_cam <= 0.0) { std::fprintf(stderr, "Invalid mass or camera radius.\n"); return 1; }
+    if (std::fabs(s.spin) >= 1.0) { std::fprintf(stderr, "Spin must satisfy |a/M| < 1.\n"); return 1; }
+    if (s.fov_y_deg <= 0.0 || s.fov_y_deg >= 179.0) {
+        std::fprintf(stderr, "Invalid FOV; expected (0, 179) degrees.\n");
+        return 1;
+    }
+    // --mode (render.cu:468-474): accurate = adaptive step doubling, ZAMO
+    // camera and invariant tracking; fast and balanced = fixed RK4, static camera
+    const std::string mode = lower(c.mode);
+    if (mode == "accurate") {
+        if (!c.integrator_set) s.integrator = NP_INTEG_ADAPTIVE;
+        s.camera = NP_CAMERA_ZAMO;
+        s.check_invariants = 1;
+    }
+    s.background = lower(c.bg) == "point" ? NP_BG_POINT : NP_BG_GRADIENT;
+    if (c.rin_isco) s.disk_rin = np_isco_radius(s.mass, s.spin);
+    const bool reinhard = lower(c.tonemap) == "reinhard";
+    if (np_scene_validate(&s) != NP_OK) { std::fprintf(stderr, "%s\n", np_last_error()); return 1; }
+
+    np_frame_t* fr = np_frame_create(s.width, s.height, nullptr);
+    if (!fr) { std::fprintf(stderr, "%s\n", np_last_error()); return 1; }
+    const size_t npix = (size_t)s.width * s.height;
+    std::vector<unsigned char> rgb8(3 * npix);
+    double kernel_ms = 0.0;
+    unsigned long long rays = 0, steps = 0;
+    int passes_done = 0;
+
+    auto render_one = [&](double phi_deg, const char* path) -> bool {
+        const int total = c.spp_total > 0 ? c.spp_total : c.samples;
+        const int batch = c.samples > 1 ? c.samples : 1;
+        const int passes = (total + batch - 1) / batch;
+        np_frame_reset(fr);
+        np_scene_t ps = s;
+        ps.phi_deg = phi_deg;
+        for (int p = 0; p < passes; ++p) {
+            ps.spp = std::min(batch, total - np_frame_spp(fr));
+            np_render_stats_t st{};
+            if (np_frame_add_pass(fr, &ps, c.precision, &st) != NP_OK) {
+                std::fprintf(stderr, "%s\n", np_last_error());
+                return false;
+            }
+            kernel_ms += st.kernel_ms + st.init_ms;
+            rays += st.rays; steps += st.steps;
+            ++passes_done;
+            const bool ckpt = p == passes - 1 || (c.checkpoint_every > 0 && (p + 1) % c.checkpoint_every == 0);
+            if (!ckpt) continue;
+            if (np_frame_tonemap(fr, c.exposure_ev, c.gamma, reinhard ? 1 : 0, rgb8.data()) != NP_OK) {
+                std::fprintf(stderr, "%s\n", np_last_error());
+                return false;
+            }
+            if (!write_ppm(path, s.width, s.height, rgb8)) { std::fprintf(stderr, "Failed to write %s\n", path); return false; }
+            if (s.check_invariants) {
+                float inv[3] = {0, 0, 0};
+                np_frame_read(fr, nullptr, nullptr, inv);
+                std::printf("[checkpoint] %s @ %d spp  H|max=%.3e  dE/E|max=%.3e  dL/L|max=%.3e\n", path, np_frame_spp(fr),
+                            inv[0], inv[1], inv[2]);
+            } else {
+                std::printf("[checkpoint] %s @ %d spp\n", path, np_frame_spp(fr));
+            }
+        }
+        if (c.out_raw) {
+            std::vector<float> mean(3 * npix), rc(npix);
+            if (np_frame_read(fr, mean.data(), rc.data(), nullptr) != NP_OK ||
+                !write_raw(c.out_raw, s.width, s.height, np_frame_spp(fr), mean, rc)) {
+                std::fprintf(stderr, "Failed to write %s\n", c.out_raw);
+                return false;
+            }
+        }
+        return true;
+    };
+
+    int rc = 0;
+    if (c.frames <= 1) {
+        if (!render_one(c.phi0_deg, c.out_path)) rc = 1;
+        else std::printf("Wrote %s\n", c.out_path);
+    } else if (!valid_pattern(c.out_pat)) {
+        std::fprintf(stderr, "Invalid --outpat (expected a single %%d-like specifier).\n");
+        rc = 1;
+    } else {
+        for (int i = 0; i < c.frames && rc == 0; ++i) {
+            const float t = (float)i / (float)c.frames;
+            const double phi = c.phi0_deg + 360.0 * c.turns * t;
+            char path[512];
+            std::snprintf(path, sizeof(path), c.out_pat, i);
+            if (!render_one(phi, path)) rc = 1;
+        }
+        if (rc == 0) std::printf("Wrote %d frames matching pattern %s\n", c.frames, c.out_pat);
+    }
+    if (rc == 0 && c.json) {
+        FILE* f = std::fopen(c.json, "w");
+        if (f) {
+            std::fprintf(f,
+                         "{\"width\": %d, \"height\": %d, \"spp\": %d, \"frames\": %d, \"passes\": %d, \"mass\": %.17g, "
+                         "\"spin\": %.17g, \"r_cam\": %.17g, \"theta_deg\": %.17g, \"fov_y_deg\": %.17g, \"units\": \"%s\", "
+                         "\"precision\": \"%s\", \"integrator\": \"%s\", \"rays\": %llu, \"steps\": %llu, "
+                         "\"kernel_ms\": %.6f, \"rays_per_s\": %.6g}\n",
+                         s.width, s.height, np_frame_spp(fr), c.frames, passes_done, s.mass, s.spin, s.r_cam, s.theta_deg,
+                         s.fov_y_deg, s.units == NP_UNITS_M ? "M" : "Rs", c.precision == NP_PREC_MIXED ? "mixed" : "fp64",
+                         s.integrator == NP_INTEG_ADAPTIVE ? "adaptive" : "rk4", rays, steps, kernel_ms,
+                         kernel_ms > 0 ? rays / (kernel_ms * 1e-3) : 0.0);
+            std::fclose(f);
+        }
+    }
+    np_frame_destroy(fr);
+    return rc;
+}

@@ -1,0 +1,39 @@
+"""The `render` command-line tool (csrc/render_cli.cpp): the reference's
+validation messages and exit codes (render.cu:431-465) without a GPU."""
+import os
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+CLI = os.path.join(ROOT, "nullpath_gb300", "lib", "render")
+
+
+def _run(*args):
+    p = subprocess.run([CLI] + list(args), capture_output=True, text=True, timeout=60)
+    return p.returncode, p.stdout, p.stderr
+
+
+@pytest.mark.parametrize("args,msg", [
+    (["--w", "0"], "Invalid image dimensions."),
+    (["-h", "-3"], "Invalid image dimensions."),
+    (["--tile", "0"], "Invalid tile height."),
+    (["--samples", "0"], "Invalid samples per pixel."),
+    (["--spp-total", "-1"], "Invalid total spp."),
+    (["--frames", "0"], "Invalid frame count."),
+    (["--mass", "0"], "Invalid mass or camera radius."),
+    (["--rcam", "-2"], "Invalid mass or camera radius."),
+    (["--spin", "1.0"], "Spin must satisfy |a/M| < 1."),
+    (["--fov", "179"], "Invalid FOV; expected (0, 179) degrees."),
+])
+def test_invalid_arguments_exit_1(built, args, msg):
+    rc, out, err = _run(*args)
+    assert rc == 1 and err.strip() == msg
+
+
+def test_no_device_reported(built):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is visible")
+    rc, out, err = _run("--w", "8", "--h", "8")
+    assert rc == 1 and "No CUDA devices found." in err

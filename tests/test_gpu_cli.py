@@ -1,0 +1,82 @@
+"""The `render` tool on the GPU: progressive passes, device tone mapping and
+the PPM / raw outputs against the library's own render of the same scene."""
+import json
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import nullpath_gb300 as npx
+
+pytestmark = pytest.mark.gpu
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+CLI = os.path.join(ROOT, "nullpath_gb300", "lib", "render")
+
+
+def _read_ppm(path):
+    data = open(path, "rb").read()
+    parts = data.split(b"\n", 3)
+    assert parts[0] == b"P6" and parts[2] == b"255"
+    w, h = map(int, parts[1].split())
+    return np.frombuffer(parts[3], dtype=np.uint8).reshape(h, w, 3)
+
+
+def _read_raw(path):
+    b = open(path, "rb").read()
+    magic, ver, w, h, spp = np.frombuffer(b[:20], dtype=np.uint32)
+    assert magic == 0x5752504E and ver == 1
+    f = np.frombuffer(b[20:], dtype=np.float32)
+    return f[:3 * w * h].reshape(3, h, w), f[3 * w * h:].reshape(h, w), int(spp)
+
+
+def _tonemap(mean, ev=0.0, gamma=2.2, reinhard=False):
+    v = mean.astype(np.float32) * np.float32(2.0 ** ev)
+    if reinhard:
+        v = v / (np.float32(1) + v)
+    if abs(gamma - 1.0) > 1e-6:
+        v = np.power(np.maximum(v, 0).astype(np.float32), np.float32(1.0 / gamma))
+    v = np.clip(v, 0, 1)
+    return (np.float32(255) * v).astype(np.uint8).transpose(1, 2, 0)
+
+
+def test_cli_passes_match_library_render(cuda, tmp_path):
+    out = str(tmp_path / "a.ppm")
+    raw = str(tmp_path / "a.raw")
+    side = str(tmp_path / "a.json")
+    p = subprocess.run([CLI, "--w", "48", "--h", "32", "--samples", "2", "--spp-total", "6", "--checkpoint-every", "2",
+                        "--spin", "0.6", "--theta", "75", "--tonemap", "reinhard", "--exposure", "1",
+                        "--out", out, "--out-raw", raw, "--json", side], capture_output=True, text=True, timeout=300)
+    assert p.returncode == 0, p.stderr
+    lines = p.stdout.strip().splitlines()
+    assert lines[-1] == "Wrote %s" % out
+    # checkpoints after every 2nd pass and after the last (render.cu:570)
+    assert [l.split("@")[1].strip() for l in lines[:-1]] == ["4 spp", "6 spp"]
+    mean, rc, spp = _read_raw(raw)
+    assert spp == 6
+    sc = npx.reference_defaults().replace(width=48, height=32, spp=6, spin=0.6, theta_deg=75.0)
+    rgb, rcross = npx.render(sc, "fp64")
+    ref = rgb.cpu().numpy() / 6.0
+    assert np.allclose(mean, ref, rtol=1e-6, atol=1e-7)
+    ppm = _read_ppm(out)
+    want = _tonemap(mean, ev=1.0, reinhard=True)
+    diff = np.abs(ppm.astype(int) - want.astype(int))
+    assert diff.max() <= 1 and (diff == 0).mean() > 0.999
+    meta = json.load(open(side))
+    assert meta["spp"] == 6 and meta["passes"] == 3 and meta["precision"] == "fp64"
+
+
+def test_cli_frames_and_pattern(cuda, tmp_path):
+    pat = str(tmp_path / "f_%03d.ppm")
+    p = subprocess.run([CLI, "--w", "24", "--h", "16", "--frames", "3", "--turns", "0.5", "--outpat", pat,
+                        "--precision", "mixed", "--benchmark", "--w", "24", "--h", "16"],
+                       capture_output=True, text=True, timeout=300)
+    assert p.returncode == 0, p.stderr
+    files = [pat % i for i in range(3)]
+    assert all(os.path.exists(f) for f in files)
+    imgs = [_read_ppm(f) for f in files]
+    # the spacetime, disk and sky are axisymmetric: every azimuth gives the same image
+    assert imgs[0].shape == (16, 24, 3) and np.array_equal(imgs[0], imgs[1]) and np.array_equal(imgs[0], imgs[2])
+    bad = subprocess.run([CLI, "--w", "8", "--h", "8", "--frames", "2", "--outpat", str(tmp_path / "x_%d_%d.ppm")],
+                         capture_output=True, text=True, timeout=120)
+    assert bad.returncode == 1 and "Invalid --outpat" in bad.stderr
