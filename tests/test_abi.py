@@ -17,7 +17,8 @@ INC = os.path.join(ROOT, "include")
 def _declared_functions():
     names = set()
     for f in os.listdir(INC):
-        if not f.endswith(".h"):
+        # np_kerr.h is a header-only C++ API (inline functions), not a C ABI
+        if not f.endswith(".h") or f == "np_kerr.h":
             continue
         src = open(os.path.join(INC, f)).read()
         src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
