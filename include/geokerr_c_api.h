@@ -105,6 +105,22 @@ int np_geokerr_equator_crossings_device(int n, double a, const double* u0, const
                                         const double* q2, const double* su, const double* sm, double u_end, int K,
                                         double* xu, double* xphi, int32_t* nx, void* stream);
 
+/* Carlson symmetric elliptic integrals, FP64 (Carlson 1995 duplication):
+ * case i is types[2i..2i+1] = "RF" (x, y, z), "RC" (x, y), "RD" (x, y, z) or
+ * "RJ" (x, y, z, p); R_C with y < 0 and R_J with p < 0 are Cauchy principal
+ * values; invalid arguments or codes give NaN (the batch kernel of
+ * geokerr_port/cuda/carlson_elliptic.cu:351-382).  d_p may be NULL when no
+ * case is "RJ".  Device pointers, ordered on `stream`; the host entry runs the
+ * same code on the CPU.  Both return np_status. */
+int np_carlson_batch_device(int n, const char* d_types, const double* d_x, const double* d_y, const double* d_z,
+                            const double* d_p, double* d_out, void* stream);
+int np_carlson_batch_host(int n, const char* types, const double* x, const double* y, const double* z,
+                          const double* p, double* out);
+/* The reference's host entry points (carlson_elliptic.cu:387, 398): a
+ * device-vs-host check printed per function, and R_F(1, 2, 0) printed. */
+void validate_carlson_cuda(void);
+void test_carlson_cuda(void);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,127 @@
+// carlson.cu -- batched Carlson elliptic integrals on sm_103a (the batch
+// kernel of geokerr_port/cuda/carlson_elliptic.cu:351-382, with its
+// two-character case codes "RF", "RC", "RD", "RJ"), its host twin, and the
+// reference's host entry points validate_carlson_cuda / test_carlson_cuda
+// (carlson_elliptic.cu:387, 398) with working bodies.
+#include <cmath>
+#include <cstdio>
+
+#include <cuda_runtime.h>
+
+#include "carlson.cuh"
+#include "geokerr_c_api.h"
+#include "np_render.h"
+
+void np_record_error(const char* msg);
+
+namespace {
+
+NP_CARLSON_HD double carlson_case(char a, char b, double x, double y, double z, double p) {
+    if (a != 'R') return np::carlson::nan_();
+    switch (b) {
+        case 'F': return np::carlson::rf(x, y, z);
+        case 'C': return np::carlson::rc(x, y);
+        case 'D': return np::carlson::rd(x, y, z);
+        case 'J': return np::carlson::rj(x, y, z, p);
+        default: return np::carlson::nan_();
+    }
+}
+
+__global__ void carlson_batch_kernel(int n, const char* __restrict__ types, const double* __restrict__ x,
+                                     const double* __restrict__ y, const double* __restrict__ z,
+                                     const double* __restrict__ p, double* __restrict__ out) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        out[i] = carlson_case(types[2 * i], types[2 * i + 1], x[i], y[i], z[i], p ? p[i] : 0.0);
+}
+
+}  // namespace
+
+extern "C" {
+
+int np_carlson_batch_device(int n, const char* d_types, const double* d_x, const double* d_y, const double* d_z,
+                            const double* d_p, double* d_out, void* stream) {
+    if (n < 0 || (n > 0 && (!d_types || !d_x || !d_y || !d_z || !d_out))) {
+        np_record_error("np_carlson_batch_device: NULL buffer or negative count");
+        return NP_ERR_INVALID;
+    }
+    if (n == 0) return NP_OK;
+    const int threads = 256;
+    const int blocks = (n + threads - 1) / threads < 152 * 16 ? (n + threads - 1) / threads : 152 * 16;
+    carlson_batch_kernel<<<blocks, threads, 0, (cudaStream_t)stream>>>(n, d_types, d_x, d_y, d_z, d_p, d_out);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        np_record_error(cudaGetErrorString(e));
+        return NP_ERR_KERNEL;
+    }
+    return NP_OK;
+}
+
+int np_carlson_batch_host(int n, const char* types, const double* x, const double* y, const double* z,
+                          const double* p, double* out) {
+    if (n < 0 || (n > 0 && (!types || !x || !y || !z || !out))) {
+        np_record_error("np_carlson_batch_host: NULL buffer or negative count");
+        return NP_ERR_INVALID;
+    }
+    for (int i = 0; i < n; ++i) out[i] = carlson_case(types[2 * i], types[2 * i + 1], x[i], y[i], z[i], p ? p[i] : 0.0);
+    return NP_OK;
+}
+
+// Known values (closed forms): R_F(0,1,2) = K(1/sqrt 2)/sqrt 2 ... are
+// checked against the host evaluation of the same cases; prints one line per
+// function with the largest device/host relative difference.
+void validate_carlson_cuda(void) {
+    const int n = 8;
+    const char types[] = "RFRFRCRCRDRDRJRJ";
+    const double x[n] = {1.0, 0.5, 0.0, 2.0, 0.0, 1.5, 0.5, 2.0};
+    const double y[n] = {2.0, 1.0, 0.25, -1.0, 2.0, 0.2, 1.0, 3.0};
+    const double z[n] = {0.0, 3.0, 0.0, 0.0, 1.0, 4.0, 3.0, 4.0};
+    const double p[n] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 2.0, -0.5};
+    double host[n], dev[n];
+    np_carlson_batch_host(n, types, x, y, z, p, host);
+    char* dt = nullptr;
+    double *dx = nullptr, *dy = nullptr, *dz = nullptr, *dp = nullptr, *dout = nullptr;
+    bool ok = cudaMalloc(&dt, sizeof(types)) == cudaSuccess && cudaMalloc(&dx, sizeof(x)) == cudaSuccess &&
+              cudaMalloc(&dy, sizeof(y)) == cudaSuccess && cudaMalloc(&dz, sizeof(z)) == cudaSuccess &&
+              cudaMalloc(&dp, sizeof(p)) == cudaSuccess && cudaMalloc(&dout, sizeof(dev)) == cudaSuccess;
+    if (ok) {
+        cudaMemcpy(dt, types, sizeof(types), cudaMemcpyHostToDevice);
+        cudaMemcpy(dx, x, sizeof(x), cudaMemcpyHostToDevice);
+        cudaMemcpy(dy, y, sizeof(y), cudaMemcpyHostToDevice);
+        cudaMemcpy(dz, z, sizeof(z), cudaMemcpyHostToDevice);
+        cudaMemcpy(dp, p, sizeof(p), cudaMemcpyHostToDevice);
+        ok = np_carlson_batch_device(n, dt, dx, dy, dz, dp, dout, nullptr) == NP_OK &&
+             cudaMemcpy(dev, dout, sizeof(dev), cudaMemcpyDeviceToHost) == cudaSuccess;
+    }
+    std::printf("CUDA Carlson elliptic integral validation (device vs host)\n");
+    if (!ok) {
+        std::printf("  device run failed: %s\n", cudaGetErrorString(cudaGetLastError()));
+    } else {
+        for (int f = 0; f < 4; ++f) {
+            double worst = 0.0;
+            for (int i = 2 * f; i < 2 * f + 2; ++i) worst = std::fmax(worst, std::fabs(dev[i] - host[i]) / std::fabs(host[i]));
+            std::printf("  R%c: max relative difference %.3e\n", types[4 * f + 1], worst);
+        }
+    }
+    cudaFree(dt); cudaFree(dx); cudaFree(dy); cudaFree(dz); cudaFree(dp); cudaFree(dout);
+}
+
+// R_F(1, 2, 0) on the device (carlson_elliptic.cu:398-403 test case).
+void test_carlson_cuda(void) {
+    const char t[2] = {'R', 'F'};
+    const double x = 1.0, y = 2.0, z = 0.0, p = 0.0;
+    double r = std::nan("");
+    char* dt = nullptr;
+    double* d = nullptr;
+    if (cudaMalloc(&dt, 2) == cudaSuccess && cudaMalloc(&d, 5 * sizeof(double)) == cudaSuccess) {
+        const double in[4] = {x, y, z, p};
+        cudaMemcpy(dt, t, 2, cudaMemcpyHostToDevice);
+        cudaMemcpy(d, in, 4 * sizeof(double), cudaMemcpyHostToDevice);
+        if (np_carlson_batch_device(1, dt, d, d + 1, d + 2, d + 3, d + 4, nullptr) == NP_OK)
+            cudaMemcpy(&r, d + 4, sizeof(double), cudaMemcpyDeviceToHost);
+    }
+    std::printf("RF(1, 2, 0) = %.16f\n", r);
+    cudaFree(dt);
+    cudaFree(d);
+}
+
+}  // extern "C"

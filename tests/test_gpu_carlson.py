@@ -1,0 +1,36 @@
+"""Carlson integrals on sm_103a against the host build of the same code, and
+the reference's host entry points."""
+import subprocess
+import sys
+
+import numpy as np
+import pytest
+
+from nullpath_gb300 import carlson
+
+pytestmark = pytest.mark.gpu
+
+
+def test_device_matches_host(cuda):
+    rng = np.random.default_rng(9)
+    n = 20000
+    kinds = list(rng.choice(["RF", "RC", "RD", "RJ"], n))
+    x, y, z, p = (10 ** rng.uniform(-4, 4, n) for _ in range(4))
+    y = np.where(rng.uniform(size=n) < 0.2, -y, y)         # R_C principal values
+    p = np.where(rng.uniform(size=n) < 0.2, -p, p)         # R_J principal values
+    y = np.where(np.array(kinds) == "RC", y, np.abs(y))
+    h = carlson.evaluate(kinds, x, y, z, p, device=False)
+    d = carlson.evaluate(kinds, x, y, z, p, device=True)
+    ok = np.isfinite(h)
+    assert ok.mean() > 0.99 and np.array_equal(np.isfinite(d), ok)
+    assert np.allclose(d[ok], h[ok], rtol=1e-13, atol=0)
+
+
+def test_reference_entry_points_run(cuda):
+    code = ("import ctypes, nullpath_gb300 as n; lib = ctypes.CDLL(n.lib_path()); "
+            "lib.test_carlson_cuda(); lib.validate_carlson_cuda()")
+    out = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=120).stdout
+    assert "RF(1, 2, 0) = 1.3110287771460" in out
+    for f in ("RF", "RC", "RD", "RJ"):
+        line = [l for l in out.splitlines() if l.strip().startswith(f + ":")][0]
+        assert float(line.split()[-1]) < 1e-13
