@@ -156,6 +156,42 @@ def batch_leg(n_scenes=256, seed=1, passes=3):
             "autotune": tune, "queue_order": "scenes by ray count, fewest first"}
 
 
+def critical_leg(W=2048, spp=16, spin=0.998, n_acc=8000):
+    """2048x2048 at a = 0.998 with 16 spp, half the rays within +-2 % of the
+    critical curve (NP_JITTER_CRITICAL), every FP64 island on; fixed RK4 and
+    adaptive step doubling at rtol 1e-7; crossing error against the Mino-time
+    solver on critical-sampled rays."""
+    import torch
+    import nullpath_gb300 as npx
+    sc = npx.benchmark_scene(width=W, height=W, spp=spp, spin=spin).replace(jitter=npx.NP_JITTER_CRITICAL,
+                                                                           islands=npx.NP_ISLANDS_ALL)
+    from nullpath_gb300 import accuracy
+    from nullpath_gb300._abi import NP_INTEG_ADAPTIVE
+    rays = W * W * spp
+    out = {"rays": rays}
+    rgb = torch.zeros((3, W, W), dtype=torch.float32, device="cuda")
+    rc = torch.zeros((W, W), dtype=torch.float32, device="cuda")
+    cache = {}
+    for name, scn, precs in (("rk4", sc, ("mixed", "fp64")),
+                             ("adaptive_rtol_1e-7", sc.replace(integrator=NP_INTEG_ADAPTIVE, rtol=1e-7), ("mixed",))):
+        npx.render(scn, "mixed", rgb=rgb, rcross=rc)
+        _, _, st = npx.render(scn, "mixed", rgb=rgb, rcross=rc, stats=True)
+        leg = {"rays_per_s": rays / ((st.kernel_ms + st.init_ms) * 1e-3), "kernel_ms": st.kernel_ms + st.init_ms,
+               "mean_steps_per_ray": st.steps / max(1, st.rays), "fp64_steps_frac": st.fp64_steps / max(1, st.steps),
+               "deferred_rays": int(st.deferred_rays)}
+        for prec in precs:
+            leg["error_vs_geokerr_" + prec] = accuracy.crossing_error(scn, n=n_acc, precision=prec, seed=3,
+                                                                      critical=True, cache=cache)
+        out[name] = leg
+    # without FP64 islands: the same crossings, for the cost of the islands
+    bare = sc.replace(islands=0)
+    _, _, st = npx.render(bare, "mixed", rgb=rgb, rcross=rc, stats=True)
+    out["rk4_no_islands"] = {"rays_per_s": rays / ((st.kernel_ms + st.init_ms) * 1e-3),
+                             "error_vs_geokerr_mixed": accuracy.crossing_error(bare, n=n_acc, precision="mixed", seed=3,
+                                                                               critical=True, cache=cache)}
+    return out
+
+
 def adjoint_leg(Ks=(16, 64, 256)):
     """Differentiable render, 256x256x4 from seed 2: target (0.7, 60 deg, 1, 3),
     current (0.5, 50 deg, 0.8, 2.5), L2 loss.  FP32 adjoint per K (forward +
@@ -369,9 +405,13 @@ def run_ours(args):
             acc["adaptive_rtol_1e-7"]["rays_per_s"] = rays_per_step / ((sa.kernel_ms + sa.init_ms) * 1e-3)
             acc["adaptive_rtol_1e-7"]["mean_steps_per_ray"] = sa.steps / max(1, sa.rays)
             out["error_vs_geokerr"] = acc
-            out["geokerr_grid"] = geokerr_grid_leg()
-            out["adjoint_256x256x4"] = adjoint_leg()
-            out["batch_256_uneven"] = batch_leg()
+            leg_s = {}
+            for key, fn in (("geokerr_grid", geokerr_grid_leg), ("adjoint_256x256x4", adjoint_leg),
+                            ("batch_256_uneven", batch_leg), ("critical_2048x2048x16_a0998", critical_leg)):
+                t_leg = time.perf_counter()
+                out[key] = fn()
+                leg_s[key] = time.perf_counter() - t_leg
+            out["leg_seconds"] = leg_s
         if args.cpu_baseline:
             v, cores, desc = cpu_baseline()
             out["cpu_baseline"] = {"value": v, "unit": "rays/s", "cores": cores, "kind": "port", "sample": desc}

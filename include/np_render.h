@@ -48,7 +48,11 @@ typedef enum np_status {
 } np_status;
 
 typedef enum np_units { NP_UNITS_RS = 0, NP_UNITS_M = 1 } np_units;
-typedef enum np_jitter { NP_JITTER_WANGHASH = 0, NP_JITTER_STRATIFIED = 1 } np_jitter;
+/* NP_JITTER_CRITICAL: stratified jitter, and every odd sample moved along its
+ * position angle in the camera's tangent plane to within +-2 % of the
+ * critical curve's radius there (seeded by `seed`), so that half the rays of
+ * a pass are near-critical (importance sampling of the photon ring). */
+typedef enum np_jitter { NP_JITTER_WANGHASH = 0, NP_JITTER_STRATIFIED = 1, NP_JITTER_CRITICAL = 2 } np_jitter;
 typedef enum np_camera { NP_CAMERA_STATIC = 0, NP_CAMERA_ZAMO = 1 } np_camera;
 typedef enum np_integrator { NP_INTEG_RK4 = 0, NP_INTEG_ADAPTIVE = 1 } np_integrator;
 typedef enum np_crossing { NP_CROSS_LINEAR = 0, NP_CROSS_HERMITE = 1 } np_crossing;
@@ -133,6 +137,10 @@ void np_scene_benchmark(np_scene_t* scene);
 
 /* Prograde ISCO radius (Bardeen, Press & Teukolsky 1972) for mass M, spin a/M. */
 double np_isco_radius(double mass, double spin);
+/* Tangent-plane radius of the critical curve of `scene`'s camera at 256
+ * position angles psi_i = -pi + 2 pi i / 256 (the table NP_JITTER_CRITICAL
+ * samples around); host computation, no GPU needed. */
+int np_critical_curve(const np_scene_t* scene, float* rho);
 
 /* Validates a scene the way render.cu:431-465 validates its flags. */
 int np_scene_validate(const np_scene_t* scene);

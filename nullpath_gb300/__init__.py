@@ -8,7 +8,7 @@ Public Python surface (a thin layer over include/np_render.h):
 """
 from ._abi import (Scene, RenderStats, isco_radius, reference_defaults, benchmark_scene,
                    NP_PREC_FP64, NP_PREC_MIXED, NP_UNITS_RS, NP_UNITS_M,
-                   NP_JITTER_WANGHASH, NP_JITTER_STRATIFIED, NP_CAMERA_STATIC, NP_CAMERA_ZAMO,
+                   NP_JITTER_WANGHASH, NP_JITTER_STRATIFIED, NP_JITTER_CRITICAL, NP_CAMERA_STATIC, NP_CAMERA_ZAMO,
                    NP_INTEG_RK4, NP_INTEG_ADAPTIVE, NP_CROSS_LINEAR, NP_CROSS_HERMITE,
                    NP_BG_GRADIENT, NP_BG_POINT, NP_ISLAND_HORIZON, NP_ISLAND_TURNING,
                    NP_ISLAND_CRITICAL, NP_ISLANDS_ALL, NP_ISLANDS_DEFAULT)

@@ -13,7 +13,7 @@ NP_ERR_NO_DEVICE = -4
 NP_ERR_TIMEOUT = -5
 
 NP_UNITS_RS, NP_UNITS_M = 0, 1
-NP_JITTER_WANGHASH, NP_JITTER_STRATIFIED = 0, 1
+NP_JITTER_WANGHASH, NP_JITTER_STRATIFIED, NP_JITTER_CRITICAL = 0, 1, 2
 NP_CAMERA_STATIC, NP_CAMERA_ZAMO = 0, 1
 NP_INTEG_RK4, NP_INTEG_ADAPTIVE = 0, 1
 NP_CROSS_LINEAR, NP_CROSS_HERMITE = 0, 1

@@ -18,6 +18,7 @@ LIBNAME = "libnullpath_gb300.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
+           "-Xcompiler", "-ffp-contract=off",
            "-I" + INCLUDE, "-I" + CSRC]
 
 CU_SOURCES = ["np_render.cu", "geokerr.cu", "adjoint.cu", "kerr_api.cu", "carlson.cu"]

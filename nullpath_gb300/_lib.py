@@ -22,6 +22,7 @@ PROTOTYPES = {
     "np_scene_defaults": (None, [C.POINTER(Scene)]),
     "np_scene_benchmark": (None, [C.POINTER(Scene)]),
     "np_isco_radius": (C.c_double, [C.c_double, C.c_double]),
+    "np_critical_curve": (C.c_int, [C.POINTER(Scene), C.c_void_p]),
     "np_scene_validate": (C.c_int, [C.POINTER(Scene)]),
     "np_render_device": (C.c_int, [C.POINTER(Scene), C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
                                    C.c_int, C.c_void_p, C.POINTER(RenderStats)]),

@@ -26,14 +26,53 @@ def doppler_g(r, E, L, M, a):
     return np.maximum(E / np.maximum(ut * (E - Om * L), 1e-18), 0.0)
 
 
-def crossing_error(scene, n=20000, precision="mixed", seed=0, orders=2):
+def critical_positions(scene, n, seed=0, band=0.02):
+    """n image positions, uniform over the frame, of which every second one
+    is moved along its position angle to within +-band of the critical curve
+    (the sampling of NP_JITTER_CRITICAL, from the library's critical-curve
+    table)."""
+    import ctypes as C
+    from ._lib import load, check
+    rho_c = np.zeros(256, dtype=np.float32)
+    check(load().np_critical_curve(C.byref(scene), rho_c.ctypes.data))
+    rng = np.random.default_rng(seed)
+    W, H = scene.width, scene.height
+    th = math.tan(math.radians(scene.fov_y_deg) / 2)
+    asp = W / H
+    px = rng.uniform(0.0, W, n)
+    py = rng.uniform(0.0, H, n)
+    cx = (px / W * 2 - 1) * asp * th
+    cy = -(py / H * 2 - 1) * th
+    psi = np.arctan2(cy, cx)
+    t = (psi + math.pi) * (256 / (2 * math.pi))
+    i0 = np.floor(t).astype(int)
+    fr = t - i0
+    i0 %= 256
+    rc = (1 - fr) * rho_c[i0] + fr * rho_c[(i0 + 1) % 256]
+    rho = rc * (1 + band * rng.uniform(-1, 1, n))
+    sel = np.arange(n) % 2 == 1
+    cx = np.where(sel, rho * np.cos(psi), cx)
+    cy = np.where(sel, rho * np.sin(psi), cy)
+    return (cx / (asp * th) + 1) / 2 * W, (1 - cy / th) / 2 * H
+
+
+def crossing_error(scene, n=20000, precision="mixed", seed=0, orders=2, critical=False, cache=None):
+    """Crossing radius, crossing azimuth and intensity of the first `orders`
+    disk crossings of n rays, traced by the renderer, against the Mino-time
+    solver's equatorial crossings of the same rays.  critical=True samples
+    half the rays within +-2 % of the critical curve.  `cache` (a dict) keeps
+    the solver's crossings between calls on the same rays (same camera, n,
+    seed, sampling), whatever the precision or integrator."""
     import torch
     from .render import trace_rays
     from . import geokerr as gk
 
-    rng = np.random.default_rng(seed)
-    px = rng.uniform(0.0, scene.width, n)
-    py = rng.uniform(0.0, scene.height, n)
+    if critical:
+        px, py = critical_positions(scene, n, seed)
+    else:
+        rng = np.random.default_rng(seed)
+        px = rng.uniform(0.0, scene.width, n)
+        py = rng.uniform(0.0, scene.height, n)
     out = trace_rays(scene, px, py, precision)
     torch.cuda.synchronize()
     consts = out["consts"].cpu().numpy()
@@ -41,11 +80,17 @@ def crossing_error(scene, n=20000, precision="mixed", seed=0, orders=2):
     M = scene.mass
     lunit = M if scene.units == 1 else 2.0 * M
     a = scene.spin * M
-    u0, mu0, l, q2, su, sm = gk.render_ray_constants(consts, scene)
-    r_far = scene.escape_r if scene.escape_r > 0 else (scene.r_cam + 20.0) * lunit
-    xu, xphi, nx = gk.equator_crossings(scene.spin, u0, mu0, l, q2, su, sm, M / r_far, 4)
-    xr_ref = np.where(xu.cpu().numpy() > 0, M / np.maximum(xu.cpu().numpy(), 1e-300), 0.0)
-    xphi_ref = xphi.cpu().numpy()
+    key = (n, seed, bool(critical), scene.width, scene.height, scene.spin, scene.theta_deg, scene.r_cam, scene.mass)
+    if cache is not None and key in cache and np.array_equal(cache[key][0], consts):
+        xr_ref, xphi_ref = cache[key][1], cache[key][2]
+    else:
+        u0, mu0, l, q2, su, sm = gk.render_ray_constants(consts, scene)
+        r_far = scene.escape_r if scene.escape_r > 0 else (scene.r_cam + 20.0) * lunit
+        xu, xphi, nx = gk.equator_crossings(scene.spin, u0, mu0, l, q2, su, sm, M / r_far, 4)
+        xr_ref = np.where(xu.cpu().numpy() > 0, M / np.maximum(xu.cpu().numpy(), 1e-300), 0.0)
+        xphi_ref = xphi.cpu().numpy()
+        if cache is not None:
+            cache[key] = (consts.copy(), xr_ref, xphi_ref)
     E = -consts[:, 0]
     L = consts[:, 1]
     rin = scene.disk_rin if scene.disk_rin > 0 else 3.0 * 2.0 * M

@@ -29,6 +29,8 @@ constexpr double kCriticalDb = 1e-3;   // in M
 // Per-scene constants, computed once on the host in double precision and
 // passed by value (kernel parameters live in the constant bank, so every
 // lane reads them as a broadcast).
+constexpr int kCritN = 256;
+
 struct SceneDev {
     int W, H, spp, sample_offset;
     long long npix, total;            // pixels, rays (= npix * spp)
@@ -52,6 +54,10 @@ struct SceneDev {
     float hmin_f, hmax_f, rtol_f, atol_f;
     double hmin, hmax;         // adaptive step bounds (hmax scales with r in units of M)
     int island_batch;
+    // NP_JITTER_CRITICAL: tangent-plane radius of the critical curve at
+    // kCritN equally spaced position angles from -pi, and the band half-width
+    float crit_rho[kCritN];
+    double crit_band;
 };
 
 // ---------------------------------------------------------------------------
@@ -78,6 +84,26 @@ __host__ __device__ __forceinline__ uint32_t mix32(uint32_t x) {
 __host__ __device__ __forceinline__ double strat_unit(uint32_t seed, uint32_t pix, uint32_t sample, uint32_t dim) {
     uint32_t h = mix32(mix32(mix32(seed + 0x9e3779b9u * (dim + 1u)) ^ pix) ^ (sample * 0x85ebca6bu));
     return (double)(h >> 8) * (1.0 / 16777216.0);
+}
+
+// Critical-curve importance sampling (NP_JITTER_CRITICAL): odd samples move
+// along their position angle psi in the camera's tangent plane to
+// rho_c(psi) (1 + band (2u - 1)), u a seeded uniform, so that half the rays
+// lie within +-band of the critical impact parameter (the tangent-plane
+// radius is b / r_cam to first order).
+__host__ __device__ __forceinline__ void critical_remap(const SceneDev& s, uint32_t pix, uint32_t sample, double& cx,
+                                                        double& cy) {
+    const double psi = atan2(cy, cx);
+    const double t = (psi + kPi) * ((double)kCritN / (2.0 * kPi));
+    int i0 = (int)floor(t);
+    const double fr = t - (double)i0;
+    i0 = ((i0 % kCritN) + kCritN) % kCritN;
+    const int i1 = (i0 + 1) % kCritN;
+    const double rc = (1.0 - fr) * (double)s.crit_rho[i0] + fr * (double)s.crit_rho[i1];
+    const double u = strat_unit(s.seed, pix, sample, 2);
+    const double rho = rc * (1.0 + s.crit_band * (2.0 * u - 1.0));
+    cx = rho * cos(psi);
+    cy = rho * sin(psi);
 }
 
 struct CamDir { double nr, nth, nph; float cam_x, cam_y; };
@@ -107,6 +133,11 @@ __device__ __forceinline__ CamDir camera_dir(const SceneDev& s, int x, int y, ui
         float ndc_y = __fsub_rn(__fmul_rn(__fdiv_rn(py, (float)s.H), 2.0f), 1.0f);
         float cx = __fmul_rn(__fmul_rn(ndc_x, s.aspect_f), s.tan_half_f);
         float cy = __fmul_rn(-ndc_y, s.tan_half_f);
+        if (!explicit_pos && s.jitter == NP_JITTER_CRITICAL && (sample & 1u)) {
+            double dx = cx, dy = cy;
+            critical_remap(s, (uint32_t)(y * s.W + x), sample, dx, dy);
+            cx = (float)dx; cy = (float)dy;
+        }
         float cz = -1.0f;
         float n2 = __fadd_rn(__fadd_rn(__fmul_rn(cx, cx), __fmul_rn(cy, cy)), __fmul_rn(cz, cz));
         float nrm = __fdiv_rn(1.0f, __fsqrt_rn(n2));
@@ -130,6 +161,8 @@ __device__ __forceinline__ CamDir camera_dir(const SceneDev& s, int x, int y, ui
         double ndc_y = __dsub_rn(__dmul_rn(__ddiv_rn(py, (double)s.H), 2.0), 1.0);
         double cx = __dmul_rn(__dmul_rn(ndc_x, s.aspect), s.tan_half);
         double cy = __dmul_rn(-ndc_y, s.tan_half);
+        if (!explicit_pos && s.jitter == NP_JITTER_CRITICAL && (sample & 1u))
+            critical_remap(s, (uint32_t)(y * s.W + x), sample, cx, cy);
         double cz = -1.0;
         double n2 = __dadd_rn(__dadd_rn(__dmul_rn(cx, cx), __dmul_rn(cy, cy)), __dmul_rn(cz, cz));
         double nrm = __ddiv_rn(1.0, __dsqrt_rn(n2));

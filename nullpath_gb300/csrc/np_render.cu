@@ -88,6 +88,42 @@ void host_metric_cov(double M, double a, double r, double th,
     ghh = Sig;
 }
 
+// Radius of the critical curve in the camera's tangent plane at kCritN
+// position angles psi_i = -pi + 2 pi i / kCritN: bisection on the radius for
+// the sign change of critical_gap (captured inside, turning outside) of the
+// camera ray through (rho cos psi, rho sin psi, -1), with the camera tetrad
+// of the scene.  Clamped to [0, frame corner].
+void build_critical_table(SceneDev& d) {
+    const double rho_max = (d.ref_units ? (double)d.tan_half_f * std::sqrt((double)d.aspect_f * d.aspect_f + 1.0)
+                                        : d.tan_half * std::sqrt(d.aspect * d.aspect + 1.0));
+    const double c = d.cos_cam, sn = d.sin_cam;
+    auto captured = [&](double rho, double psi) {
+        const double cx = rho * std::cos(psi), cy = rho * std::sin(psi), cz = -1.0;
+        const double nrm = 1.0 / std::sqrt(cx * cx + cy * cy + cz * cz);
+        const double nr = cz * nrm, nth = cy * nrm, nph = cx * nrm;
+        const double Pt = d.T0 + nph * d.T1, Pp = d.P0 + nph * d.P1, Pr = nr * d.R1, Ph = nth * d.H1;
+        (void)Pr;
+        const double pt = d.gtt * Pt + d.gtp * Pp, pth = d.ghh * Ph, pph = d.gtp * Pt + d.gpp * Pp;
+        const double E = -pt, L = pph;
+        const double Q = pth * pth + c * c * (L * L / (sn * sn) - d.a * d.a * E * E);
+        return critical_gap(E, L, Q, d.a, d.M, d.r_plus) > 0.0;
+    };
+    for (int i = 0; i < kCritN; ++i) {
+        const double psi = -kPi + 2.0 * kPi * (double)i / (double)kCritN;
+        double lo = 0.0, hi = rho_max, out;
+        if (!captured(lo, psi)) out = 0.0;
+        else if (captured(hi, psi)) out = rho_max;
+        else {
+            for (int it = 0; it < 60; ++it) {
+                const double mid = 0.5 * (lo + hi);
+                if (captured(mid, psi)) lo = mid; else hi = mid;
+            }
+            out = 0.5 * (lo + hi);
+        }
+        d.crit_rho[i] = (float)out;
+    }
+}
+
 // Builds the per-scene constants; camera tetrads follow bh_kerr.h:781-826
 // (static observer) and 910-967 (ZAMO), the static observer falling back to
 // the ZAMO inside the ergosphere (render.cu:163-170).
@@ -203,6 +239,8 @@ int prepare_scene(const np_scene_t& sc, SceneDev& d) {
         d.R1 = std::sqrt(std::fmax(kEps, Del / Sig));
         d.H1 = 1.0 / std::sqrt(Sig);
     }
+    d.crit_band = 0.02;
+    if (sc.jitter == NP_JITTER_CRITICAL) build_critical_table(d);
     return NP_OK;
 }
 
@@ -641,6 +679,17 @@ void np_scene_defaults(np_scene_t* s) {
     s->check_invariants = 0; s->islands = NP_ISLANDS_DEFAULT;
 }
 
+int np_critical_curve(const np_scene_t* scene, float* rho) {
+    if (!scene || !rho) return fail(NP_ERR_INVALID, "NULL argument");
+    np_scene_t sc = *scene;
+    sc.jitter = NP_JITTER_CRITICAL;
+    SceneDev d;
+    int rc = prepare_scene(sc, d);
+    if (rc != NP_OK) return rc;
+    for (int i = 0; i < kCritN; ++i) rho[i] = d.crit_rho[i];
+    return NP_OK;
+}
+
 double np_isco_radius(double mass, double spin) {
     double a = spin;
     double z1 = 1.0 + std::cbrt(1.0 - a * a) * (std::cbrt(1.0 + a) + std::cbrt(1.0 - a));
@@ -673,6 +722,8 @@ int np_scene_validate(const np_scene_t* s) {
     if (s->max_steps <= 0) return fail(NP_ERR_INVALID, "Invalid step cap.");
     if (!(s->step_scale > 0.0)) return fail(NP_ERR_INVALID, "Invalid step scale.");
     if (s->units != NP_UNITS_RS && s->units != NP_UNITS_M) return fail(NP_ERR_INVALID, "Invalid units.");
+    if (s->jitter != NP_JITTER_WANGHASH && s->jitter != NP_JITTER_STRATIFIED && s->jitter != NP_JITTER_CRITICAL)
+        return fail(NP_ERR_INVALID, "Invalid jitter mode.");
     if (s->integrator != NP_INTEG_RK4 && s->integrator != NP_INTEG_ADAPTIVE)
         return fail(NP_ERR_INVALID, "Invalid integrator.");
     if ((long long)s->width * s->height > (1ll << 40) / std::max(1, s->spp))

@@ -397,15 +397,15 @@ __device__ __forceinline__ bool mray_island(MRay<PHI>& R, const SceneDev& s, con
     return mray_finish_step(R, s, k, h, r0, th0, k0r, k0t, ph0, k0p);
 }
 
-// Closeness of a ray to the critical curve.  R(r) = P(r)^2 - Delta K
+// Signed closeness of a ray to the critical curve.  R(r) = P(r)^2 - Delta K
 // (K = Q + (L - aE)^2) has a double root at the spherical photon orbit r_c
 // exactly for critical rays; r_c solves R'(r) = 0, the depressed cubic
-//   4 E^2 r^3 + (4 a^2 E^2 - 4 a E L - 2 K) r + 2 M K = 0,
-// and near the curve |R(r_c)| / (E^2 r_c^4) ~ |dR/db| |b - b_crit| / r_c^4.
-// The scale 0.385/M is that derivative for the Schwarzschild photon sphere,
-// so the test reads |b - b_crit| < db_thr (in M).
-__device__ __forceinline__ bool near_critical(double E, double L, double Q, double a, double M,
-                                              double rp, double db_thr) {
+//   4 E^2 r^3 + (4 a^2 E^2 - 4 a E L - 2 K) r + 2 M K = 0.
+// Returns R(r_c) / (E^2 r_c^4): positive for rays that fall in (no radial
+// turning point outside the horizon), negative for rays that turn, and a
+// huge positive value when R has no minimum outside r_+ (captured).  Near the
+// curve |R(r_c)| / (E^2 r_c^4) ~ |dR/db| |b - b_crit| / r_c^4.
+__host__ __device__ __forceinline__ double critical_gap(double E, double L, double Q, double a, double M, double rp) {
     double K = Q + (L - a * E) * (L - a * E);
     double c3 = 4.0 * E * E;
     double c1 = 4.0 * a * a * E * E - 4.0 * a * E * L - 2.0 * K;
@@ -421,12 +421,19 @@ __device__ __forceinline__ bool near_critical(double E, double L, double Q, doub
         r -= dr;
         if (fabs(dr) < 1e-12 * r) break;
     }
-    if (!(r > rp)) return false;
+    if (!(r > rp)) return 1e300;
     double r2 = r * r, a2 = a * a;
     double P = (r2 + a2) * E - a * L;
     double Del = r2 - 2.0 * M * r + a2;
-    double R = P * P - Del * K;
-    return fabs(R) / (E * E * r2 * r2) < 0.385 * db_thr / M;
+    return (P * P - Del * K) / (E * E * r2 * r2);
+}
+
+// |b - b_crit| < db_thr (in M): the scale 0.385/M is |dR/db| / r_c^4 of the
+// Schwarzschild photon sphere.
+__host__ __device__ __forceinline__ bool near_critical(double E, double L, double Q, double a, double M,
+                                                       double rp, double db_thr) {
+    double g = critical_gap(E, L, Q, a, M, rp);
+    return g < 1e299 && fabs(g) < 0.385 * db_thr / M;
 }
 
 // RK4 increments d = h/6 (k1 + 2 k2 + 2 k3 + k4) of (r, theta, p_r, p_theta[, phi])

@@ -31,6 +31,8 @@ def load():
         lib.npo_trace_rays.argtypes = [S, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                        C.c_void_p, C.c_void_p, C.c_int]
         lib.npo_trace_rays.restype = C.c_int
+        lib.npo_critical_curve.argtypes = [S, C.c_void_p]
+        lib.npo_critical_curve.restype = C.c_int
         lib.npo_metric_inv.argtypes = [C.c_double] * 4 + [C.c_void_p]
         lib.npo_metric_inv.restype = None
         lib.npo_metric_inv_derivs.argtypes = [C.c_double] * 4 + [C.c_void_p, C.c_void_p]
@@ -203,3 +205,11 @@ def geokerr_crossings(u0, mu0, a, l, q2, su, sm, u_end=1e-3, K=4):
     xu, xphi = np.zeros(K), np.zeros(K)
     n = lib.npo_geokerr_crossings(u0, mu0, a, l, q2, su, sm, u_end, K, _vp(xu), _vp(xphi))
     return n, xu, xphi
+
+
+def critical_curve(scene):
+    """The oracle's critical-curve table (256 tangent-plane radii) of `scene`."""
+    rho = np.zeros(256, dtype=np.float32)
+    if load().npo_critical_curve(C.byref(scene), rho.ctypes.data) != 0:
+        raise RuntimeError("npo_critical_curve failed")
+    return rho

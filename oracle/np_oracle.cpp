@@ -341,7 +341,34 @@ struct Frame {
     float bg_sigma_rad, bg_peak;
     uint32_t seed;
     double rtol, atol;
+    float crit_rho[256];          // NP_JITTER_CRITICAL: critical-curve radius per position angle
+    double crit_band;
 };
+
+// R(r_c) / (E^2 r_c^4) at the largest root r_c of R'(r) = 0 for
+// R(r) = P^2 - Delta K: > 0 for rays without a radial turning point outside
+// the horizon (captured), < 0 for turning rays; 1e300 when R has no minimum
+// outside r_+ (captured).
+static double critical_gap(double E, double L, double Q, double a, double M, double rp) {
+    double K = Q + (L - a * E) * (L - a * E);
+    double c3 = 4.0 * E * E;
+    double c1 = 4.0 * a * a * E * E - 4.0 * a * E * L - 2.0 * K;
+    double c0 = 2.0 * M * K;
+    double r = std::sqrt(std::fmax(0.0, -c1 / c3)) + 4.0 * M;
+    for (int it = 0; it < 30; ++it) {
+        double fv = (c3 * r * r + c1) * r + c0;
+        double fp = 3.0 * c3 * r * r + c1;
+        if (fp <= 0.0) break;
+        double dr = fv / fp;
+        r -= dr;
+        if (std::fabs(dr) < 1e-12 * r) break;
+    }
+    if (!(r > rp)) return 1e300;
+    double r2 = r * r, a2 = a * a;
+    double P = (r2 + a2) * E - a * L;
+    double Del = r2 - 2.0 * M * r + a2;
+    return (P * P - Del * K) / (E * E * r2 * r2);
+}
 
 static Frame make_frame(const np_scene_t& s) {
     Frame f{};
@@ -388,7 +415,54 @@ static Frame make_frame(const np_scene_t& s) {
     f.bg_sigma_rad = (float)s.bg_sigma_deg * kPiF / 180.0f;
     f.bg_peak = (float)s.bg_brightness;
     f.rtol = s.rtol; f.atol = s.atol;
+    f.crit_band = 0.02;
+    if (s.jitter == NP_JITTER_CRITICAL) {
+        // bisection on the tangent-plane radius along each position angle
+        const double rho_max = f.ref_units ? (double)f.tan_half_f * std::sqrt((double)f.aspect_f * f.aspect_f + 1.0)
+                                           : f.tan_half * std::sqrt(f.aspect * f.aspect + 1.0);
+        const double rp = f.M + std::sqrt(std::fmax(0.0, f.M * f.M - f.a * f.a));
+        const double c = std::cos(f.th_cam), sn = std::sin(f.th_cam);
+        auto captured = [&](double rho, double psi) {
+            double cx = rho * std::cos(psi), cy = rho * std::sin(psi), cz = -1.0;
+            double nrm = 1.0 / std::sqrt(cx * cx + cy * cy + cz * cz);
+            State y = f.zamo ? camera_zamo(f.M, f.a, f.r_cam, f.th_cam, f.ph_cam, cz * nrm, cy * nrm, cx * nrm)
+                             : camera_static(f.M, f.a, f.r_cam, f.th_cam, f.ph_cam, cz * nrm, cy * nrm, cx * nrm);
+            double E = -y.pt, L = y.pph;
+            double Q = y.pth * y.pth + c * c * (L * L / (sn * sn) - f.a * f.a * E * E);
+            return critical_gap(E, L, Q, f.a, f.M, rp) > 0.0;
+        };
+        for (int i = 0; i < 256; ++i) {
+            double psi = -kPi + 2.0 * kPi * (double)i / 256.0;
+            double lo = 0.0, hi = rho_max, out;
+            if (!captured(lo, psi)) out = 0.0;
+            else if (captured(hi, psi)) out = rho_max;
+            else {
+                for (int it = 0; it < 60; ++it) {
+                    double mid = 0.5 * (lo + hi);
+                    if (captured(mid, psi)) lo = mid; else hi = mid;
+                }
+                out = 0.5 * (lo + hi);
+            }
+            f.crit_rho[i] = (float)out;
+        }
+    }
     return f;
+}
+
+// Odd samples of NP_JITTER_CRITICAL move along their position angle to
+// rho_c(psi) (1 + band (2u - 1)) in the tangent plane.
+static void critical_remap(const Frame& f, uint32_t pix, uint32_t sample, double& cx, double& cy) {
+    double psi = std::atan2(cy, cx);
+    double t = (psi + kPi) * (256.0 / (2.0 * kPi));
+    int i0 = (int)std::floor(t);
+    double fr = t - (double)i0;
+    i0 = ((i0 % 256) + 256) % 256;
+    int i1 = (i0 + 1) % 256;
+    double rc = (1.0 - fr) * (double)f.crit_rho[i0] + fr * (double)f.crit_rho[i1];
+    double u = strat_unit(f.seed, pix, sample, 2);
+    double rho = rc * (1.0 + f.crit_band * (2.0 * u - 1.0));
+    cx = rho * std::cos(psi);
+    cy = rho * std::sin(psi);
 }
 
 // Camera direction for sample `sample` of pixel (x, y) (render.cu:143-159),
@@ -416,6 +490,11 @@ static Dir camera_dir(const Frame& f, const np_scene_t& s, int x, int y, uint32_
         float ndc_y = (py / (float)s.height) * 2.0f - 1.0f;
         float cx = ndc_x * f.aspect_f * f.tan_half_f;
         float cy = -ndc_y * f.tan_half_f;
+        if (!explicit_pos && f.jitter == NP_JITTER_CRITICAL && (sample & 1u)) {
+            double dx = cx, dy = cy;
+            critical_remap(f, (uint32_t)(y * s.width + x), sample, dx, dy);
+            cx = (float)dx; cy = (float)dy;
+        }
         float cz = -1.0f;
         float nrm = 1.0f / std::sqrt(cx * cx + cy * cy + cz * cz);
         cx *= nrm; cy *= nrm; cz *= nrm;
@@ -438,6 +517,8 @@ static Dir camera_dir(const Frame& f, const np_scene_t& s, int x, int y, uint32_
         double ndc_y = (py / s.height) * 2.0 - 1.0;
         double cx = ndc_x * f.aspect * f.tan_half;
         double cy = -ndc_y * f.tan_half;
+        if (!explicit_pos && f.jitter == NP_JITTER_CRITICAL && (sample & 1u))
+            critical_remap(f, (uint32_t)(y * s.width + x), sample, cx, cy);
         double cz = -1.0;
         double nrm = 1.0 / std::sqrt(cx * cx + cy * cy + cz * cz);
         cx *= nrm; cy *= nrm; cz *= nrm;
@@ -731,6 +812,15 @@ int npo_trace_rays(const np_scene_t* sc, int n, const double* px, const double* 
 }
 
 int npo_abi_version(void) { return NP_ABI_VERSION; }
+
+int npo_critical_curve(const np_scene_t* sc, float* rho) {
+    if (!sc || !rho) return -1;
+    np_scene_t s = *sc;
+    s.jitter = NP_JITTER_CRITICAL;
+    Frame f = make_frame(s);
+    for (int i = 0; i < 256; ++i) rho[i] = f.crit_rho[i];
+    return 0;
+}
 
 // Raw metric blocks (order tt, tphi, phiphi, rr, thth) for unit checks.
 void npo_metric_inv(double M, double a, double r, double th, double* g5) { metric_inv(M, a, r, th, g5); }

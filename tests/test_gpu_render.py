@@ -172,3 +172,15 @@ def test_mixed_adaptive_matches_oracle(cuda):
     for prec in ("fp64", "mixed"):
         rgb, rc = _render_np(sc, prec)
         _compare(rgb, rc, ref_rgb, ref_rc, 1e-3, 3e-4, 0.95)
+
+
+def test_critical_sampling_matches_oracle(cuda):
+    """NP_JITTER_CRITICAL at a = 0.998: half the samples sit within +-2 % of
+    the critical curve, where outcomes are most sensitive to rounding, so the
+    bars are per-pixel agreement fractions."""
+    sc = benchmark_scene(width=40, height=40, spp=4, spin=0.998).replace(jitter=npx.NP_JITTER_CRITICAL)
+    ref_rgb, ref_rc = oracle.render(sc)
+    for prec, frac in (("fp64", 0.97), ("mixed", 0.9)):
+        rgb, rc = _render_np(sc, prec)
+        close = np.isclose(rgb, ref_rgb, rtol=1e-3, atol=1e-6).all(axis=0).mean()
+        assert close >= frac, (prec, close)
