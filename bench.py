@@ -361,7 +361,9 @@ def run_ours(args):
             "kernel_ms": {"tracer": kern_ms, "ray_init": statistics.mean(s.init_ms for s in stats)},
             "roofline": {"bound": "fp32" if args.precision == "mixed" else "fp64", "achieved": achieved,
                          "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
-                         "traffic": None,
+                         "traffic": oc["dram_bytes_per_ray"] * rays_per_step,
+                         "traffic_source": "ncu DRAM bytes per ray of render_mixed_kernel (640x360x4 capture) "
+                                           "scaled to the rays of one launch",
                          "peak_source": "measured in this run by np_measure_fma_peak (register FMA loop)"},
             "e2e": {"value": ws * rays_per_step / (e2e * 1e-3), "unit": "rays/s", "h2d_bytes_per_step": C.sizeof(sc),
                     "d2h_bytes_per_step": 4 * H * W * 4},
