@@ -275,7 +275,8 @@ def run_ours(args):
     lib = npx.load()
     # FP64 within 0.1 M of the horizon, at turning points and for near-critical
     # impact parameters: every island of the mixed path
-    sc = npx.benchmark_scene(seed=rank).replace(islands=npx.NP_ISLANDS_ALL)
+    from nullpath_gb300 import replicas
+    sc = replicas.rank_scene(npx.benchmark_scene(seed=0).replace(islands=npx.NP_ISLANDS_ALL), rank)
     H, W = sc.height, sc.width
     rays_per_step = W * H * sc.spp
     rgb = torch.zeros((3, H, W), dtype=torch.float32, device="cuda")
@@ -306,11 +307,7 @@ def run_ours(args):
     barrier()
     wall = time.perf_counter() - t0
     step_ms = [a.elapsed_time(b) for a, b in ev]
-    ms = statistics.mean(step_ms)
-    if ws > 1:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = replicas.max_over_ranks(statistics.mean(step_ms), device="cuda")
 
     # end-to-end through the host API: scene in, host image out (copies inside)
     pinned_rgb = torch.empty((3, H, W), dtype=torch.float32).pin_memory()
@@ -325,11 +322,7 @@ def run_ours(args):
                                           None, None))
         if i > 0:
             e2e_ms.append((time.perf_counter() - s0) * 1e3)
-    e2e = statistics.mean(e2e_ms)
-    if ws > 1:
-        t = torch.tensor([e2e], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e = float(t.item())
+    e2e = replicas.max_over_ranks(statistics.mean(e2e_ms), device="cuda")
 
     if sampler is not None:
         sampler.terminate()
@@ -345,7 +338,7 @@ def run_ours(args):
         achieved = flop_step * steps_main / (kern_ms * 1e-3) / 1e12
         peak = ctypes_peak(lib, 0 if args.precision == "mixed" else 1)
         out = {
-            "metric": METRIC, "value": ws * rays_per_step / (ms * 1e-3), "unit": "rays/s",
+            "metric": METRIC, "value": replicas.aggregate_rays_per_s(rays_per_step, ms, ws), "unit": "rays/s",
             "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32+f64" if args.precision == "mixed" else "f64", "data": "synthetic",
@@ -365,7 +358,8 @@ def run_ours(args):
                          "traffic_source": "ncu DRAM bytes per ray of render_mixed_kernel (640x360x4 capture) "
                                            "scaled to the rays of one launch",
                          "peak_source": "measured in this run by np_measure_fma_peak (register FMA loop)"},
-            "e2e": {"value": ws * rays_per_step / (e2e * 1e-3), "unit": "rays/s", "h2d_bytes_per_step": C.sizeof(sc),
+            "e2e": {"value": replicas.aggregate_rays_per_s(rays_per_step, e2e, ws), "unit": "rays/s",
+                    "h2d_bytes_per_step": C.sizeof(sc),
                     "d2h_bytes_per_step": 4 * H * W * 4},
             "gpu_launches": 3 * args.steps,
             "clocks": clocks,
