@@ -116,6 +116,18 @@ int np_carlson_batch_device(int n, const char* d_types, const double* d_x, const
                             const double* d_p, double* d_out, void* stream);
 int np_carlson_batch_host(int n, const char* types, const double* x, const double* y, const double* z,
                           const double* p, double* out);
+/* Semi-analytic Mino times with Carlson's R_F (E = 1, a the spin, l[i] =
+ * L/E, q2[i] = Q/E^2): lam_u[i] = int du / sqrt(U(u)) from ua[i] to ub[i] and
+ * lam_mu[i] = int dmu / sqrt(M(mu)) from mua[i] to mub[i], each on one
+ * monotonic segment of the radial and polar motion (no turning point strictly
+ * inside; endpoints may be turning points).  The radial form needs U's roots
+ * real (NaN otherwise), the polar form q2 > 0 (NaN otherwise).  Device
+ * pointers on `stream`, or host pointers; np_status. */
+int np_geokerr_mino_times_device(int n, double a, const double* d_ua, const double* d_ub, const double* d_mua,
+                                 const double* d_mub, const double* d_l, const double* d_q2, double* d_lam_u,
+                                 double* d_lam_mu, void* stream);
+int np_geokerr_mino_times_host(int n, double a, const double* ua, const double* ub, const double* mua,
+                               const double* mub, const double* l, const double* q2, double* lam_u, double* lam_mu);
 /* The reference's host entry points (carlson_elliptic.cu:387, 398): a
  * device-vs-host check printed per function, and R_F(1, 2, 0) printed. */
 void validate_carlson_cuda(void);

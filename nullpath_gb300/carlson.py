@@ -49,3 +49,37 @@ def evaluate(kinds, x, y, z=None, p=None, device=True):
                                       C.c_void_p(out.data_ptr()), C.c_void_p(torch.cuda.current_stream().cuda_stream)))
     torch.cuda.synchronize()
     return out.cpu().numpy()
+
+
+_MINO = {
+    "np_geokerr_mino_times_device": (C.c_int, [C.c_int, C.c_double] + [C.c_void_p] * 8 + [C.c_void_p]),
+    "np_geokerr_mino_times_host": (C.c_int, [C.c_int, C.c_double] + [C.c_void_p] * 8),
+}
+
+
+def mino_times(a, ua, ub, mua, mub, l, q2, device=True):
+    """Semi-analytic Mino times (lam_u, lam_mu) of monotonic radial and polar
+    segments with Carlson's R_F (np_geokerr_mino_times_*)."""
+    lib = _lib()
+    if not getattr(lib, "_mino_ready", False):
+        for name, (res, args) in _MINO.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        lib._mino_ready = True
+    ins = [np.ascontiguousarray(np.broadcast_to(np.asarray(v, dtype=np.float64), np.shape(ua)))
+           for v in (ua, ub, mua, mub, l, q2)]
+    n = ins[0].size
+    if not device:
+        lu, lm = np.empty(n), np.empty(n)
+        check(lib.np_geokerr_mino_times_host(n, a, *[v.ctypes.data for v in ins], lu.ctypes.data, lm.ctypes.data))
+        return lu, lm
+    import torch
+    d = [torch.from_numpy(v.ravel().copy()).cuda() for v in ins]
+    lu = torch.empty(n, dtype=torch.float64, device="cuda")
+    lm = torch.empty(n, dtype=torch.float64, device="cuda")
+    check(lib.np_geokerr_mino_times_device(n, a, *[C.c_void_p(t.data_ptr()) for t in d], C.c_void_p(lu.data_ptr()),
+                                           C.c_void_p(lm.data_ptr()),
+                                           C.c_void_p(torch.cuda.current_stream().cuda_stream)))
+    torch.cuda.synchronize()
+    return lu.cpu().numpy(), lm.cpu().numpy()

@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 
 #include "carlson.cuh"
+#include "mino_carlson.cuh"
 #include "geokerr_c_api.h"
 #include "np_render.h"
 
@@ -34,9 +35,52 @@ __global__ void carlson_batch_kernel(int n, const char* __restrict__ types, cons
         out[i] = carlson_case(types[2 * i], types[2 * i + 1], x[i], y[i], z[i], p ? p[i] : 0.0);
 }
 
+__global__ void mino_times_kernel(int n, double a, const double* __restrict__ ua, const double* __restrict__ ub,
+                                  const double* __restrict__ mua, const double* __restrict__ mub,
+                                  const double* __restrict__ l, const double* __restrict__ q2,
+                                  double* __restrict__ lam_u, double* __restrict__ lam_mu) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        lam_u[i] = np::mino::mino_u(a, l[i], q2[i], ua[i], ub[i]);
+        lam_mu[i] = np::mino::mino_mu(a, l[i], q2[i], mua[i], mub[i]);
+    }
+}
+
 }  // namespace
 
 extern "C" {
+
+int np_geokerr_mino_times_device(int n, double a, const double* d_ua, const double* d_ub, const double* d_mua,
+                                 const double* d_mub, const double* d_l, const double* d_q2, double* d_lam_u,
+                                 double* d_lam_mu, void* stream) {
+    if (n < 0 || (n > 0 && (!d_ua || !d_ub || !d_mua || !d_mub || !d_l || !d_q2 || !d_lam_u || !d_lam_mu))) {
+        np_record_error("np_geokerr_mino_times_device: NULL buffer or negative count");
+        return NP_ERR_INVALID;
+    }
+    if (n == 0) return NP_OK;
+    const int threads = 128;
+    const int blocks = (n + threads - 1) / threads < 152 * 16 ? (n + threads - 1) / threads : 152 * 16;
+    mino_times_kernel<<<blocks, threads, 0, (cudaStream_t)stream>>>(n, a, d_ua, d_ub, d_mua, d_mub, d_l, d_q2, d_lam_u,
+                                                                   d_lam_mu);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        np_record_error(cudaGetErrorString(e));
+        return NP_ERR_KERNEL;
+    }
+    return NP_OK;
+}
+
+int np_geokerr_mino_times_host(int n, double a, const double* ua, const double* ub, const double* mua,
+                               const double* mub, const double* l, const double* q2, double* lam_u, double* lam_mu) {
+    if (n < 0 || (n > 0 && (!ua || !ub || !mua || !mub || !l || !q2 || !lam_u || !lam_mu))) {
+        np_record_error("np_geokerr_mino_times_host: NULL buffer or negative count");
+        return NP_ERR_INVALID;
+    }
+    for (int i = 0; i < n; ++i) {
+        lam_u[i] = np::mino::mino_u(a, l[i], q2[i], ua[i], ub[i]);
+        lam_mu[i] = np::mino::mino_mu(a, l[i], q2[i], mua[i], mub[i]);
+    }
+    return NP_OK;
+}
 
 int np_carlson_batch_device(int n, const char* d_types, const double* d_x, const double* d_y, const double* d_z,
                             const double* d_p, double* d_out, void* stream) {

@@ -1,0 +1,161 @@
+// mino_carlson.cuh -- Mino-time integrals of Kerr null geodesics in closed
+// form with Carlson's R_F, for host and device (the semi-analytic route of
+// GEOMU / GEOR, geokerr_original.f:771-1187, 2672-3136, for the cases below).
+//
+// With E = 1, l = L/E, q2 = Q/E^2 and u = 1/r, mu = cos(theta):
+//   radial potential  U(u)  = 1 + B u^2 + 2 K u^3 - a^2 q2 u^4,
+//   polar potential   M(mu) = q2 + B mu^2 - a^2 mu^4,
+//   B = a^2 - l^2 - q2,  K = (l - a)^2 + q2,
+// and Mino time is lambda = int du / sqrt(U) = int dmu / sqrt(M) along the ray.
+//
+// Polar (q2 > 0): M = a^2 (mu_+^2 - mu^2)(mu^2 + mu_-^2), so
+//   int_0^mu dmu / sqrt(M) = (mu / sqrt(q2)) R_F(1, 1 - mu^2/mu_+^2, 1 + mu^2/mu_-^2)
+// (DLMF 19.29.4 with two quadratic factors of the form 1 + c t^2), written
+// with 1/mu_-^2 = 2 a^2 / (sqrt(D) - B), mu_+^2 = 2 q2 / (sqrt(D) - B),
+// D = B^2 + 4 a^2 q2, which stay finite as a -> 0.
+//
+// Radial: on an interval between consecutive real roots r_j < u < r_j+1
+// where U > 0, U = |c| prod_i (a_i + b_i u) with positive linear factors, and
+//   int_y^x du / sqrt(U) = 2 R_F(U12^2, U13^2, U14^2) / sqrt(|c|),
+//   U_ij = (X_i X_j Y_k Y_l + Y_i Y_j X_k X_l) / (x - y),
+//   X_i = sqrt(a_i + b_i x), Y_i = sqrt(a_i + b_i y)
+// (B. C. Carlson, "A table of elliptic integrals of the first kind", Math.
+// Comp. 49 (1987) 595-606, eq. 2.1; DLMF 19.29.4-19.29.7).  A cubic U
+// (a q2 = 0) uses a constant fourth factor.  The roots come from the
+// Aberth-Ehrlich simultaneous iteration on the complex plane, polished by
+// Newton steps; potentials with complex roots return NaN (their Carlson
+// forms with quadratic factors are not implemented here; the Mino-time Taylor
+// solver covers every case).
+#pragma once
+
+#include <cmath>
+
+#include "carlson.cuh"
+
+namespace np {
+namespace mino {
+
+struct Cx { double re, im; };
+NP_CARLSON_HD Cx cadd(Cx a, Cx b) { return Cx{a.re + b.re, a.im + b.im}; }
+NP_CARLSON_HD Cx csub(Cx a, Cx b) { return Cx{a.re - b.re, a.im - b.im}; }
+NP_CARLSON_HD Cx cmul(Cx a, Cx b) { return Cx{a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re}; }
+NP_CARLSON_HD Cx cdiv(Cx a, Cx b) {
+    const double d = b.re * b.re + b.im * b.im;
+    return Cx{(a.re * b.re + a.im * b.im) / d, (a.im * b.re - a.re * b.im) / d};
+}
+
+// Roots of sum_{k<=n} c[k] x^k (c[n] != 0, n <= 4) by Aberth-Ehrlich.
+// Returns the number of roots found real (stored sorted in r) or -1 when the
+// iteration did not converge.
+NP_CARLSON_HD int real_roots(const double* c, int n, double* r) {
+    Cx z[4];
+    double R = 0.0;
+    for (int k = 0; k < n; ++k) R = std::fmax(R, std::fabs(c[k] / c[n]));
+    R = 1.0 + R;
+    for (int k = 0; k < n; ++k) {
+        const double ang = 0.4 + 2.0 * 3.141592653589793 * k / n;
+        z[k] = Cx{R * std::cos(ang), R * std::sin(ang)};
+    }
+    bool conv = false;
+    for (int it = 0; it < 200 && !conv; ++it) {
+        conv = true;
+        for (int k = 0; k < n; ++k) {
+            Cx p{c[n], 0.0}, dp{0.0, 0.0};
+            for (int j = n - 1; j >= 0; --j) {
+                dp = cadd(cmul(dp, z[k]), p);
+                p = cadd(cmul(p, z[k]), Cx{c[j], 0.0});
+            }
+            if (p.re == 0.0 && p.im == 0.0) continue;
+            const Cx w = cdiv(p, dp);
+            Cx s{0.0, 0.0};
+            for (int j = 0; j < n; ++j)
+                if (j != k) s = cadd(s, cdiv(Cx{1.0, 0.0}, csub(z[k], z[j])));
+            const Cx step = cdiv(w, csub(Cx{1.0, 0.0}, cmul(w, s)));
+            z[k] = csub(z[k], step);
+            if (std::fabs(step.re) + std::fabs(step.im) > 1e-15 * (1.0 + std::fabs(z[k].re) + std::fabs(z[k].im)))
+                conv = false;
+        }
+    }
+    if (!conv) return -1;
+    int m = 0;
+    for (int k = 0; k < n; ++k) {
+        if (std::fabs(z[k].im) > 1e-7 * (1.0 + std::fabs(z[k].re))) continue;
+        double x = z[k].re;
+        for (int it = 0; it < 3; ++it) {       // Newton polish on the real polynomial
+            double p = c[n], dp = 0.0;
+            for (int j = n - 1; j >= 0; --j) { dp = dp * x + p; p = p * x + c[j]; }
+            if (dp == 0.0) break;
+            x -= p / dp;
+        }
+        r[m++] = x;
+    }
+    for (int i = 1; i < m; ++i)
+        for (int j = i; j > 0 && r[j - 1] > r[j]; --j) { double t = r[j]; r[j] = r[j - 1]; r[j - 1] = t; }
+    return m;
+}
+
+// int_{u_a}^{u_b} du / sqrt(U(u)) for u_a, u_b in one interval of U > 0
+// bounded by real roots (the Mino time of a monotonic radial segment).
+NP_CARLSON_HD double mino_u(double a, double l, double q2, double u_a, double u_b) {
+    const double B = a * a - l * l - q2, K = (l - a) * (l - a) + q2;
+    double c[5] = {1.0, 0.0, B, 2.0 * K, -a * a * q2};
+    int n = c[4] != 0.0 ? 4 : (c[3] != 0.0 ? 3 : 0);
+    if (n == 0) return carlson::nan_();
+    double r[4];
+    const int m = real_roots(c, n, r);
+    if (m != n) return carlson::nan_();                 // complex roots: not in closed form here
+    double y = std::fmin(u_a, u_b), x = std::fmax(u_a, u_b);
+    if (x == y) return 0.0;
+    // the interval (r_j, r_j+1) containing both endpoints (roots may be touched)
+    const double tol = 1e-12 * (1.0 + std::fabs(x));
+    double lo = -INFINITY, hi = INFINITY;
+    for (int i = 0; i < m; ++i) {
+        if (r[i] <= y + tol) lo = r[i];
+        if (r[i] >= x - tol && hi == INFINITY) hi = r[i];
+    }
+    for (int i = 0; i < m; ++i)
+        if (r[i] > lo && r[i] < hi) return carlson::nan_();      // a root inside the segment
+    x = std::fmin(x, hi);
+    y = std::fmax(y, lo);
+    double ai[4], bi[4];
+    int above = 0;
+    for (int i = 0; i < m; ++i) {
+        if (r[i] <= lo) { ai[i] = -r[i]; bi[i] = 1.0; }
+        else { ai[i] = r[i]; bi[i] = -1.0; ++above; }
+    }
+    if (m == 3) { ai[3] = 1.0; bi[3] = 0.0; }
+    // U = c_n prod (u - r_i) = c_n (-1)^above prod (a_i + b_i u) must be positive
+    const double lead = c[n] * ((above & 1) ? -1.0 : 1.0);
+    if (!(lead > 0.0)) return carlson::nan_();
+    double X[4], Y[4];
+    for (int i = 0; i < 4; ++i) {
+        X[i] = std::sqrt(std::fmax(0.0, ai[i] + bi[i] * x));
+        Y[i] = std::sqrt(std::fmax(0.0, ai[i] + bi[i] * y));
+    }
+    const double d = x - y;
+    const double U12 = (X[0] * X[1] * Y[2] * Y[3] + Y[0] * Y[1] * X[2] * X[3]) / d;
+    const double U13 = (X[0] * X[2] * Y[1] * Y[3] + Y[0] * Y[2] * X[1] * X[3]) / d;
+    const double U14 = (X[0] * X[3] * Y[1] * Y[2] + Y[0] * Y[3] * X[1] * X[2]) / d;
+    return 2.0 * carlson::rf(U12 * U12, U13 * U13, U14 * U14) / std::sqrt(lead);
+}
+
+// int_0^mu dmu / sqrt(M(mu)), q2 > 0 and |mu| <= mu_+ (odd in mu).
+NP_CARLSON_HD double mino_mu_prim(double a, double l, double q2, double mu) {
+    if (!(q2 > 0.0)) return carlson::nan_();
+    const double B = a * a - l * l - q2;
+    const double sD = std::sqrt(B * B + 4.0 * a * a * q2);
+    const double den = sD - B;                          // > 0 for q2 > 0
+    const double inv_mp2 = den / (2.0 * q2), inv_mm2 = 2.0 * a * a / den;
+    const double m2 = mu * mu;
+    const double t = 1.0 - m2 * inv_mp2;
+    if (t < -1e-12) return carlson::nan_();
+    return mu / std::sqrt(q2) * carlson::rf(1.0, std::fmax(0.0, t), 1.0 + m2 * inv_mm2);
+}
+
+// Mino time between mu_a and mu_b on one monotonic polar branch.
+NP_CARLSON_HD double mino_mu(double a, double l, double q2, double mu_a, double mu_b) {
+    return std::fabs(mino_mu_prim(a, l, q2, mu_b) - mino_mu_prim(a, l, q2, mu_a));
+}
+
+}  // namespace mino
+}  // namespace np

@@ -34,3 +34,21 @@ def test_reference_entry_points_run(cuda):
     for f in ("RF", "RC", "RD", "RJ"):
         line = [l for l in out.splitlines() if l.strip().startswith(f + ":")][0]
         assert float(line.split()[-1]) < 1e-13
+
+
+def test_mino_times_device_matches_host(cuda):
+    rng = np.random.default_rng(12)
+    n = 4096
+    a = 0.7
+    l = rng.uniform(-5, 5, n)
+    q2 = rng.uniform(0.5, 30, n)
+    ua = np.full(n, 0.002)
+    ub = rng.uniform(0.01, 0.15, n)
+    mua = np.zeros(n)
+    mub = rng.uniform(-0.3, 0.3, n)
+    h = carlson.mino_times(a, ua, ub, mua, mub, l, q2, device=False)
+    d = carlson.mino_times(a, ua, ub, mua, mub, l, q2, device=True)
+    for x, y in zip(h, d):
+        ok = np.isfinite(x)
+        assert np.array_equal(ok, np.isfinite(y)) and ok.mean() > 0.2
+        assert np.allclose(y[ok], x[ok], rtol=1e-12, atol=0)

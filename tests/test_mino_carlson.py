@@ -1,0 +1,78 @@
+"""Semi-analytic Mino times with Carlson's R_F (csrc/mino_carlson.cuh, host
+build) against adaptive quadrature and against the Mino-time Taylor solver's
+samples of the same geodesics (oracle/geokerr_oracle.cpp)."""
+import math
+
+import numpy as np
+import pytest
+
+from nullpath_gb300 import carlson
+import oracle
+
+
+def _U(u, a, l, q2):
+    B, K = a * a - l * l - q2, (l - a) ** 2 + q2
+    return 1 + B * u * u + 2 * K * u ** 3 - a * a * q2 * u ** 4
+
+
+def _M(mu, a, l, q2):
+    B = a * a - l * l - q2
+    return q2 + B * mu * mu - a * a * mu ** 4
+
+
+def test_against_quadrature(built):
+    integrate = pytest.importorskip("scipy.integrate")
+    rng = np.random.default_rng(2)
+    checked = 0
+    for _ in range(300):
+        a = rng.uniform(0.0, 0.99)
+        l = rng.uniform(-8, 8)
+        q2 = rng.uniform(0.1, 40)
+        # a radial segment from large r inwards that stays where U > 0
+        u1 = rng.uniform(0.005, 0.2)
+        us = np.linspace(0.001, u1, 200)
+        if (_U(us, a, l, q2) <= 0).any():
+            continue
+        lu, lm = carlson.mino_times(a, 0.001, u1, 0.0, 0.3, l, q2, device=False)
+        if np.isnan(lu):
+            continue                      # complex roots: not in closed form here
+        ref = integrate.quad(lambda u: 1 / math.sqrt(_U(u, a, l, q2)), 0.001, u1, epsabs=1e-14, epsrel=1e-13)[0]
+        assert abs(lu - ref) <= 1e-11 * ref, (a, l, q2, lu, ref)
+        if _M(0.3, a, l, q2) > 0 and all(_M(m, a, l, q2) > 0 for m in np.linspace(0, 0.3, 50)):
+            refm = integrate.quad(lambda m: 1 / math.sqrt(_M(m, a, l, q2)), 0.0, 0.3, epsabs=1e-14, epsrel=1e-13)[0]
+            assert abs(lm - refm) <= 1e-11 * refm
+        checked += 1
+    assert checked > 50
+
+
+def test_against_taylor_solver_samples(built):
+    """Along exact Mino-time samples of a geodesic (the Taylor solver of the
+    GEOKERR path), the Carlson Mino time from the start to each sample before
+    the first turning point equals the sample's lambda."""
+    rng = np.random.default_rng(4)
+    done = 0
+    for _ in range(60):
+        a = rng.uniform(0.1, 0.95)
+        l = rng.uniform(-4, 4)
+        q2 = rng.uniform(1, 30)
+        u0, mu0 = 0.01, rng.uniform(-0.6, 0.6)
+        rc, s = oracle.geokerr_stream(u0, 0.5, mu0, a, l, q2, 0.0, 0.02, 40)
+        if rc != 0:
+            continue
+        u, mu, lam = s["u"], s["mu"], s["affine"]
+        du, dmu = np.diff(u), np.diff(mu)
+        # the monotonic prefix of both motions
+        k = 1
+        while k < len(u) and du[k - 1] > 0 and np.sign(dmu[k - 1]) == np.sign(dmu[0]):
+            k += 1
+        k -= 1          # a turning point can fall inside the last interval
+        if k < 4:
+            continue
+        lu, lm = carlson.mino_times(a, np.full(k, u0), u[:k], np.full(k, mu0), mu[:k], l, q2, device=False)
+        ok = np.isfinite(lu)
+        if ok.sum() < 3:
+            continue
+        assert np.allclose(lu[ok], lam[:k][ok], rtol=1e-10, atol=1e-12), (a, l, q2)
+        assert np.allclose(lm, lam[:k], rtol=1e-10, atol=1e-12), (a, l, q2)
+        done += 1
+    assert done >= 10
