@@ -625,4 +625,31 @@ NP_HD inline bool integrateGeodesic(GeodesicState& state, const SchwarzschildMet
     return state.r > metric.Rs + 0.001f && state.theta > 0.001f && state.theta < BH_PI - 0.001f;
 }
 
+/* Closest approach of an equatorial Schwarzschild photon with impact
+ * parameter b (schwarzschild_blackhole.cu:24-37): the largest root of
+ * r^3 - b^2 r + b^2 Rs = 0 in trigonometric form; false (no turning point
+ * outside the horizon) for b <= b_crit = (3 sqrt(3)/2) Rs. */
+NP_HD inline bool schwarzschild_rmin_analytic(float Rs, float b, float* rmin_out) {
+    if (Rs <= 0.0f || b <= 0.0f || rmin_out == nullptr) return false;
+    const double beta = (double)b / (double)Rs;
+    const double beta_crit = 1.5 * sqrt(3.0);
+    if (beta <= beta_crit) return false;
+    double c = -beta_crit / beta;
+    c = c < -1.0 ? -1.0 : (c > 1.0 ? 1.0 : c);
+    const double x = (2.0 * beta / sqrt(3.0)) * cos(acos(c) / 3.0);
+    *rmin_out = (float)(x * (double)Rs);
+    return isfinite(*rmin_out) && *rmin_out > Rs;
+}
+
+/* Deflection table of equatorial Schwarzschild photons (bh_types.h:281-300). */
+struct GeodesicLookupTable {
+    float* impact_parameters;
+    float* deflection_angles;
+    float* bending_angles;
+    float* closest_approaches;
+    int* ray_status;
+    int num_entries;
+    float mass;
+};
+
 #endif /* NP_KERR_H */

@@ -325,6 +325,22 @@ int np_frame_spp(const np_frame_t* f);
 int np_frame_tonemap(np_frame_t* f, float exposure_ev, float gamma, int reinhard, unsigned char* h_rgb8);
 int np_frame_read(np_frame_t* f, float* h_rgb_mean, float* h_rcross, float* h_inv3);
 
+/* ------------------------------------------------------------------------
+ * Schwarzschild deflection table (schwarzschild_blackhole.cu:44-266):
+ * equatorial photons from r_start with impact parameter b[i] (lengths in the
+ * units of `mass`), FP32 RK4 of bh_schwarzschild.h; deflection[i] = total
+ * phi swept, rmin[i] = closest approach (the analytic root for escaping
+ * rays), status[i] = 0 escaped, 1 captured, 2 near the photon sphere, 3 step
+ * budget spent.  np_schwarzschild_precompute is the reference's
+ * precomputeGeodesics with host arrays (b filled log-spaced, bending = deflection
+ * - pi for escaped rays, NaN otherwise). */
+int np_schwarzschild_deflection_device(float mass, float r_start, int n, const float* d_b, float* d_deflection,
+                                       float* d_rmin, int32_t* d_status, void* stream);
+int np_schwarzschild_deflection_host(float mass, float r_start, int n, const float* b, float* deflection, float* rmin,
+                                     int32_t* status);
+int np_schwarzschild_precompute(float mass, int n, float* b, float* deflection, float* bending, float* rmin,
+                                int32_t* status);
+
 #ifdef __cplusplus
 }
 #endif

@@ -21,7 +21,7 @@ NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler"
            "-Xcompiler", "-ffp-contract=off",
            "-I" + INCLUDE, "-I" + CSRC]
 
-CU_SOURCES = ["np_render.cu", "geokerr.cu", "adjoint.cu", "kerr_api.cu", "carlson.cu"]
+CU_SOURCES = ["np_render.cu", "geokerr.cu", "adjoint.cu", "kerr_api.cu", "carlson.cu", "schwarzschild.cu"]
 
 
 def _nvcc():

@@ -1,0 +1,33 @@
+"""Schwarzschild deflection table on sm_103a against the host build, and the
+reference-style table builder."""
+import math
+
+import numpy as np
+import pytest
+
+from nullpath_gb300 import schwarzschild
+
+pytestmark = pytest.mark.gpu
+
+
+def test_device_matches_host(cuda):
+    b = np.geomspace(0.3, 60.0, 2048) * 3 * math.sqrt(3)
+    dh, rh, sh = schwarzschild.deflection(1.0, b, device=False)
+    dd, rd, sd = schwarzschild.deflection(1.0, b, device=True)
+    assert (sh == sd).mean() > 0.995
+    ok = (sh == sd) & (sh == 0)
+    # FP32 RK4 with and without contracted multiply-adds
+    assert np.allclose(dd[ok], dh[ok], rtol=2e-4, atol=1e-5)
+    assert np.array_equal(rd[ok], rh[ok])          # analytic turning radius for escaped rays
+
+
+def test_precompute_table(cuda):
+    t = schwarzschild.precompute(1.0, 512)
+    bc = 3 * math.sqrt(3)
+    assert t["b"][0] == pytest.approx(0.3 * bc, rel=1e-6) and t["b"][-1] == pytest.approx(20 * bc, rel=1e-6)
+    esc = t["status"] == 0
+    assert (esc == (t["b"] > bc * 1.001)).mean() > 0.99
+    assert np.all(np.isnan(t["bending"][~esc])) and np.allclose(t["bending"][esc], t["deflection"][esc] - np.float32(math.pi))
+    # weak field: bending -> 2 Rs / b = 4 M / b
+    far = t["b"] > 50
+    assert np.allclose(t["bending"][far], 4.0 / t["b"][far], rtol=0.15)
