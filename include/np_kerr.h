@@ -638,7 +638,8 @@ NP_HD inline bool schwarzschild_rmin_analytic(float Rs, float b, float* rmin_out
     c = c < -1.0 ? -1.0 : (c > 1.0 ? 1.0 : c);
     const double x = (2.0 * beta / sqrt(3.0)) * cos(acos(c) / 3.0);
     *rmin_out = (float)(x * (double)Rs);
-    return isfinite(*rmin_out) && *rmin_out > Rs;
+    const float rr = *rmin_out;
+    return rr == rr && rr < 3.0e38f && rr > Rs;     // finite and outside the horizon
 }
 
 /* Deflection table of equatorial Schwarzschild photons (bh_types.h:281-300). */
