@@ -35,3 +35,20 @@ def test_turning_radius_and_deflection(built):
         part = lambda ua: integrate.quad(g, 0.0, math.sqrt(1 - ua / um), args=(ua,), epsabs=1e-13, epsrel=1e-12)[0]
         exact = part(1 / r0) + part(1 / (r0 + 1.0))
         assert abs(di - exact) <= 5e-4 * exact + 2e-5, (bi, di, exact)
+
+
+def test_strong_deflection_limit(built):
+    """Near b_crit the bending follows Bozza's strong-deflection limit
+    alpha = -ln(b/b_c - 1) + b_bar, b_bar = ln(216 (7 - 4 sqrt 3)) - pi
+    (V. Bozza, Phys. Rev. D 66, 103001, 2002), up to its O(b - b_c) term;
+    the rays start and end at r0 = 1000 M, which adds -2 asin(b / r0)."""
+    bc = 3 * math.sqrt(3)
+    bbar = math.log(216 * (7 - 4 * math.sqrt(3))) - math.pi
+    eps = np.array([1e-3, 3e-3, 1e-2])
+    b = (bc * (1 + eps)).astype(np.float32)
+    d, _, s = schwarzschild.deflection(1.0, b, r_start=1000.0, device=False)
+    assert (s == 0).all()
+    e_true = b.astype(np.float64) / bc - 1            # the float32 b actually traced
+    alpha = d - math.pi + 2 * np.arcsin(b.astype(np.float64) / 1000.0)
+    bozza = -np.log(e_true) + bbar
+    assert (np.abs(alpha - bozza) < 3.0 * e_true + 2e-3).all(), (alpha, bozza)
