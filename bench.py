@@ -133,6 +133,34 @@ def geokerr_grid_leg(n_side=128, nup=32, cpu_sample=1024):
             "max_rel_diff_gpu_vs_cpu": worst, "all_sampled": bool((got["n"] == nup).all())}
 
 
+def adjoint_headline_leg(K=64):
+    """Forward + adjoint on the 1280x720x4, a = 0.9 scene (FP32 adjoint,
+    checkpoint interval K): L2 loss against a render at (a = 0.7, theta =
+    74.5 deg, gain 1, q 3); rays/s of forward + backward and the production
+    forward render's rays/s on the same scene."""
+    import math
+    import torch
+    import nullpath_gb300 as npx
+    from nullpath_gb300 import diff
+    base = npx.benchmark_scene()
+    rays = base.width * base.height * base.spp
+    adj = diff.Adjoint()
+    st = diff.AdjointStats()
+    target = adj.forward(diff.scene_with(base, 0.7, 1.3, 1.0, 3.0), "mixed", K)
+    cur = diff.scene_with(base, 0.9, math.radians(80.0), 1.0, 3.0)
+    for _ in range(2):
+        img = adj.forward(cur, "mixed", K, stats=st)
+        g = adj.backward(2.0 * (img - target), stats=st)
+    adj.close()
+    npx.render(cur, "mixed")
+    _, _, fst = npx.render(cur, "mixed", stats=True)
+    fwd_ms = fst.kernel_ms + fst.init_ms
+    tot = st.forward_ms + st.backward_ms
+    return {"K": K, "forward_ms": st.forward_ms, "backward_ms": st.backward_ms,
+            "fwd_adj_rays_per_s": rays / (tot * 1e-3), "forward_render_rays_per_s": rays / (fwd_ms * 1e-3),
+            "cost_vs_forward": tot / fwd_ms, "workspace_bytes": int(st.workspace_bytes), "gradient": g.tolist()}
+
+
 def batch_leg(n_scenes=256, seed=1, passes=3):
     """256 uneven scenes (spin U[0, 0.998], inclination U[5, 85] deg,
     resolution from {64, 128, 256, 512}^2, 1-8 spp, 1-3 disk orders, seed 1)
@@ -403,6 +431,7 @@ def run_ours(args):
             out["error_vs_geokerr"] = acc
             leg_s = {}
             for key, fn in (("geokerr_grid", geokerr_grid_leg), ("adjoint_256x256x4", adjoint_leg),
+                            ("adjoint_1280x720x4", adjoint_headline_leg),
                             ("batch_256_uneven", batch_leg), ("critical_2048x2048x16_a0998", critical_leg)):
                 t_leg = time.perf_counter()
                 out[key] = fn()
