@@ -128,6 +128,18 @@ int np_geokerr_mino_times_device(int n, double a, const double* d_ua, const doub
                                  double* d_lam_mu, void* stream);
 int np_geokerr_mino_times_host(int n, double a, const double* ua, const double* ub, const double* mua,
                                const double* mub, const double* l, const double* q2, double* lam_u, double* lam_mu);
+/* Polar motion in closed form (q2[i] > 0): mu at Mino time lam[i] of the
+ * geodesic with mu(0) = mu0[i] and sign sm[i] of dmu/dlambda at 0, through
+ * any number of turning points: mu = mu_+ cn(omega lambda - sm F, k) with
+ * Jacobi cn (AGM / descending Landen) and F from Carlson's R_F (the role of
+ * GEOMU's Jacobi inversion, geokerr_original.f:1147-1178).  NaN for q2 <= 0. */
+int np_geokerr_mu_of_lambda_device(int n, double a, const double* d_l, const double* d_q2, const double* d_mu0,
+                                   const double* d_sm, const double* d_lam, double* d_mu, void* stream);
+int np_geokerr_mu_of_lambda_host(int n, double a, const double* l, const double* q2, const double* mu0,
+                                 const double* sm, const double* lam, double* mu);
+/* Jacobi elliptic functions sn, cn, dn(u[i] | m[i]), 0 <= m <= 1 (the role of
+ * SNCNDN, geokerr_original.f:3277-3347), on the host. */
+int np_jacobi_host(int n, const double* u, const double* m, double* sn, double* cn, double* dn);
 /* The reference's host entry points (carlson_elliptic.cu:387, 398): a
  * device-vs-host check printed per function, and R_F(1, 2, 0) printed. */
 void validate_carlson_cuda(void);

@@ -83,3 +83,49 @@ def mino_times(a, ua, ub, mua, mub, l, q2, device=True):
                                            C.c_void_p(torch.cuda.current_stream().cuda_stream)))
     torch.cuda.synchronize()
     return lu.cpu().numpy(), lm.cpu().numpy()
+
+
+_POLAR = {
+    "np_geokerr_mu_of_lambda_host": (C.c_int, [C.c_int, C.c_double] + [C.c_void_p] * 6),
+    "np_geokerr_mu_of_lambda_device": (C.c_int, [C.c_int, C.c_double] + [C.c_void_p] * 6 + [C.c_void_p]),
+    "np_jacobi_host": (C.c_int, [C.c_int] + [C.c_void_p] * 5),
+}
+
+
+def _polar_lib():
+    lib = _lib()
+    if not getattr(lib, "_polar_ready", False):
+        for name, (res, args) in _POLAR.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        lib._polar_ready = True
+    return lib
+
+
+def jacobi(u, m):
+    """(sn, cn, dn)(u | m) on the host."""
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    m = np.ascontiguousarray(np.broadcast_to(np.asarray(m, dtype=np.float64), u.shape))
+    out = [np.empty(u.size) for _ in range(3)]
+    check(_polar_lib().np_jacobi_host(u.size, u.ctypes.data, m.ctypes.data, *[o.ctypes.data for o in out]))
+    return tuple(out)
+
+
+def mu_of_lambda(a, l, q2, mu0, sm, lam, device=True):
+    """Closed-form polar motion mu(lambda) (np_geokerr_mu_of_lambda_*)."""
+    lam = np.ascontiguousarray(lam, dtype=np.float64)
+    ins = [np.ascontiguousarray(np.broadcast_to(np.asarray(v, dtype=np.float64), lam.shape)) for v in (l, q2, mu0, sm)]
+    n = lam.size
+    lib = _polar_lib()
+    if not device:
+        out = np.empty(n)
+        check(lib.np_geokerr_mu_of_lambda_host(n, a, *[v.ctypes.data for v in ins], lam.ctypes.data, out.ctypes.data))
+        return out
+    import torch
+    d = [torch.from_numpy(v.ravel().copy()).cuda() for v in ins + [lam]]
+    out = torch.empty(n, dtype=torch.float64, device="cuda")
+    check(lib.np_geokerr_mu_of_lambda_device(n, a, *[C.c_void_p(t.data_ptr()) for t in d], C.c_void_p(out.data_ptr()),
+                                             C.c_void_p(torch.cuda.current_stream().cuda_stream)))
+    torch.cuda.synchronize()
+    return out.cpu().numpy()

@@ -45,9 +45,53 @@ __global__ void mino_times_kernel(int n, double a, const double* __restrict__ ua
     }
 }
 
+__global__ void mu_of_lambda_kernel(int n, double a, const double* __restrict__ l, const double* __restrict__ q2,
+                                    const double* __restrict__ mu0, const double* __restrict__ sm,
+                                    const double* __restrict__ lam, double* __restrict__ mu) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        mu[i] = np::mino::mu_of_lambda(a, l[i], q2[i], mu0[i], sm[i], lam[i]);
+}
+
 }  // namespace
 
 extern "C" {
+
+int np_geokerr_mu_of_lambda_device(int n, double a, const double* d_l, const double* d_q2, const double* d_mu0,
+                                   const double* d_sm, const double* d_lam, double* d_mu, void* stream) {
+    if (n < 0 || (n > 0 && (!d_l || !d_q2 || !d_mu0 || !d_sm || !d_lam || !d_mu))) {
+        np_record_error("np_geokerr_mu_of_lambda_device: NULL buffer or negative count");
+        return NP_ERR_INVALID;
+    }
+    if (n == 0) return NP_OK;
+    const int threads = 128;
+    const int blocks = (n + threads - 1) / threads < 152 * 16 ? (n + threads - 1) / threads : 152 * 16;
+    mu_of_lambda_kernel<<<blocks, threads, 0, (cudaStream_t)stream>>>(n, a, d_l, d_q2, d_mu0, d_sm, d_lam, d_mu);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        np_record_error(cudaGetErrorString(e));
+        return NP_ERR_KERNEL;
+    }
+    return NP_OK;
+}
+
+int np_geokerr_mu_of_lambda_host(int n, double a, const double* l, const double* q2, const double* mu0,
+                                 const double* sm, const double* lam, double* mu) {
+    if (n < 0 || (n > 0 && (!l || !q2 || !mu0 || !sm || !lam || !mu))) {
+        np_record_error("np_geokerr_mu_of_lambda_host: NULL buffer or negative count");
+        return NP_ERR_INVALID;
+    }
+    for (int i = 0; i < n; ++i) mu[i] = np::mino::mu_of_lambda(a, l[i], q2[i], mu0[i], sm[i], lam[i]);
+    return NP_OK;
+}
+
+int np_jacobi_host(int n, const double* u, const double* m, double* sn, double* cn, double* dn) {
+    if (n < 0 || (n > 0 && (!u || !m || !sn || !cn || !dn))) {
+        np_record_error("np_jacobi_host: NULL buffer or negative count");
+        return NP_ERR_INVALID;
+    }
+    for (int i = 0; i < n; ++i) np::mino::jacobi_sncndn(u[i], m[i], sn[i], cn[i], dn[i]);
+    return NP_OK;
+}
 
 int np_geokerr_mino_times_device(int n, double a, const double* d_ua, const double* d_ub, const double* d_mua,
                                  const double* d_mub, const double* d_l, const double* d_q2, double* d_lam_u,

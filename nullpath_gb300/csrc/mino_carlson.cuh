@@ -157,5 +157,65 @@ NP_CARLSON_HD double mino_mu(double a, double l, double q2, double mu_a, double 
     return std::fabs(mino_mu_prim(a, l, q2, mu_b) - mino_mu_prim(a, l, q2, mu_a));
 }
 
+// Jacobi elliptic functions sn, cn, dn of argument u and parameter m = k^2
+// (0 <= m <= 1) by the arithmetic-geometric mean and descending Landen
+// transformation (Abramowitz & Stegun 16.4).
+NP_CARLSON_HD void jacobi_sncndn(double u, double m, double& sn, double& cn, double& dn) {
+    if (m < 1e-16) { sn = std::sin(u); cn = std::cos(u); dn = 1.0; return; }
+    if (m > 1.0 - 1e-16) {
+        const double t = std::tanh(u), c = 1.0 / std::cosh(u);
+        sn = t; cn = c; dn = c;
+        return;
+    }
+    double a[16], c[16];
+    a[0] = 1.0;
+    double b = std::sqrt(1.0 - m);
+    c[0] = std::sqrt(m);
+    int n = 0;
+    while (n < 15 && std::fabs(c[n]) > 1e-16 * a[n]) {
+        a[n + 1] = 0.5 * (a[n] + b);
+        c[n + 1] = 0.5 * (a[n] - b);
+        b = std::sqrt(a[n] * b);
+        ++n;
+    }
+    double phi = std::ldexp(1.0, n) * a[n] * u;
+    double phi_prev = phi;
+    for (int j = n; j > 0; --j) {
+        phi_prev = phi;
+        phi = 0.5 * (phi + std::asin(c[j] / a[j] * std::sin(phi)));
+    }
+    sn = std::sin(phi);
+    cn = std::cos(phi);
+    dn = n > 0 ? cn / std::cos(phi_prev - phi) : std::sqrt(1.0 - m * sn * sn);
+}
+
+// Polar motion in closed form (the role of GEOMU's Jacobi inversion,
+// geokerr_original.f:1147-1178, for q2 > 0):
+//   mu(lambda) = mu_+ cn(omega lambda - sm F, k),
+//   omega^2 = a^2 (mu_+^2 + mu_-^2),  k^2 = mu_+^2 / (mu_+^2 + mu_-^2),
+//   F = F(acos(mu0 / mu_+), k) = sin(phi) R_F(cos^2 phi, 1 - k^2 sin^2 phi, 1),
+// which solves (dmu/dlambda)^2 = M(mu) through its turning points; sm is the
+// sign of dmu/dlambda at lambda = 0 (mu = cos(theta)).
+NP_CARLSON_HD double mu_of_lambda(double a, double l, double q2, double mu0, double sm, double lam) {
+    if (!(q2 > 0.0)) return carlson::nan_();
+    const double B = a * a - l * l - q2;
+    const double sD = std::sqrt(B * B + 4.0 * a * a * q2);
+    const double den = sD - B;
+    const double mp2 = 2.0 * q2 / den;                 // mu_+^2
+    const double a2mp2 = a * a * mp2, a2mm2 = 0.5 * den;   // a^2 mu_+^2, a^2 mu_-^2
+    const double w2 = a2mp2 + a2mm2;
+    const double omega = std::sqrt(w2), m = a2mp2 / w2;
+    const double mp = std::sqrt(mp2);
+    const double c0 = std::fmax(-1.0, std::fmin(1.0, mu0 / mp));
+    const double phi = std::acos(c0);
+    const double s = std::sin(phi), c = std::cos(phi);
+    // F(phi) for phi in [0, pi]: beyond pi/2, F = 2K - F(pi - phi)
+    const double Fh = s * carlson::rf(c * c, 1.0 - m * s * s, 1.0);
+    const double F = c0 >= 0.0 ? Fh : 2.0 * carlson::rf(0.0, 1.0 - m, 1.0) - Fh;
+    double sn, cn, dn;
+    jacobi_sncndn(omega * lam - (sm < 0.0 ? -1.0 : 1.0) * F, m, sn, cn, dn);
+    return mp * cn;
+}
+
 }  // namespace mino
 }  // namespace np

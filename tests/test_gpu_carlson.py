@@ -55,3 +55,16 @@ def test_mino_times_device_matches_host(cuda):
         ok = np.isfinite(x) & np.isfinite(y)
         assert ok.mean() > 0.2
         assert np.allclose(y[ok], x[ok], rtol=1e-11, atol=0)
+
+
+def test_polar_motion_device_matches_host(cuda):
+    rng = np.random.default_rng(13)
+    n = 4096
+    l = rng.uniform(-5, 5, n)
+    q2 = rng.uniform(0.5, 30, n)
+    mu0 = rng.uniform(-0.3, 0.3, n)
+    sm = rng.choice([-1.0, 1.0], n)
+    lam = rng.uniform(0, 10, n)
+    h = carlson.mu_of_lambda(0.8, l, q2, mu0, sm, lam, device=False)
+    d = carlson.mu_of_lambda(0.8, l, q2, mu0, sm, lam, device=True)
+    assert np.isfinite(h).all() and np.allclose(d, h, rtol=0, atol=1e-11)

@@ -76,3 +76,47 @@ def test_against_taylor_solver_samples(built):
         assert np.allclose(lm, lam[:k], rtol=1e-10, atol=1e-12), (a, l, q2)
         done += 1
     assert done >= 10
+
+
+def test_jacobi_against_scipy(built):
+    sp = pytest.importorskip("scipy.special")
+    rng = np.random.default_rng(6)
+    u = rng.uniform(-20, 20, 3000)
+    m = np.concatenate([rng.uniform(0, 1, 2990), [0.0, 1e-17, 1.0, 1 - 1e-17, 0.5, 0.999999, 1e-9, 0.3, 0.7, 0.9]])
+    sn, cn, dn = carlson.jacobi(u, m)
+    rs, rc, rd, _ = sp.ellipj(u, m)
+    assert np.allclose(sn, rs, atol=2e-13) and np.allclose(cn, rc, atol=2e-13) and np.allclose(dn, rd, atol=2e-13)
+
+
+def test_polar_motion_against_taylor_solver(built):
+    """mu(lambda) in closed form (Jacobi cn, Carlson R_F) against the Taylor
+    solver's exact Mino-time samples, through several polar turning points."""
+    rng = np.random.default_rng(8)
+    done = 0
+    for _ in range(150):
+        a = rng.uniform(0.0, 0.99)
+        l = rng.uniform(-5, 5)
+        q2 = rng.uniform(0.5, 30)
+        mu0 = rng.uniform(-0.5, 0.5)
+        sm = rng.choice([-1.0, 1.0])
+        B = a * a - l * l - q2
+        mp2 = 2 * q2 / (math.sqrt(B * B + 4 * a * a * q2) - B)
+        if mu0 * mu0 >= mp2:
+            continue
+        # in Mino time the polar motion does not depend on the radial one
+        rc, s = oracle.geokerr_stream(1e-3, 0.5, mu0, a, l, q2, 0.0, 0.02, 200)
+        if rc != 0:
+            continue
+        # keep the samples before the ray reaches the horizon (u stops moving)
+        live = np.ones(len(s["u"]), bool)
+        stop = np.flatnonzero(np.diff(s["u"]) == 0.0)
+        if len(stop):
+            live[stop[0] + 1:] = False
+        if live.sum() < 15:
+            continue
+        # geokerr_stream's dmu/dlambda starts negative for mu0 > 0
+        sm_stream = -1.0 if mu0 > 0 else 1.0
+        mu = carlson.mu_of_lambda(a, l, q2, mu0, sm_stream, s["affine"][live], device=False)
+        assert np.allclose(mu, s["mu"][live], atol=1e-10), (a, l, q2, mu0, np.abs(mu - s["mu"][live]).max())
+        done += 1
+    assert done >= 20
