@@ -120,8 +120,9 @@ int np_carlson_batch_host(int n, const char* types, const double* x, const doubl
  * L/E, q2[i] = Q/E^2): lam_u[i] = int du / sqrt(U(u)) from ua[i] to ub[i] and
  * lam_mu[i] = int dmu / sqrt(M(mu)) from mua[i] to mub[i], each on one
  * monotonic segment of the radial and polar motion (no turning point strictly
- * inside; endpoints may be turning points).  The radial form needs U's roots
- * real (NaN otherwise), the polar form q2 > 0 (NaN otherwise).  Device
+ * inside; endpoints may be turning points).  The radial form covers four
+ * (three) real roots of U and one complex root pair, the polar form q2 > 0
+ * (NaN otherwise).  Device
  * pointers on `stream`, or host pointers; np_status. */
 int np_geokerr_mino_times_device(int n, double a, const double* d_ua, const double* d_ub, const double* d_mua,
                                  const double* d_mub, const double* d_l, const double* d_q2, double* d_lam_u,

@@ -23,9 +23,9 @@
 // Comp. 49 (1987) 595-606, eq. 2.1; DLMF 19.29.4-19.29.7).  A cubic U
 // (a q2 = 0) uses a constant fourth factor.  The roots come from the
 // Aberth-Ehrlich simultaneous iteration on the complex plane, polished by
-// Newton steps; potentials with complex roots return NaN (their Carlson
-// forms with quadratic factors are not implemented here; the Mino-time Taylor
-// solver covers every case).
+// Newton steps.  With one complex root pair the segment integral is an
+// incomplete F(phi | m) in the forms of Byrd & Friedman 259.00 (quartic) and
+// 239.00 (cubic), evaluated with R_F.
 #pragma once
 
 #include <cmath>
@@ -46,8 +46,9 @@ NP_CARLSON_HD Cx cdiv(Cx a, Cx b) {
 
 // Roots of sum_{k<=n} c[k] x^k (c[n] != 0, n <= 4) by Aberth-Ehrlich.
 // Returns the number of roots found real (stored sorted in r) or -1 when the
-// iteration did not converge.
-NP_CARLSON_HD int real_roots(const double* c, int n, double* r) {
+// iteration did not converge; a complex pair is returned in (rho, sigma)
+// (rho +- i sigma, sigma > 0) when there is one.
+NP_CARLSON_HD int real_roots(const double* c, int n, double* r, double* rho = nullptr, double* sigma = nullptr) {
     Cx z[4];
     double R = 0.0;
     for (int k = 0; k < n; ++k) R = std::fmax(R, std::fabs(c[k] / c[n]));
@@ -79,7 +80,10 @@ NP_CARLSON_HD int real_roots(const double* c, int n, double* r) {
     if (!conv) return -1;
     int m = 0;
     for (int k = 0; k < n; ++k) {
-        if (std::fabs(z[k].im) > 1e-7 * (1.0 + std::fabs(z[k].re))) continue;
+        if (std::fabs(z[k].im) > 1e-7 * (1.0 + std::fabs(z[k].re))) {
+            if (rho && sigma && z[k].im > 0.0) { *rho = z[k].re; *sigma = z[k].im; }
+            continue;
+        }
         double x = z[k].re;
         for (int it = 0; it < 3; ++it) {       // Newton polish on the real polynomial
             double p = c[n], dp = 0.0;
@@ -94,6 +98,40 @@ NP_CARLSON_HD int real_roots(const double* c, int n, double* r) {
     return m;
 }
 
+// Incomplete elliptic integral of the first kind F(phi | m) for phi in
+// [0, pi] with Carlson's R_F (beyond pi/2, F = 2K - F(pi - phi)).
+NP_CARLSON_HD double ell_f(double phi, double m) {
+    const double s = std::sin(phi), c = std::cos(phi);
+    const double f = s * carlson::rf(c * c, 1.0 - m * s * s, 1.0);
+    return c >= 0.0 ? f : 2.0 * carlson::rf(0.0, 1.0 - m, 1.0) - f;
+}
+
+// int_{r1}^{u} du / sqrt((u - r1)(r2 - u)((u - rho)^2 + sigma^2)) for
+// r1 <= u <= r2 (P. F. Byrd & M. D. Friedman, Handbook of Elliptic Integrals
+// for Engineers and Scientists, 1971, 259.00): F(acos X | m) / sqrt(A B),
+// A^2 = (r2 - rho)^2 + sigma^2, B^2 = (r1 - rho)^2 + sigma^2,
+// X = ((r2 - u) B - (u - r1) A) / ((r2 - u) B + (u - r1) A),
+// m = ((r2 - r1)^2 - (A - B)^2) / (4 A B).
+NP_CARLSON_HD double quartic_pair_prim(double r1, double r2, double rho, double sigma, double u) {
+    const double A = std::sqrt((r2 - rho) * (r2 - rho) + sigma * sigma);
+    const double B = std::sqrt((r1 - rho) * (r1 - rho) + sigma * sigma);
+    const double m = std::fmin(1.0, std::fmax(0.0, ((r2 - r1) * (r2 - r1) - (A - B) * (A - B)) / (4.0 * A * B)));
+    const double p = (r2 - u) * B, q = (u - r1) * A;
+    const double X = std::fmax(-1.0, std::fmin(1.0, (p - q) / (p + q)));
+    return ell_f(std::acos(X), m) / std::sqrt(A * B);
+}
+
+// int_{r1}^{u} du / sqrt((u - r1)((u - rho)^2 + sigma^2)) for u >= r1
+// (Byrd & Friedman 239.00): F(acos X | m) / sqrt(A), A^2 = (rho - r1)^2 +
+// sigma^2, X = (A - (u - r1)) / (A + (u - r1)), m = (A + rho - r1) / (2 A).
+NP_CARLSON_HD double cubic_pair_prim(double r1, double rho, double sigma, double u) {
+    const double A = std::sqrt((rho - r1) * (rho - r1) + sigma * sigma);
+    const double m = std::fmin(1.0, std::fmax(0.0, (A + rho - r1) / (2.0 * A)));
+    const double d = u - r1;
+    const double X = std::fmax(-1.0, std::fmin(1.0, (A - d) / (A + d)));
+    return ell_f(std::acos(X), m) / std::sqrt(A);
+}
+
 // int_{u_a}^{u_b} du / sqrt(U(u)) for u_a, u_b in one interval of U > 0
 // bounded by real roots (the Mino time of a monotonic radial segment).
 NP_CARLSON_HD double mino_u(double a, double l, double q2, double u_a, double u_b) {
@@ -101,9 +139,26 @@ NP_CARLSON_HD double mino_u(double a, double l, double q2, double u_a, double u_
     double c[5] = {1.0, 0.0, B, 2.0 * K, -a * a * q2};
     int n = c[4] != 0.0 ? 4 : (c[3] != 0.0 ? 3 : 0);
     if (n == 0) return carlson::nan_();
-    double r[4];
-    const int m = real_roots(c, n, r);
-    if (m != n) return carlson::nan_();                 // complex roots: not in closed form here
+    double r[4], rho = 0.0, sigma = 0.0;
+    const int m = real_roots(c, n, r, &rho, &sigma);
+    if (m < 0) return carlson::nan_();
+    if (m == n - 2 && sigma > 0.0) {
+        // one complex pair: two real roots bracketing u (quartic, c4 < 0) or
+        // one real root below u (cubic, c3 > 0)
+        const double ya = std::fmin(u_a, u_b), xb = std::fmax(u_a, u_b);
+        if (n == 4) {
+            if (!(c[4] < 0.0) || ya < r[0] - 1e-12 || xb > r[1] + 1e-12) return carlson::nan_();
+            const double lo = r[0], hi = r[1];
+            const double ga = quartic_pair_prim(lo, hi, rho, sigma, std::fmin(hi, std::fmax(lo, ya)));
+            const double gb = quartic_pair_prim(lo, hi, rho, sigma, std::fmin(hi, std::fmax(lo, xb)));
+            return std::fabs(gb - ga) / std::sqrt(-c[4]);
+        }
+        if (!(c[3] > 0.0) || ya < r[0] - 1e-12) return carlson::nan_();
+        const double ga = cubic_pair_prim(r[0], rho, sigma, std::fmax(r[0], ya));
+        const double gb = cubic_pair_prim(r[0], rho, sigma, std::fmax(r[0], xb));
+        return std::fabs(gb - ga) / std::sqrt(c[3]);
+    }
+    if (m != n) return carlson::nan_();
     double y = std::fmin(u_a, u_b), x = std::fmax(u_a, u_b);
     if (x == y) return 0.0;
     // the interval (r_j, r_j+1) containing both endpoints (roots may be touched)

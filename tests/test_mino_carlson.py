@@ -34,10 +34,10 @@ def test_against_quadrature(built):
         if (_U(us, a, l, q2) <= 0).any():
             continue
         lu, lm = carlson.mino_times(a, 0.001, u1, 0.0, 0.3, l, q2, device=False)
-        if np.isnan(lu):
-            continue                      # complex roots: not in closed form here
+        assert np.isfinite(lu), (a, l, q2)     # real roots or one complex pair: both in closed form
         ref = integrate.quad(lambda u: 1 / math.sqrt(_U(u, a, l, q2)), 0.001, u1, epsabs=1e-14, epsrel=1e-13)[0]
-        assert abs(lu - ref) <= 1e-11 * ref, (a, l, q2, lu, ref)
+        # a small a q2 makes the quartic nearly cubic (a far root): 1e-9
+        assert abs(lu - ref) <= 1e-9 * ref, (a, l, q2, lu, ref)
         if _M(0.3, a, l, q2) > 0 and all(_M(m, a, l, q2) > 0 for m in np.linspace(0, 0.3, 50)):
             refm = integrate.quad(lambda m: 1 / math.sqrt(_M(m, a, l, q2)), 0.0, 0.3, epsabs=1e-14, epsrel=1e-13)[0]
             assert abs(lm - refm) <= 1e-11 * refm
@@ -69,13 +69,11 @@ def test_against_taylor_solver_samples(built):
         if k < 4:
             continue
         lu, lm = carlson.mino_times(a, np.full(k, u0), u[:k], np.full(k, mu0), mu[:k], l, q2, device=False)
-        ok = np.isfinite(lu)
-        if ok.sum() < 3:
-            continue
-        assert np.allclose(lu[ok], lam[:k][ok], rtol=1e-10, atol=1e-12), (a, l, q2)
+        assert np.isfinite(lu).all()
+        assert np.allclose(lu, lam[:k], rtol=1e-10, atol=1e-12), (a, l, q2)
         assert np.allclose(lm, lam[:k], rtol=1e-10, atol=1e-12), (a, l, q2)
         done += 1
-    assert done >= 10
+    assert done >= 30
 
 
 def test_jacobi_against_scipy(built):
