@@ -138,6 +138,18 @@ int np_geokerr_mu_of_lambda_device(int n, double a, const double* d_l, const dou
                                    const double* d_sm, const double* d_lam, double* d_mu, void* stream);
 int np_geokerr_mu_of_lambda_host(int n, double a, const double* l, const double* q2, const double* mu0,
                                  const double* sm, const double* lam, double* mu);
+/* Equatorial crossings in closed form (GEOR with mu_f = 0,
+ * geokerr_original.f:2672-3136, semi-analytic): the polar motion gives each
+ * crossing's Mino time, the radial Mino-time integral (Carlson R_F) is
+ * inverted there.  Same rays, signs and stopping rules as
+ * np_geokerr_equator_crossings_device; xu[n][K] only (no phi); nx[i] = -1
+ * for q2[i] <= 0. */
+int np_geokerr_equator_crossings_cf_device(int n, double a, const double* d_u0, const double* d_mu0, const double* d_l,
+                                           const double* d_q2, const double* d_su, const double* d_sm, double u_end,
+                                           int K, double* d_xu, int32_t* d_nx, void* stream);
+int np_geokerr_equator_crossings_cf_host(int n, double a, const double* u0, const double* mu0, const double* l,
+                                         const double* q2, const double* su, const double* sm, double u_end, int K,
+                                         double* xu, int32_t* nx);
 /* Jacobi elliptic functions sn, cn, dn(u[i] | m[i]), 0 <= m <= 1 (the role of
  * SNCNDN, geokerr_original.f:3277-3347), on the host. */
 int np_jacobi_host(int n, const double* u, const double* m, double* sn, double* cn, double* dn);

@@ -82,21 +82,30 @@ def crossing_error(scene, n=20000, precision="mixed", seed=0, orders=2, critical
     a = scene.spin * M
     key = (n, seed, bool(critical), scene.width, scene.height, scene.spin, scene.theta_deg, scene.r_cam, scene.mass)
     if cache is not None and key in cache and np.array_equal(cache[key][0], consts):
-        xr_ref, xphi_ref = cache[key][1], cache[key][2]
+        xr_ref, xphi_ref, cross_check = cache[key][1], cache[key][2], cache[key][3]
     else:
         u0, mu0, l, q2, su, sm = gk.render_ray_constants(consts, scene)
         r_far = scene.escape_r if scene.escape_r > 0 else (scene.r_cam + 20.0) * lunit
         xu, xphi, nx = gk.equator_crossings(scene.spin, u0, mu0, l, q2, su, sm, M / r_far, 4)
         xr_ref = np.where(xu.cpu().numpy() > 0, M / np.maximum(xu.cpu().numpy(), 1e-300), 0.0)
         xphi_ref = xphi.cpu().numpy()
+        # the same crossings in closed form (Jacobi polar motion, inverted
+        # Carlson radial integral): an independent check of the solver
+        from .carlson import equator_crossings_cf
+        cf_u, cf_n = equator_crossings_cf(scene.spin, u0, mu0, l, q2, su, sm, M / r_far, 4, device=True)
+        tx, tn = xu.cpu().numpy(), nx.cpu().numpy()
+        same = cf_n == tn
+        both = same[:, None] & (np.arange(4)[None, :] < np.maximum(tn, 0)[:, None]) & (tx > 0)
+        cross_check = {"count_agreement": float(same.mean()),
+                       "max_rel_u_diff": float((np.abs(cf_u[both] - tx[both]) / tx[both]).max()) if both.any() else 0.0}
         if cache is not None:
-            cache[key] = (consts.copy(), xr_ref, xphi_ref)
+            cache[key] = (consts.copy(), xr_ref, xphi_ref, cross_check)
     E = -consts[:, 0]
     L = consts[:, 1]
     rin = scene.disk_rin if scene.disk_rin > 0 else 3.0 * 2.0 * M
     rout = scene.disk_rout if scene.disk_rout > 0 else 20.0 * 2.0 * M
     q = scene.emissivity_q
-    res = {"rays": n, "precision": precision}
+    res = {"rays": n, "precision": precision, "solver_vs_closed_form": cross_check}
     for k in range(orders):
         r = cross[:, k, 0]
         rr = xr_ref[:, k]

@@ -129,3 +129,35 @@ def mu_of_lambda(a, l, q2, mu0, sm, lam, device=True):
                                              C.c_void_p(torch.cuda.current_stream().cuda_stream)))
     torch.cuda.synchronize()
     return out.cpu().numpy()
+
+
+def equator_crossings_cf(a, u0, mu0, l, q2, su, sm, u_end=1e-3, K=4, device=False):
+    """Closed-form equatorial crossings (np_geokerr_equator_crossings_cf_*):
+    (xu [n, K], nx [n])."""
+    lib = _lib()
+    if not getattr(lib, "_cf_ready", False):
+        lib.np_geokerr_equator_crossings_cf_host.restype = C.c_int
+        lib.np_geokerr_equator_crossings_cf_host.argtypes = [C.c_int, C.c_double] + [C.c_void_p] * 6 + \
+            [C.c_double, C.c_int, C.c_void_p, C.c_void_p]
+        lib.np_geokerr_equator_crossings_cf_device.restype = C.c_int
+        lib.np_geokerr_equator_crossings_cf_device.argtypes = [C.c_int, C.c_double] + [C.c_void_p] * 6 + \
+            [C.c_double, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+        lib._cf_ready = True
+    ins = [np.ascontiguousarray(np.atleast_1d(np.asarray(v, dtype=np.float64))) for v in (u0, mu0, l, q2, su, sm)]
+    n = max(v.size for v in ins)
+    ins = [np.ascontiguousarray(np.broadcast_to(v, (n,))) for v in ins]
+    if not device:
+        xu = np.zeros((n, K))
+        nx = np.zeros(n, np.int32)
+        check(lib.np_geokerr_equator_crossings_cf_host(n, a, *[v.ctypes.data for v in ins], u_end, K, xu.ctypes.data,
+                                                       nx.ctypes.data))
+        return xu, nx
+    import torch
+    d = [torch.from_numpy(v.copy()).cuda() for v in ins]
+    xu = torch.zeros((n, K), dtype=torch.float64, device="cuda")
+    nx = torch.zeros(n, dtype=torch.int32, device="cuda")
+    check(lib.np_geokerr_equator_crossings_cf_device(n, a, *[C.c_void_p(t.data_ptr()) for t in d], u_end, K,
+                                                     C.c_void_p(xu.data_ptr()), C.c_void_p(nx.data_ptr()),
+                                                     C.c_void_p(torch.cuda.current_stream().cuda_stream)))
+    torch.cuda.synchronize()
+    return xu.cpu().numpy(), nx.cpu().numpy()

@@ -52,9 +52,55 @@ __global__ void mu_of_lambda_kernel(int n, double a, const double* __restrict__ 
         mu[i] = np::mino::mu_of_lambda(a, l[i], q2[i], mu0[i], sm[i], lam[i]);
 }
 
+__global__ void crossings_cf_kernel(int n, double a, const double* __restrict__ u0, const double* __restrict__ mu0,
+                                    const double* __restrict__ l, const double* __restrict__ q2,
+                                    const double* __restrict__ su, const double* __restrict__ sm, double u_end, int K,
+                                    double* __restrict__ xu, int32_t* __restrict__ nx) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        double* x = xu + (size_t)i * K;
+        for (int k = 0; k < K; ++k) x[k] = 0.0;
+        nx[i] = np::mino::equator_crossings_cf(a, u0[i], mu0[i], l[i], q2[i], su[i], sm[i], u_end, K, x);
+    }
+}
+
 }  // namespace
 
 extern "C" {
+
+int np_geokerr_equator_crossings_cf_device(int n, double a, const double* d_u0, const double* d_mu0, const double* d_l,
+                                           const double* d_q2, const double* d_su, const double* d_sm, double u_end,
+                                           int K, double* d_xu, int32_t* d_nx, void* stream) {
+    if (n < 0 || K < 1 || (n > 0 && (!d_u0 || !d_mu0 || !d_l || !d_q2 || !d_su || !d_sm || !d_xu || !d_nx))) {
+        np_record_error("np_geokerr_equator_crossings_cf_device: bad arguments");
+        return NP_ERR_INVALID;
+    }
+    if (n == 0) return NP_OK;
+    const int threads = 128;
+    const int blocks = (n + threads - 1) / threads < 152 * 16 ? (n + threads - 1) / threads : 152 * 16;
+    crossings_cf_kernel<<<blocks, threads, 0, (cudaStream_t)stream>>>(n, a, d_u0, d_mu0, d_l, d_q2, d_su, d_sm, u_end, K,
+                                                                     d_xu, d_nx);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        np_record_error(cudaGetErrorString(e));
+        return NP_ERR_KERNEL;
+    }
+    return NP_OK;
+}
+
+int np_geokerr_equator_crossings_cf_host(int n, double a, const double* u0, const double* mu0, const double* l,
+                                         const double* q2, const double* su, const double* sm, double u_end, int K,
+                                         double* xu, int32_t* nx) {
+    if (n < 0 || K < 1 || (n > 0 && (!u0 || !mu0 || !l || !q2 || !su || !sm || !xu || !nx))) {
+        np_record_error("np_geokerr_equator_crossings_cf_host: bad arguments");
+        return NP_ERR_INVALID;
+    }
+    for (int i = 0; i < n; ++i) {
+        double* x = xu + (size_t)i * K;
+        for (int k = 0; k < K; ++k) x[k] = 0.0;
+        nx[i] = np::mino::equator_crossings_cf(a, u0[i], mu0[i], l[i], q2[i], su[i], sm[i], u_end, K, x);
+    }
+    return NP_OK;
+}
 
 int np_geokerr_mu_of_lambda_device(int n, double a, const double* d_l, const double* d_q2, const double* d_mu0,
                                    const double* d_sm, const double* d_lam, double* d_mu, void* stream) {

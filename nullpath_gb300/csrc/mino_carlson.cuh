@@ -272,5 +272,116 @@ NP_CARLSON_HD double mu_of_lambda(double a, double l, double q2, double mu0, dou
     return mp * cn;
 }
 
+// ---------------------------------------------------------------------------
+// Equatorial crossings in closed form (GEOR with mu_f = 0,
+// geokerr_original.f:2672-3136): the polar motion gives the Mino times of
+// the crossings, lambda_j = ((2j + 1) K(k) + s_mu F) / omega; the radial
+// motion is unfolded into G(u) = int_lo^u du / sqrt(U) on the interval of U > 0
+// holding u0 (turning point at its upper end) and inverted at each lambda_j by
+// safeguarded Newton steps (dG/du = 1/sqrt(U)).
+
+struct RadialCF {
+    double a, l, q2, c[5];
+    int n;                      // degree of U
+    double lo, hi;              // interval of U > 0 containing u0 (hi may be +inf)
+    double r[4], rho, sigma;    // real roots, complex pair
+    int nreal;
+};
+
+NP_CARLSON_HD double U_of(const RadialCF& R, double u) {
+    double p = R.c[R.n];
+    for (int j = R.n - 1; j >= 0; --j) p = p * u + R.c[j];
+    return p;
+}
+
+NP_CARLSON_HD bool radial_setup(double a, double l, double q2, double u0, RadialCF& R) {
+    const double B = a * a - l * l - q2, K = (l - a) * (l - a) + q2;
+    R.a = a; R.l = l; R.q2 = q2;
+    R.c[0] = 1.0; R.c[1] = 0.0; R.c[2] = B; R.c[3] = 2.0 * K; R.c[4] = -a * a * q2;
+    R.n = R.c[4] != 0.0 ? 4 : (R.c[3] != 0.0 ? 3 : 0);
+    if (R.n == 0) return false;
+    R.rho = 0.0; R.sigma = 0.0;
+    R.nreal = real_roots(R.c, R.n, R.r, &R.rho, &R.sigma);
+    if (R.nreal < 0) return false;
+    R.lo = -INFINITY; R.hi = INFINITY;
+    for (int i = 0; i < R.nreal; ++i) {
+        if (R.r[i] <= u0) R.lo = R.r[i];
+        else if (R.hi == INFINITY) R.hi = R.r[i];
+    }
+    return R.lo > -INFINITY && U_of(R, u0) >= 0.0;
+}
+
+// G(u) = int_lo^u du / sqrt(U), lo <= u <= hi.
+NP_CARLSON_HD double radial_G(const RadialCF& R, double u) {
+    if (R.nreal == R.n - 2 && R.sigma > 0.0) {
+        if (R.n == 4) return quartic_pair_prim(R.r[0], R.r[1], R.rho, R.sigma, u) / std::sqrt(-R.c[4]);
+        return cubic_pair_prim(R.r[0], R.rho, R.sigma, u) / std::sqrt(R.c[3]);
+    }
+    return mino_u(R.a, R.l, R.q2, R.lo, u);
+}
+
+// u in [lo, min(hi, u_cap)] with G(u) = g (G increasing), by Newton steps
+// kept inside a bisection bracket.
+NP_CARLSON_HD double radial_invert(const RadialCF& R, double g, double u_cap) {
+    double lo = R.lo, hi = std::fmin(R.hi, u_cap);
+    double u = 0.5 * (lo + hi);
+    for (int it = 0; it < 100; ++it) {
+        const double f = radial_G(R, u) - g;
+        if (f > 0.0) hi = u; else lo = u;
+        const double Uu = U_of(R, u);
+        double un = Uu > 0.0 ? u - f * std::sqrt(Uu) : 0.5 * (lo + hi);
+        if (!(un > lo && un < hi)) un = 0.5 * (lo + hi);
+        if (std::fabs(un - u) <= 1e-15 * (1.0 + std::fabs(u))) { u = un; break; }
+        u = un;
+    }
+    return u;
+}
+
+// Crossing u values of a ray leaving (u0, mu0) with signs su (du/dlambda) and
+// sm (dmu/dlambda): up to K crossings in xu, their count returned; the ray
+// ends at the horizon u_h or when it has climbed out to u <= u_end.
+// Returns -1 when the potentials are outside the closed forms (q2 <= 0).
+NP_CARLSON_HD int equator_crossings_cf(double a, double u0, double mu0, double l, double q2, double su, double sm,
+                                       double u_end, int K, double* xu) {
+    if (!(q2 > 0.0)) return -1;
+    RadialCF R;
+    if (!radial_setup(a, l, q2, u0, R)) return -1;
+    const double rp = 1.0 + std::sqrt(std::fmax(0.0, 1.0 - a * a));
+    const double u_h = 1.0 / rp;
+    // polar: mu = mu_+ cn(omega lambda - sm F, k)
+    const double B = a * a - l * l - q2;
+    const double sD = std::sqrt(B * B + 4.0 * a * a * q2);
+    const double den = sD - B;
+    const double mp2 = 2.0 * q2 / den;
+    const double w2 = a * a * mp2 + 0.5 * den;
+    const double omega = std::sqrt(w2), m = a * a * mp2 / w2;
+    const double mp = std::sqrt(mp2);
+    const double F = ell_f(std::acos(std::fmax(-1.0, std::fmin(1.0, mu0 / mp))), m);
+    const double Kc = carlson::rf(0.0, 1.0 - m, 1.0);
+    const double sgn = sm < 0.0 ? -1.0 : 1.0;
+    // radial unfolding: s = G(u0) + su lambda on the way in, mirrored at hi
+    const double G0 = radial_G(R, u0);
+    const double Gmax = R.hi < INFINITY ? radial_G(R, R.hi) : INFINITY;
+    const double Gh = u_h < R.hi ? radial_G(R, u_h) : INFINITY;      // horizon before the turning point
+    const double Gend = radial_G(R, std::fmax(R.lo, u_end));
+    int nx = 0;
+    for (int j = -2; nx < K && j < 64; ++j) {
+        const double lam = ((2.0 * j + 1.0) * Kc + sgn * F) / omega;
+        if (lam < 0.0) continue;
+        double sU = G0 + (su >= 0.0 ? 1.0 : -1.0) * lam;    // unfolded radial coordinate
+        double g;
+        if (su >= 0.0) {
+            if (sU >= Gh) break;                             // fell through the horizon first
+            g = sU <= Gmax ? sU : 2.0 * Gmax - sU;           // past the turning point: outward
+            if (sU > Gmax && g <= Gend) break;               // escaped
+        } else {
+            g = sU;
+            if (g <= Gend) break;
+        }
+        xu[nx++] = radial_invert(R, g, u_h);
+    }
+    return nx;
+}
+
 }  // namespace mino
 }  // namespace np

@@ -68,3 +68,17 @@ def test_polar_motion_device_matches_host(cuda):
     h = carlson.mu_of_lambda(0.8, l, q2, mu0, sm, lam, device=False)
     d = carlson.mu_of_lambda(0.8, l, q2, mu0, sm, lam, device=True)
     assert np.isfinite(h).all() and np.allclose(d, h, rtol=0, atol=1e-11)
+
+
+def test_closed_form_crossings_device_matches_host(cuda):
+    import nullpath_gb300 as npx
+    from nullpath_gb300 import geokerr as gk
+    sc = npx.benchmark_scene(width=128, height=72, spp=1)
+    rng = np.random.default_rng(5)
+    out = npx.trace_rays(sc, rng.uniform(0, 128, 4096), rng.uniform(0, 72, 4096), "fp64")
+    u0, mu0, l, q2, su, sm = gk.render_ray_constants(out["consts"].cpu().numpy(), sc)
+    hx, hn = carlson.equator_crossings_cf(sc.spin, u0, mu0, l, q2, su, sm, 1e-3, 4, device=False)
+    dx, dn = carlson.equator_crossings_cf(sc.spin, u0, mu0, l, q2, su, sm, 1e-3, 4, device=True)
+    assert (hn == dn).mean() > 0.995
+    same = hn == dn
+    assert np.allclose(dx[same], hx[same], rtol=1e-12, atol=0)

@@ -118,3 +118,27 @@ def test_polar_motion_against_taylor_solver(built):
         assert np.allclose(mu, s["mu"][live], atol=1e-10), (a, l, q2, mu0, np.abs(mu - s["mu"][live]).max())
         done += 1
     assert done >= 20
+
+
+@pytest.mark.parametrize("spin,theta", [(0.9, 80.0), (0.998, 60.0), (0.3, 20.0)])
+def test_closed_form_crossings_match_taylor_solver(built, spin, theta):
+    """Equatorial crossings in closed form (polar Jacobi motion + inverted
+    radial Carlson integral) against the Mino-time Taylor solver on the
+    renderer's own camera rays: same crossing counts, u within 1e-11."""
+    import nullpath_gb300 as npx
+    from nullpath_gb300 import geokerr as gk
+    sc = npx.benchmark_scene(width=64, height=36, spp=1, spin=spin).replace(theta_deg=theta)
+    rng = np.random.default_rng(3)
+    px, py = rng.uniform(0, 64, 200), rng.uniform(0, 36, 200)
+    ref = oracle.trace_rays(sc, px, py)
+    u0, mu0, l, q2, su, sm = gk.render_ray_constants(ref["consts"], sc)
+    u_end = 1.0 / sc.escape_r
+    xu, nx = carlson.equator_crossings_cf(spin, u0, mu0, l, q2, su, sm, u_end, 4)
+    agree = 0
+    for i in range(len(px)):
+        n, tx, _ = oracle.geokerr_crossings(u0[i], mu0[i], spin, l[i], q2[i], su[i], sm[i], u_end, 4)
+        if n == nx[i]:
+            agree += 1
+            k = max(n, 0)
+            assert np.allclose(xu[i][:k], tx[:k], rtol=1e-11, atol=0), (i, xu[i][:k], tx[:k])
+    assert agree >= 0.99 * len(px)
