@@ -213,3 +213,41 @@ def critical_curve(scene):
     if load().npo_critical_curve(C.byref(scene), rho.ctypes.data) != 0:
         raise RuntimeError("npo_critical_curve failed")
     return rho
+
+
+# ---------------------------------------------------------------------------
+# GEOKERR validation harness core (gkval_core.cpp) and the gkval binary
+
+GKVAL_BIN = os.path.join(HERE, "gkval")
+
+
+def gkval():
+    """liboracle.so with the gkv_* prototypes set."""
+    lib = load()
+    if not getattr(lib, "_gkv_ready", False):
+        D, U64, I, V, SZ = C.c_double, C.c_uint64, C.c_int, C.c_void_p, C.c_size_t
+        protos = {
+            "gkv_field_name": ([I], C.c_char_p),
+            "gkv_field_index": ([C.c_char_p], I),
+            "gkv_sha256": ([V, SZ, V], None),
+            "gkv_placeholder_hash": ([V, SZ, V], None),
+            "gkv_ulp_distance": ([D, D], U64),
+            "gkv_accept_sample": ([D, D, D, D, U64], I),
+            "gkv_first_fail": ([V, V, SZ, D, D, U64], C.c_int64),
+            "gkv_unwrap": ([V, SZ], None),
+            "gkv_quantize": ([D, I, C.POINTER(U64)], I),
+            "gkv_hash_leaf": ([I, C.c_char_p, U64, I, U64, U64, V, SZ, V], None),
+            "gkv_hash_node": ([I, V, V, V], None),
+            "gkv_merkle": ([I, V, SZ, V], None),
+            "gkv_save_fail_window": ([C.c_char_p, U64, I, U64, U64, V, V], I),
+            "gkv_load_fail_window": ([C.c_char_p, U64, I, U64, U64, V, V], I),
+            "gkv_fail_window_bounds": ([U64, U64, U64, U64, C.POINTER(U64), C.POINTER(U64)], None),
+            "gkv_adaptive_grid": ([D] * 6 + [U64, D, C.POINTER(D), C.POINTER(D)], I),
+            "gkv_check_fp_env": ([I], I),
+        }
+        for name, (args, res) in protos.items():
+            fn = getattr(lib, name)
+            fn.argtypes = args
+            fn.restype = res
+        lib._gkv_ready = True
+    return lib

@@ -1,6 +1,8 @@
 """Readers of the reference's GEOKERR fixtures (binary layouts of
 geokerr_port/validation/gkval_adapters.c:546-555,645-649 and
-gkval_io.c:153-166), copied into this folder unchanged."""
+gkval_io.c:153-166), copied into this folder unchanged.  gkval_manifests/
+holds the reference's run manifests (geokerr_port/validation/runs/<ID>/
+manifest.json), also unchanged."""
 import os
 import struct
 
