@@ -36,7 +36,7 @@
 extern "C" {
 #endif
 
-#define NP_ABI_VERSION 1
+#define NP_ABI_VERSION 2
 
 typedef enum np_status {
     NP_OK = 0,
@@ -54,8 +54,17 @@ typedef enum np_units { NP_UNITS_RS = 0, NP_UNITS_M = 1 } np_units;
  * a pass are near-critical (importance sampling of the photon ring). */
 typedef enum np_jitter { NP_JITTER_WANGHASH = 0, NP_JITTER_STRATIFIED = 1, NP_JITTER_CRITICAL = 2 } np_jitter;
 typedef enum np_camera { NP_CAMERA_STATIC = 0, NP_CAMERA_ZAMO = 1 } np_camera;
-typedef enum np_integrator { NP_INTEG_RK4 = 0, NP_INTEG_ADAPTIVE = 1 } np_integrator;
-typedef enum np_crossing { NP_CROSS_LINEAR = 0, NP_CROSS_HERMITE = 1 } np_crossing;
+/* NP_INTEG_RKF78: research mode (FP64 only).  Fehlberg's embedded 7(8)
+ * pair, the 8th-order solution propagated, error control on (r, theta, phi,
+ * p_r, p_theta, p_phi) with the scene's rtol/atol, and, when inv_gate > 0,
+ * invariant-gated acceptance: a step is also rejected (h halved) when
+ * |H| / E^2 or |Q - Q0| / max(|Q0|, (E M)^2) (Carter constant) exceeds
+ * inv_gate after it. */
+typedef enum np_integrator { NP_INTEG_RK4 = 0, NP_INTEG_ADAPTIVE = 1, NP_INTEG_RKF78 = 2 } np_integrator;
+/* NP_CROSS_ROOT (FP64 only): theta = pi/2 located by bracketed root finding
+ * on re-integrations of the crossing step from its start, so the crossing is
+ * as accurate as the integrator itself (no interpolant error). */
+typedef enum np_crossing { NP_CROSS_LINEAR = 0, NP_CROSS_HERMITE = 1, NP_CROSS_ROOT = 2 } np_crossing;
 typedef enum np_background { NP_BG_GRADIENT = 0, NP_BG_POINT = 1 } np_background;
 
 /* Arithmetic of the geodesic integration.
@@ -108,6 +117,7 @@ typedef struct np_scene {
     double bg_brightness;         /* render.cu:41 */
     int32_t check_invariants;     /* render.cu:32 */
     int32_t islands;              /* NP_ISLAND_* mask of the mixed path */
+    double inv_gate;              /* NP_INTEG_RKF78 invariant gate; <= 0 disables */
 } np_scene_t;
 
 /* Per-call statistics, filled when the pointer is non-NULL. */
@@ -172,6 +182,15 @@ int np_trace_rays_device(const np_scene_t* scene, int precision, int n,
                          const double* d_px, const double* d_py,
                          double* d_consts, double* d_cross, int32_t* d_status,
                          void* stream);
+
+/* Conserved-quantity drift of explicit rays on the FP64 path (any FP64
+ * integrator): per ray i, drift[2*i] = max |H| / E^2 and drift[2*i+1] =
+ * max |Q - Q0| / max(|Q0|, (E M)^2) over its accepted steps (H the
+ * Hamiltonian, Q Carter's constant, E = -p_t; E and L = p_phi are exact
+ * constants of this formulation), steps[i] = accepted steps.  Ray
+ * positions as np_trace_rays_device; device pointers. */
+int np_trace_invariants_device(const np_scene_t* scene, int n, const double* d_px, const double* d_py,
+                               double* d_drift, int32_t* d_steps, void* stream);
 
 /* ------------------------------------------------------------------------
  * Differentiable render (adjoint).  The image is the mean over samples of

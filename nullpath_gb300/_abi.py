@@ -15,8 +15,8 @@ NP_ERR_TIMEOUT = -5
 NP_UNITS_RS, NP_UNITS_M = 0, 1
 NP_JITTER_WANGHASH, NP_JITTER_STRATIFIED, NP_JITTER_CRITICAL = 0, 1, 2
 NP_CAMERA_STATIC, NP_CAMERA_ZAMO = 0, 1
-NP_INTEG_RK4, NP_INTEG_ADAPTIVE = 0, 1
-NP_CROSS_LINEAR, NP_CROSS_HERMITE = 0, 1
+NP_INTEG_RK4, NP_INTEG_ADAPTIVE, NP_INTEG_RKF78 = 0, 1, 2
+NP_CROSS_LINEAR, NP_CROSS_HERMITE, NP_CROSS_ROOT = 0, 1, 2
 NP_BG_GRADIENT, NP_BG_POINT = 0, 1
 NP_PREC_FP64, NP_PREC_MIXED = 0, 1
 NP_ISLAND_HORIZON, NP_ISLAND_TURNING, NP_ISLAND_CRITICAL = 1, 2, 4
@@ -42,6 +42,7 @@ class Scene(C.Structure):
         ("crossing", C.c_int32), ("background", C.c_int32),
         ("bg_sigma_deg", C.c_double), ("bg_brightness", C.c_double),
         ("check_invariants", C.c_int32), ("islands", C.c_int32),
+        ("inv_gate", C.c_double),
     ]
 
     def copy(self):
@@ -87,7 +88,7 @@ def reference_defaults():
                  disk_on=1, disk_max_orders=1, disk_rin=0.0, disk_rout=0.0,
                  emissivity_q=2.0, disk_gain=1.0, crossing=NP_CROSS_LINEAR,
                  background=NP_BG_GRADIENT, bg_sigma_deg=1.0, bg_brightness=3.0,
-                 check_invariants=0, islands=NP_ISLANDS_DEFAULT)
+                 check_invariants=0, islands=NP_ISLANDS_DEFAULT, inv_gate=0.0)
 
 
 def benchmark_scene(width=1280, height=720, spp=4, spin=0.9, seed=0):
@@ -102,4 +103,4 @@ def benchmark_scene(width=1280, height=720, spp=4, spin=0.9, seed=0):
                  disk_on=1, disk_max_orders=3, disk_rin=isco_radius(1.0, spin), disk_rout=20.0,
                  emissivity_q=3.0, disk_gain=1.0, crossing=NP_CROSS_HERMITE,
                  background=NP_BG_GRADIENT, bg_sigma_deg=1.0, bg_brightness=3.0,
-                 check_invariants=0, islands=NP_ISLANDS_DEFAULT)
+                 check_invariants=0, islands=NP_ISLANDS_DEFAULT, inv_gate=0.0)

@@ -30,6 +30,8 @@ PROTOTYPES = {
                                  C.POINTER(RenderStats)]),
     "np_trace_rays_device": (C.c_int, [C.POINTER(Scene), C.c_int, C.c_int, C.c_void_p, C.c_void_p,
                                        C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "np_trace_invariants_device": (C.c_int, [C.POINTER(Scene), C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                             C.c_void_p, C.c_void_p]),
     "np_measure_fma_peak": (C.c_int, [C.c_int, C.POINTER(C.c_double)]),
     "np_tune": (C.c_int, [C.c_int, C.c_int]),
     "np_render_device_noalloc": (C.c_int, [C.POINTER(Scene), C.c_int, C.c_void_p, C.c_void_p, C.c_int,

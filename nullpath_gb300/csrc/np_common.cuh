@@ -53,6 +53,7 @@ struct SceneDev {
     float r_plus_f, r_band_f, pi_lim_f, rin_f, rout_f, r_far_f, h_unit_f, inv_M_f;
     float hmin_f, hmax_f, rtol_f, atol_f;
     double hmin, hmax;         // adaptive step bounds (hmax scales with r in units of M)
+    double inv_gate;           // invariant gate of the embedded 7(8) integrator (0 = off)
     int island_batch;
     // NP_JITTER_CRITICAL: tangent-plane radius of the critical curve at
     // kCritN equally spaced position angles from -pi, and the band half-width

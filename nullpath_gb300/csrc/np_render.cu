@@ -142,6 +142,7 @@ int prepare_scene(const np_scene_t& sc, SceneDev& d) {
     d.crossing = sc.crossing; d.bg_mode = sc.background; d.disk_on = sc.disk_on;
     d.check_inv = sc.check_invariants;
     d.islands = sc.islands;
+    d.inv_gate = sc.inv_gate > 0.0 ? sc.inv_gate : 0.0;
     // Step doubling at a tight rtol works at the FP32 precision floor where p_r
     // or p_theta changes sign; its turning-point steps are always FP64.
     if (sc.integrator == NP_INTEG_ADAPTIVE) d.islands |= NP_ISLAND_TURNING;
@@ -284,6 +285,7 @@ __device__ __forceinline__ void flush_counters(Counters* ctr, unsigned long long
 // FP64 reference-form tracer.  With `list` non-null the kernel traces the
 // rays named by list[0 .. ctr->deferred) (deferred near-critical rays of the
 // mixed pass); otherwise every ray index in [0, total).
+template <int MODE>
 __global__ void __launch_bounds__(kBlock)
 render_fp64_kernel(const SceneDev s, float* __restrict__ srgb, float* __restrict__ rcross,
                    float* __restrict__ inv3, Counters* __restrict__ ctr, const long long* __restrict__ list) {
@@ -315,7 +317,7 @@ render_fp64_kernel(const SceneDev s, float* __restrict__ srgb, float* __restrict
         }
         if (!__any_sync(FULL, have)) break;
         if (have) {
-            bool done = fp64_advance(s, R, inv3, n_evals);
+            bool done = fp64_advance<MODE, false>(s, R, inv3, n_evals);
             n_steps++;
             if (done) {
                 bool captured = R.status == 1;
@@ -522,7 +524,11 @@ __global__ void trace_rays_kernel(const SceneDev s, int precision, int n, const 
     if (precision == NP_PREC_FP64) {
         RayFP64<true> R;
         fp64_init(s, m, R);
-        while (!fp64_advance(s, R, nullptr, ev)) {}
+        if (s.integrator == NP_INTEG_RKF78) {
+            while (!fp64_advance<kFp64Rkf78, false>(s, R, nullptr, ev)) {}
+        } else {
+            while (!fp64_advance<kFp64Rk4, false>(s, R, nullptr, ev)) {}
+        }
         for (int j = 0; j < 4; ++j) { xr[j] = R.xr[j]; xphi[j] = R.xphi[j]; }
         ncross = R.crossings; st = R.status;
     } else if ((s.islands & kIslandCritical) && near_critical(E, L, Q, s.a, s.M, s.r_plus, kCriticalDb)) {
@@ -546,6 +552,27 @@ __global__ void trace_rays_kernel(const SceneDev s, int precision, int n, const 
     }
     if (cross) for (int j = 0; j < 4; ++j) { cross[8 * i + 2 * j] = xr[j]; cross[8 * i + 2 * j + 1] = xphi[j]; }
     if (status) status[i] = st + 16 * min(ncross, 15);
+}
+
+// Drift of H and Carter's Q along FP64 rays (explicit positions, one per thread).
+__global__ void trace_invariants_kernel(const SceneDev s, int n, const double* __restrict__ px,
+                                        const double* __restrict__ py, double* __restrict__ drift,
+                                        int32_t* __restrict__ steps) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    CamDir dir = camera_dir(s, 0, 0, 0, true, px[i], py[i]);
+    Momentum m = camera_momentum(s, dir);
+    unsigned long long ev = 0;
+    RayFP64<false> R;
+    fp64_init(s, m, R);
+    if (s.integrator == NP_INTEG_RKF78) {
+        while (!fp64_advance<kFp64Rkf78, true>(s, R, nullptr, ev)) {}
+    } else {
+        while (!fp64_advance<kFp64Rk4, true>(s, R, nullptr, ev)) {}
+    }
+    drift[2 * i] = R.dH;
+    drift[2 * i + 1] = R.dQ;
+    if (steps) steps[i] = R.step;
 }
 
 // Register-resident FMA throughput probe: 8 independent chains per thread.
@@ -629,6 +656,18 @@ int grid_for(const void* kernel) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kBlock, 0);
     if (per_sm < 1) per_sm = 1;
     return sms * per_sm;
+}
+
+// FP64 pass: one instantiation per integrator family, so the 7(8) pair's
+// stage storage does not raise the register count of the RK4 kernel.
+void launch_fp64(const SceneDev& s, float* srgb, float* rcross, float* inv3, Counters* ctr, cudaStream_t st) {
+    if (s.integrator == NP_INTEG_RKF78) {
+        render_fp64_kernel<kFp64Rkf78><<<grid_for((const void*)render_fp64_kernel<kFp64Rkf78>), kBlock, 0, st>>>(
+            s, srgb, rcross, inv3, ctr, nullptr);
+    } else {
+        render_fp64_kernel<kFp64Rk4><<<grid_for((const void*)render_fp64_kernel<kFp64Rk4>), kBlock, 0, st>>>(
+            s, srgb, rcross, inv3, ctr, nullptr);
+    }
 }
 
 template <int MINB>
@@ -724,17 +763,29 @@ int np_scene_validate(const np_scene_t* s) {
     if (s->units != NP_UNITS_RS && s->units != NP_UNITS_M) return fail(NP_ERR_INVALID, "Invalid units.");
     if (s->jitter != NP_JITTER_WANGHASH && s->jitter != NP_JITTER_STRATIFIED && s->jitter != NP_JITTER_CRITICAL)
         return fail(NP_ERR_INVALID, "Invalid jitter mode.");
-    if (s->integrator != NP_INTEG_RK4 && s->integrator != NP_INTEG_ADAPTIVE)
+    if (s->integrator != NP_INTEG_RK4 && s->integrator != NP_INTEG_ADAPTIVE && s->integrator != NP_INTEG_RKF78)
         return fail(NP_ERR_INVALID, "Invalid integrator.");
+    if (s->crossing != NP_CROSS_LINEAR && s->crossing != NP_CROSS_HERMITE && s->crossing != NP_CROSS_ROOT)
+        return fail(NP_ERR_INVALID, "Invalid crossing mode.");
+    if (!(s->inv_gate >= 0.0 && s->inv_gate < 1.0)) return fail(NP_ERR_INVALID, "Invalid invariant gate.");
     if ((long long)s->width * s->height > (1ll << 40) / std::max(1, s->spp))
         return fail(NP_ERR_INVALID, "Image too large.");
     return NP_OK;
 }
 
+// The embedded 7(8) integrator and root-found crossings exist on the FP64
+// path only.
+static int check_path(const np_scene_t& sc, int precision) {
+    if (precision != NP_PREC_FP64 && precision != NP_PREC_MIXED) return fail(NP_ERR_INVALID, "Invalid precision.");
+    if (precision == NP_PREC_MIXED && (sc.integrator == NP_INTEG_RKF78 || sc.crossing == NP_CROSS_ROOT))
+        return fail(NP_ERR_INVALID, "The rkf78 integrator and root crossings need precision fp64.");
+    return NP_OK;
+}
+
 int np_render_device(const np_scene_t* scene, int precision, float* d_rgb, float* d_rcross, float* d_inv3,
                      int accumulate, void* stream_v, np_render_stats_t* stats) {
-    if (!d_rgb) return fail(NP_ERR_INVALID, "rgb buffer is NULL");
-    if (precision != NP_PREC_FP64 && precision != NP_PREC_MIXED) return fail(NP_ERR_INVALID, "Invalid precision.");
+    if (!d_rgb || !scene) return fail(NP_ERR_INVALID, "NULL argument");
+    if (int e = check_path(*scene, precision)) return e;
     SceneDev s;
     int rc = prepare_scene(*scene, s);
     if (rc != NP_OK) return rc;
@@ -747,8 +798,7 @@ int np_render_device(const np_scene_t* scene, int precision, float* d_rgb, float
     NP_CU(cudaMemsetAsync(sc->ctr, 0, sizeof(Counters), st), NP_ERR_KERNEL);
     if (stats) NP_CU(cudaEventRecord(sc->ev0, st), NP_ERR_KERNEL);
     if (precision == NP_PREC_FP64) {
-        render_fp64_kernel<<<grid_for((const void*)render_fp64_kernel), kBlock, 0, st>>>(
-            s, sc->srgb, d_rcross, d_inv3, sc->ctr, nullptr);
+        launch_fp64(s, sc->srgb, d_rcross, d_inv3, sc->ctr, st);
         NP_CU(cudaGetLastError(), NP_ERR_KERNEL);
         if (stats) NP_CU(cudaEventRecord(sc->ev1, st), NP_ERR_KERNEL);
     } else {
@@ -824,14 +874,27 @@ int np_render_host(const np_scene_t* scene, int precision, float* h_rgb, float* 
 
 int np_trace_rays_device(const np_scene_t* scene, int precision, int n, const double* d_px, const double* d_py,
                          double* d_consts, double* d_cross, int32_t* d_status, void* stream_v) {
-    if (n < 0 || (n > 0 && (!d_px || !d_py))) return fail(NP_ERR_INVALID, "bad ray arrays");
-    if (precision != NP_PREC_FP64 && precision != NP_PREC_MIXED) return fail(NP_ERR_INVALID, "Invalid precision.");
+    if (n < 0 || (n > 0 && (!d_px || !d_py)) || !scene) return fail(NP_ERR_INVALID, "bad ray arrays");
+    if (int e = check_path(*scene, precision)) return e;
     SceneDev s;
     int rc = prepare_scene(*scene, s);
     if (rc != NP_OK) return rc;
     if (n == 0) return NP_OK;
     cudaStream_t st = (cudaStream_t)stream_v;
     trace_rays_kernel<<<(n + 127) / 128, 128, 0, st>>>(s, precision, n, d_px, d_py, d_consts, d_cross, d_status);
+    NP_CU(cudaGetLastError(), NP_ERR_KERNEL);
+    return NP_OK;
+}
+
+int np_trace_invariants_device(const np_scene_t* scene, int n, const double* d_px, const double* d_py,
+                               double* d_drift, int32_t* d_steps, void* stream_v) {
+    if (n < 0 || (n > 0 && (!d_px || !d_py || !d_drift)) || !scene) return fail(NP_ERR_INVALID, "bad ray arrays");
+    SceneDev s;
+    int rc = prepare_scene(*scene, s);
+    if (rc != NP_OK) return rc;
+    if (n == 0) return NP_OK;
+    cudaStream_t st = (cudaStream_t)stream_v;
+    trace_invariants_kernel<<<(n + 127) / 128, 128, 0, st>>>(s, n, d_px, d_py, d_drift, d_steps);
     NP_CU(cudaGetLastError(), NP_ERR_KERNEL);
     return NP_OK;
 }
@@ -918,7 +981,7 @@ std::mutex g_na_mu;
 extern "C" int np_render_device_noalloc(const np_scene_t* scene, int precision, float* d_rgb, float* d_rcross,
                                         int accumulate, void* stream_v) {
     if (!scene || !d_rgb) return fail(NP_ERR_INVALID, "scene or rgb buffer is NULL");
-    if (precision != NP_PREC_FP64 && precision != NP_PREC_MIXED) return fail(NP_ERR_INVALID, "Invalid precision.");
+    if (int e = check_path(*scene, precision)) return e;
     SceneDev s;
     int rc = prepare_scene(*scene, s);
     if (rc != NP_OK) return rc;
@@ -946,8 +1009,7 @@ extern "C" int np_render_device_noalloc(const np_scene_t* scene, int precision, 
     float* srgb = (float*)(base + kNaSrgb);
     NP_CU(cudaMemsetAsync(ctr, 0, sizeof(Counters), st), NP_ERR_KERNEL);
     if (precision == NP_PREC_FP64) {
-        render_fp64_kernel<<<grid_for((const void*)render_fp64_kernel), kBlock, 0, st>>>(
-            s, srgb, d_rcross, nullptr, ctr, nullptr);
+        launch_fp64(s, srgb, d_rcross, nullptr, ctr, st);
     } else {
         InitSoA soa{(float4*)(base + kNaA), (float4*)(base + kNaB), (float*)(base + kNaCy),
                     (unsigned char*)(base + kNaFlag), (long long*)(base + kNaList)};
@@ -1255,7 +1317,8 @@ np_batch_t* np_batch_create(const np_scene_t* scenes, int n, int precision, void
     b->ray_off.assign((size_t)n + 1, 0);
     b->pix_off.assign((size_t)n + 1, 0);
     for (int i = 0; i < n; ++i) {
-        int rc = prepare_scene(scenes[i], byidx[(size_t)i]);
+        int rc = check_path(scenes[i], NP_PREC_MIXED);
+        if (rc == NP_OK) rc = prepare_scene(scenes[i], byidx[(size_t)i]);
         if (rc != NP_OK) {
             std::string msg = g_last_error;
             batch_free(b);

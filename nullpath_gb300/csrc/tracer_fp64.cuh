@@ -138,6 +138,121 @@ __device__ __forceinline__ double adaptive_ref(St8& y, double M, double a, doubl
     return 0.0;
 }
 
+// Fehlberg's embedded 7(8) pair (E. Fehlberg, NASA TR R-287, 1968): 13
+// stages, the 8th-order solution propagated, the local error estimate
+// h 41/840 (k1 + k11 - k12 - k13).  The metric depends on (r, theta) only
+// and p_t, p_phi are constants, so a stage input needs the (r, theta, p_r,
+// p_theta) parts of earlier stages; t and phi are accumulated into the
+// solution as each stage is evaluated.  Returns the weighted error norm
+// over (r, theta, phi, p_r, p_theta, p_phi) (p_phi's error is zero).
+struct K4 { double r, th, pr, pth; };
+
+__device__ __forceinline__ K4 k4_of(const St8& f) { return K4{f.r, f.th, f.pr, f.pth}; }
+
+__device__ __forceinline__ double rkf78_ref(const St8& y, double M, double a, double rp, double h, double rtol,
+                                            double atol, St8& out, St8& k1full) {
+    St8 z = y, f;
+    double st = 0.0, sph = 0.0, eph = 0.0;   // h-free sums of b_i k_i.t, b_i k_i.ph, e_i k_i.ph
+    auto eval = [&](double b, double e) {
+        rhs_ref(z, M, a, rp, f);
+        st += b * f.t; sph += b * f.ph; eph += e * f.ph;
+        return k4_of(f);
+    };
+    auto set = [&](double dr, double dth, double dpr, double dpth) {
+        z.r = y.r + h * dr; z.th = y.th + h * dth; z.pr = y.pr + h * dpr; z.pth = y.pth + h * dpth;
+    };
+    const double e1 = 41.0 / 840.0;
+    K4 k1 = eval(0.0, e1);
+    k1full = f;
+    set(2.0 / 27 * k1.r, 2.0 / 27 * k1.th, 2.0 / 27 * k1.pr, 2.0 / 27 * k1.pth);
+    K4 k2 = eval(0.0, 0.0);
+#define NP_S3(c) (1.0 / 36 * k1.c + 1.0 / 12 * k2.c)
+    set(NP_S3(r), NP_S3(th), NP_S3(pr), NP_S3(pth));
+    K4 k3 = eval(0.0, 0.0);
+#define NP_S4(c) (1.0 / 24 * k1.c + 1.0 / 8 * k3.c)
+    set(NP_S4(r), NP_S4(th), NP_S4(pr), NP_S4(pth));
+    K4 k4 = eval(0.0, 0.0);
+#define NP_S5(c) (5.0 / 12 * k1.c - 25.0 / 16 * k3.c + 25.0 / 16 * k4.c)
+    set(NP_S5(r), NP_S5(th), NP_S5(pr), NP_S5(pth));
+    K4 k5 = eval(0.0, 0.0);
+#define NP_S6(c) (1.0 / 20 * k1.c + 1.0 / 4 * k4.c + 1.0 / 5 * k5.c)
+    set(NP_S6(r), NP_S6(th), NP_S6(pr), NP_S6(pth));
+    K4 k6 = eval(34.0 / 105, 0.0);
+#define NP_S7(c) (-25.0 / 108 * k1.c + 125.0 / 108 * k4.c - 65.0 / 27 * k5.c + 125.0 / 54 * k6.c)
+    set(NP_S7(r), NP_S7(th), NP_S7(pr), NP_S7(pth));
+    K4 k7 = eval(9.0 / 35, 0.0);
+#define NP_S8(c) (31.0 / 300 * k1.c + 61.0 / 225 * k5.c - 2.0 / 9 * k6.c + 13.0 / 900 * k7.c)
+    set(NP_S8(r), NP_S8(th), NP_S8(pr), NP_S8(pth));
+    K4 k8 = eval(9.0 / 35, 0.0);
+#define NP_S9(c) (2.0 * k1.c - 53.0 / 6 * k4.c + 704.0 / 45 * k5.c - 107.0 / 9 * k6.c + 67.0 / 90 * k7.c + 3.0 * k8.c)
+    set(NP_S9(r), NP_S9(th), NP_S9(pr), NP_S9(pth));
+    K4 k9 = eval(9.0 / 280, 0.0);
+#define NP_S10(c) (-91.0 / 108 * k1.c + 23.0 / 108 * k4.c - 976.0 / 135 * k5.c + 311.0 / 54 * k6.c \
+                   - 19.0 / 60 * k7.c + 17.0 / 6 * k8.c - 1.0 / 12 * k9.c)
+    set(NP_S10(r), NP_S10(th), NP_S10(pr), NP_S10(pth));
+    K4 k10 = eval(9.0 / 280, 0.0);
+#define NP_S11(c) (2383.0 / 4100 * k1.c - 341.0 / 164 * k4.c + 4496.0 / 1025 * k5.c - 301.0 / 82 * k6.c \
+                   + 2133.0 / 4100 * k7.c + 45.0 / 82 * k8.c + 45.0 / 164 * k9.c + 18.0 / 41 * k10.c)
+    set(NP_S11(r), NP_S11(th), NP_S11(pr), NP_S11(pth));
+    K4 k11 = eval(0.0, e1);
+#define NP_S12(c) (3.0 / 205 * k1.c - 6.0 / 41 * k6.c - 3.0 / 205 * k7.c - 3.0 / 41 * k8.c + 3.0 / 41 * k9.c \
+                   + 6.0 / 41 * k10.c)
+    set(NP_S12(r), NP_S12(th), NP_S12(pr), NP_S12(pth));
+    K4 k12 = eval(41.0 / 840, -e1);
+#define NP_S13(c) (-1777.0 / 4100 * k1.c - 341.0 / 164 * k4.c + 4496.0 / 1025 * k5.c - 289.0 / 82 * k6.c \
+                   + 2193.0 / 4100 * k7.c + 51.0 / 82 * k8.c + 33.0 / 164 * k9.c + 12.0 / 41 * k10.c + k12.c)
+    set(NP_S13(r), NP_S13(th), NP_S13(pr), NP_S13(pth));
+    K4 k13 = eval(41.0 / 840, -e1);
+#define NP_B8(c) (34.0 / 105 * k6.c + 9.0 / 35 * k7.c + 9.0 / 35 * k8.c + 9.0 / 280 * k9.c + 9.0 / 280 * k10.c \
+                  + 41.0 / 840 * k12.c + 41.0 / 840 * k13.c)
+#define NP_E(c) (e1 * (k1.c + k11.c - k12.c - k13.c))
+    out = y;
+    out.t = y.t + h * st;
+    out.ph = y.ph + h * sph;
+    out.r = y.r + h * NP_B8(r);
+    out.th = y.th + h * NP_B8(th);
+    out.pr = y.pr + h * NP_B8(pr);
+    out.pth = y.pth + h * NP_B8(pth);
+    auto w = [&](double err, double u, double v) {
+        double sc = atol + rtol * fmax(fabs(u), fabs(v));
+        return fabs(h * err) / fmax(sc, 1e-30);
+    };
+    double e = fmax(fmax(w(NP_E(r), y.r, out.r), w(NP_E(th), y.th, out.th)),
+                    fmax(fmax(w(eph, y.ph, out.ph), w(NP_E(pr), y.pr, out.pr)), w(NP_E(pth), y.pth, out.pth)));
+#undef NP_S3
+#undef NP_S4
+#undef NP_S5
+#undef NP_S6
+#undef NP_S7
+#undef NP_S8
+#undef NP_S9
+#undef NP_S10
+#undef NP_S11
+#undef NP_S12
+#undef NP_S13
+#undef NP_B8
+#undef NP_E
+    return e;
+}
+
+// Hamiltonian H = g^{mu nu} p_mu p_nu / 2 and Carter's constant
+// Q = p_theta^2 + cos^2 theta (L^2 / sin^2 theta - a^2 E^2) of a state.
+__device__ __forceinline__ void h_and_q(const St8& y, double M, double a, double& H, double& Q) {
+    double sn, c;
+    sincos(y.th, &sn, &c);
+    double r2 = y.r * y.r, a2 = a * a;
+    double s2 = fmax(kEps, sn * sn);
+    double Sig = fmax(kEps, r2 + a2 * c * c);
+    double Del = r2 - 2.0 * M * y.r + a2;
+    double A = (r2 + a2) * (r2 + a2) - a2 * Del * s2;
+    double grr = fmax(kEps, Del) / Sig, ghh = 1.0 / Sig;
+    double gtt = -A / fmax(kEps, Sig * Del), gtp = -2.0 * M * a * y.r / fmax(kEps, Sig * Del);
+    double gpp = (Del - a2 * s2) / fmax(kEps, Sig * Del * s2);
+    H = 0.5 * (gtt * y.pt * y.pt + 2.0 * gtp * y.pt * y.pph + gpp * y.pph * y.pph + grr * y.pr * y.pr
+               + ghh * y.pth * y.pth);
+    Q = y.pth * y.pth + c * c * (y.pph * y.pph / s2 - a2 * y.pt * y.pt);
+}
+
 __device__ __forceinline__ void invariants_ref(const SceneDev& s, const St8& y, double pt0, double pph0, float* inv3) {
     double sn, c;
     sincos(y.th, &sn, &c);
@@ -157,11 +272,15 @@ __device__ __forceinline__ void invariants_ref(const SceneDev& s, const St8& y, 
 }
 
 // Per-lane ray of the FP64 tracer.  With REC the first four equatorial
-// crossings (any radius) are recorded for the per-ray report.
+// crossings (any radius) are recorded for the per-ray report.  q0 and qs
+// are Carter's constant at the camera and its drift scale max(|Q0|,
+// (E M)^2); dH and dQ the largest |H| / E^2 and |Q - Q0| / qs seen (drift
+// tracking only).
 template <bool REC>
 struct RayFP64 {
     St8 y, prev;
     double min_r, h_adapt, first_r, pt0, pph0;
+    double q0, qs, dH, dQ;
     double xr[REC ? 4 : 1], xphi[REC ? 4 : 1];
     float disk[3];
     int step, orders, crossings, status;   // status: 0 escaped, 1 captured, 2 step cap
@@ -175,14 +294,68 @@ __device__ __forceinline__ void fp64_init(const SceneDev& s, const Momentum& m, 
     R.h_adapt = 0.0;
     R.first_r = 0.0;
     R.pt0 = m.pt; R.pph0 = m.pph;
+    double H0, Q0;
+    h_and_q(R.y, s.M, s.a, H0, Q0);
+    R.q0 = Q0;
+    R.qs = fmax(fabs(Q0), m.pt * m.pt * s.M * s.M);
+    R.dH = fabs(H0) / (m.pt * m.pt);
+    R.dQ = 0.0;
     R.disk[0] = R.disk[1] = R.disk[2] = 0.0f;
     R.step = 0; R.orders = 0; R.crossings = 0; R.status = 2;
     if (REC) for (int k = 0; k < 4; ++k) { R.xr[k] = 0.0; R.xphi[k] = 0.0; }
 }
 
+// Integrator families of fp64_advance: RK4 and step doubling (chosen by
+// the scene at run time), or the embedded 7(8) pair.
+constexpr int kFp64Rk4 = 0;
+constexpr int kFp64Rkf78 = 1;
+
+// One step of size h from y with the family's single-step map (the
+// crossing root finder re-integrates the crossing step with it).
+template <int MODE>
+__device__ __forceinline__ void fp64_single_step(const SceneDev& s, const St8& y, double h, St8& out,
+                                                 unsigned long long& evals) {
+    St8 k1;
+    if (MODE == kFp64Rkf78) {
+        rkf78_ref(y, s.M, s.a, s.r_plus, h, s.rtol, s.atol, out, k1);
+        evals += 13;
+    } else {
+        rk4_ref(y, s.M, s.a, s.r_plus, h, out, k1);
+        evals += 4;
+    }
+}
+
+// Crossing of theta = pi/2 inside the step prev -> (prev advanced by h):
+// Newton iteration on the fraction u of the step, each iterate a fresh
+// single step of u h from prev, safeguarded by the sign bracket [0, 1].
+// Returns the state at the crossing.
+template <int MODE>
+__device__ __forceinline__ St8 fp64_root_crossing(const SceneDev& s, const St8& prev, double h, double dp, double u0,
+                                                  unsigned long long& evals) {
+    const double hp = kPi * 0.5;
+    double lo = 0.0, hi = 1.0, u = u0;
+    St8 z = prev, f;
+    for (int it = 0; it < 10; ++it) {
+        fp64_single_step<MODE>(s, prev, u * h, z, evals);
+        double g = z.th - hp;
+        if (g == 0.0) break;
+        if ((g > 0.0) == (dp > 0.0)) lo = u; else hi = u;
+        rhs_ref(z, s.M, s.a, s.r_plus, f);
+        evals += 1;
+        double dg = h * f.th;
+        double un = (dg != 0.0) ? u - g / dg : 0.5 * (lo + hi);
+        if (!(un > lo && un < hi)) un = 0.5 * (lo + hi);
+        bool done = fabs(un - u) < 1e-15;
+        u = un;
+        if (done) break;
+    }
+    return z;
+}
+
 // Advances the ray by one accepted step; returns true when it terminated.
-// `evals` counts right-hand-side evaluations.
-template <bool REC>
+// `evals` counts right-hand-side evaluations; with TRK the drift of H and
+// Q is tracked over the accepted steps.
+template <int MODE, bool TRK, bool REC>
 __device__ __forceinline__ bool fp64_advance(const SceneDev& s, RayFP64<REC>& R, float* inv3, unsigned long long& evals) {
     if (R.step >= s.max_steps) { R.status = 2; return true; }
     const double M = s.M, a = s.a, rp = s.r_plus;
@@ -190,7 +363,38 @@ __device__ __forceinline__ bool fp64_advance(const SceneDev& s, RayFP64<REC>& R,
     bool ok = false;
     double h_used = 0.0;
     St8 k1;
-    if (s.integrator == NP_INTEG_ADAPTIVE) {
+    if (MODE == kFp64Rkf78) {
+        // same step bounds as step doubling; growth and shrink factors of an
+        // order-7 error estimate, 0.9 e^(-1/8) within [0.2, 4] ([0.1, 1) on rejection)
+        const double hmin = s.hmin, hmax = s.ref_units ? s.hmax : s.hmax * scale;
+        double h = (R.h_adapt > 0.0) ? R.h_adapt : s.h_unit * scale;
+        h = fmin(fmax(h, hmin), hmax);
+        for (int att = 0; att < 24; ++att) {
+            St8 out;
+            double e = rkf78_ref(R.y, M, a, rp, h, s.rtol, s.atol, out, k1);
+            evals += 13;
+            bool alive = out.r > rp + 1e-12 && out.th > 1e-9 && out.th < kPi - 1e-9 && e == e;
+            bool acc = alive && e <= 1.0;
+            bool gated = false;
+            if (acc && s.inv_gate > 0.0 && h > hmin * 1.01) {
+                double H, Q;
+                h_and_q(out, M, a, H, Q);
+                gated = fabs(H) > s.inv_gate * R.pt0 * R.pt0 || fabs(Q - R.q0) > s.inv_gate * R.qs;
+                acc = !gated;
+            }
+            if (acc) {
+                ok = true; h_used = h;
+                R.y = out;
+                double sc2 = fmin(fmax(1.0, out.r / (0.5 * s.Rs)), 100.0);
+                double grow = fmin(4.0, fmax(0.2, kSafety * pow(fmax(e, 1e-16), -0.125)));
+                R.h_adapt = fmin(fmax(h * grow, hmin), s.ref_units ? s.hmax : s.hmax * sc2);
+                break;
+            }
+            if (h <= hmin * 1.01) break;
+            double fac = (!alive || gated) ? 0.5 : fmin(0.9, fmax(0.1, kSafety * pow(e, -0.125)));
+            h = fmax(h * fac, hmin);
+        }
+    } else if (s.integrator == NP_INTEG_ADAPTIVE) {
         // bounds: BH_RK_HMIN/HMAX (bh_common.h:245,253) for reference scenes;
         // hmax scaled like the fixed step law for scenes in units of M
         const double hmin = s.hmin, hmax = s.ref_units ? s.hmax : s.hmax * scale;
@@ -220,6 +424,12 @@ __device__ __forceinline__ bool fp64_advance(const SceneDev& s, RayFP64<REC>& R,
     }
     R.step++;
     if (!ok) { R.status = 1; return true; }
+    if (TRK) {
+        double H, Q;
+        h_and_q(R.y, M, a, H, Q);
+        R.dH = fmax(R.dH, fabs(H) / (R.pt0 * R.pt0));
+        R.dQ = fmax(R.dQ, fabs(Q - R.q0) / R.qs);
+    }
     R.min_r = fmin(R.min_r, R.y.r);
     const double hp = kPi * 0.5;
     double dp = R.prev.th - hp, dc = R.y.th - hp;
@@ -228,7 +438,11 @@ __device__ __forceinline__ bool fp64_advance(const SceneDev& s, RayFP64<REC>& R,
     if (sc || nz) {
         double alpha = fabs(dp) / (fabs(dp) + fabs(dc) + 1e-30);
         double rc, phc;
-        if (s.crossing == NP_CROSS_HERMITE && sc) {
+        if (s.crossing == NP_CROSS_ROOT && sc) {
+            St8 z = fp64_root_crossing<MODE>(s, R.prev, h_used, dp, alpha, evals);
+            rc = z.r;
+            phc = z.ph;
+        } else if (s.crossing == NP_CROSS_HERMITE && sc) {
             St8 f1;
             rhs_ref(R.y, M, a, rp, f1);
             evals += 1;

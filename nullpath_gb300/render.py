@@ -83,3 +83,20 @@ def trace_rays(scene, px, py, precision="mixed"):
     check(lib.np_trace_rays_device(C.byref(scene), precision_code(precision), n, _ptr(px), _ptr(py),
                                    _ptr(consts), _ptr(cross), _ptr(status), C.c_void_p(stream.cuda_stream)))
     return {"consts": consts, "cross": cross, "status": status}
+
+
+def trace_invariants(scene, px, py):
+    """FP64 rays through image positions (px, py): returns (drift[n, 2], steps[n])
+    as CUDA tensors, drift = (max |H| / E^2, max |Q - Q0| / max(|Q0|, (E M)^2))
+    over each ray's accepted steps (Q is Carter's constant)."""
+    import torch
+    lib = load()
+    px = torch.as_tensor(px, dtype=torch.float64, device="cuda").contiguous()
+    py = torch.as_tensor(py, dtype=torch.float64, device="cuda").contiguous()
+    n = px.numel()
+    drift = torch.zeros((n, 2), dtype=torch.float64, device="cuda")
+    steps = torch.zeros((n,), dtype=torch.int32, device="cuda")
+    stream = torch.cuda.current_stream()
+    check(lib.np_trace_invariants_device(C.byref(scene), n, _ptr(px), _ptr(py), _ptr(drift), _ptr(steps),
+                                         C.c_void_p(stream.cuda_stream)))
+    return drift, steps

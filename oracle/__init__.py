@@ -31,6 +31,10 @@ def load():
         lib.npo_trace_rays.argtypes = [S, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                        C.c_void_p, C.c_void_p, C.c_int]
         lib.npo_trace_rays.restype = C.c_int
+        lib.npo_trace_invariants.argtypes = [S, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
+        lib.npo_trace_invariants.restype = C.c_int
+        lib.npo_rkf78_tableau.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+        lib.npo_rkf78_tableau.restype = None
         lib.npo_critical_curve.argtypes = [S, C.c_void_p]
         lib.npo_critical_curve.restype = C.c_int
         lib.npo_metric_inv.argtypes = [C.c_double] * 4 + [C.c_void_p]
@@ -102,6 +106,28 @@ def trace_rays(scene, px, py, threads=0):
                           _vp(steps), threads) != 0:
         raise RuntimeError("oracle trace failed")
     return {"consts": consts, "cross": cross, "status": status, "steps": steps}
+
+
+def trace_invariants(scene, px, py, threads=0):
+    """Per-ray (max |H|/E^2, max |dQ|/Q scale) and step counts, as np_trace_invariants_device."""
+    lib = load()
+    px = np.ascontiguousarray(px, np.float64)
+    py = np.ascontiguousarray(py, np.float64)
+    n = px.size
+    drift = np.zeros((n, 2), np.float64)
+    steps = np.zeros(n, np.int32)
+    if lib.npo_trace_invariants(C.byref(scene), n, _vp(px), _vp(py), _vp(drift), _vp(steps), threads) != 0:
+        raise RuntimeError("oracle trace_invariants failed")
+    return drift, steps
+
+
+def rkf78_tableau():
+    """(A[13,13], b8[13], err[13]) of the oracle's Fehlberg 7(8) pair."""
+    A = np.zeros((13, 13))
+    b = np.zeros(13)
+    e = np.zeros(13)
+    load().npo_rkf78_tableau(_vp(A), _vp(b), _vp(e))
+    return A, b, e
 
 
 def metric_inv(lib, M, a, r, th):

@@ -228,6 +228,76 @@ static double adaptive_step(State& y, double M, double a, double& h, double rtol
     return 0.0;
 }
 
+// Fehlberg 7(8) tableau (E. Fehlberg, NASA TR R-287, 1968, table X):
+// 13 stages, rows of the coupling matrix, 8th-order weights, and the
+// error weights (7th minus 8th order: 41/840 on k1, k11 and -41/840 on k12, k13).
+static const double kF78A[13][12] = {
+    {},
+    {2.0 / 27},
+    {1.0 / 36, 1.0 / 12},
+    {1.0 / 24, 0, 1.0 / 8},
+    {5.0 / 12, 0, -25.0 / 16, 25.0 / 16},
+    {1.0 / 20, 0, 0, 1.0 / 4, 1.0 / 5},
+    {-25.0 / 108, 0, 0, 125.0 / 108, -65.0 / 27, 125.0 / 54},
+    {31.0 / 300, 0, 0, 0, 61.0 / 225, -2.0 / 9, 13.0 / 900},
+    {2.0, 0, 0, -53.0 / 6, 704.0 / 45, -107.0 / 9, 67.0 / 90, 3.0},
+    {-91.0 / 108, 0, 0, 23.0 / 108, -976.0 / 135, 311.0 / 54, -19.0 / 60, 17.0 / 6, -1.0 / 12},
+    {2383.0 / 4100, 0, 0, -341.0 / 164, 4496.0 / 1025, -301.0 / 82, 2133.0 / 4100, 45.0 / 82, 45.0 / 164, 18.0 / 41},
+    {3.0 / 205, 0, 0, 0, 0, -6.0 / 41, -3.0 / 205, -3.0 / 41, 3.0 / 41, 6.0 / 41, 0},
+    {-1777.0 / 4100, 0, 0, -341.0 / 164, 4496.0 / 1025, -289.0 / 82, 2193.0 / 4100, 51.0 / 82, 33.0 / 164,
+     12.0 / 41, 0, 1.0},
+};
+static const double kF78B[13] = {0, 0, 0, 0, 0, 34.0 / 105, 9.0 / 35, 9.0 / 35, 9.0 / 280, 9.0 / 280, 0,
+                                 41.0 / 840, 41.0 / 840};
+static const double kF78E[13] = {41.0 / 840, 0, 0, 0, 0, 0, 0, 0, 0, 0, 41.0 / 840, -41.0 / 840, -41.0 / 840};
+
+static inline double& comp(State& y, int i) {
+    double* p[8] = {&y.t, &y.r, &y.th, &y.ph, &y.pt, &y.pr, &y.pth, &y.pph};
+    return *p[i];
+}
+static inline double compc(const State& y, int i) {
+    const double p[8] = {y.t, y.r, y.th, y.ph, y.pt, y.pr, y.pth, y.pph};
+    return p[i];
+}
+
+// One 7(8) step: out = 8th-order solution; returns the error norm over
+// (r, theta, phi, p_r, p_theta, p_phi) with the step-doubling weights.
+static double rkf78(const State& y, double M, double a, double h, double rtol, double atol, State& out) {
+    State k[13];
+    for (int j = 0; j < 13; ++j) {
+        State z = y;
+        for (int c = 0; c < 8; ++c) {
+            double acc = 0.0;
+            for (int i = 0; i < j; ++i) acc += kF78A[j][i] * compc(k[i], c);
+            comp(z, c) = comp(z, c) + h * acc;
+        }
+        rhs(z, M, a, k[j]);
+    }
+    out = y;
+    double e = 0.0;
+    for (int c = 0; c < 8; ++c) {
+        double acc = 0.0, err = 0.0;
+        for (int i = 0; i < 13; ++i) { acc += kF78B[i] * compc(k[i], c); err += kF78E[i] * compc(k[i], c); }
+        comp(out, c) = compc(y, c) + h * acc;
+        if (c == 1 || c == 2 || c == 3 || c == 5 || c == 6 || c == 7) {
+            double sc = atol + rtol * std::fmax(std::fabs(compc(y, c)), std::fabs(compc(out, c)));
+            e = std::fmax(e, std::fabs(h * err) / std::fmax(sc, 1e-30));
+        }
+    }
+    return e;
+}
+
+// Hamiltonian and Carter's constant of a state.
+static void h_and_q(const State& y, double M, double a, double& H, double& Q) {
+    double g[5];
+    metric_inv(M, a, y.r, y.th, g);
+    H = 0.5 * (g[0] * y.pt * y.pt + 2.0 * g[1] * y.pt * y.pph + g[2] * y.pph * y.pph + g[3] * y.pr * y.pr
+               + g[4] * y.pth * y.pth);
+    double c = std::cos(y.th), sn = std::sin(y.th);
+    double s2 = std::fmax(kEps, sn * sn);
+    Q = y.pth * y.pth + c * c * (y.pph * y.pph / s2 - a * a * y.pt * y.pt);
+}
+
 // Static-observer tetrad -> covariant momentum (bh_kerr.h:781-826).
 static State camera_static(double M, double a, double r, double th, double ph,
                            double nr, double nth, double nph) {
@@ -340,7 +410,7 @@ struct Frame {
     int max_steps, max_orders, integrator, crossing, bg_mode, disk_on, jitter, strata;
     float bg_sigma_rad, bg_peak;
     uint32_t seed;
-    double rtol, atol;
+    double rtol, atol, inv_gate;
     float crit_rho[256];          // NP_JITTER_CRITICAL: critical-curve radius per position angle
     double crit_band;
 };
@@ -405,6 +475,7 @@ static Frame make_frame(const np_scene_t& s) {
     f.max_steps = s.max_steps;
     f.max_orders = std::max(1, s.disk_max_orders);
     f.integrator = s.integrator;
+    f.inv_gate = s.inv_gate > 0.0 ? s.inv_gate : 0.0;
     f.crossing = s.crossing;
     f.bg_mode = s.background;
     f.disk_on = s.disk_on;
@@ -560,6 +631,7 @@ struct RayOut {
     long steps = 0;
     State last{};
     double pt0 = 0.0, pph0 = 0.0;
+    double dH = 0.0, dQ = 0.0;    // max |H| / E^2, max |Q - Q0| / max(|Q0|, (E M)^2)
     float inv[3] = {0, 0, 0};
 };
 
@@ -601,11 +673,44 @@ static inline double hermite_eval(double y0, double y1, double m0, double m1, do
     return (2 * s3 - 3 * s2 + 1) * y0 + (s3 - 2 * s2 + s) * m0 + (-2 * s3 + 3 * s2) * y1 + (s3 - s2) * m1;
 }
 
+// Single step of the integrator family (RK4 for RK4 and step doubling).
+static void single_step(const Frame& f, const State& y, double h, State& out) {
+    if (f.integrator == NP_INTEG_RKF78) rkf78(y, f.M, f.a, h, f.rtol, f.atol, out);
+    else rk4(y, f.M, f.a, h, out, nullptr);
+}
+
+// theta = pi/2 inside the step prev -> prev + h: Newton on the step
+// fraction u with fresh single steps of u h from prev, kept inside the sign
+// bracket [0, 1] (bisection when Newton leaves it).
+static State root_crossing(const Frame& f, const State& prev, double h, double dp, double u0) {
+    const double hp = kPi * 0.5;
+    double lo = 0.0, hi = 1.0, u = u0;
+    State z = prev, fz;
+    for (int it = 0; it < 10; ++it) {
+        single_step(f, prev, u * h, z);
+        double g = z.th - hp;
+        if (g == 0.0) break;
+        if ((g > 0.0) == (dp > 0.0)) lo = u; else hi = u;
+        rhs(z, f.M, f.a, fz);
+        double dg = h * fz.th;
+        double un = (dg != 0.0) ? u - g / dg : 0.5 * (lo + hi);
+        if (!(un > lo && un < hi)) un = 0.5 * (lo + hi);
+        bool done = std::fabs(un - u) < 1e-15;
+        u = un;
+        if (done) break;
+    }
+    return z;
+}
+
 // Traces one ray in FP64 following render.cu:161-251.
-static void trace(const Frame& f, const Dir& d, bool track_inv, RayOut& o) {
+static void trace(const Frame& f, const Dir& d, bool track_inv, RayOut& o, bool track_drift = false) {
     State y = f.zamo ? camera_zamo(f.M, f.a, f.r_cam, f.th_cam, f.ph_cam, d.nr, d.nth, d.nph)
                      : camera_static(f.M, f.a, f.r_cam, f.th_cam, f.ph_cam, d.nr, d.nth, d.nph);
     o.pt0 = y.pt; o.pph0 = y.pph;
+    double H0, Q0;
+    h_and_q(y, f.M, f.a, H0, Q0);
+    const double E2 = y.pt * y.pt, qs = std::fmax(std::fabs(Q0), E2 * f.M * f.M);
+    o.dH = std::fabs(H0) / E2;
     o.min_r = y.r;
     State prev = y;
     double h_adapt = 0.0;
@@ -617,7 +722,39 @@ static void trace(const Frame& f, const Dir& d, bool track_inv, RayOut& o) {
         bool ok = false;
         double h_used = 0.0;
         State k1{};
-        if (f.integrator == NP_INTEG_ADAPTIVE) {
+        if (f.integrator == NP_INTEG_RKF78) {
+            // step bounds of step doubling; factors 0.9 e^(-1/8) in [0.2, 4]
+            // on acceptance, [0.1, 0.9] on rejection, halving on a gate or
+            // horizon rejection; the gate is not applied at the smallest step
+            const double hmin = f.ref_units ? kHMin : kHMin * f.M;
+            const double hmax = f.ref_units ? kHMax : 10.0 * f.h_unit * scale;
+            double h = (h_adapt > 0.0) ? h_adapt : f.h_unit * scale;
+            h = std::fmin(std::fmax(h, hmin), hmax);
+            for (int att = 0; att < 24; ++att) {
+                State out;
+                double e = rkf78(y, f.M, f.a, h, f.rtol, f.atol, out);
+                bool alive = alive_adaptive(out, f.M, f.a) && e == e;
+                bool acc = alive && e <= 1.0, gated = false;
+                if (acc && f.inv_gate > 0.0 && h > hmin * 1.01) {
+                    double H, Q;
+                    h_and_q(out, f.M, f.a, H, Q);
+                    gated = std::fabs(H) > f.inv_gate * E2 || std::fabs(Q - Q0) > f.inv_gate * qs;
+                    acc = !gated;
+                }
+                if (acc) {
+                    ok = true; h_used = h;
+                    rhs(y, f.M, f.a, k1);
+                    y = out;
+                    double sc2 = std::fmin(std::fmax(1.0, y.r / (0.5 * f.Rs)), 100.0);
+                    double grow = std::fmin(4.0, std::fmax(0.2, kSafety * std::pow(std::fmax(e, 1e-16), -0.125)));
+                    h_adapt = std::fmin(std::fmax(h * grow, hmin), f.ref_units ? kHMax : 10.0 * f.h_unit * sc2);
+                    break;
+                }
+                if (h <= hmin * 1.01) break;
+                double fac = (!alive || gated) ? 0.5 : std::fmin(0.9, std::fmax(0.1, kSafety * std::pow(e, -0.125)));
+                h = std::fmax(h * fac, hmin);
+            }
+        } else if (f.integrator == NP_INTEG_ADAPTIVE) {
             // BH_RK_HMIN/HMAX for reference scenes; in units of M the largest
             // step is 10 x the fixed step law at the current radius
             const double hmin = f.ref_units ? kHMin : kHMin * f.M;
@@ -646,6 +783,12 @@ static void trace(const Frame& f, const Dir& d, bool track_inv, RayOut& o) {
         }
         o.steps++;
         if (!ok) { o.captured = true; o.status = 1; break; }
+        if (track_drift) {
+            double H, Q;
+            h_and_q(y, f.M, f.a, H, Q);
+            o.dH = std::fmax(o.dH, std::fabs(H) / E2);
+            o.dQ = std::fmax(o.dQ, std::fabs(Q - Q0) / qs);
+        }
         o.min_r = std::fmin(o.min_r, y.r);
         double dp = prev.th - half_pi, dc = y.th - half_pi;
         const double eps = 1e-8;
@@ -654,7 +797,11 @@ static void trace(const Frame& f, const Dir& d, bool track_inv, RayOut& o) {
         if (sign_change || near_zero) {
             double alpha = std::fabs(dp) / (std::fabs(dp) + std::fabs(dc) + 1e-30);
             double rc, phc;
-            if (f.crossing == NP_CROSS_HERMITE && sign_change) {
+            if (f.crossing == NP_CROSS_ROOT && sign_change) {
+                State z = root_crossing(f, prev, h_used, dp, alpha);
+                rc = z.r;
+                phc = z.ph;
+            } else if (f.crossing == NP_CROSS_HERMITE && sign_change) {
                 State f1;
                 rhs(y, f.M, f.a, f1);
                 double s = hermite_root(dp, dc, h_used * k1.th, h_used * f1.th, alpha);
@@ -809,6 +956,38 @@ int npo_trace_rays(const np_scene_t* sc, int n, const double* px, const double* 
         if (steps) steps[i] = (int32_t)o.steps;
     }
     return NP_OK;
+}
+
+// Conserved-quantity drift of explicit rays; layout as np_trace_invariants_device.
+int npo_trace_invariants(const np_scene_t* sc, int n, const double* px, const double* py, double* drift,
+                         int32_t* steps, int nthreads) {
+    if (!sc || n < 0 || !px || !py || !drift) return NP_ERR_INVALID;
+    const np_scene_t s = *sc;
+    Frame f = make_frame(s);
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+    (void)nthreads;
+#endif
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int i = 0; i < n; ++i) {
+        Dir d = camera_dir(f, s, 0, 0, 0, true, px[i], py[i]);
+        RayOut o;
+        trace(f, d, false, o, true);
+        drift[2 * i] = o.dH;
+        drift[2 * i + 1] = o.dQ;
+        if (steps) steps[i] = (int32_t)o.steps;
+    }
+    return NP_OK;
+}
+
+// The 7(8) tableau (rows of A, weights b8, error weights) for order checks.
+void npo_rkf78_tableau(double* A, double* b, double* e) {
+    for (int j = 0; j < 13; ++j) {
+        for (int i = 0; i < 13; ++i) A[13 * j + i] = i < 12 ? kF78A[j][i] : 0.0;
+        b[j] = kF78B[j];
+        e[j] = kF78E[j];
+    }
 }
 
 int npo_abi_version(void) { return NP_ABI_VERSION; }
