@@ -220,6 +220,41 @@ def critical_leg(W=2048, spp=16, spin=0.998, n_acc=8000):
     return out
 
 
+def research_leg(n_acc=20000, n_drift=4000):
+    """Research mode on the 1280x720 benchmark camera, 1 spp: FP64 Fehlberg
+    7(8) at rtol 1e-12 / atol 1e-14, root-found crossings, invariant gate
+    1e-12.  Throughput of the FP64 render kernel, crossing error against the
+    Mino-time solver, and the drift of H and of Carter's Q along the rays;
+    the FP64 RK4 reference integrator with Hermite crossings on the same
+    rays for comparison."""
+    import numpy as np
+    import torch
+    import nullpath_gb300 as npx
+    from nullpath_gb300 import accuracy
+    from nullpath_gb300._abi import NP_INTEG_RKF78, NP_CROSS_ROOT
+    base = npx.benchmark_scene(spp=1)
+    res = base.replace(integrator=NP_INTEG_RKF78, crossing=NP_CROSS_ROOT, rtol=1e-12, atol=1e-14, inv_gate=1e-12)
+    rays = base.width * base.height
+    rgb = torch.zeros((3, base.height, base.width), dtype=torch.float32, device="cuda")
+    rc = torch.zeros((base.height, base.width), dtype=torch.float32, device="cuda")
+    rng = np.random.default_rng(7)
+    px, py = rng.uniform(0, base.width, n_drift), rng.uniform(0, base.height, n_drift)
+    out = {"rays": rays}
+    cache = {}
+    for name, scn in (("rkf78_root_gate", res), ("rk4_hermite", base)):
+        npx.render(scn, "fp64", rgb=rgb, rcross=rc)
+        _, _, st = npx.render(scn, "fp64", rgb=rgb, rcross=rc, stats=True)
+        d, steps = npx.trace_invariants(scn, px, py)
+        torch.cuda.synchronize()
+        d = d.cpu().numpy()
+        out[name] = {"rays_per_s": rays / (st.kernel_ms * 1e-3), "kernel_ms": st.kernel_ms,
+                     "mean_steps_per_ray": st.steps / max(1, st.rays), "rhs_per_ray": st.rhs_evals / max(1, st.rays),
+                     "error_vs_geokerr": accuracy.crossing_error(scn, n=n_acc, precision="fp64", seed=11, cache=cache),
+                     "drift_H_max": float(d[:, 0].max()), "drift_H_p99": float(np.quantile(d[:, 0], 0.99)),
+                     "drift_Q_max": float(d[:, 1].max()), "drift_Q_p99": float(np.quantile(d[:, 1], 0.99))}
+    return out
+
+
 def adjoint_leg(Ks=(16, 64, 256)):
     """Differentiable render, 256x256x4 from seed 2: target (0.7, 60 deg, 1, 3),
     current (0.5, 50 deg, 0.8, 2.5), L2 loss.  FP32 adjoint per K (forward +
@@ -432,7 +467,8 @@ def run_ours(args):
             leg_s = {}
             for key, fn in (("geokerr_grid", geokerr_grid_leg), ("adjoint_256x256x4", adjoint_leg),
                             ("adjoint_1280x720x4", adjoint_headline_leg),
-                            ("batch_256_uneven", batch_leg), ("critical_2048x2048x16_a0998", critical_leg)):
+                            ("batch_256_uneven", batch_leg), ("critical_2048x2048x16_a0998", critical_leg),
+                            ("research_rkf78_1280x720x1", research_leg)):
                 t_leg = time.perf_counter()
                 out[key] = fn()
                 leg_s[key] = time.perf_counter() - t_leg

@@ -843,6 +843,7 @@ int np_render_host(const np_scene_t* scene, int precision, float* h_rgb, float* 
     if (!scene || !h_rgb) return fail(NP_ERR_INVALID, "NULL argument");
     int rc = np_scene_validate(scene);
     if (rc != NP_OK) return rc;
+    if (int e = check_path(*scene, precision)) return e;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) return fail(NP_ERR_NO_DEVICE, "No CUDA devices found.");
     size_t npix = (size_t)scene->width * scene->height;

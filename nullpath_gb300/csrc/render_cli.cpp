@@ -14,8 +14,12 @@
 //   --escape-r R        escape radius
 //   --max-steps N       step cap per ray
 //   --precision fp64|mixed
-//   --integrator rk4|adaptive, --rtol X, --atol X
-//   --crossing linear|hermite
+//   --integrator rk4|adaptive|rkf78, --rtol X, --atol X
+//   --crossing linear|hermite|root
+//   --inv-gate X        invariant gate of the rkf78 integrator (|H|, Carter Q)
+//   --mode research     FP64, rkf78 at rtol 1e-12 / atol 1e-14, root-found
+//                       crossings, invariant gate 1e-12, ZAMO camera and
+//                       invariant tracking (explicit flags take precedence)
 //   --islands N         FP64 island mask of the mixed path (NP_ISLAND_*)
 //   --benchmark         the 1280x720, a=0.9 benchmark scene (other flags may follow)
 //   --out-raw FILE      float32 mean RGB [3][H][W] and first-crossing radius [H][W]
@@ -52,7 +56,8 @@ struct Cli {
     const char* out_raw = nullptr;
     const char* json = nullptr;
     bool rin_isco = false;
-    bool integrator_set = false;
+    bool integrator_set = false, rtol_set = false, atol_set = false, crossing_set = false, gate_set = false;
+    bool precision_set = false;
 };
 
 std::string lower(const char* s) {
@@ -147,14 +152,23 @@ void parse(int argc, char** argv, Cli& c) {
         else if (a == "--emissivity-q") f(s.emissivity_q);
         else if (a == "--escape-r") f(s.escape_r);
         else if (a == "--max-steps") n(s.max_steps);
-        else if (a == "--precision" && has()) c.precision = lower(argv[++i]) == "mixed" ? NP_PREC_MIXED : NP_PREC_FP64;
+        else if (a == "--precision" && has()) {
+            c.precision = lower(argv[++i]) == "mixed" ? NP_PREC_MIXED : NP_PREC_FP64;
+            c.precision_set = true;
+        }
         else if (a == "--integrator" && has()) {
-            s.integrator = lower(argv[++i]) == "adaptive" ? NP_INTEG_ADAPTIVE : NP_INTEG_RK4;
+            std::string v = lower(argv[++i]);
+            s.integrator = v == "adaptive" ? NP_INTEG_ADAPTIVE : v == "rkf78" ? NP_INTEG_RKF78 : NP_INTEG_RK4;
             c.integrator_set = true;
         }
-        else if (a == "--rtol") f(s.rtol);
-        else if (a == "--atol") f(s.atol);
-        else if (a == "--crossing" && has()) s.crossing = lower(argv[++i]) == "hermite" ? NP_CROSS_HERMITE : NP_CROSS_LINEAR;
+        else if (a == "--rtol") { f(s.rtol); c.rtol_set = true; }
+        else if (a == "--atol") { f(s.atol); c.atol_set = true; }
+        else if (a == "--inv-gate") { f(s.inv_gate); c.gate_set = true; }
+        else if (a == "--crossing" && has()) {
+            std::string v = lower(argv[++i]);
+            s.crossing = v == "hermite" ? NP_CROSS_HERMITE : v == "root" ? NP_CROSS_ROOT : NP_CROSS_LINEAR;
+            c.crossing_set = true;
+        }
         else if (a == "--islands") n(s.islands);
         else if (a == "--out-raw") str(c.out_raw);
         else if (a == "--json") str(c.json);
@@ -187,6 +201,19 @@ int main(int argc, char** argv) {
         if (!c.integrator_set) s.integrator = NP_INTEG_ADAPTIVE;
         s.camera = NP_CAMERA_ZAMO;
         s.check_invariants = 1;
+    } else if (mode == "research") {
+        if (!c.precision_set) c.precision = NP_PREC_FP64;
+        if (!c.integrator_set) s.integrator = NP_INTEG_RKF78;
+        if (!c.rtol_set) s.rtol = 1e-12;
+        if (!c.atol_set) s.atol = 1e-14;
+        if (!c.crossing_set) s.crossing = NP_CROSS_ROOT;
+        if (!c.gate_set) s.inv_gate = 1e-12;
+        s.camera = NP_CAMERA_ZAMO;
+        s.check_invariants = 1;
+    }
+    if (c.precision == NP_PREC_MIXED && (s.integrator == NP_INTEG_RKF78 || s.crossing == NP_CROSS_ROOT)) {
+        std::fprintf(stderr, "The rkf78 integrator and root crossings need --precision fp64.\n");
+        return 1;
     }
     s.background = lower(c.bg) == "point" ? NP_BG_POINT : NP_BG_GRADIENT;
     if (c.rin_isco) s.disk_rin = np_isco_radius(s.mass, s.spin);
@@ -268,12 +295,18 @@ int main(int argc, char** argv) {
             std::fprintf(f,
                          "{\"width\": %d, \"height\": %d, \"spp\": %d, \"frames\": %d, \"passes\": %d, \"mass\": %.17g, "
                          "\"spin\": %.17g, \"r_cam\": %.17g, \"theta_deg\": %.17g, \"fov_y_deg\": %.17g, \"units\": \"%s\", "
-                         "\"precision\": \"%s\", \"integrator\": \"%s\", \"rays\": %llu, \"steps\": %llu, "
+                         "\"precision\": \"%s\", \"integrator\": \"%s\", \"integrator_order\": %d, "
+                         "\"mode\": \"%s\", \"crossing\": \"%s\", \"rtol\": %.17g, \"atol\": %.17g, "
+                         "\"inv_gate\": %.17g, \"camera\": \"%s\", \"seed\": %u, \"jitter\": %d, "
+                         "\"rays\": %llu, \"steps\": %llu, "
                          "\"kernel_ms\": %.6f, \"rays_per_s\": %.6g}\n",
                          s.width, s.height, np_frame_spp(fr), c.frames, passes_done, s.mass, s.spin, s.r_cam, s.theta_deg,
                          s.fov_y_deg, s.units == NP_UNITS_M ? "M" : "Rs", c.precision == NP_PREC_MIXED ? "mixed" : "fp64",
-                         s.integrator == NP_INTEG_ADAPTIVE ? "adaptive" : "rk4", rays, steps, kernel_ms,
-                         kernel_ms > 0 ? rays / (kernel_ms * 1e-3) : 0.0);
+                         s.integrator == NP_INTEG_ADAPTIVE ? "adaptive" : s.integrator == NP_INTEG_RKF78 ? "rkf78" : "rk4",
+                         s.integrator == NP_INTEG_RKF78 ? 8 : 4, mode.c_str(),
+                         s.crossing == NP_CROSS_ROOT ? "root" : s.crossing == NP_CROSS_HERMITE ? "hermite" : "linear",
+                         s.rtol, s.atol, s.inv_gate, s.camera == NP_CAMERA_ZAMO ? "zamo" : "static", s.seed, s.jitter,
+                         rays, steps, kernel_ms, kernel_ms > 0 ? rays / (kernel_ms * 1e-3) : 0.0);
             std::fclose(f);
         }
     }

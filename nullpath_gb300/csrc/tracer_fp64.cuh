@@ -235,9 +235,12 @@ __device__ __forceinline__ double rkf78_ref(const St8& y, double M, double a, do
     return e;
 }
 
-// Hamiltonian H = g^{mu nu} p_mu p_nu / 2 and Carter's constant
-// Q = p_theta^2 + cos^2 theta (L^2 / sin^2 theta - a^2 E^2) of a state.
-__device__ __forceinline__ void h_and_q(const St8& y, double M, double a, double& H, double& Q) {
+// Hamiltonian H = g^{mu nu} p_mu p_nu / 2, its scale Hs = the same sum of
+// absolute terms (so |H| / Hs is the relative cancellation error, which
+// stays meaningful near the horizon where the terms grow like 1/Delta),
+// and Carter's constant Q = p_theta^2 + cos^2 theta (L^2 / sin^2 theta -
+// a^2 E^2) of a state.
+__device__ __forceinline__ void h_and_q(const St8& y, double M, double a, double& H, double& Hs, double& Q) {
     double sn, c;
     sincos(y.th, &sn, &c);
     double r2 = y.r * y.r, a2 = a * a;
@@ -248,8 +251,10 @@ __device__ __forceinline__ void h_and_q(const St8& y, double M, double a, double
     double grr = fmax(kEps, Del) / Sig, ghh = 1.0 / Sig;
     double gtt = -A / fmax(kEps, Sig * Del), gtp = -2.0 * M * a * y.r / fmax(kEps, Sig * Del);
     double gpp = (Del - a2 * s2) / fmax(kEps, Sig * Del * s2);
-    H = 0.5 * (gtt * y.pt * y.pt + 2.0 * gtp * y.pt * y.pph + gpp * y.pph * y.pph + grr * y.pr * y.pr
-               + ghh * y.pth * y.pth);
+    double t0 = gtt * y.pt * y.pt, t1 = 2.0 * gtp * y.pt * y.pph, t2 = gpp * y.pph * y.pph;
+    double t3 = grr * y.pr * y.pr, t4 = ghh * y.pth * y.pth;
+    H = 0.5 * (t0 + t1 + t2 + t3 + t4);
+    Hs = 0.5 * (fabs(t0) + fabs(t1) + fabs(t2) + fabs(t3) + fabs(t4));
     Q = y.pth * y.pth + c * c * (y.pph * y.pph / s2 - a2 * y.pt * y.pt);
 }
 
@@ -274,7 +279,7 @@ __device__ __forceinline__ void invariants_ref(const SceneDev& s, const St8& y, 
 // Per-lane ray of the FP64 tracer.  With REC the first four equatorial
 // crossings (any radius) are recorded for the per-ray report.  q0 and qs
 // are Carter's constant at the camera and its drift scale max(|Q0|,
-// (E M)^2); dH and dQ the largest |H| / E^2 and |Q - Q0| / qs seen (drift
+// (E M)^2); dH and dQ the largest |H| / Hs and |Q - Q0| / qs seen (drift
 // tracking only).
 template <bool REC>
 struct RayFP64 {
@@ -294,11 +299,11 @@ __device__ __forceinline__ void fp64_init(const SceneDev& s, const Momentum& m, 
     R.h_adapt = 0.0;
     R.first_r = 0.0;
     R.pt0 = m.pt; R.pph0 = m.pph;
-    double H0, Q0;
-    h_and_q(R.y, s.M, s.a, H0, Q0);
+    double H0, Hs0, Q0;
+    h_and_q(R.y, s.M, s.a, H0, Hs0, Q0);
     R.q0 = Q0;
     R.qs = fmax(fabs(Q0), m.pt * m.pt * s.M * s.M);
-    R.dH = fabs(H0) / (m.pt * m.pt);
+    R.dH = fabs(H0) / fmax(Hs0, 1e-300);
     R.dQ = 0.0;
     R.disk[0] = R.disk[1] = R.disk[2] = 0.0f;
     R.step = 0; R.orders = 0; R.crossings = 0; R.status = 2;
@@ -377,9 +382,9 @@ __device__ __forceinline__ bool fp64_advance(const SceneDev& s, RayFP64<REC>& R,
             bool acc = alive && e <= 1.0;
             bool gated = false;
             if (acc && s.inv_gate > 0.0 && h > hmin * 1.01) {
-                double H, Q;
-                h_and_q(out, M, a, H, Q);
-                gated = fabs(H) > s.inv_gate * R.pt0 * R.pt0 || fabs(Q - R.q0) > s.inv_gate * R.qs;
+                double H, Hs, Q;
+                h_and_q(out, M, a, H, Hs, Q);
+                gated = fabs(H) > s.inv_gate * Hs || fabs(Q - R.q0) > s.inv_gate * R.qs;
                 acc = !gated;
             }
             if (acc) {
@@ -425,9 +430,9 @@ __device__ __forceinline__ bool fp64_advance(const SceneDev& s, RayFP64<REC>& R,
     R.step++;
     if (!ok) { R.status = 1; return true; }
     if (TRK) {
-        double H, Q;
-        h_and_q(R.y, M, a, H, Q);
-        R.dH = fmax(R.dH, fabs(H) / (R.pt0 * R.pt0));
+        double H, Hs, Q;
+        h_and_q(R.y, M, a, H, Hs, Q);
+        R.dH = fmax(R.dH, fabs(H) / fmax(Hs, 1e-300));
         R.dQ = fmax(R.dQ, fabs(Q - R.q0) / R.qs);
     }
     R.min_r = fmin(R.min_r, R.y.r);

@@ -287,12 +287,14 @@ static double rkf78(const State& y, double M, double a, double h, double rtol, d
     return e;
 }
 
-// Hamiltonian and Carter's constant of a state.
-static void h_and_q(const State& y, double M, double a, double& H, double& Q) {
+// Hamiltonian, the sum of its absolute terms, and Carter's constant of a state.
+static void h_and_q(const State& y, double M, double a, double& H, double& Hs, double& Q) {
     double g[5];
     metric_inv(M, a, y.r, y.th, g);
-    H = 0.5 * (g[0] * y.pt * y.pt + 2.0 * g[1] * y.pt * y.pph + g[2] * y.pph * y.pph + g[3] * y.pr * y.pr
-               + g[4] * y.pth * y.pth);
+    const double t[5] = {g[0] * y.pt * y.pt, 2.0 * g[1] * y.pt * y.pph, g[2] * y.pph * y.pph, g[3] * y.pr * y.pr,
+                         g[4] * y.pth * y.pth};
+    H = 0.5 * (t[0] + t[1] + t[2] + t[3] + t[4]);
+    Hs = 0.5 * (std::fabs(t[0]) + std::fabs(t[1]) + std::fabs(t[2]) + std::fabs(t[3]) + std::fabs(t[4]));
     double c = std::cos(y.th), sn = std::sin(y.th);
     double s2 = std::fmax(kEps, sn * sn);
     Q = y.pth * y.pth + c * c * (y.pph * y.pph / s2 - a * a * y.pt * y.pt);
@@ -631,7 +633,7 @@ struct RayOut {
     long steps = 0;
     State last{};
     double pt0 = 0.0, pph0 = 0.0;
-    double dH = 0.0, dQ = 0.0;    // max |H| / E^2, max |Q - Q0| / max(|Q0|, (E M)^2)
+    double dH = 0.0, dQ = 0.0;    // max |H| / Hs, max |Q - Q0| / max(|Q0|, (E M)^2)
     float inv[3] = {0, 0, 0};
 };
 
@@ -707,10 +709,10 @@ static void trace(const Frame& f, const Dir& d, bool track_inv, RayOut& o, bool 
     State y = f.zamo ? camera_zamo(f.M, f.a, f.r_cam, f.th_cam, f.ph_cam, d.nr, d.nth, d.nph)
                      : camera_static(f.M, f.a, f.r_cam, f.th_cam, f.ph_cam, d.nr, d.nth, d.nph);
     o.pt0 = y.pt; o.pph0 = y.pph;
-    double H0, Q0;
-    h_and_q(y, f.M, f.a, H0, Q0);
+    double H0, Hs0, Q0;
+    h_and_q(y, f.M, f.a, H0, Hs0, Q0);
     const double E2 = y.pt * y.pt, qs = std::fmax(std::fabs(Q0), E2 * f.M * f.M);
-    o.dH = std::fabs(H0) / E2;
+    o.dH = std::fabs(H0) / std::fmax(Hs0, 1e-300);
     o.min_r = y.r;
     State prev = y;
     double h_adapt = 0.0;
@@ -736,9 +738,9 @@ static void trace(const Frame& f, const Dir& d, bool track_inv, RayOut& o, bool 
                 bool alive = alive_adaptive(out, f.M, f.a) && e == e;
                 bool acc = alive && e <= 1.0, gated = false;
                 if (acc && f.inv_gate > 0.0 && h > hmin * 1.01) {
-                    double H, Q;
-                    h_and_q(out, f.M, f.a, H, Q);
-                    gated = std::fabs(H) > f.inv_gate * E2 || std::fabs(Q - Q0) > f.inv_gate * qs;
+                    double H, Hs, Q;
+                    h_and_q(out, f.M, f.a, H, Hs, Q);
+                    gated = std::fabs(H) > f.inv_gate * Hs || std::fabs(Q - Q0) > f.inv_gate * qs;
                     acc = !gated;
                 }
                 if (acc) {
@@ -784,9 +786,9 @@ static void trace(const Frame& f, const Dir& d, bool track_inv, RayOut& o, bool 
         o.steps++;
         if (!ok) { o.captured = true; o.status = 1; break; }
         if (track_drift) {
-            double H, Q;
-            h_and_q(y, f.M, f.a, H, Q);
-            o.dH = std::fmax(o.dH, std::fabs(H) / E2);
+            double H, Hs, Q;
+            h_and_q(y, f.M, f.a, H, Hs, Q);
+            o.dH = std::fmax(o.dH, std::fabs(H) / std::fmax(Hs, 1e-300));
             o.dQ = std::fmax(o.dQ, std::fabs(Q - Q0) / qs);
         }
         o.min_r = std::fmin(o.min_r, y.r);

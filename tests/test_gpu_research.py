@@ -1,0 +1,93 @@
+"""Research mode on the GPU (FP64 path, Fehlberg 7(8) with root-found
+crossings and invariant gating) against the CPU oracle, against the
+Mino-time GEOKERR crossings, and through the CLI's --mode research."""
+import json
+import os
+import subprocess
+
+import numpy as np
+import pytest
+import torch
+
+import oracle
+import nullpath_gb300 as npx
+from nullpath_gb300 import accuracy
+from nullpath_gb300._abi import benchmark_scene, NP_INTEG_RKF78, NP_CROSS_ROOT
+
+pytestmark = pytest.mark.gpu
+
+RESEARCH = dict(integrator=NP_INTEG_RKF78, crossing=NP_CROSS_ROOT, rtol=1e-12, atol=1e-14, inv_gate=1e-12)
+
+
+def _rays(n, w=64, h=36, seed=3):
+    rng = np.random.default_rng(seed)
+    return rng.uniform(0, w, n), rng.uniform(0, h, n)
+
+
+def test_research_rays_match_oracle(cuda):
+    sc = benchmark_scene(width=64, height=36, spp=1).replace(**RESEARCH)
+    px, py = _rays(400)
+    g = npx.trace_rays(sc, px, py, "fp64")
+    torch.cuda.synchronize()
+    o = oracle.trace_rays(sc, px, py)
+    gs, os_ = g["status"].cpu().numpy(), o["status"]
+    assert (gs == os_).mean() > 0.99
+    same = gs == os_
+    gc, oc = g["cross"].cpu().numpy()[same], o["cross"][same]
+    n = (gs[same] >> 4).clip(0, 4)
+    mask = np.arange(4)[None, :] < n[:, None]
+    for j in (0, 1):
+        a, b = gc[:, :, j][mask], oc[:, :, j][mask]
+        assert a.size > 100
+        assert np.max(np.abs(a - b) / np.maximum(np.abs(b), 1.0)) < 1e-10, j
+
+
+def test_research_crossings_match_geokerr(cuda):
+    """Order-1 and order-2 crossing radius and azimuth against the Mino-time
+    solver on 4000 rays of the 1280x720 benchmark camera."""
+    sc = benchmark_scene().replace(**RESEARCH)
+    res = accuracy.crossing_error(sc, n=4000, precision="fp64", seed=5, orders=2)
+    print(json.dumps(res))
+    o1, o2 = res["order1"], res["order2"]
+    assert o1["crossings"] > 1000 and o1["r_err_max"] < 1e-8 and o1["phi_err_max"] < 1e-8
+    assert o2["r_err_p99"] < 1e-8 and o2["phi_err_p99"] < 1e-8
+    assert o1["I_relerr_max"] < 1e-8
+
+
+def test_research_drift_matches_oracle(cuda):
+    sc = benchmark_scene(width=64, height=36, spp=1).replace(**RESEARCH)
+    px, py = _rays(300, seed=4)
+    d, st = npx.trace_invariants(sc, px, py)
+    torch.cuda.synchronize()
+    d, st = d.cpu().numpy(), st.cpu().numpy()
+    do, so = oracle.trace_invariants(sc, px, py)
+    assert d[:, 0].max() < 1e-10 and d[:, 1].max() < 1e-10
+    assert np.quantile(d[:, 1], 0.99) < 1e-11
+    assert (np.abs(st - so) <= 2).mean() > 0.95
+    # the same rays under fixed-step RK4 lose the constraint near the horizon
+    d4, _ = npx.trace_invariants(benchmark_scene(width=64, height=36, spp=1), px, py)
+    assert d4.cpu().numpy()[:, 0].max() > 1e-3
+
+
+def test_research_render_matches_oracle(cuda):
+    sc = benchmark_scene(width=96, height=54, spp=1).replace(**RESEARCH)
+    rgb, rc = npx.render(sc, "fp64")
+    torch.cuda.synchronize()
+    ref_rgb, ref_rc = oracle.render(sc)
+    got = rgb.cpu().numpy()
+    bad = np.abs(got - ref_rgb) > 1e-4 * (1.0 + np.abs(ref_rgb))
+    assert bad.any(axis=0).mean() < 0.003, bad.any(axis=0).mean()
+
+
+def test_cli_research_mode_sidecar(cuda, tmp_path):
+    cli = os.path.join(os.path.dirname(npx.lib_path()), "render")
+    side = tmp_path / "side.json"
+    p = subprocess.run([cli, "--benchmark", "--mode", "research", "--w", "64", "--h", "36", "--samples", "1",
+                        "--out", str(tmp_path / "r.ppm"), "--json", str(side)],
+                       capture_output=True, text=True, timeout=300)
+    assert p.returncode == 0, p.stderr
+    d = json.loads(side.read_text())
+    assert (d["precision"], d["integrator"], d["integrator_order"], d["crossing"], d["camera"]) == \
+        ("fp64", "rkf78", 8, "root", "zamo")
+    assert d["rtol"] == 1e-12 and d["atol"] == 1e-14 and d["inv_gate"] == 1e-12 and d["mode"] == "research"
+    assert d["rays"] == 64 * 36 and d["steps"] > 0
