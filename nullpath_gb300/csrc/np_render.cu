@@ -54,6 +54,7 @@ namespace {
 
 constexpr int kBlock = 128;
 constexpr int kChunk = 64;
+constexpr int kStepsPerTurn = 2;   // FP32 steps per pass of the mixed tracer's scheduling loop
 
 // Tunables (set through np_tune; the autotuner searches them).
 struct Tuning {
@@ -477,9 +478,16 @@ render_mixed_kernel(const SceneDev s, const InitSoA soa, float* __restrict__ srg
                 n_steps++; n_f64++; n_evals += 5;
             }
         } else if (have && !R.pending) {
-            int r = s.integrator == NP_INTEG_ADAPTIVE ? mray_step32_adaptive(R, s, k) : mray_step32(R, s, k);
-            if (r != STEP_PARK) { n_steps++; n_evals += s.integrator == NP_INTEG_ADAPTIVE ? 11 : 4; }
-            done = r == STEP_DONE;
+            // kStepsPerTurn FP32 steps per pass of the scheduling loop: the
+            // ballots and queue checks above are paid once per pass; a lane
+            // that ends or parks early idles for the rest of the pass
+#pragma unroll 1
+            for (int j = 0; j < kStepsPerTurn; ++j) {
+                int r = s.integrator == NP_INTEG_ADAPTIVE ? mray_step32_adaptive(R, s, k) : mray_step32(R, s, k);
+                if (r != STEP_PARK) { n_steps++; n_evals += s.integrator == NP_INTEG_ADAPTIVE ? 11 : 4; }
+                done = r == STEP_DONE;
+                if (r != STEP_CONT) break;
+            }
         }
         if (done) {
             float col[3];
@@ -1183,9 +1191,13 @@ __global__ void __launch_bounds__(BLOCK, MINB) batch_mixed_kernel(const BatchDev
                 n_steps++; n_f64++; n_evals += 5;
             }
         } else if (have && !R.pending) {
-            int r = S.integrator == NP_INTEG_ADAPTIVE ? mray_step32_adaptive(R, S, k) : mray_step32(R, S, k);
-            if (r != STEP_PARK) { n_steps++; n_evals += S.integrator == NP_INTEG_ADAPTIVE ? 11 : 4; }
-            done = r == STEP_DONE;
+#pragma unroll 1
+            for (int j = 0; j < kStepsPerTurn; ++j) {
+                int r = S.integrator == NP_INTEG_ADAPTIVE ? mray_step32_adaptive(R, S, k) : mray_step32(R, S, k);
+                if (r != STEP_PARK) { n_steps++; n_evals += S.integrator == NP_INTEG_ADAPTIVE ? 11 : 4; }
+                done = r == STEP_DONE;
+                if (r != STEP_CONT) break;
+            }
         }
         if (done) {
             float col[3];

@@ -67,11 +67,39 @@ struct SpaceK {
 
 struct F5 { float r, th, pr, pth, ph; };
 
+// sin and cos of theta on [0, pi] (and a little beyond) in FP32 without
+// general range reduction.  theta is folded to |z| <= pi/4 with two-part
+// constants, z = theta, theta - pi/2 or pi - theta (exact differences where
+// they matter), so both results keep full relative accuracy near the poles
+// and near the equator; then the Taylor series of sin through z^11 and of
+// cos through z^10 (truncation below 2e-10 for |z| <= pi/4), in Horner form.
+__device__ __forceinline__ void sincos_polar(float th, float& sn, float& cs) {
+    const float PI_HI = 3.14159274101257324f, PI_LO = -8.74227766e-8f;       // fl(pi), pi - fl(pi)
+    const float PI2_HI = 1.57079637050628662f, PI2_LO = -4.37113883e-8f;    // fl(pi/2), pi/2 - fl(pi/2)
+    const bool mid = th >= 0.785398163f, top = th > 2.35619449f;
+    float z = top ? __fadd_rn(__fsub_rn(PI_HI, th), PI_LO) : (mid ? __fsub_rn(__fsub_rn(th, PI2_HI), PI2_LO) : th);
+    float z2 = z * z;
+    float ps = fmaf(z2, -1.0f / 39916800.0f, 1.0f / 362880.0f);
+    ps = fmaf(z2, ps, -1.0f / 5040.0f);
+    ps = fmaf(z2, ps, 1.0f / 120.0f);
+    ps = fmaf(z2, ps, -1.0f / 6.0f);
+    ps = z * fmaf(z2, ps, 1.0f);
+    float pc = fmaf(z2, -1.0f / 3628800.0f, 1.0f / 40320.0f);
+    pc = fmaf(z2, pc, -1.0f / 720.0f);
+    pc = fmaf(z2, pc, 1.0f / 24.0f);
+    pc = fmaf(z2, pc, -0.5f);
+    pc = fmaf(z2, pc, 1.0f);
+    // [0, pi/4): (sin z, cos z); [pi/4, 3pi/4]: (cos z, -sin z); (3pi/4, ...]: (sin z, -cos z)
+    const bool mid_only = mid && !top;
+    sn = mid_only ? pc : ps;
+    cs = mid_only ? -ps : (top ? -pc : pc);
+}
+
 // Carter-form Hamilton equations in FP32.
 template <bool PHI>
 __device__ __forceinline__ F5 rhs_f(float r, float th, float pr, float pth, const RayK& c, const SpaceK& k) {
     float sn, cs;
-    sincosf(th, &sn, &cs);
+    sincos_polar(th, sn, cs);
     float s2 = fmaxf(sn * sn, 1e-30f);
     float is2 = rcp_approx(s2);
     float r2 = r * r;
