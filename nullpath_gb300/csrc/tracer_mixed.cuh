@@ -73,11 +73,28 @@ struct F5 { float r, th, pr, pth, ph; };
 // they matter), so both results keep full relative accuracy near the poles
 // and near the equator; then the Taylor series of sin through z^11 and of
 // cos through z^10 (truncation below 2e-10 for |z| <= pi/4), in Horner form.
-__device__ __forceinline__ void sincos_polar(float th, float& sn, float& cs) {
+// Host builds (the accuracy probe) compile this with FP contraction off, so
+// the plain operators round like the device intrinsics.
+__host__ __device__ __forceinline__ float add_rn(float a, float b) {
+#ifdef __CUDA_ARCH__
+    return __fadd_rn(a, b);
+#else
+    return a + b;
+#endif
+}
+__host__ __device__ __forceinline__ float sub_rn(float a, float b) {
+#ifdef __CUDA_ARCH__
+    return __fsub_rn(a, b);
+#else
+    return a - b;
+#endif
+}
+
+__host__ __device__ __forceinline__ void sincos_polar(float th, float& sn, float& cs) {
     const float PI_HI = 3.14159274101257324f, PI_LO = -8.74227766e-8f;       // fl(pi), pi - fl(pi)
     const float PI2_HI = 1.57079637050628662f, PI2_LO = -4.37113883e-8f;    // fl(pi/2), pi/2 - fl(pi/2)
     const bool mid = th >= 0.785398163f, top = th > 2.35619449f;
-    float z = top ? __fadd_rn(__fsub_rn(PI_HI, th), PI_LO) : (mid ? __fsub_rn(__fsub_rn(th, PI2_HI), PI2_LO) : th);
+    float z = top ? add_rn(sub_rn(PI_HI, th), PI_LO) : (mid ? sub_rn(sub_rn(th, PI2_HI), PI2_LO) : th);
     float z2 = z * z;
     float ps = fmaf(z2, -1.0f / 39916800.0f, 1.0f / 362880.0f);
     ps = fmaf(z2, ps, -1.0f / 5040.0f);
