@@ -168,10 +168,10 @@ def test_mixed_adaptive_matches_oracle(cuda):
     # scene.  The mixed path in addition measures the error on its compensated
     # increments with an FP32 rounding floor, so it accepts other steps still.
     # Colours within 1e-3 relative on >= 95% of pixels, crossing radius p99
-    # within 3e-4 M for both paths.
+    # within 4e-4 M (two such truncation errors) for both paths.
     for prec in ("fp64", "mixed"):
         rgb, rc = _render_np(sc, prec)
-        _compare(rgb, rc, ref_rgb, ref_rc, 1e-3, 3e-4, 0.95)
+        _compare(rgb, rc, ref_rgb, ref_rc, 1e-3, 4e-4, 0.95)
 
 
 def test_critical_sampling_matches_oracle(cuda):
