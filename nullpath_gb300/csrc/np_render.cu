@@ -55,6 +55,11 @@ namespace {
 constexpr int kBlock = 128;
 constexpr int kChunk = 64;
 constexpr int kStepsPerTurn = 2;   // FP32 steps per pass of the mixed tracer's scheduling loop
+// Lanes with a pending root-found crossing that trigger the warp's search
+// (FP64 tracer).  A search costs the warp about four single steps and a
+// lane crosses the equator about once in 200 attempts; six balances the
+// stall of the other lanes against the wait of the pending ones.
+constexpr int kCrossBatch = 6;
 
 // Tunables (set through np_tune; the autotuner searches them).
 struct Tuning {
@@ -317,18 +322,25 @@ render_fp64_kernel(const SceneDev s, float* __restrict__ srgb, float* __restrict
             }
         }
         if (!__any_sync(FULL, have)) break;
-        if (have) {
-            bool done = fp64_advance<MODE, false>(s, R, inv3, n_evals);
+        // Root-found crossings wait until kCrossBatch lanes of the warp have
+        // one (or no lane can step) and are then found together.
+        unsigned pend = __ballot_sync(FULL, have && R.xpend);
+        unsigned act = __ballot_sync(FULL, have && !R.xpend);
+        bool done = false;
+        if (pend && ((int)__popc(pend) >= kCrossBatch || !act)) {
+            if (have && R.xpend) done = fp64_resolve<MODE>(s, R, inv3, n_evals);
+        } else if (have && !R.xpend) {
+            done = fp64_advance<MODE, false, true>(s, R, inv3, n_evals);
             n_steps++;
-            if (done) {
-                bool captured = R.status == 1;
-                if (s.check_inv && inv3 && !captured && !(R.orders > 0 && s.disk_on))
-                    invariants_ref(s, R.y, R.pt0, R.pph0, inv3);
-                float col[3];
-                sample_colour(s, captured, R.orders, R.disk, (float)R.min_r, dir.cam_y, col);
-                write_sample(s, srgb, rcross, p, sl, col, R.first_r);
-                have = false;
-            }
+        }
+        if (done) {
+            bool captured = R.status == 1;
+            if (s.check_inv && inv3 && !captured && !(R.orders > 0 && s.disk_on))
+                invariants_ref(s, R.y, R.pt0, R.pph0, inv3);
+            float col[3];
+            sample_colour(s, captured, R.orders, R.disk, (float)R.min_r, dir.cam_y, col);
+            write_sample(s, srgb, rcross, p, sl, col, R.first_r);
+            have = false;
         }
     }
     flush_counters(ctr, n_rays, n_steps, list ? n_steps : 0, n_evals);

@@ -286,9 +286,11 @@ struct RayFP64 {
     St8 y, prev;
     double min_r, h_adapt, first_r, pt0, pph0;
     double q0, qs, dH, dQ;
+    double x_h, x_dp, x_alpha;             // pending root-found crossing: step size, start offset, linear guess
     double xr[REC ? 4 : 1], xphi[REC ? 4 : 1];
     float disk[3];
     int step, orders, crossings, status;   // status: 0 escaped, 1 captured, 2 step cap
+    bool xpend;                            // the last step crossed the equator; its root is not yet found
 };
 
 template <bool REC>
@@ -307,6 +309,7 @@ __device__ __forceinline__ void fp64_init(const SceneDev& s, const Momentum& m, 
     R.dQ = 0.0;
     R.disk[0] = R.disk[1] = R.disk[2] = 0.0f;
     R.step = 0; R.orders = 0; R.crossings = 0; R.status = 2;
+    R.xpend = false; R.x_h = R.x_dp = R.x_alpha = 0.0;
     if (REC) for (int k = 0; k < 4; ++k) { R.xr[k] = 0.0; R.xphi[k] = 0.0; }
 }
 
@@ -357,10 +360,44 @@ __device__ __forceinline__ St8 fp64_root_crossing(const SceneDev& s, const St8& 
     return z;
 }
 
+// Book-keeping of one equatorial crossing at radius rc, azimuth phc (alpha
+// the linear fraction of the step, for the conserved momenta there).
+template <bool REC>
+__device__ __forceinline__ void fp64_record_crossing(const SceneDev& s, RayFP64<REC>& R, double rc, double phc,
+                                                     double alpha, float* inv3) {
+    if (REC) {
+        if (R.crossings < 4) { R.xr[R.crossings] = rc; R.xphi[R.crossings] = phc; }
+    }
+    R.crossings++;
+    if (R.orders < s.max_orders && rc >= s.rin && rc <= s.rout) {
+        double pt = R.prev.pt + alpha * (R.y.pt - R.prev.pt);
+        double pph = R.prev.pph + alpha * (R.y.pph - R.prev.pph);
+        float g = (float)doppler_g(rc, pt, pph, s.M, s.a);
+        shade_disk((float)rc, g, s.qf, s.gain, R.disk);
+        if (R.orders == 0) R.first_r = rc;
+        R.orders++;
+        if (s.check_inv && inv3) {
+            St8 cr = R.y; cr.r = rc; cr.th = kPi * 0.5; cr.pt = pt; cr.pph = pph;
+            invariants_ref(s, cr, R.pt0, R.pph0, inv3);
+        }
+    }
+}
+
+// End of an accepted step: the next step starts here; escape test.
+template <bool REC>
+__device__ __forceinline__ bool fp64_step_tail(const SceneDev& s, RayFP64<REC>& R) {
+    R.prev = R.y;
+    if (R.y.r > s.r_far && R.step > 11) { R.status = 0; return true; }
+    return false;
+}
+
 // Advances the ray by one accepted step; returns true when it terminated.
 // `evals` counts right-hand-side evaluations; with TRK the drift of H and
-// Q is tracked over the accepted steps.
-template <int MODE, bool TRK, bool REC>
+// Q is tracked over the accepted steps.  With DEFER a root-found crossing
+// is left pending (R.xpend) for fp64_resolve, which a warp runs for all its
+// pending lanes at once: a lone lane's root search would otherwise hold the
+// other 31 lanes of its warp for about four single steps.
+template <int MODE, bool TRK, bool DEFER = false, bool REC>
 __device__ __forceinline__ bool fp64_advance(const SceneDev& s, RayFP64<REC>& R, float* inv3, unsigned long long& evals) {
     if (R.step >= s.max_steps) { R.status = 2; return true; }
     const double M = s.M, a = s.a, rp = s.r_plus;
@@ -444,6 +481,11 @@ __device__ __forceinline__ bool fp64_advance(const SceneDev& s, RayFP64<REC>& R,
         double alpha = fabs(dp) / (fabs(dp) + fabs(dc) + 1e-30);
         double rc, phc;
         if (s.crossing == NP_CROSS_ROOT && sc) {
+            if (DEFER) {
+                // the root is found later, together with other lanes' (fp64_resolve)
+                R.xpend = true; R.x_h = h_used; R.x_dp = dp; R.x_alpha = alpha;
+                return false;
+            }
             St8 z = fp64_root_crossing<MODE>(s, R.prev, h_used, dp, alpha, evals);
             rc = z.r;
             phc = z.ph;
@@ -458,26 +500,20 @@ __device__ __forceinline__ bool fp64_advance(const SceneDev& s, RayFP64<REC>& R,
             rc = R.prev.r + alpha * (R.y.r - R.prev.r);
             phc = R.prev.ph + alpha * (R.y.ph - R.prev.ph);
         }
-        if (REC) {
-            if (R.crossings < 4) { R.xr[R.crossings] = rc; R.xphi[R.crossings] = phc; }
-        }
-        R.crossings++;
-        if (R.orders < s.max_orders && rc >= s.rin && rc <= s.rout) {
-            double pt = R.prev.pt + alpha * (R.y.pt - R.prev.pt);
-            double pph = R.prev.pph + alpha * (R.y.pph - R.prev.pph);
-            float g = (float)doppler_g(rc, pt, pph, M, a);
-            shade_disk((float)rc, g, s.qf, s.gain, R.disk);
-            if (R.orders == 0) R.first_r = rc;
-            R.orders++;
-            if (s.check_inv && inv3) {
-                St8 cr = R.y; cr.r = rc; cr.th = hp; cr.pt = pt; cr.pph = pph;
-                invariants_ref(s, cr, R.pt0, R.pph0, inv3);
-            }
-        }
+        fp64_record_crossing(s, R, rc, phc, alpha, inv3);
     }
-    R.prev = R.y;
-    if (R.y.r > s.r_far && R.step > 11) { R.status = 0; return true; }
-    return false;
+    return fp64_step_tail(s, R);
+}
+
+// Root of a crossing deferred by fp64_advance<MODE, TRK, true>, then the
+// rest of that step; returns true when the ray terminated.
+template <int MODE, bool REC>
+__device__ __forceinline__ bool fp64_resolve(const SceneDev& s, RayFP64<REC>& R, float* inv3,
+                                             unsigned long long& evals) {
+    St8 z = fp64_root_crossing<MODE>(s, R.prev, R.x_h, R.x_dp, R.x_alpha, evals);
+    R.xpend = false;
+    fp64_record_crossing(s, R, z.r, z.ph, R.x_alpha, inv3);
+    return fp64_step_tail(s, R);
 }
 
 }  // namespace np
