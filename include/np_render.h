@@ -57,9 +57,10 @@ typedef enum np_camera { NP_CAMERA_STATIC = 0, NP_CAMERA_ZAMO = 1 } np_camera;
 /* NP_INTEG_RKF78: research mode (FP64 only).  Fehlberg's embedded 7(8)
  * pair, the 8th-order solution propagated, error control on (r, theta, phi,
  * p_r, p_theta, p_phi) with the scene's rtol/atol, and, when inv_gate > 0,
- * invariant-gated acceptance: a step is also rejected (h halved) when
- * |H| / E^2 or |Q - Q0| / max(|Q0|, (E M)^2) (Carter constant) exceeds
- * inv_gate after it. */
+ * invariant-gated acceptance: a step is also rejected (h halved) when its
+ * change of the Hamiltonian, relative to the sum of the Hamiltonian's
+ * absolute terms, or its change of Carter's constant Q, relative to
+ * max(|Q0|, (E M)^2), exceeds inv_gate. */
 typedef enum np_integrator { NP_INTEG_RK4 = 0, NP_INTEG_ADAPTIVE = 1, NP_INTEG_RKF78 = 2 } np_integrator;
 /* NP_CROSS_ROOT (FP64 only): theta = pi/2 located by bracketed root finding
  * on re-integrations of the crossing step from its start, so the crossing is
@@ -255,10 +256,14 @@ int np_render_device_noalloc(const np_scene_t* scene, int precision,
  *                         island step (1..32, default 8)
  *   NP_TUNE_MIN_BLOCKS    register cap of the tracer as resident 128-thread
  *                         blocks per SM (3, 4, 5, 6 or 8; default 4)
- *   NP_TUNE_CHUNK         ray indices a warp takes per atomic (default 64) */
+ *   NP_TUNE_CHUNK         ray indices a warp takes per atomic (default 64)
+ *   NP_TUNE_CROSS_BATCH   lanes of a warp with a pending root-found crossing
+ *                         (NP_CROSS_ROOT, FP64 path) that trigger the search
+ *                         of all of them (1-32, default 6; 1 = at once) */
 #define NP_TUNE_ISLAND_BATCH 1
 #define NP_TUNE_MIN_BLOCKS 2
 #define NP_TUNE_CHUNK 3
+#define NP_TUNE_CROSS_BATCH 4
 int np_tune(int param, int value);
 
 /* Measures the sustained FMA throughput of this GPU's SIMT pipes with a

@@ -55,6 +55,7 @@ struct SceneDev {
     double hmin, hmax;         // adaptive step bounds (hmax scales with r in units of M)
     double inv_gate;           // invariant gate of the embedded 7(8) integrator (0 = off)
     int island_batch;
+    int cross_batch;           // pending root-found crossings that trigger a warp's search (FP64 tracer)
     // NP_JITTER_CRITICAL: tangent-plane radius of the critical curve at
     // kCritN equally spaced position angles from -pi, and the band half-width
     float crit_rho[kCritN];

@@ -55,15 +55,15 @@ namespace {
 constexpr int kBlock = 128;
 constexpr int kChunk = 64;
 constexpr int kStepsPerTurn = 2;   // FP32 steps per pass of the mixed tracer's scheduling loop
-// Lanes with a pending root-found crossing that trigger the warp's search
-// (FP64 tracer).  A search costs the warp about four single steps and a
-// lane crosses the equator about once in 200 attempts; six balances the
-// stall of the other lanes against the wait of the pending ones.
-constexpr int kCrossBatch = 6;
 
 // Tunables (set through np_tune; the autotuner searches them).
 struct Tuning {
     int island_batch = 8;   // parked lanes that trigger a batched FP64 island step
+    // Lanes with a pending root-found crossing that trigger the warp's
+    // search (FP64 tracer).  A search costs the warp about four single
+    // steps; batching trades the stall of the other lanes against the wait
+    // of the pending ones.
+    int cross_batch = 6;
     int min_blocks = 4;     // register cap of the mixed tracer (blocks of 128 per SM)
     int chunk = 64;         // ray indices a warp takes from the global counter at once
 };
@@ -199,6 +199,7 @@ int prepare_scene(const np_scene_t& sc, SceneDev& d) {
         d.hmin_f = (float)d.hmin; d.hmax_f = (float)d.hmax;
         d.rtol_f = (float)d.rtol; d.atol_f = (float)d.atol;
         d.island_batch = g_tune.island_batch;
+        d.cross_batch = g_tune.cross_batch;
     }
     const double M = d.M, a = d.a, r = d.r_cam, th = d.th_cam;
     double gtt, gtp, gpp, grr, ghh;
@@ -322,16 +323,17 @@ render_fp64_kernel(const SceneDev s, float* __restrict__ srgb, float* __restrict
             }
         }
         if (!__any_sync(FULL, have)) break;
-        // Root-found crossings wait until kCrossBatch lanes of the warp have
+        // Root-found crossings wait until cross_batch lanes of the warp have
         // one (or no lane can step) and are then found together.
         unsigned pend = __ballot_sync(FULL, have && R.xpend);
         unsigned act = __ballot_sync(FULL, have && !R.xpend);
         bool done = false;
-        if (pend && ((int)__popc(pend) >= kCrossBatch || !act)) {
+        if (pend && ((int)__popc(pend) >= s.cross_batch || !act)) {
             if (have && R.xpend) done = fp64_resolve<MODE>(s, R, inv3, n_evals);
         } else if (have && !R.xpend) {
+            const int s0 = R.step;
             done = fp64_advance<MODE, false, true>(s, R, inv3, n_evals);
-            n_steps++;
+            n_steps += (unsigned long long)(R.step - s0);   // a rejected 7(8) attempt takes no step
         }
         if (done) {
             bool captured = R.status == 1;
@@ -922,6 +924,10 @@ int np_trace_invariants_device(const np_scene_t* scene, int n, const double* d_p
 
 int np_tune(int param, int value) {
     switch (param) {
+        case NP_TUNE_CROSS_BATCH:
+            if (value < 1 || value > 32) return fail(NP_ERR_INVALID, "crossing batch must be in [1, 32]");
+            g_tune.cross_batch = value;
+            return NP_OK;
         case NP_TUNE_ISLAND_BATCH:
             if (value < 1 || value > 32) return fail(NP_ERR_INVALID, "island batch must be in [1, 32]");
             g_tune.island_batch = value;

@@ -286,10 +286,12 @@ struct RayFP64 {
     St8 y, prev;
     double min_r, h_adapt, first_r, pt0, pph0;
     double q0, qs, dH, dQ;
+    double cur_H, cur_Q;                   // H and Q at the current state (the invariant gate's reference)
     double x_h, x_dp, x_alpha;             // pending root-found crossing: step size, start offset, linear guess
     double xr[REC ? 4 : 1], xphi[REC ? 4 : 1];
     float disk[3];
     int step, orders, crossings, status;   // status: 0 escaped, 1 captured, 2 step cap
+    int att;                               // rejected 7(8) attempts of the current step
     bool xpend;                            // the last step crossed the equator; its root is not yet found
 };
 
@@ -304,6 +306,8 @@ __device__ __forceinline__ void fp64_init(const SceneDev& s, const Momentum& m, 
     double H0, Hs0, Q0;
     h_and_q(R.y, s.M, s.a, H0, Hs0, Q0);
     R.q0 = Q0;
+    R.cur_H = H0; R.cur_Q = Q0;
+    R.att = 0;
     R.qs = fmax(fabs(Q0), m.pt * m.pt * s.M * s.M);
     R.dH = fabs(H0) / fmax(Hs0, 1e-300);
     R.dQ = 0.0;
@@ -406,36 +410,47 @@ __device__ __forceinline__ bool fp64_advance(const SceneDev& s, RayFP64<REC>& R,
     double h_used = 0.0;
     St8 k1;
     if (MODE == kFp64Rkf78) {
-        // same step bounds as step doubling; growth and shrink factors of an
-        // order-7 error estimate, 0.9 e^(-1/8) within [0.2, 4] ([0.1, 1) on rejection)
+        // One attempt per call: a rejected attempt shrinks h and returns, so
+        // a lane that needs many attempts (near the horizon) takes them over
+        // several passes of the warp's loop while the other lanes step.
+        // Same step bounds as step doubling; controller 0.9 e^(-1/8) within
+        // [0.2, 4] on acceptance, [0.1, 0.9] on rejection, halving on a
+        // horizon or gate rejection; at most 24 attempts per step, and a
+        // step that fails at the smallest h ends the ray as captured (the
+        // limits of step doubling).  The gate bounds this step's change of
+        // H and Q (not their drift since the camera, which no step size could
+        // undo) and is not applied at the smallest step.
         const double hmin = s.hmin, hmax = s.ref_units ? s.hmax : s.hmax * scale;
         double h = (R.h_adapt > 0.0) ? R.h_adapt : s.h_unit * scale;
         h = fmin(fmax(h, hmin), hmax);
-        for (int att = 0; att < 24; ++att) {
-            St8 out;
-            double e = rkf78_ref(R.y, M, a, rp, h, s.rtol, s.atol, out, k1);
-            evals += 13;
-            bool alive = out.r > rp + 1e-12 && out.th > 1e-9 && out.th < kPi - 1e-9 && e == e;
-            bool acc = alive && e <= 1.0;
-            bool gated = false;
-            if (acc && s.inv_gate > 0.0 && h > hmin * 1.01) {
-                double H, Hs, Q;
-                h_and_q(out, M, a, H, Hs, Q);
-                gated = fabs(H) > s.inv_gate * Hs || fabs(Q - R.q0) > s.inv_gate * R.qs;
+        St8 out;
+        double e = rkf78_ref(R.y, M, a, rp, h, s.rtol, s.atol, out, k1);
+        evals += 13;
+        bool alive = out.r > rp + 1e-12 && out.th > 1e-9 && out.th < kPi - 1e-9 && e == e;
+        bool acc = alive && e <= 1.0;
+        bool gated = false;
+        double H = 0.0, Hs = 0.0, Q = 0.0;
+        if (acc && s.inv_gate > 0.0) {
+            h_and_q(out, M, a, H, Hs, Q);
+            if (h > hmin * 1.01) {
+                gated = fabs(H - R.cur_H) > s.inv_gate * Hs || fabs(Q - R.cur_Q) > s.inv_gate * R.qs;
                 acc = !gated;
             }
-            if (acc) {
-                ok = true; h_used = h;
-                R.y = out;
-                double sc2 = fmin(fmax(1.0, out.r / (0.5 * s.Rs)), 100.0);
-                double grow = fmin(4.0, fmax(0.2, kSafety * pow(fmax(e, 1e-16), -0.125)));
-                R.h_adapt = fmin(fmax(h * grow, hmin), s.ref_units ? s.hmax : s.hmax * sc2);
-                break;
-            }
-            if (h <= hmin * 1.01) break;
-            double fac = (!alive || gated) ? 0.5 : fmin(0.9, fmax(0.1, kSafety * pow(e, -0.125)));
-            h = fmax(h * fac, hmin);
         }
+        if (!acc) {
+            R.att++;
+            if (h <= hmin * 1.01 || R.att >= 24) { R.step++; R.status = 1; return true; }
+            double fac = (!alive || gated) ? 0.5 : fmin(0.9, fmax(0.1, kSafety * pow(e, -0.125)));
+            R.h_adapt = fmax(h * fac, hmin);
+            return false;
+        }
+        R.att = 0;
+        ok = true; h_used = h;
+        R.y = out;
+        if (s.inv_gate > 0.0) { R.cur_H = H; R.cur_Q = Q; }
+        double sc2 = fmin(fmax(1.0, out.r / (0.5 * s.Rs)), 100.0);
+        double grow = fmin(4.0, fmax(0.2, kSafety * pow(fmax(e, 1e-16), -0.125)));
+        R.h_adapt = fmin(fmax(h * grow, hmin), s.ref_units ? s.hmax : s.hmax * sc2);
     } else if (s.integrator == NP_INTEG_ADAPTIVE) {
         // bounds: BH_RK_HMIN/HMAX (bh_common.h:245,253) for reference scenes;
         // hmax scaled like the fixed step law for scenes in units of M

@@ -712,6 +712,7 @@ static void trace(const Frame& f, const Dir& d, bool track_inv, RayOut& o, bool 
     double H0, Hs0, Q0;
     h_and_q(y, f.M, f.a, H0, Hs0, Q0);
     const double E2 = y.pt * y.pt, qs = std::fmax(std::fabs(Q0), E2 * f.M * f.M);
+    double cur_H = H0, cur_Q = Q0;   // the invariant gate's reference: H and Q at the current state
     o.dH = std::fabs(H0) / std::fmax(Hs0, 1e-300);
     o.min_r = y.r;
     State prev = y;
@@ -727,7 +728,8 @@ static void trace(const Frame& f, const Dir& d, bool track_inv, RayOut& o, bool 
         if (f.integrator == NP_INTEG_RKF78) {
             // step bounds of step doubling; factors 0.9 e^(-1/8) in [0.2, 4]
             // on acceptance, [0.1, 0.9] on rejection, halving on a gate or
-            // horizon rejection; the gate is not applied at the smallest step
+            // horizon rejection; the gate bounds the step's change of H and
+            // Q and is not applied at the smallest step
             const double hmin = f.ref_units ? kHMin : kHMin * f.M;
             const double hmax = f.ref_units ? kHMax : 10.0 * f.h_unit * scale;
             double h = (h_adapt > 0.0) ? h_adapt : f.h_unit * scale;
@@ -737,16 +739,19 @@ static void trace(const Frame& f, const Dir& d, bool track_inv, RayOut& o, bool 
                 double e = rkf78(y, f.M, f.a, h, f.rtol, f.atol, out);
                 bool alive = alive_adaptive(out, f.M, f.a) && e == e;
                 bool acc = alive && e <= 1.0, gated = false;
-                if (acc && f.inv_gate > 0.0 && h > hmin * 1.01) {
-                    double H, Hs, Q;
+                double H = 0.0, Hs = 0.0, Q = 0.0;
+                if (acc && f.inv_gate > 0.0) {
                     h_and_q(out, f.M, f.a, H, Hs, Q);
-                    gated = std::fabs(H) > f.inv_gate * Hs || std::fabs(Q - Q0) > f.inv_gate * qs;
-                    acc = !gated;
+                    if (h > hmin * 1.01) {
+                        gated = std::fabs(H - cur_H) > f.inv_gate * Hs || std::fabs(Q - cur_Q) > f.inv_gate * qs;
+                        acc = !gated;
+                    }
                 }
                 if (acc) {
                     ok = true; h_used = h;
                     rhs(y, f.M, f.a, k1);
                     y = out;
+                    if (f.inv_gate > 0.0) { cur_H = H; cur_Q = Q; }
                     double sc2 = std::fmin(std::fmax(1.0, y.r / (0.5 * f.Rs)), 100.0);
                     double grow = std::fmin(4.0, std::fmax(0.2, kSafety * std::pow(std::fmax(e, 1e-16), -0.125)));
                     h_adapt = std::fmin(std::fmax(h * grow, hmin), f.ref_units ? kHMax : 10.0 * f.h_unit * sc2);

@@ -113,17 +113,18 @@ def test_root_crossings_tighten_rk4(rays):
 
 def test_invariant_drift_and_gate(rays):
     """Research settings keep |H| / (sum of its terms) and |dQ| / Q-scale
-    at the 1e-11 level over every accepted step; at rtol 1e-10 the gate cuts
-    the Carter drift below what error control alone leaves."""
+    at the 1e-11 level over every accepted step.  At rtol 1e-10 a gate of
+    1e-12 on each step's change of H and Q cuts the Carter drift more than
+    tenfold for a few percent more steps."""
     px, py = rays
     d, steps = oracle.trace_invariants(_scene(**RESEARCH), px, py)
     assert d[:, 0].max() < 1e-10 and d[:, 1].max() < 1e-10
     assert np.quantile(d[:, 1], 0.99) < 1e-11
     loose = dict(RESEARCH, rtol=1e-10, atol=1e-12, inv_gate=0.0)
     d0, s0 = oracle.trace_invariants(_scene(**loose), px, py)
-    d1, s1 = oracle.trace_invariants(_scene(**dict(loose, inv_gate=1e-11)), px, py)
-    assert np.quantile(d1[:, 1], 0.99) < 0.5 * np.quantile(d0[:, 1], 0.99)
-    assert s1.mean() > s0.mean()       # gated steps are rejected and retaken smaller
+    d1, s1 = oracle.trace_invariants(_scene(**dict(loose, inv_gate=1e-12)), px, py)
+    assert np.quantile(d1[:, 1], 0.99) < 0.1 * np.quantile(d0[:, 1], 0.99)
+    assert s0.mean() < s1.mean() < 1.1 * s0.mean()     # gated steps are rejected and retaken smaller
     # the reference's fixed-step RK4 loses the constraint near the horizon
     d4, _ = oracle.trace_invariants(_scene(), px, py)
     assert d4[:, 0].max() > 1e-3
