@@ -259,7 +259,7 @@ int np_render_device_noalloc(const np_scene_t* scene, int precision,
  *   NP_TUNE_CHUNK         ray indices a warp takes per atomic (default 64)
  *   NP_TUNE_CROSS_BATCH   lanes of a warp with a pending root-found crossing
  *                         (NP_CROSS_ROOT, FP64 path) that trigger the search
- *                         of all of them (1-32, default 6; 1 = at once) */
+ *                         of all of them (1-32, default 12; 1 = at once) */
 #define NP_TUNE_ISLAND_BATCH 1
 #define NP_TUNE_MIN_BLOCKS 2
 #define NP_TUNE_CHUNK 3
