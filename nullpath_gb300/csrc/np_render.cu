@@ -54,7 +54,7 @@ namespace {
 
 constexpr int kBlock = 128;
 constexpr int kChunk = 64;
-constexpr int kStepsPerTurn = 2;   // FP32 steps per pass of the mixed tracer's scheduling loop
+constexpr int kStepsPerTurn = 4;   // FP32 steps per pass of the mixed tracer's scheduling loop
 
 // Tunables (set through np_tune; the autotuner searches them).
 struct Tuning {
