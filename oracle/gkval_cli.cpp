@@ -24,7 +24,9 @@
  * gkval_adapters.c:666-695); "oracle" runs the restatement against itself
  * (a pipeline self-check).  --plant moves one port sample of one field by a
  * number of ULPs after the port solver returns, so tests can check that a
- * planted difference is found where it was put.
+ * planted difference is found where it was put.  Like the reference's CUDA
+ * adapter, the GPU port takes no t0, so cases with t0 != 0 differ in t by
+ * t0 (a cases file normally leaves t0 at 0).
  *
  * Per case and field the S samples are compared in segments of 1024; phi is
  * unwrapped per segment; the first rejected sample ends the case and writes
