@@ -50,6 +50,33 @@ __device__ __forceinline__ void hl_add(HiLo& v, float d) {
     v.lo = __fsub_rn(e, __fsub_rn(v.hi, s));
 }
 
+// Packed FP32 pairs: the f32x2 arithmetic of sm_100-class GPUs does two
+// IEEE round-to-nearest operations in one instruction.  The FP32 step is
+// issue-bound, and its (r, theta) and (p_r, p_theta) updates pair up
+// exactly; on the 1280x720x4 frame this took the kernel from 85.1 to 81.4 ms.
+struct P2 { unsigned long long v; };
+__device__ __forceinline__ P2 p2(float a, float b) {
+    P2 r; asm("mov.b64 %0, {%1, %2};" : "=l"(r.v) : "f"(a), "f"(b)); return r;
+}
+__device__ __forceinline__ void p2_get(P2 x, float& a, float& b) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(x.v));
+}
+__device__ __forceinline__ P2 add2(P2 a, P2 b) { P2 r; asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v)); return r; }
+__device__ __forceinline__ P2 sub2(P2 a, P2 b) { P2 r; asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v)); return r; }
+__device__ __forceinline__ P2 mul2(P2 a, P2 b) { P2 r; asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v)); return r; }
+__device__ __forceinline__ P2 fma2(P2 a, P2 b, P2 c) {
+    P2 r; asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r.v) : "l"(a.v), "l"(b.v), "l"(c.v)); return r;
+}
+// hl_add on two (hi, lo) pairs at once.
+__device__ __forceinline__ void hl_add2(P2& hi, P2& lo, P2 d) {
+    P2 s = add2(hi, d);
+    P2 bb = sub2(s, hi);
+    P2 e = add2(sub2(hi, sub2(s, bb)), sub2(d, bb));
+    e = add2(e, lo);
+    hi = add2(s, e);
+    lo = sub2(e, sub2(hi, s));
+}
+
 // theta - pi/2 of a (hi, lo) angle, exact while |theta - pi/2| < pi/2.
 __device__ __forceinline__ float dtheta_eq(const HiLo& th) {
     const float PI2_HI = 1.57079637050628662109375f;   // fl(pi/2)
@@ -397,17 +424,32 @@ __device__ __forceinline__ int mray_step32(MRay<PHI>& R, const SceneDev& s, cons
     const HiLo r0 = R.r, th0 = R.th, pr0 = R.pr, pth0 = R.pth, ph0 = R.ph;
     const float k0r = R.k[0], k0t = R.k[1], k0p = R.k[4];
     const float hh = 0.5f * h;
-    F5 k2 = rhs_f<PHI>(R.r.hi + fmaf(hh, R.k[0], R.r.lo), R.th.hi + fmaf(hh, R.k[1], R.th.lo),
-                       R.pr.hi + fmaf(hh, R.k[2], R.pr.lo), R.pth.hi + fmaf(hh, R.k[3], R.pth.lo), R.c, k);
-    F5 k3 = rhs_f<PHI>(R.r.hi + fmaf(hh, k2.r, R.r.lo), R.th.hi + fmaf(hh, k2.th, R.th.lo),
-                       R.pr.hi + fmaf(hh, k2.pr, R.pr.lo), R.pth.hi + fmaf(hh, k2.pth, R.pth.lo), R.c, k);
-    F5 k4 = rhs_f<PHI>(R.r.hi + fmaf(h, k3.r, R.r.lo), R.th.hi + fmaf(h, k3.th, R.th.lo),
-                       R.pr.hi + fmaf(h, k3.pr, R.pr.lo), R.pth.hi + fmaf(h, k3.pth, R.pth.lo), R.c, k);
+    // (r, theta) and (p_r, p_theta) as packed pairs
+    const P2 hiA = p2(R.r.hi, R.th.hi), loA = p2(R.r.lo, R.th.lo);
+    const P2 hiB = p2(R.pr.hi, R.pth.hi), loB = p2(R.pr.lo, R.pth.lo);
+    const P2 hh2 = p2(hh, hh), h2 = p2(h, h);
+    float a0, a1, b0, b1;
+    const P2 k1A = p2(R.k[0], R.k[1]), k1B = p2(R.k[2], R.k[3]);
+    p2_get(add2(hiA, fma2(hh2, k1A, loA)), a0, a1);
+    p2_get(add2(hiB, fma2(hh2, k1B, loB)), b0, b1);
+    F5 k2 = rhs_f<PHI>(a0, a1, b0, b1, R.c, k);
+    const P2 k2A = p2(k2.r, k2.th), k2B = p2(k2.pr, k2.pth);
+    p2_get(add2(hiA, fma2(hh2, k2A, loA)), a0, a1);
+    p2_get(add2(hiB, fma2(hh2, k2B, loB)), b0, b1);
+    F5 k3 = rhs_f<PHI>(a0, a1, b0, b1, R.c, k);
+    const P2 k3A = p2(k3.r, k3.th), k3B = p2(k3.pr, k3.pth);
+    p2_get(add2(hiA, fma2(h2, k3A, loA)), a0, a1);
+    p2_get(add2(hiB, fma2(h2, k3B, loB)), b0, b1);
+    F5 k4 = rhs_f<PHI>(a0, a1, b0, b1, R.c, k);
     const float h6 = h * (1.0f / 6.0f);
-    hl_add(R.r, h6 * (R.k[0] + 2.0f * (k2.r + k3.r) + k4.r));
-    hl_add(R.th, h6 * (R.k[1] + 2.0f * (k2.th + k3.th) + k4.th));
-    hl_add(R.pr, h6 * (R.k[2] + 2.0f * (k2.pr + k3.pr) + k4.pr));
-    hl_add(R.pth, h6 * (R.k[3] + 2.0f * (k2.pth + k3.pth) + k4.pth));
+    const P2 h62 = p2(h6, h6), two = p2(2.0f, 2.0f);
+    P2 dA = mul2(h62, add2(fma2(two, add2(k2A, k3A), k1A), p2(k4.r, k4.th)));
+    P2 dB = mul2(h62, add2(fma2(two, add2(k2B, k3B), k1B), p2(k4.pr, k4.pth)));
+    P2 nhA = hiA, nlA = loA, nhB = hiB, nlB = loB;
+    hl_add2(nhA, nlA, dA);
+    hl_add2(nhB, nlB, dB);
+    p2_get(nhA, R.r.hi, R.th.hi); p2_get(nlA, R.r.lo, R.th.lo);
+    p2_get(nhB, R.pr.hi, R.pth.hi); p2_get(nlB, R.pr.lo, R.pth.lo);
     if (PHI) hl_add(R.ph, h6 * (R.k[4] + 2.0f * (k2.ph + k3.ph) + k4.ph));
     if (s.islands & kIslandTurning) {
         bool turn = ((pr0.hi > 0.0f) != (R.pr.hi > 0.0f)) || ((pth0.hi > 0.0f) != (R.pth.hi > 0.0f));
