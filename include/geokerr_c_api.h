@@ -71,6 +71,52 @@ void compute_geokerr_complete_cuda(const double* h_u0, const double* h_uf, const
                                    double* h_lambda_results, double* h_muf_results,
                                    int* h_ncase_results, char* h_valid_results, int n_cases);
 
+/* Final state after Mino time lambda_max (geokerr_port/cuda/geokerr_cuda.cu:
+ * 319-323 and geokerr_improved.cu:378-382, whose bodies there are
+ * placeholders): ray i with spin a_vals[i] starts at r0_vals[i],
+ * mu0_vals[i] with E_vals[i] > 0, L_vals[i], Q2_vals[i] (any normalisation),
+ * outgoing in r and increasing in mu as those wrappers integrate; outputs
+ * r, mu, phi and t (phi, t from 0) at Mino time lambda_max of that
+ * normalisation, integrated exactly by the Mino-time solver (n_steps is
+ * accepted and not needed).  A ray that reaches the horizon or r = infinity
+ * first keeps its last state there; a forbidden start gives NaN.  Both
+ * names run the same solver. */
+void geokerr_cuda_batch(const double* a_vals, const double* r0_vals, const double* mu0_vals,
+                        const double* E_vals, const double* L_vals, const double* Q2_vals,
+                        double* r_final, double* mu_final, double* phi_final, double* t_final,
+                        int n_geodesics, int n_steps, double lambda_max);
+void geokerr_improved_batch(const double* a_vals, const double* r0_vals, const double* mu0_vals,
+                            const double* E_vals, const double* L_vals, const double* Q2_vals,
+                            double* r_final, double* mu_final, double* phi_final, double* t_final,
+                            int n_geodesics, int n_steps, double lambda_max);
+
+/* Mino time from u0 to uf (geokerr_port/cuda/mino_time_cuda.cu:270-280, a
+ * placeholder there): the radial motion with sign su[i] reaching uf[i]
+ * directly (tpr[i] = 0) or after its radial turning point (tpr[i] = 1).
+ * lambda is fixed by the radial motion, so muf, tpm and ncase are accepted
+ * and not needed; valid[i] = 0 when uf is not reached that way. */
+void compute_mino_time_batch_cuda(const double* h_u0, const double* h_uf, const double* h_mu0,
+                                  const double* h_muf, const double* h_a, const double* h_l,
+                                  const double* h_q2, const int* h_tpm, const int* h_tpr,
+                                  const int* h_su, const int* h_sm, const int* h_ncase,
+                                  double* h_lambda_results, char* h_valid_results, int n_cases);
+
+/* The Fortran single-case entry (geokerr_port/reference/geokerr_single.f:1-3,
+ * called by geokerr_compare.cu:27-33), arguments by reference: Mino time
+ * from u0 to uf and mu there, as compute_geokerr_complete_cuda for one ray
+ * (muf is accepted and not needed). */
+void geokerr_single_case_(double* u0, double* uf, double* mu0, double* muf, double* a, double* l, double* q2,
+                          int* su, int* sm, double* lambda, double* muf_out, int* ncase, int* valid);
+
+/* State at Mino time lam[i] of ray i (spin a[i]) leaving (u0[i], mu0[i])
+ * with signs su[i], sm[i] of du/dlambda and dmu/dlambda: u, mu, t and phi
+ * (t and phi from 0); valid[i] = 0 when the ray reached the horizon or
+ * u = 0 first (the last state before it is returned) or started in a
+ * forbidden region (NaN).  Host arrays; returns np_status. */
+int np_geokerr_final_state_host(int n, const double* a, const double* u0, const double* mu0, const double* l,
+                                const double* q2, const double* su, const double* sm, const double* lam,
+                                double* u, double* mu, double* t, double* phi, char* valid);
+
 /* Batched GEOKERR sampler (geokerr_original.f:357-605 with USEGEOR false,
  * PHIT true, NPTS = 0): ray i uses u0[i], uf[i], mu0[i], l[i], q2[i],
  * su[i], sm[i] and the common spin a, TPR flag, nup and offset; outputs are

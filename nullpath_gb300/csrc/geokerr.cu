@@ -25,6 +25,7 @@
 #include <cstring>
 #include <string>
 #include <algorithm>
+#include <vector>
 
 #include <cuda_runtime.h>
 
@@ -439,10 +440,13 @@ __global__ void stream_kernel(double u0, double uf, double mu0, double a, double
 // Mino time from u0 to the first arrival at uf and mu there; ncase 1 when
 // uf is reached before a radial turning point, 2 after it, 3 when the ray
 // has no turning point (it falls in or escapes).
+// With after_tp (may be null) and after_tp[i] != 0, arrivals before the
+// radial turning point are skipped: the arrival on the way back out.
 __global__ void complete_kernel(int n, const double* __restrict__ u0, const double* __restrict__ uf,
                                 const double* __restrict__ mu0, const double* __restrict__ a,
                                 const double* __restrict__ l, const double* __restrict__ q2,
                                 const int* __restrict__ su_in, const int* __restrict__ sm_in,
+                                const int* __restrict__ after_tp,
                                 double* lam_out, double* muf_out, int* ncase, char* valid) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -456,6 +460,7 @@ __global__ void complete_kernel(int n, const double* __restrict__ u0, const doub
     double ub;
     const bool has_tp = find_turning(p, s, su, ub);
     const double target = uf[i];
+    const bool need_tp = after_tp && after_tp[i] != 0;
     double lam_a = 0.0;
     bool passed = false;
     Ser c;
@@ -467,6 +472,7 @@ __global__ void complete_kernel(int n, const double* __restrict__ u0, const doub
         if ((e.du > 0) != (s.du > 0) && e.du != 0.0 && s.du != 0.0) s_r = solve(c.u, 0.0, 0.0, h, true);
         double seg_lo[2] = {0.0, s_r}, seg_hi[2] = {s_r >= 0.0 ? s_r : h, h};
         for (int g = 0; g < (s_r >= 0.0 ? 2 : 1); ++g) {
+            if (need_tp && !(passed || g == 1)) continue;
             double ga = hv(c.u, seg_lo[g]) - target, gb = hv(c.u, seg_hi[g]) - target;
             if (ga == 0.0 || gb == 0.0 || (ga > 0) != (gb > 0)) {
                 double x = solve(c.u, target, seg_lo[g], seg_hi[g], false);
@@ -522,7 +528,108 @@ __global__ void crossings_kernel(int n, double a, const double* __restrict__ u0,
     nx[i] = found;
 }
 
+// State at Mino time lam[i] of ray i (spin a[i]) leaving (u0[i], mu0[i])
+// with signs su[i], sm[i] of du/dlambda and dmu/dlambda: u, mu, t and phi
+// (t and phi from 0 at the start).  A ray that reaches the horizon or u = 0
+// first keeps the last state before it and is flagged 0 in valid; a
+// forbidden start gives NaN.
+__global__ void final_state_kernel(int n, const double* __restrict__ a, const double* __restrict__ u0,
+                                   const double* __restrict__ mu0, const double* __restrict__ l,
+                                   const double* __restrict__ q2, const double* __restrict__ su,
+                                   const double* __restrict__ sm, const double* __restrict__ lam, double* uo,
+                                   double* muo, double* to, double* pho, char* valid) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double nan_v = nan("");
+    uo[i] = nan_v; muo[i] = nan_v; to[i] = nan_v; pho[i] = nan_v; valid[i] = 0;
+    if (!(fabs(a[i]) < 1.0) || !(lam[i] >= 0.0)) return;
+    Par p = make_par(a[i], l[i], q2[i], mu0[i]);
+    double U0, M0;
+    if (!start_potentials(p, u0[i], mu0[i], U0, M0)) return;
+    St s{u0[i], (su[i] >= 0.0 ? 1.0 : -1.0) * sqrt(U0), mu0[i], (sm[i] >= 0.0 ? 1.0 : -1.0) * sqrt(M0), 0.0, 0.0, 0.0};
+    const double target = lam[i];
+    double lam_a = 0.0;
+    Ser c;
+    for (int it = 0; it < kMaxSteps; ++it) {
+        taylor(p, s, c, true);
+        double h = step_size(p, c, s, true);
+        if (lam_a + h >= target) {
+            double x = target - lam_a;
+            uo[i] = hv(c.u, x); muo[i] = hv(c.m, x); to[i] = hv(c.t, x); pho[i] = hv(c.ph, x);
+            valid[i] = 1;
+            return;
+        }
+        St e = advance(c, h, true);
+        if (e.u >= p.uplus || e.u <= 0.0 || !isfinite(e.t)) break;
+        s = e;
+        lam_a += h;
+    }
+    uo[i] = s.u; muo[i] = s.m; to[i] = s.t; pho[i] = s.ph;
+}
+
 int grid(int n, int b) { return (n + b - 1) / b; }
+
+// Host arrays in, final states out (geokerr_cuda_batch and friends): copies
+// n rays' inputs to the device, runs final_state_kernel, copies back.
+// Returns false when the device work failed.
+bool final_states_host(int n, const double* a, const double* u0, const double* mu0, const double* l,
+                       const double* q2, const double* su, const double* sm, const double* lam, double* uo,
+                       double* muo, double* to, double* pho, char* valid) {
+    const size_t m = (size_t)n;
+    char* d = nullptr;
+    if (cudaMalloc(&d, m * (12 * sizeof(double) + 1)) != cudaSuccess) return false;
+    double* dd = (double*)d;
+    const double* ins[8] = {a, u0, mu0, l, q2, su, sm, lam};
+    bool ok = true;
+    for (int k = 0; k < 8 && ok; ++k)
+        ok = cudaMemcpy(dd + k * m, ins[k], m * sizeof(double), cudaMemcpyHostToDevice) == cudaSuccess;
+    char* dv = (char*)(dd + 12 * m);
+    if (ok) {
+        final_state_kernel<<<grid(n, 64), 64>>>(n, dd, dd + m, dd + 2 * m, dd + 3 * m, dd + 4 * m, dd + 5 * m,
+                                                dd + 6 * m, dd + 7 * m, dd + 8 * m, dd + 9 * m, dd + 10 * m,
+                                                dd + 11 * m, dv);
+        ok = cudaDeviceSynchronize() == cudaSuccess;
+    }
+    double* outs[4] = {uo, muo, to, pho};
+    for (int k = 0; k < 4 && ok; ++k)
+        ok = cudaMemcpy(outs[k], dd + (8 + k) * m, m * sizeof(double), cudaMemcpyDeviceToHost) == cudaSuccess;
+    if (ok) ok = cudaMemcpy(valid, dv, m, cudaMemcpyDeviceToHost) == cudaSuccess;
+    cudaFree(d);
+    return ok;
+}
+
+// geokerr_cuda_batch / geokerr_improved_batch: per ray, E, L, Q2 in any
+// normalisation (l = L/E, q2 = Q2/E^2; the Mino time of the E = 1 problem
+// is E lambda_max), outgoing in r and increasing in mu as the reference's
+// wrappers integrate (geokerr_cuda.cu:259-264).
+void batch_final(const double* a_vals, const double* r0_vals, const double* mu0_vals, const double* E_vals,
+                 const double* L_vals, const double* Q2_vals, double* r_final, double* mu_final, double* phi_final,
+                 double* t_final, int n, double lambda_max) {
+    if (n <= 0 || !a_vals || !r0_vals || !mu0_vals || !E_vals || !L_vals || !Q2_vals || !r_final || !mu_final ||
+        !phi_final || !t_final)
+        return;
+    std::vector<double> u0(n), l(n), q2(n), su(n, -1.0), sm(n, 1.0), lam(n), uo(n), mo(n), to(n), po(n);
+    std::vector<char> valid(n);
+    for (int i = 0; i < n; ++i) {
+        const double E = E_vals[i];
+        u0[i] = r0_vals[i] > 0.0 ? 1.0 / r0_vals[i] : nan("");
+        l[i] = E > 0.0 ? L_vals[i] / E : nan("");
+        q2[i] = E > 0.0 ? Q2_vals[i] / (E * E) : nan("");
+        lam[i] = E > 0.0 ? E * lambda_max : nan("");
+    }
+    const double nan_v = nan("");
+    if (!final_states_host(n, a_vals, u0.data(), mu0_vals, l.data(), q2.data(), su.data(), sm.data(), lam.data(),
+                           uo.data(), mo.data(), to.data(), po.data(), valid.data())) {
+        for (int i = 0; i < n; ++i) r_final[i] = mu_final[i] = phi_final[i] = t_final[i] = nan_v;
+        return;
+    }
+    for (int i = 0; i < n; ++i) {
+        r_final[i] = uo[i] > 0.0 ? 1.0 / uo[i] : nan_v;
+        mu_final[i] = mo[i];
+        phi_final[i] = po[i];
+        t_final[i] = to[i];
+    }
+}
 
 }  // namespace
 
@@ -736,7 +843,8 @@ void compute_geokerr_complete_cuda(const double* h_u0, const double* h_uf, const
     cudaMemcpy(dq2, h_q2, n * sizeof(double), cudaMemcpyHostToDevice);
     cudaMemcpy(dsu, h_su, n * sizeof(int), cudaMemcpyHostToDevice);
     cudaMemcpy(dsm, h_sm, n * sizeof(int), cudaMemcpyHostToDevice);
-    complete_kernel<<<grid(n_cases, 64), 64>>>(n_cases, du0, duf, dmu0, da, dl, dq2, dsu, dsm, dlam, dmuf, dnc, dv);
+    complete_kernel<<<grid(n_cases, 64), 64>>>(n_cases, du0, duf, dmu0, da, dl, dq2, dsu, dsm, nullptr, dlam, dmuf,
+                                               dnc, dv);
     if (cudaDeviceSynchronize() == cudaSuccess) {
         cudaMemcpy(h_lambda_results, dlam, n * sizeof(double), cudaMemcpyDeviceToHost);
         cudaMemcpy(h_muf_results, dmuf, n * sizeof(double), cudaMemcpyDeviceToHost);
@@ -746,6 +854,85 @@ void compute_geokerr_complete_cuda(const double* h_u0, const double* h_uf, const
         for (size_t i = 0; i < n; ++i) h_valid_results[i] = 0;
     }
     cudaFree(d);
+}
+
+void geokerr_cuda_batch(const double* a_vals, const double* r0_vals, const double* mu0_vals, const double* E_vals,
+                        const double* L_vals, const double* Q2_vals, double* r_final, double* mu_final,
+                        double* phi_final, double* t_final, int n_geodesics, int n_steps, double lambda_max) {
+    (void)n_steps;   // the Mino-time solver needs no step count
+    batch_final(a_vals, r0_vals, mu0_vals, E_vals, L_vals, Q2_vals, r_final, mu_final, phi_final, t_final,
+                n_geodesics, lambda_max);
+}
+
+void geokerr_improved_batch(const double* a_vals, const double* r0_vals, const double* mu0_vals,
+                            const double* E_vals, const double* L_vals, const double* Q2_vals, double* r_final,
+                            double* mu_final, double* phi_final, double* t_final, int n_geodesics, int n_steps,
+                            double lambda_max) {
+    (void)n_steps;
+    batch_final(a_vals, r0_vals, mu0_vals, E_vals, L_vals, Q2_vals, r_final, mu_final, phi_final, t_final,
+                n_geodesics, lambda_max);
+}
+
+int np_geokerr_final_state_host(int n, const double* a, const double* u0, const double* mu0, const double* l,
+                                const double* q2, const double* su, const double* sm, const double* lam, double* u,
+                                double* mu, double* t, double* phi, char* valid) {
+    if (n < 0 || (n > 0 && (!a || !u0 || !mu0 || !l || !q2 || !su || !sm || !lam || !u || !mu || !t || !phi ||
+                            !valid)))
+        return gk_fail(NP_ERR_INVALID, "bad arguments");
+    if (n == 0) return NP_OK;
+    return final_states_host(n, a, u0, mu0, l, q2, su, sm, lam, u, mu, t, phi, valid)
+               ? NP_OK : gk_fail(NP_ERR_KERNEL, "final-state kernel failed");
+}
+
+void compute_mino_time_batch_cuda(const double* h_u0, const double* h_uf, const double* h_mu0, const double* h_muf,
+                                  const double* h_a, const double* h_l, const double* h_q2, const int* h_tpm,
+                                  const int* h_tpr, const int* h_su, const int* h_sm, const int* h_ncase,
+                                  double* h_lambda_results, char* h_valid_results, int n_cases) {
+    (void)h_muf; (void)h_tpm; (void)h_ncase;
+    if (n_cases <= 0 || !h_u0 || !h_uf || !h_mu0 || !h_a || !h_l || !h_q2 || !h_tpr || !h_su || !h_sm ||
+        !h_lambda_results || !h_valid_results)
+        return;
+    const size_t n = n_cases;
+    const size_t bytes = n * (8 * sizeof(double) + 4 * sizeof(int) + 1) + 1024;
+    char* d = nullptr;
+    if (cudaMalloc(&d, bytes) != cudaSuccess) {
+        for (size_t i = 0; i < n; ++i) h_valid_results[i] = 0;
+        return;
+    }
+    double* dd = (double*)d;
+    double *du0 = dd, *duf = dd + n, *dmu0 = dd + 2 * n, *da = dd + 3 * n, *dl = dd + 4 * n, *dq2 = dd + 5 * n;
+    double *dlam = dd + 6 * n, *dmuf = dd + 7 * n;
+    int* di = (int*)(dd + 8 * n);
+    int *dsu = di, *dsm = di + n, *dnc = di + 2 * n, *dtp = di + 3 * n;
+    char* dv = (char*)(di + 4 * n);
+    bool ok = cudaMemcpy(du0, h_u0, n * sizeof(double), cudaMemcpyHostToDevice) == cudaSuccess &&
+              cudaMemcpy(duf, h_uf, n * sizeof(double), cudaMemcpyHostToDevice) == cudaSuccess &&
+              cudaMemcpy(dmu0, h_mu0, n * sizeof(double), cudaMemcpyHostToDevice) == cudaSuccess &&
+              cudaMemcpy(da, h_a, n * sizeof(double), cudaMemcpyHostToDevice) == cudaSuccess &&
+              cudaMemcpy(dl, h_l, n * sizeof(double), cudaMemcpyHostToDevice) == cudaSuccess &&
+              cudaMemcpy(dq2, h_q2, n * sizeof(double), cudaMemcpyHostToDevice) == cudaSuccess &&
+              cudaMemcpy(dsu, h_su, n * sizeof(int), cudaMemcpyHostToDevice) == cudaSuccess &&
+              cudaMemcpy(dsm, h_sm, n * sizeof(int), cudaMemcpyHostToDevice) == cudaSuccess &&
+              cudaMemcpy(dtp, h_tpr, n * sizeof(int), cudaMemcpyHostToDevice) == cudaSuccess;
+    if (ok) {
+        complete_kernel<<<grid(n_cases, 64), 64>>>(n_cases, du0, duf, dmu0, da, dl, dq2, dsu, dsm, dtp, dlam, dmuf,
+                                                   dnc, dv);
+        ok = cudaDeviceSynchronize() == cudaSuccess &&
+             cudaMemcpy(h_lambda_results, dlam, n * sizeof(double), cudaMemcpyDeviceToHost) == cudaSuccess &&
+             cudaMemcpy(h_valid_results, dv, n, cudaMemcpyDeviceToHost) == cudaSuccess;
+    }
+    if (!ok)
+        for (size_t i = 0; i < n; ++i) h_valid_results[i] = 0;
+    cudaFree(d);
+}
+
+void geokerr_single_case_(double* u0, double* uf, double* mu0, double* muf, double* a, double* l, double* q2,
+                          int* su, int* sm, double* lambda, double* muf_out, int* ncase, int* valid) {
+    (void)muf;
+    if (!u0 || !uf || !mu0 || !a || !l || !q2 || !su || !sm || !lambda || !muf_out || !ncase || !valid) return;
+    char v = 0;
+    compute_geokerr_complete_cuda(u0, uf, mu0, a, l, q2, su, sm, lambda, muf_out, ncase, &v, 1);
+    *valid = v ? 1 : 0;
 }
 
 }  // extern "C"

@@ -21,6 +21,11 @@ _PROTOS = {
     "np_geokerr_eval_lambda_device": (I, [I, D] + [V] * 8 + [I] + [V] * 8 + [V, V]),
     "np_geokerr_eval_lambda_work_bytes": (C.c_size_t, [I, I]),
     "np_geokerr_equator_crossings_device": (I, [I, D] + [V] * 6 + [D, I] + [V] * 3 + [V]),
+    "np_geokerr_final_state_host": (I, [I] + [V] * 14),
+    "geokerr_cuda_batch": (None, [V] * 10 + [I, I, D]),
+    "geokerr_improved_batch": (None, [V] * 10 + [I, I, D]),
+    "compute_mino_time_batch_cuda": (None, [V] * 14 + [I]),
+    "geokerr_single_case_": (None, [V] * 13),
 }
 
 
@@ -79,6 +84,53 @@ def complete(u0, uf, mu0, a, l, q2, su, sm):
     nc, valid = np.zeros(n, np.int32), np.zeros(n, np.int8)
     lib.compute_geokerr_complete_cuda(*[_vp(x) for x in ins], _vp(lam), _vp(muf), _vp(nc), _vp(valid), n)
     return lam, muf, nc, valid
+
+
+def final_state(a, u0, mu0, l, q2, su, sm, lam):
+    """np_geokerr_final_state_host: (u, mu, t, phi, valid) at Mino time lam per ray."""
+    lib = _lib()
+    f = lambda x: np.ascontiguousarray(np.broadcast_to(np.asarray(x, np.float64), np.shape(u0)), np.float64)
+    ins = [f(v) for v in (a, u0, mu0, l, q2, su, sm, lam)]
+    n = ins[1].size
+    outs = [np.zeros(n) for _ in range(4)]
+    valid = np.zeros(n, np.int8)
+    check(lib.np_geokerr_final_state_host(n, *[_vp(x) for x in ins], *[_vp(x) for x in outs], _vp(valid)))
+    return (*outs, valid)
+
+
+def cuda_batch(a, r0, mu0, E, L, Q2, lambda_max, n_steps=1000, improved=False):
+    """geokerr_cuda_batch / geokerr_improved_batch: final (r, mu, phi, t) per ray."""
+    lib = _lib()
+    f = lambda x: np.ascontiguousarray(x, np.float64)
+    ins = [f(v) for v in (a, r0, mu0, E, L, Q2)]
+    n = ins[0].size
+    outs = [np.zeros(n) for _ in range(4)]
+    fn = lib.geokerr_improved_batch if improved else lib.geokerr_cuda_batch
+    fn(*[_vp(x) for x in ins], *[_vp(x) for x in outs], n, n_steps, lambda_max)
+    return tuple(outs)
+
+
+def mino_time_batch(u0, uf, mu0, muf, a, l, q2, tpm, tpr, su, sm, ncase):
+    """compute_mino_time_batch_cuda: (lambda, valid) per case."""
+    lib = _lib()
+    f = lambda x: np.ascontiguousarray(x, np.float64)
+    i = lambda x: np.ascontiguousarray(x, np.int32)
+    ins = [f(u0), f(uf), f(mu0), f(muf), f(a), f(l), f(q2), i(tpm), i(tpr), i(su), i(sm), i(ncase)]
+    n = ins[0].size
+    lam, valid = np.zeros(n), np.zeros(n, np.int8)
+    lib.compute_mino_time_batch_cuda(*[_vp(x) for x in ins], _vp(lam), _vp(valid), n)
+    return lam, valid
+
+
+def single_case(u0, uf, mu0, a, l, q2, su, sm, muf=0.0):
+    """geokerr_single_case_ (by-reference arguments): (lambda, muf, ncase, valid)."""
+    lib = _lib()
+    d = [C.c_double(v) for v in (u0, uf, mu0, muf, a, l, q2)]
+    iv = [C.c_int(int(su)), C.c_int(int(sm))]
+    lam, mo, nc, ok = C.c_double(), C.c_double(), C.c_int(), C.c_int()
+    lib.geokerr_single_case_(*[C.byref(x) for x in d], *[C.byref(x) for x in iv], C.byref(lam), C.byref(mo),
+                             C.byref(nc), C.byref(ok))
+    return lam.value, mo.value, nc.value, ok.value
 
 
 def _t(x):

@@ -164,6 +164,8 @@ def _geo_protos(lib):
     lib.npo_geokerr_stream.restype = I
     lib.npo_geokerr_crossings.argtypes = [D] * 8 + [I, V, V]
     lib.npo_geokerr_crossings.restype = I
+    lib.npo_geokerr_final.argtypes = [D] * 8 + [V]
+    lib.npo_geokerr_final.restype = I
     lib._geo_ready = True
 
 
@@ -231,6 +233,15 @@ def geokerr_crossings(u0, mu0, a, l, q2, su, sm, u_end=1e-3, K=4):
     xu, xphi = np.zeros(K), np.zeros(K)
     n = lib.npo_geokerr_crossings(u0, mu0, a, l, q2, su, sm, u_end, K, _vp(xu), _vp(xphi))
     return n, xu, xphi
+
+
+def geokerr_final(u0, mu0, a, l, q2, su, sm, lam):
+    """(valid, [u, mu, t, phi]) at Mino time lam of the ray leaving (u0, mu0)."""
+    lib = load()
+    _geo_protos(lib)
+    out = np.zeros(4)
+    ok = lib.npo_geokerr_final(u0, mu0, a, l, q2, su, sm, lam, _vp(out))
+    return ok, out
 
 
 def critical_curve(scene):

@@ -508,6 +508,39 @@ int npo_geokerr_crossings(double u0, double mu0, double a, double l, double q2, 
     return found;
 }
 
+// State at Mino time lam of the ray leaving (u0, mu0) with signs su, sm:
+// out = (u, mu, t, phi); returns 1, or 0 when the ray reached the horizon
+// or u = 0 first (out = the last state before it) or the start is
+// forbidden (out = NaN).  Restates np_geokerr_final_state_host.
+int npo_geokerr_final(double u0, double mu0, double a, double l, double q2, double su, double sm, double lam,
+                      double* out) {
+    using namespace geo;
+    const double nan_v = std::nan("");
+    out[0] = out[1] = out[2] = out[3] = nan_v;
+    if (!(std::fabs(a) < 1.0) || !(lam >= 0.0)) return 0;
+    Params p = make_params(a, l, q2, mu0);
+    double U0, M0;
+    if (!start_potentials(p, u0, mu0, U0, M0)) return 0;
+    State s{u0, (su >= 0.0 ? 1.0 : -1.0) * std::sqrt(U0), mu0, (sm >= 0.0 ? 1.0 : -1.0) * std::sqrt(M0), 0, 0, 0};
+    double lam_a = 0.0;
+    for (int it = 0; it < 400000; ++it) {
+        Series c;
+        taylor(p, s, c);
+        double h = step_size(p, c, s, true);
+        if (lam_a + h >= lam) {
+            double x = lam - lam_a;
+            out[0] = horner(c.u, x); out[1] = horner(c.m, x); out[2] = horner(c.t, x); out[3] = horner(c.ph, x);
+            return 1;
+        }
+        State e = advance(c, h);
+        if (e.u >= p.uplus || e.u <= 0.0 || !std::isfinite(e.t)) break;
+        s = e;
+        lam_a += h;
+    }
+    out[0] = s.u; out[1] = s.m; out[2] = s.t; out[3] = s.ph;
+    return 0;
+}
+
 // geokerr_phi_omega (geokerr_eval_lambda.f90:299-306): dphi/dlambda at u0.
 double npo_geokerr_phi_omega(double u0, double mu0, double a, double Lz, double Q2) {
     (void)Q2;

@@ -82,3 +82,24 @@ def test_equatorial_edge_case(built, case):
         assert abs(pts["lam"][k] - lam) <= 1e-9 * abs(lam) + 1e-12, (k, pts["lam"][k], lam)
         assert abs(pts["dt"][k] - dt) <= 1e-8 * abs(dt) + 1e-10, (k, pts["dt"][k], dt)
         assert abs(pts["dphi"][k] - dph) <= 1e-8 * abs(dph) + 1e-10, (k, pts["dphi"][k], dph)
+
+
+@pytest.mark.parametrize("a,b,r0,su", [(0.9, 50.0, 1000.0, 1), (0.5, 4.0, 20.0, -1), (0.998, 3.0, 100.0, 1),
+                                        (0.0, 8.0, 50.0, 1)])
+def test_final_state_matches_quadrature(built, a, b, r0, su):
+    """The restatement's state at a given Mino time (the solver behind
+    geokerr_cuda_batch): for an equatorial ray, the Mino time from u0 to the
+    returned u, and t and phi there, agree with adaptive quadrature."""
+    u0 = 1.0 / r0
+    # outgoing rays reach u = 0 at Mino time ~u0, ingoing ones turn or fall in after ~1/b
+    lam_total = 0.8 * u0 if su < 0 else 0.5 / b
+    for frac in (0.25, 0.5, 1.0):
+        lam = frac * lam_total
+        ok, out = oracle.geokerr_final(u0, 0.0, a, b, 0.0, float(su), 1.0, lam)
+        assert ok == 1 and abs(out[1]) < 1e-15
+        U = lambda x: 1.0 + (a * a - b * b) * x * x + 2.0 * (a - b) ** 2 * x ** 3
+        lo, hi = sorted((u0, out[0]))
+        mino = quad(lambda x: 1.0 / math.sqrt(U(x)), lo, hi, epsabs=0.0, epsrel=1e-13, limit=200)[0]
+        assert abs(mino - lam) <= 1e-10 * lam, (mino, lam)
+        lam_aff, dt, dph = _integrals(a, b, u0, out[0])
+        assert abs(out[2] - dt) <= 1e-8 * abs(dt) + 1e-10 and abs(out[3] - dph) <= 1e-8 * abs(dph) + 1e-10

@@ -152,3 +152,67 @@ def test_edge_case_families_match_oracle(cuda):
             assert np.array_equal(got["tpr"][i], ref["tpr"])
             checked += 1
     assert checked >= 55
+
+
+def _final_cases():
+    rng = np.random.default_rng(9)
+    n = 24
+    a = rng.uniform(0.0, 0.99, n)
+    r0 = rng.uniform(8.0, 200.0, n)
+    mu0 = rng.uniform(-0.8, 0.8, n)
+    E = rng.uniform(0.5, 2.0, n)
+    L = E * rng.uniform(-6.0, 6.0, n)
+    Q2 = E * E * rng.uniform(0.5, 30.0, n)
+    return a, r0, mu0, E, L, Q2
+
+
+def test_final_state_and_batch_entry_points_match_oracle(cuda):
+    """geokerr_cuda_batch / geokerr_improved_batch (real solver behind the
+    reference's placeholder wrappers): outgoing in r, increasing in mu, E != 1
+    through the Mino-time scaling lambda_1 = E lambda; against the oracle's
+    state at the same Mino time."""
+    a, r0, mu0, E, L, Q2 = _final_cases()
+    lam_max = 0.02
+    for improved in (False, True):
+        r, mu, phi, t = gk.cuda_batch(a, r0, mu0, E, L, Q2, lam_max, improved=improved)
+        checked = 0
+        for i in range(a.size):
+            ok, ref = oracle.geokerr_final(1.0 / r0[i], mu0[i], a[i], L[i] / E[i], Q2[i] / E[i] ** 2, -1.0, 1.0,
+                                           E[i] * lam_max)
+            if not np.isfinite(ref[0]):
+                assert not np.isfinite(r[i])
+                continue
+            assert abs(1.0 / r[i] - ref[0]) <= 1e-12 * ref[0] + 1e-15, i
+            assert abs(mu[i] - ref[1]) <= 1e-12 and abs(t[i] - ref[2]) <= 1e-11 * (1 + abs(ref[2]))
+            assert abs(phi[i] - ref[3]) <= 1e-11 * (1 + abs(ref[3]))
+            checked += 1
+        assert checked >= 12
+    # the host-array final-state entry with explicit signs, against the oracle
+    u0 = 1.0 / r0
+    lam = np.full(a.size, 0.01)
+    for su, sm in ((1.0, -1.0), (-1.0, 1.0)):
+        u, mu, t, phi, valid = gk.final_state(a, u0, mu0, L / E, Q2 / E ** 2, su, sm, lam)
+        for i in range(a.size):
+            ok, ref = oracle.geokerr_final(u0[i], mu0[i], a[i], L[i] / E[i], Q2[i] / E[i] ** 2, su, sm, lam[i])
+            assert valid[i] == ok, i
+            if ok:
+                assert abs(u[i] - ref[0]) <= 1e-12 * ref[0] and abs(mu[i] - ref[1]) <= 1e-12, i
+
+
+def test_mino_time_batch_round_trip_and_single_case(cuda):
+    """compute_mino_time_batch_cuda: the Mino time to uf, then the final state
+    at that time is back at uf (directly, tpr = 0, and after the radial turning
+    point, tpr = 1); geokerr_single_case_ equals compute_geokerr_complete_cuda."""
+    a, l, q2 = 0.7, 6.0, 12.0          # ingoing from r = 100 with a radial turning point near r = 7
+    u0, uf, mu0 = 0.01, 0.05, 0.3
+    lam, valid = gk.mino_time_batch([u0, u0], [uf, uf], [mu0, mu0], [0.0, 0.0], [a, a], [l, l], [q2, q2],
+                                    [0, 0], [0, 1], [1, 1], [1, 1], [0, 0])
+    assert valid.tolist() == [1, 1] and lam[1] > lam[0] > 0.0
+    u, mu, t, phi, ok = gk.final_state(np.full(2, a), np.full(2, u0), np.full(2, mu0), np.full(2, l),
+                                       np.full(2, q2), np.full(2, 1.0), np.full(2, 1.0), lam)
+    assert ok.tolist() == [1, 1]
+    assert np.all(np.abs(u - uf) < 1e-10 * uf), u
+    lam1, muf1, nc1, v1 = gk.single_case(u0, uf, mu0, a, l, q2, 1, 1)
+    lam2, muf2, nc2, v2 = gk.complete([u0], [uf], [mu0], [a], [l], [q2], [1], [1])
+    assert v1 == 1 and v2[0] == 1 and lam1 == lam2[0] and muf1 == muf2[0] and nc1 == nc2[0]
+    assert abs(lam1 - lam[0]) <= 1e-12 * lam[0]
