@@ -21,7 +21,7 @@ _PROTOS = {
     "np_geokerr_eval_lambda_device": (I, [I, D] + [V] * 8 + [I] + [V] * 8 + [V, V]),
     "np_geokerr_eval_lambda_work_bytes": (C.c_size_t, [I, I]),
     "np_geokerr_equator_crossings_device": (I, [I, D] + [V] * 6 + [D, I] + [V] * 3 + [V]),
-    "np_geokerr_final_state_host": (I, [I] + [V] * 14),
+    "np_geokerr_final_state_host": (I, [I] + [V] * 13),
     "geokerr_cuda_batch": (None, [V] * 10 + [I, I, D]),
     "geokerr_improved_batch": (None, [V] * 10 + [I, I, D]),
     "compute_mino_time_batch_cuda": (None, [V] * 14 + [I]),

@@ -166,6 +166,8 @@ def _geo_protos(lib):
     lib.npo_geokerr_crossings.restype = I
     lib.npo_geokerr_final.argtypes = [D] * 8 + [V]
     lib.npo_geokerr_final.restype = I
+    lib.npo_geokerr_mino_time.argtypes = [D] * 8 + [I, C.POINTER(D)]
+    lib.npo_geokerr_mino_time.restype = I
     lib._geo_ready = True
 
 
@@ -242,6 +244,15 @@ def geokerr_final(u0, mu0, a, l, q2, su, sm, lam):
     out = np.zeros(4)
     ok = lib.npo_geokerr_final(u0, mu0, a, l, q2, su, sm, lam, _vp(out))
     return ok, out
+
+
+def geokerr_mino_time(u0, uf, mu0, a, l, q2, su, sm, after_tp=False):
+    """(valid, lambda): Mino time from u0 to uf, directly or after the radial turning point."""
+    lib = load()
+    _geo_protos(lib)
+    lam = C.c_double()
+    ok = lib.npo_geokerr_mino_time(u0, uf, mu0, a, l, q2, su, sm, int(bool(after_tp)), C.byref(lam))
+    return ok, lam.value
 
 
 def critical_curve(scene):

@@ -541,6 +541,45 @@ int npo_geokerr_final(double u0, double mu0, double a, double l, double q2, doub
     return 0;
 }
 
+// Mino time from u0 to the first arrival at uf of the ray leaving with
+// signs su, sm (after_tp != 0: the first arrival after the radial turning
+// point); returns 1 with *lam, or 0 when uf is not reached that way.
+// Restates compute_mino_time_batch_cuda / compute_geokerr_complete_cuda.
+int npo_geokerr_mino_time(double u0, double uf, double mu0, double a, double l, double q2, double su, double sm,
+                          int after_tp, double* lam) {
+    using namespace geo;
+    *lam = std::nan("");
+    if (!(std::fabs(a) < 1.0)) return 0;
+    Params p = make_params(a, l, q2, mu0);
+    double U0, M0;
+    if (!start_potentials(p, u0, mu0, U0, M0)) return 0;
+    State s{u0, (su >= 0.0 ? 1.0 : -1.0) * std::sqrt(U0), mu0, (sm >= 0.0 ? 1.0 : -1.0) * std::sqrt(M0), 0, 0, 0};
+    double lam_a = 0.0;
+    bool passed = false;
+    for (int it = 0; it < 400000; ++it) {
+        Series c;
+        taylor(p, s, c);
+        double h = step_size(p, c, s, false);
+        State e = advance(c, h);
+        double s_r = -1.0;
+        if ((e.du > 0) != (s.du > 0) && e.du != 0.0 && s.du != 0.0) s_r = solve(c.u, 0.0, 0.0, h, true);
+        const double lo[2] = {0.0, s_r}, hi[2] = {s_r >= 0.0 ? s_r : h, h};
+        for (int g = 0; g < (s_r >= 0.0 ? 2 : 1); ++g) {
+            if (after_tp && !(passed || g == 1)) continue;
+            double ga = horner(c.u, lo[g]) - uf, gb = horner(c.u, hi[g]) - uf;
+            if (ga == 0.0 || gb == 0.0 || (ga > 0) != (gb > 0)) {
+                *lam = lam_a + solve(c.u, uf, lo[g], hi[g], false);
+                return 1;
+            }
+        }
+        if (s_r >= 0.0) passed = true;
+        if (e.u >= p.uplus || e.u <= 0.0) return 0;
+        s = e;
+        lam_a += h;
+    }
+    return 0;
+}
+
 // geokerr_phi_omega (geokerr_eval_lambda.f90:299-306): dphi/dlambda at u0.
 double npo_geokerr_phi_omega(double u0, double mu0, double a, double Lz, double Q2) {
     (void)Q2;

@@ -103,3 +103,22 @@ def test_final_state_matches_quadrature(built, a, b, r0, su):
         assert abs(mino - lam) <= 1e-10 * lam, (mino, lam)
         lam_aff, dt, dph = _integrals(a, b, u0, out[0])
         assert abs(out[2] - dt) <= 1e-8 * abs(dt) + 1e-10 and abs(out[3] - dph) <= 1e-8 * abs(dph) + 1e-10
+
+
+def test_mino_time_round_trip(built):
+    """The restatement of compute_mino_time_batch_cuda: the Mino time to
+    uf, directly and after the radial turning point, brings the state at that
+    time back to uf; the direct time matches quadrature of 1/sqrt(U)."""
+    a, l, q2, u0, uf, mu0 = 0.7, 6.0, 12.0, 0.01, 0.05, 0.3
+    ok0, lam0 = oracle.geokerr_mino_time(u0, uf, mu0, a, l, q2, 1.0, 1.0, False)
+    ok1, lam1 = oracle.geokerr_mino_time(u0, uf, mu0, a, l, q2, 1.0, 1.0, True)
+    assert ok0 == 1 and ok1 == 1 and lam1 > lam0 > 0.0
+    for lam in (lam0, lam1):
+        ok, out = oracle.geokerr_final(u0, mu0, a, l, q2, 1.0, 1.0, lam)
+        assert ok == 1 and abs(out[0] - uf) <= 1e-12 * uf, (lam, out)
+    U = lambda x: 1.0 + (a * a - q2 - l * l) * x * x + 2.0 * ((a - l) ** 2 + q2) * x ** 3 - a * a * q2 * x ** 4
+    direct = quad(lambda x: 1.0 / math.sqrt(U(x)), u0, uf, epsabs=0.0, epsrel=1e-13)[0]
+    assert abs(direct - lam0) <= 1e-11 * lam0
+    # a ray that turns before uf never gets there directly; after the turn it escapes
+    ok, _ = oracle.geokerr_mino_time(u0, 0.5, mu0, a, l, q2, 1.0, 1.0, False)
+    assert ok == 0
