@@ -5,7 +5,8 @@
 //                        persistent, one ray per lane with per-lane refill.
 //   render_mixed_kernel  FP32/compensated Carter-form integrator with FP64
 //                        islands; near-critical rays are appended to a
-//                        deferred list and finished by render_fp64_kernel.
+//                        deferred list and traced whole in FP64 by the
+//                        first warps of the same launch.
 //   resolve_kernel       sums the per-sample colours of a pass in sample
 //                        order into the planar image (progressive spp).
 //   trace_rays_kernel    explicit rays, per-ray crossing report.
@@ -290,16 +291,14 @@ __device__ __forceinline__ void flush_counters(Counters* ctr, unsigned long long
     }
 }
 
-// FP64 reference-form tracer.  With `list` non-null the kernel traces the
-// rays named by list[0 .. ctr->deferred) (deferred near-critical rays of the
-// mixed pass); otherwise every ray index in [0, total).
+// FP64 reference-form tracer over every ray index in [0, total).
 template <int MODE>
 __global__ void __launch_bounds__(kBlock)
 render_fp64_kernel(const SceneDev s, float* __restrict__ srgb, float* __restrict__ rcross,
-                   float* __restrict__ inv3, Counters* __restrict__ ctr, const long long* __restrict__ list) {
+                   float* __restrict__ inv3, Counters* __restrict__ ctr) {
     const unsigned FULL = 0xffffffffu;
-    unsigned long long* counter = list ? &ctr->work2 : &ctr->work;
-    const long long total = list ? (long long)ctr->deferred : s.total;
+    unsigned long long* counter = &ctr->work;
+    const long long total = s.total;
     WarpQueue q{0, 0};
     bool drained = false;
     RayFP64<false> R;
@@ -314,7 +313,7 @@ render_fp64_kernel(const SceneDev s, float* __restrict__ srgb, float* __restrict
             long long idx = warp_take(q, need, counter, total, kChunk);
             drained = q.base >= total;
             if (!have && idx >= 0) {
-                item = list ? list[idx] : idx;
+                item = idx;
                 int x, y; uint32_t sid;
                 ray_coords(s, item, p, sl, x, y, sid);
                 dir = camera_dir(s, x, y, sid, false, 0.0, 0.0);
@@ -346,7 +345,7 @@ render_fp64_kernel(const SceneDev s, float* __restrict__ srgb, float* __restrict
             have = false;
         }
     }
-    flush_counters(ctr, n_rays, n_steps, list ? n_steps : 0, n_evals);
+    flush_counters(ctr, n_rays, n_steps, 0, n_evals);
 }
 
 // Per-ray initial data of the mixed path, structure of arrays:
@@ -686,10 +685,10 @@ int grid_for(const void* kernel) {
 void launch_fp64(const SceneDev& s, float* srgb, float* rcross, float* inv3, Counters* ctr, cudaStream_t st) {
     if (s.integrator == NP_INTEG_RKF78) {
         render_fp64_kernel<kFp64Rkf78><<<grid_for((const void*)render_fp64_kernel<kFp64Rkf78>), kBlock, 0, st>>>(
-            s, srgb, rcross, inv3, ctr, nullptr);
+            s, srgb, rcross, inv3, ctr);
     } else {
         render_fp64_kernel<kFp64Rk4><<<grid_for((const void*)render_fp64_kernel<kFp64Rk4>), kBlock, 0, st>>>(
-            s, srgb, rcross, inv3, ctr, nullptr);
+            s, srgb, rcross, inv3, ctr);
     }
 }
 
