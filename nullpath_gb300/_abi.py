@@ -104,3 +104,12 @@ def benchmark_scene(width=1280, height=720, spp=4, spin=0.9, seed=0):
                  emissivity_q=3.0, disk_gain=1.0, crossing=NP_CROSS_HERMITE,
                  background=NP_BG_GRADIENT, bg_sigma_deg=1.0, bg_brightness=3.0,
                  check_invariants=0, islands=NP_ISLANDS_DEFAULT, inv_gate=0.0)
+
+
+def research_scene(scene, rtol=1e-12, atol=1e-14, inv_gate=1e-12):
+    """`scene` in research mode, as the CLI's --mode research sets it: the
+    embedded 7(8) integrator at tight tolerances, root-found crossings, the
+    invariant gate, the ZAMO camera and invariant tracking.  Render it with
+    precision "fp64"."""
+    return scene.replace(integrator=NP_INTEG_RKF78, crossing=NP_CROSS_ROOT, rtol=rtol, atol=atol,
+                         inv_gate=inv_gate, camera=NP_CAMERA_ZAMO, check_invariants=1)

@@ -37,3 +37,25 @@ def test_no_device_reported(built):
         pytest.skip("a GPU is visible")
     rc, out, err = _run("--w", "8", "--h", "8")
     assert rc == 1 and "No CUDA devices found." in err
+
+
+@pytest.mark.parametrize("args", [
+    ["--precision", "mixed", "--integrator", "rkf78"],
+    ["--precision", "mixed", "--crossing", "root"],
+    ["--mode", "research", "--precision", "mixed"],
+])
+def test_research_settings_need_fp64(built, args):
+    """The embedded 7(8) integrator and root-found crossings run on the FP64
+    path only; the CLI refuses them with --precision mixed before touching a
+    device."""
+    rc, out, err = _run("--w", "8", "--h", "8", *args)
+    assert rc == 1 and err.strip() == "The rkf78 integrator and root crossings need --precision fp64."
+
+
+@pytest.mark.parametrize("args,msg", [
+    (["--inv-gate", "-1"], "Invalid invariant gate."),
+    (["--inv-gate", "2"], "Invalid invariant gate."),
+])
+def test_invalid_research_arguments(built, args, msg):
+    rc, out, err = _run("--w", "8", "--h", "8", *args)
+    assert rc == 1 and err.strip() == msg
