@@ -19,7 +19,11 @@
  *   Doppler factor ............. include/bh_kerr.h:833-862
  * plus the benchmark-scene extensions (lengths in M, stratified seeded
  * jitter, r^-q emissivity, configurable disk edges / escape radius / step
- * cap, cubic-Hermite crossing location) that the CUDA path also implements.
+ * cap, cubic-Hermite crossing location) that the CUDA path also implements,
+ * and the research mode of the reference's accuracy plan (docs/PLAN.md:
+ * 35-66): Fehlberg's embedded 7(8) pair (NASA TR R-287, 1968) as a plain
+ * tableau loop, the invariant gate on each step's change of H and Carter's
+ * Q, root-found crossings and the per-ray drift report.
  *
  * Compile with -ffp-contract=off so that no fused multiply-add changes the
  * rounding between x86 and Arm hosts.
