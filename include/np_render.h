@@ -348,6 +348,14 @@ int np_frame_add_pass(np_frame_t* f, const np_scene_t* scene, int precision, np_
 int np_frame_spp(const np_frame_t* f);
 int np_frame_tonemap(np_frame_t* f, float exposure_ev, float gamma, int reinhard, unsigned char* h_rgb8);
 int np_frame_read(np_frame_t* f, float* h_rgb_mean, float* h_rcross, float* h_inv3);
+/* Accumulator state for checkpoint/resume (host buffers): colour sums
+ * [3][H][W] (not means), the first-crossing radius [H][W], the invariant
+ * maxima [3] and the samples accumulated.  A frame loaded with a saved
+ * state and given the same further passes ends bit-identical to one that
+ * was never interrupted (the passes' sample indices continue from spp).
+ * h_rcross and h_inv3 may be NULL (load: zeros). */
+int np_frame_save(np_frame_t* f, float* h_sum, float* h_rcross, float* h_inv3, int* spp);
+int np_frame_load(np_frame_t* f, const float* h_sum, const float* h_rcross, const float* h_inv3, int spp);
 
 /* ------------------------------------------------------------------------
  * Schwarzschild deflection table (schwarzschild_blackhole.cu:44-266):

@@ -1721,6 +1721,41 @@ int np_frame_tonemap(np_frame_t* f, float exposure_ev, float gamma, int reinhard
     return NP_OK;
 }
 
+int np_frame_save(np_frame_t* f, float* h_sum, float* h_rcross, float* h_inv3, int* spp) {
+    if (!f || !h_sum || !spp) return fail(NP_ERR_INVALID, "NULL argument");
+    const size_t np_ = (size_t)f->W * f->H;
+    NP_CU(cudaMemcpyAsync(h_sum, f->d_sum, 3 * np_ * sizeof(float), cudaMemcpyDeviceToHost, f->stream),
+          NP_ERR_KERNEL);
+    if (h_rcross)
+        NP_CU(cudaMemcpyAsync(h_rcross, f->d_rc, np_ * sizeof(float), cudaMemcpyDeviceToHost, f->stream),
+              NP_ERR_KERNEL);
+    if (h_inv3)
+        NP_CU(cudaMemcpyAsync(h_inv3, f->d_inv, 3 * sizeof(float), cudaMemcpyDeviceToHost, f->stream), NP_ERR_KERNEL);
+    NP_CU(cudaStreamSynchronize(f->stream), NP_ERR_KERNEL);
+    *spp = f->spp_done;
+    return NP_OK;
+}
+
+int np_frame_load(np_frame_t* f, const float* h_sum, const float* h_rcross, const float* h_inv3, int spp) {
+    if (!f || !h_sum) return fail(NP_ERR_INVALID, "NULL argument");
+    if (spp < 0) return fail(NP_ERR_INVALID, "negative sample count");
+    const size_t np_ = (size_t)f->W * f->H;
+    NP_CU(cudaMemcpyAsync(f->d_sum, h_sum, 3 * np_ * sizeof(float), cudaMemcpyHostToDevice, f->stream),
+          NP_ERR_KERNEL);
+    if (h_rcross)
+        NP_CU(cudaMemcpyAsync(f->d_rc, h_rcross, np_ * sizeof(float), cudaMemcpyHostToDevice, f->stream),
+              NP_ERR_KERNEL);
+    else
+        NP_CU(cudaMemsetAsync(f->d_rc, 0, np_ * sizeof(float), f->stream), NP_ERR_KERNEL);
+    if (h_inv3)
+        NP_CU(cudaMemcpyAsync(f->d_inv, h_inv3, 3 * sizeof(float), cudaMemcpyHostToDevice, f->stream), NP_ERR_KERNEL);
+    else
+        NP_CU(cudaMemsetAsync(f->d_inv, 0, 4 * sizeof(float), f->stream), NP_ERR_KERNEL);
+    NP_CU(cudaStreamSynchronize(f->stream), NP_ERR_KERNEL);
+    f->spp_done = spp;
+    return NP_OK;
+}
+
 int np_frame_read(np_frame_t* f, float* h_rgb_mean, float* h_rcross, float* h_inv3) {
     if (!f) return fail(NP_ERR_INVALID, "frame is NULL");
     if (f->spp_done <= 0) return fail(NP_ERR_INVALID, "no pass rendered");

@@ -24,6 +24,12 @@
 //   --benchmark         the 1280x720, a=0.9 benchmark scene (other flags may follow)
 //   --out-raw FILE      float32 mean RGB [3][H][W] and first-crossing radius [H][W]
 //   --json FILE         a sidecar with the scene, passes and timings
+//   --accum-out FILE    the accumulator (colour sums, first-crossing radius,
+//                       invariant maxima, samples done) at every checkpoint
+//   --resume FILE       continue from such a file to --spp-total; the result
+//                       is bit-identical to an uninterrupted run with the same
+//                       --samples per pass
+#include <algorithm>
 #include <cctype>
 #include <cmath>
 #include <cstdio>
@@ -55,6 +61,8 @@ struct Cli {
     int precision = NP_PREC_FP64;
     const char* out_raw = nullptr;
     const char* json = nullptr;
+    const char* accum_out = nullptr;
+    const char* resume = nullptr;
     bool rin_isco = false;
     bool integrator_set = false, rtol_set = false, atol_set = false, crossing_set = false, gate_set = false;
     bool precision_set = false;
@@ -90,6 +98,49 @@ bool write_ppm(const char* path, int w, int h, const std::vector<unsigned char>&
     size_t n = std::fwrite(rgb.data(), 1, rgb.size(), f);
     std::fclose(f);
     return n == rgb.size();
+}
+
+// Accumulator file: u32 "NPAC", version 1, W, H, samples done; then float
+// colour sums [3][H][W], first-crossing radius [H][W], invariant maxima [3].
+struct Accum {
+    int w = 0, h = 0, spp = 0;
+    std::vector<float> sum, rc, inv;
+};
+constexpr unsigned kAccumMagic = 0x4341504eu;   // "NPAC"
+
+bool write_accum(const char* path, const Accum& a) {
+    FILE* f = std::fopen(path, "wb");
+    if (!f) return false;
+    const unsigned hdr[5] = {kAccumMagic, 1u, (unsigned)a.w, (unsigned)a.h, (unsigned)a.spp};
+    bool ok = std::fwrite(hdr, sizeof(hdr), 1, f) == 1 &&
+              std::fwrite(a.sum.data(), sizeof(float), a.sum.size(), f) == a.sum.size() &&
+              std::fwrite(a.rc.data(), sizeof(float), a.rc.size(), f) == a.rc.size() &&
+              std::fwrite(a.inv.data(), sizeof(float), a.inv.size(), f) == a.inv.size();
+    ok = (std::fclose(f) == 0) && ok;
+    return ok;
+}
+
+// Reads an accumulator file for a w x h frame; returns an error message or "".
+std::string read_accum(const char* path, int w, int h, Accum& a) {
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return std::string("Cannot read ") + path + ".";
+    unsigned hdr[5];
+    std::string err;
+    if (std::fread(hdr, sizeof(hdr), 1, f) != 1 || hdr[0] != kAccumMagic || hdr[1] != 1u) {
+        err = std::string(path) + " is not an accumulator file.";
+    } else if ((int)hdr[2] != w || (int)hdr[3] != h) {
+        err = std::string(path) + " holds a different image size.";
+    } else {
+        const size_t npix = (size_t)w * h;
+        a.w = w; a.h = h; a.spp = (int)hdr[4];
+        a.sum.resize(3 * npix); a.rc.resize(npix); a.inv.resize(3);
+        if (std::fread(a.sum.data(), sizeof(float), a.sum.size(), f) != a.sum.size() ||
+            std::fread(a.rc.data(), sizeof(float), a.rc.size(), f) != a.rc.size() ||
+            std::fread(a.inv.data(), sizeof(float), a.inv.size(), f) != a.inv.size())
+            err = std::string(path) + " is truncated.";
+    }
+    std::fclose(f);
+    return err;
 }
 
 bool write_raw(const char* path, int w, int h, int spp, const std::vector<float>& rgb, const std::vector<float>& rc) {
@@ -172,6 +223,8 @@ void parse(int argc, char** argv, Cli& c) {
         else if (a == "--islands") n(s.islands);
         else if (a == "--out-raw") str(c.out_raw);
         else if (a == "--json") str(c.json);
+        else if (a == "--accum-out") str(c.accum_out);
+        else if (a == "--resume") str(c.resume);
     }
 }
 
@@ -219,6 +272,15 @@ int main(int argc, char** argv) {
     if (c.rin_isco) s.disk_rin = np_isco_radius(s.mass, s.spin);
     const bool reinhard = lower(c.tonemap) == "reinhard";
     if (np_scene_validate(&s) != NP_OK) { std::fprintf(stderr, "%s\n", np_last_error()); return 1; }
+    if ((c.resume || c.accum_out) && c.frames > 1) {
+        std::fprintf(stderr, "--resume and --accum-out need a single frame.\n");
+        return 1;
+    }
+    Accum resumed;
+    if (c.resume) {
+        std::string err = read_accum(c.resume, s.width, s.height, resumed);
+        if (!err.empty()) { std::fprintf(stderr, "%s\n", err.c_str()); return 1; }
+    }
 
     np_frame_t* fr = np_frame_create(s.width, s.height, nullptr);
     if (!fr) { std::fprintf(stderr, "%s\n", np_last_error()); return 1; }
@@ -231,22 +293,43 @@ int main(int argc, char** argv) {
     auto render_one = [&](double phi_deg, const char* path) -> bool {
         const int total = c.spp_total > 0 ? c.spp_total : c.samples;
         const int batch = c.samples > 1 ? c.samples : 1;
-        const int passes = (total + batch - 1) / batch;
         np_frame_reset(fr);
+        if (c.resume && np_frame_load(fr, resumed.sum.data(), resumed.rc.data(), resumed.inv.data(),
+                                      resumed.spp) != NP_OK) {
+            std::fprintf(stderr, "%s\n", np_last_error());
+            return false;
+        }
+        const int remaining = std::max(0, total - np_frame_spp(fr));
+        const int passes = std::max(1, (remaining + batch - 1) / batch);
         np_scene_t ps = s;
         ps.phi_deg = phi_deg;
         for (int p = 0; p < passes; ++p) {
-            ps.spp = std::min(batch, total - np_frame_spp(fr));
-            np_render_stats_t st{};
-            if (np_frame_add_pass(fr, &ps, c.precision, &st) != NP_OK) {
-                std::fprintf(stderr, "%s\n", np_last_error());
-                return false;
+            if (remaining == 0) {
+                // the accumulator already holds the requested samples: write it out
+                if (np_frame_spp(fr) <= 0) { std::fprintf(stderr, "Nothing to render.\n"); return false; }
+            } else {
+                ps.spp = std::min(batch, total - np_frame_spp(fr));
+                np_render_stats_t st{};
+                if (np_frame_add_pass(fr, &ps, c.precision, &st) != NP_OK) {
+                    std::fprintf(stderr, "%s\n", np_last_error());
+                    return false;
+                }
+                kernel_ms += st.kernel_ms + st.init_ms;
+                rays += st.rays; steps += st.steps;
+                ++passes_done;
             }
-            kernel_ms += st.kernel_ms + st.init_ms;
-            rays += st.rays; steps += st.steps;
-            ++passes_done;
             const bool ckpt = p == passes - 1 || (c.checkpoint_every > 0 && (p + 1) % c.checkpoint_every == 0);
             if (!ckpt) continue;
+            if (c.accum_out) {
+                Accum a;
+                a.w = s.width; a.h = s.height;
+                a.sum.resize(3 * npix); a.rc.resize(npix); a.inv.resize(3);
+                if (np_frame_save(fr, a.sum.data(), a.rc.data(), a.inv.data(), &a.spp) != NP_OK ||
+                    !write_accum(c.accum_out, a)) {
+                    std::fprintf(stderr, "Failed to write %s\n", c.accum_out);
+                    return false;
+                }
+            }
             if (np_frame_tonemap(fr, c.exposure_ev, c.gamma, reinhard ? 1 : 0, rgb8.data()) != NP_OK) {
                 std::fprintf(stderr, "%s\n", np_last_error());
                 return false;

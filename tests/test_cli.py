@@ -59,3 +59,24 @@ def test_research_settings_need_fp64(built, args):
 def test_invalid_research_arguments(built, args, msg):
     rc, out, err = _run("--w", "8", "--h", "8", *args)
     assert rc == 1 and err.strip() == msg
+
+
+def test_resume_file_checks(built, tmp_path):
+    """--resume reads and checks the accumulator file before any device work."""
+    import struct
+    rc, out, err = _run("--w", "8", "--h", "8", "--resume", str(tmp_path / "absent.npac"))
+    assert rc == 1 and err.strip() == "Cannot read %s." % (tmp_path / "absent.npac")
+    bad = tmp_path / "bad.npac"
+    bad.write_bytes(b"not an accumulator")
+    rc, out, err = _run("--w", "8", "--h", "8", "--resume", str(bad))
+    assert rc == 1 and err.strip() == "%s is not an accumulator file." % bad
+    other = tmp_path / "other.npac"
+    other.write_bytes(struct.pack("<5I", 0x4341504E, 1, 4, 4, 2) + b"\0" * 4 * (3 * 16 + 16 + 3))
+    rc, out, err = _run("--w", "8", "--h", "8", "--resume", str(other))
+    assert rc == 1 and err.strip() == "%s holds a different image size." % other
+    short = tmp_path / "short.npac"
+    short.write_bytes(struct.pack("<5I", 0x4341504E, 1, 8, 8, 2) + b"\0" * 16)
+    rc, out, err = _run("--w", "8", "--h", "8", "--resume", str(short))
+    assert rc == 1 and err.strip() == "%s is truncated." % short
+    rc, out, err = _run("--w", "8", "--h", "8", "--frames", "3", "--accum-out", str(tmp_path / "a.npac"))
+    assert rc == 1 and err.strip() == "--resume and --accum-out need a single frame."

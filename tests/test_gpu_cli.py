@@ -80,3 +80,27 @@ def test_cli_frames_and_pattern(cuda, tmp_path):
     bad = subprocess.run([CLI, "--w", "8", "--h", "8", "--frames", "2", "--outpat", str(tmp_path / "x_%d_%d.ppm")],
                          capture_output=True, text=True, timeout=120)
     assert bad.returncode == 1 and "Invalid --outpat" in bad.stderr
+
+
+def test_resume_is_bit_identical(cuda, tmp_path):
+    """An interrupted render resumed from its accumulator file ends
+    bit-identical to the uninterrupted one (same --samples per pass)."""
+    common = ["--w", "40", "--h", "24", "--samples", "2", "--spin", "0.7", "--theta", "70", "--precision", "mixed"]
+    full_raw, full_ppm = str(tmp_path / "full.raw"), str(tmp_path / "full.ppm")
+    p = subprocess.run([CLI] + common + ["--spp-total", "8", "--out", full_ppm, "--out-raw", full_raw],
+                       capture_output=True, text=True, timeout=300)
+    assert p.returncode == 0, p.stderr
+    acc = str(tmp_path / "half.npac")
+    p = subprocess.run([CLI] + common + ["--spp-total", "4", "--out", str(tmp_path / "half.ppm"),
+                                         "--accum-out", acc], capture_output=True, text=True, timeout=300)
+    assert p.returncode == 0, p.stderr
+    res_raw, res_ppm = str(tmp_path / "res.raw"), str(tmp_path / "res.ppm")
+    p = subprocess.run([CLI] + common + ["--spp-total", "8", "--resume", acc, "--out", res_ppm, "--out-raw", res_raw],
+                       capture_output=True, text=True, timeout=300)
+    assert p.returncode == 0, p.stderr
+    assert p.stdout.strip().splitlines()[-2].split("@")[1].strip() == "8 spp"
+    m1, r1, s1 = _read_raw(full_raw)
+    m2, r2, s2 = _read_raw(res_raw)
+    assert s1 == s2 == 8
+    assert np.array_equal(m1, m2) and np.array_equal(r1, r2)
+    assert np.array_equal(_read_ppm(full_ppm), _read_ppm(res_ppm))
