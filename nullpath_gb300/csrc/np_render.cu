@@ -776,12 +776,13 @@ int np_scene_validate(const np_scene_t* s) {
     if (s->width <= 0 || s->height <= 0) return fail(NP_ERR_INVALID, "Invalid image dimensions.");
     if (s->spp <= 0) return fail(NP_ERR_INVALID, "Invalid samples per pixel.");
     if (s->sample_offset < 0) return fail(NP_ERR_INVALID, "Invalid sample offset.");
-    if (!(s->mass > 0.0) || !(s->r_cam > 0.0)) return fail(NP_ERR_INVALID, "Invalid mass or camera radius.");
+    if (!(s->mass > 0.0) || !(s->r_cam > 0.0) || !std::isfinite(s->mass) || !std::isfinite(s->r_cam))
+        return fail(NP_ERR_INVALID, "Invalid mass or camera radius.");
     if (!(std::fabs(s->spin) < 1.0)) return fail(NP_ERR_INVALID, "Spin must satisfy |a/M| < 1.");
     if (!(s->fov_y_deg > 0.0 && s->fov_y_deg < 179.0))
         return fail(NP_ERR_INVALID, "Invalid FOV; expected (0, 179) degrees.");
     if (s->max_steps <= 0) return fail(NP_ERR_INVALID, "Invalid step cap.");
-    if (!(s->step_scale > 0.0)) return fail(NP_ERR_INVALID, "Invalid step scale.");
+    if (!(s->step_scale > 0.0) || !std::isfinite(s->step_scale)) return fail(NP_ERR_INVALID, "Invalid step scale.");
     if (s->units != NP_UNITS_RS && s->units != NP_UNITS_M) return fail(NP_ERR_INVALID, "Invalid units.");
     if (s->jitter != NP_JITTER_WANGHASH && s->jitter != NP_JITTER_STRATIFIED && s->jitter != NP_JITTER_CRITICAL)
         return fail(NP_ERR_INVALID, "Invalid jitter mode.");
@@ -790,6 +791,15 @@ int np_scene_validate(const np_scene_t* s) {
     if (s->crossing != NP_CROSS_LINEAR && s->crossing != NP_CROSS_HERMITE && s->crossing != NP_CROSS_ROOT)
         return fail(NP_ERR_INVALID, "Invalid crossing mode.");
     if (!(s->inv_gate >= 0.0 && s->inv_gate < 1.0)) return fail(NP_ERR_INVALID, "Invalid invariant gate.");
+    // non-finite values in any other field would only surface as NaN images
+    auto fin = [](double v) { return std::isfinite(v); };
+    if (!fin(s->theta_deg) || !fin(s->phi_deg)) return fail(NP_ERR_INVALID, "Invalid camera angle.");
+    if (!(s->rtol > 0.0) || !(s->atol >= 0.0) || !fin(s->rtol) || !fin(s->atol))
+        return fail(NP_ERR_INVALID, "Invalid tolerances.");
+    if (!fin(s->escape_r)) return fail(NP_ERR_INVALID, "Invalid escape radius.");
+    if (!fin(s->disk_rin) || !fin(s->disk_rout) || !fin(s->emissivity_q) || !fin(s->disk_gain))
+        return fail(NP_ERR_INVALID, "Invalid disk parameters.");
+    if (!fin(s->bg_sigma_deg) || !fin(s->bg_brightness)) return fail(NP_ERR_INVALID, "Invalid background parameters.");
     if ((long long)s->width * s->height > (1ll << 40) / std::max(1, s->spp))
         return fail(NP_ERR_INVALID, "Image too large.");
     return NP_OK;

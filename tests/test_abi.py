@@ -116,3 +116,23 @@ def test_uneven_scene_draws():
     assert all(1 <= s.spp <= 8 and 1 <= s.disk_max_orders <= 3 for s in a)
     assert all(0.0 <= s.spin <= 0.998 and 5.0 <= s.theta_deg <= 85.0 for s in a)
     assert {s.width for s in a} == set(RESOLUTIONS)
+
+
+def test_non_finite_fields_are_rejected(built):
+    """Fault injection on the host: NaN or infinite values in any floating
+    field of the scene are refused with NP_ERR_INVALID and a message, before
+    any device work."""
+    lib = npx.load()
+    base = npx.benchmark_scene(width=8, height=8, spp=1)
+    assert lib.np_scene_validate(C.byref(base)) == 0
+    nan, inf = float("nan"), float("inf")
+    for f, typ in Scene._fields_:
+        if typ is not C.c_double:
+            continue
+        for v in (nan, inf, -inf):
+            t = base.replace(**{f: v})
+            assert lib.np_scene_validate(C.byref(t)) == npx._abi.NP_ERR_INVALID, (f, v)
+            assert lib.np_last_error(), f
+    # tolerances must be positive (rtol) and non-negative (atol)
+    assert lib.np_scene_validate(C.byref(base.replace(rtol=0.0))) == npx._abi.NP_ERR_INVALID
+    assert lib.np_scene_validate(C.byref(base.replace(atol=-1.0))) == npx._abi.NP_ERR_INVALID
