@@ -354,7 +354,9 @@ def run_ours(args):
         npx.render(sc, args.precision, rgb=rgb, rcross=rc)
     torch.cuda.synchronize()
 
-    clock_path = os.path.join(ROOT, "gpurun_out", "bench_clocks_rank%d.csv" % rank)
+    import tempfile
+    clock_path = os.path.join(os.environ.get("NP_BENCH_CLOCKS_DIR", tempfile.gettempdir()),
+                              "np_bench_clocks_rank%d.csv" % rank)
     os.makedirs(os.path.dirname(clock_path), exist_ok=True)
     sampler, fh = _clock_sampler(clock_path)
 
