@@ -305,7 +305,7 @@ def run_reference(args):
     desc = None
     cores = os.cpu_count()
     for i in range(args.warmup + args.steps):
-        v, cores, desc = cpu_baseline(rows_every=90)
+        v, cores, desc = cpu_baseline(rows_every=args.ref_rows_every)
         if i >= args.warmup:
             per_step.append(v)
     val = statistics.mean(per_step)
@@ -504,6 +504,8 @@ def main():
     ap.add_argument("--no-fp64-frame", dest="fp64_frame", action="store_false")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--no-accuracy", dest="accuracy", action="store_false")
+    ap.add_argument("--ref-rows-every", type=int, default=90,
+                    help="reference arm: time every n-th row of the frame per step")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
