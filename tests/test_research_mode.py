@@ -152,3 +152,41 @@ def test_cli_research_mode_refuses_mixed(built):
     p = subprocess.run([cli, "--mode", "research", "--precision", "mixed", "--w", "8", "--h", "8"],
                        capture_output=True, text=True, timeout=60)
     assert p.returncode == 1 and "precision fp64" in p.stderr
+
+
+def test_research_in_reference_units_and_zamo(built):
+    """Research mode on a reference-default scene (lengths in Rs, M = 10,
+    static camera) and on the ZAMO camera of research_scene(): crossing radii
+    against the Mino-time solver.  The reference's camera builds the ray
+    direction in FP32 (render.cu:137-159), so its momentum is null only to
+    ~1e-7 and the Mino-time constants describe a slightly different ray:
+    there the bar is 1e-6; in units of M (FP64 camera) it is 1e-10."""
+    from nullpath_gb300._abi import reference_defaults, research_scene
+    rng = np.random.default_rng(5)
+    for sc in (reference_defaults().replace(width=32, height=18, spp=1, spin=0.9, theta_deg=80.0, fov_y_deg=55.0,
+                                            integrator=NP_INTEG_RKF78, crossing=NP_CROSS_ROOT, rtol=1e-12,
+                                            atol=1e-14, inv_gate=1e-12),
+               research_scene(benchmark_scene(width=32, height=18, spp=1))):
+        px, py = rng.uniform(0, sc.width, 120), rng.uniform(0, sc.height, 120)
+        o = oracle.trace_rays(sc, px, py)
+        M = sc.mass
+        csc = sc
+        if sc.units == 0:
+            # reference scenes set the camera and the spin up in float
+            # (render.cu:137-139, 161-170): theta = fl(fl(theta) fl(pi)) / 180,
+            # a = fl(fl(a/M) M)
+            th = np.float32(np.float32(sc.theta_deg) * np.float32(np.pi)) / np.float32(180.0)
+            af = np.float32(np.float32(sc.spin) * np.float32(M))
+            csc = sc.replace(theta_deg=float(th) * 180.0 / np.pi, spin=float(af) / M)
+        u0, mu0, l, q2, su, sm = gk.render_ray_constants(o["consts"], csc)
+        lunit = M if sc.units == 1 else 2.0 * M
+        r_far = sc.escape_r if sc.escape_r > 0 else (sc.r_cam + 10.0) * lunit
+        errs = []
+        for i in range(len(px)):
+            k, xu, _ = oracle.geokerr_crossings(u0[i], mu0[i], csc.spin, l[i], q2[i], su[i], sm[i], M / r_far, 4)
+            n = min(k, int(o["status"][i]) >> 4, 4)
+            for j in range(n):
+                r_ref = M / xu[j]
+                errs.append(abs(o["cross"][i, j, 0] - r_ref) / r_ref)
+        bar = 1e-6 if sc.units == 0 else 1e-10
+        assert len(errs) > 20 and max(errs) < bar, (sc.units, len(errs), max(errs))
