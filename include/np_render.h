@@ -36,7 +36,7 @@
 extern "C" {
 #endif
 
-#define NP_ABI_VERSION 2
+#define NP_ABI_VERSION 3
 
 typedef enum np_status {
     NP_OK = 0,
@@ -54,17 +54,31 @@ typedef enum np_units { NP_UNITS_RS = 0, NP_UNITS_M = 1 } np_units;
  * a pass are near-critical (importance sampling of the photon ring). */
 typedef enum np_jitter { NP_JITTER_WANGHASH = 0, NP_JITTER_STRATIFIED = 1, NP_JITTER_CRITICAL = 2 } np_jitter;
 typedef enum np_camera { NP_CAMERA_STATIC = 0, NP_CAMERA_ZAMO = 1 } np_camera;
-/* NP_INTEG_RKF78: research mode (FP64 only).  Fehlberg's embedded 7(8)
- * pair, the 8th-order solution propagated, error control on (r, theta, phi,
- * p_r, p_theta, p_phi) with the scene's rtol/atol, and, when inv_gate > 0,
- * invariant-gated acceptance: a step is also rejected (h halved) when its
- * change of the Hamiltonian, relative to the sum of the Hamiltonian's
- * absolute terms, or its change of Carter's constant Q, relative to
- * max(|Q0|, (E M)^2), exceeds inv_gate. */
+/* NP_INTEG_RKF78: Fehlberg's embedded 7(8) pair, the 8th-order solution
+ * propagated, one attempt per scheduling pass of a lane.
+ *   NP_PREC_FP64   research mode: error control on (r, theta, phi, p_r,
+ *                  p_theta, p_phi) with the scene's rtol/atol, and, when
+ *                  inv_gate > 0, invariant-gated acceptance: a step is also
+ *                  rejected (h halved) when its change of the Hamiltonian,
+ *                  relative to the sum of the Hamiltonian's absolute terms,
+ *                  or its change of Carter's constant Q, relative to
+ *                  max(|Q0|, (E M)^2), exceeds inv_gate.
+ *   NP_PREC_MIXED  the Carter-form system in compensated FP32, error control
+ *                  on (r, theta, p_r, p_theta) with rtol and atol (atol at
+ *                  least 1e-9 M); FP64 islands take 7(8) steps at rtol,
+ *                  near-critical rays are traced whole in FP64 at
+ *                  rtol_fp64, and a ray inside the horizon band that
+ *                  provably falls in (no radial turning point left) ends
+ *                  there.  inv_gate is not used.  With NP_CROSS_ROOT a
+ *                  crossing is landed on the equator by one more 7(8) step
+ *                  in theta (Henon's method). */
 typedef enum np_integrator { NP_INTEG_RK4 = 0, NP_INTEG_ADAPTIVE = 1, NP_INTEG_RKF78 = 2 } np_integrator;
-/* NP_CROSS_ROOT (FP64 only): theta = pi/2 located by bracketed root finding
- * on re-integrations of the crossing step from its start, so the crossing is
- * as accurate as the integrator itself (no interpolant error). */
+/* NP_CROSS_ROOT: the crossing is as accurate as the integrator itself (no
+ * interpolant error).  FP64 path: theta = pi/2 located by bracketed root
+ * finding on re-integrations of the crossing step from its start.  Mixed
+ * path (NP_INTEG_RKF78 only): one 7(8) step from the crossing step's start
+ * with theta as the independent variable lands on theta = pi/2 exactly
+ * (M. Henon, Physica D 5, 1982). */
 typedef enum np_crossing { NP_CROSS_LINEAR = 0, NP_CROSS_HERMITE = 1, NP_CROSS_ROOT = 2 } np_crossing;
 typedef enum np_background { NP_BG_GRADIENT = 0, NP_BG_POINT = 1 } np_background;
 
@@ -119,6 +133,9 @@ typedef struct np_scene {
     int32_t check_invariants;     /* render.cu:32 */
     int32_t islands;              /* NP_ISLAND_* mask of the mixed path */
     double inv_gate;              /* NP_INTEG_RKF78 invariant gate; <= 0 disables */
+    double rtol_fp64;             /* rtol of the near-critical rays the mixed 7(8) path traces
+                                     whole in FP64; <= 0 means min(rtol, 1e-10) (its island steps
+                                     keep rtol) */
 } np_scene_t;
 
 /* Per-call statistics, filled when the pointer is non-NULL. */
@@ -259,11 +276,15 @@ int np_render_device_noalloc(const np_scene_t* scene, int precision,
  *   NP_TUNE_CHUNK         ray indices a warp takes per atomic (default 64)
  *   NP_TUNE_CROSS_BATCH   lanes of a warp with a pending root-found crossing
  *                         (NP_CROSS_ROOT, FP64 path) that trigger the search
- *                         of all of them (1-32, default 12; 1 = at once) */
+ *                         of all of them (1-32, default 12; 1 = at once)
+ *   NP_TUNE_MIN_BLOCKS78  register cap of the mixed 7(8) tracer (3 or 4;
+ *                         default 3: its FP32 loop, with the FP64 island
+ *                         step inlined, needs about 168 registers) */
 #define NP_TUNE_ISLAND_BATCH 1
 #define NP_TUNE_MIN_BLOCKS 2
 #define NP_TUNE_CHUNK 3
 #define NP_TUNE_CROSS_BATCH 4
+#define NP_TUNE_MIN_BLOCKS78 5
 int np_tune(int param, int value);
 
 /* Measures the sustained FMA throughput of this GPU's SIMT pipes with a

@@ -2,6 +2,8 @@
 
 Public Python surface (a thin layer over include/np_render.h):
     Scene, reference_defaults(), benchmark_scene()   scene description
+    accurate_scene(scene)                            the same scene on the mixed 7(8) path (FP32 under
+                                                     error control, Henon crossings)
     research_scene(scene)                            the same scene in research mode (FP64 7(8))
     render(scene, precision)                         device render (torch tensors)
     render_host(scene, precision)                    host buffers in, host buffers out
@@ -9,7 +11,7 @@ Public Python surface (a thin layer over include/np_render.h):
     trace_invariants(scene, px, py)                  per-ray drift of H and Carter's Q (FP64)
 """
 from ._abi import (Scene, RenderStats, isco_radius, reference_defaults, benchmark_scene, research_scene,
-                   NP_PREC_FP64, NP_PREC_MIXED, NP_UNITS_RS, NP_UNITS_M,
+                   accurate_scene, NP_PREC_FP64, NP_PREC_MIXED, NP_UNITS_RS, NP_UNITS_M,
                    NP_JITTER_WANGHASH, NP_JITTER_STRATIFIED, NP_JITTER_CRITICAL, NP_CAMERA_STATIC, NP_CAMERA_ZAMO,
                    NP_INTEG_RK4, NP_INTEG_ADAPTIVE, NP_INTEG_RKF78, NP_CROSS_LINEAR, NP_CROSS_HERMITE,
                    NP_CROSS_ROOT,
@@ -20,6 +22,6 @@ from .render import render, render_host, trace_rays, trace_invariants, precision
 
 __all__ = [
     "Scene", "RenderStats", "isco_radius", "reference_defaults", "benchmark_scene", "research_scene",
-    "render", "render_host", "trace_rays", "trace_invariants", "precision_code", "load", "lib_path", "NullPathError",
+    "accurate_scene", "render", "render_host", "trace_rays", "trace_invariants", "precision_code", "load", "lib_path", "NullPathError",
     "NP_PREC_FP64", "NP_PREC_MIXED",
 ]

@@ -54,6 +54,9 @@ struct SceneDev {
     float hmin_f, hmax_f, rtol_f, atol_f;
     double hmin, hmax;         // adaptive step bounds (hmax scales with r in units of M)
     double inv_gate;           // invariant gate of the embedded 7(8) integrator (0 = off)
+    double rtol64;             // rtol of the FP64 7(8) islands and near-critical rays of the mixed path
+    float atol78_f;            // atol of the FP32 7(8) steps: the scene's, at least 1e-9 M (FP32 resolution)
+    int cert_capture;          // 7(8) path: rays certified to fall in end at the horizon band (disk outside it)
     int island_batch;
     int cross_batch;           // pending root-found crossings that trigger a warp's search (FP64 tracer)
     // NP_JITTER_CRITICAL: tangent-plane radius of the critical curve at

@@ -18,6 +18,7 @@
 #include <mutex>
 #include <string>
 #include <vector>
+#include <type_traits>
 
 #include "np_common.cuh"
 #include "tracer_fp64.cuh"
@@ -67,6 +68,7 @@ struct Tuning {
     // 12 lanes gave 329 / 367 / 393 / 402 k rays/s.
     int cross_batch = 12;
     int min_blocks = 4;     // register cap of the mixed tracer (blocks of 128 per SM)
+    int min_blocks78 = 3;   // the same for the mixed 7(8) tracer
     int chunk = 64;         // ray indices a warp takes from the global counter at once
 };
 Tuning g_tune;
@@ -151,6 +153,7 @@ int prepare_scene(const np_scene_t& sc, SceneDev& d) {
     d.check_inv = sc.check_invariants;
     d.islands = sc.islands;
     d.inv_gate = sc.inv_gate > 0.0 ? sc.inv_gate : 0.0;
+    d.rtol64 = sc.rtol_fp64 > 0.0 ? sc.rtol_fp64 : std::fmin(sc.rtol, 1e-10);
     // Step doubling at a tight rtol works at the FP32 precision floor where p_r
     // or p_theta changes sign; its turning-point steps are always FP64.
     if (sc.integrator == NP_INTEG_ADAPTIVE) d.islands |= NP_ISLAND_TURNING;
@@ -200,6 +203,8 @@ int prepare_scene(const np_scene_t& sc, SceneDev& d) {
         else { d.hmin = kHMin * d.M; d.hmax = 10.0 * d.h_unit; }
         d.hmin_f = (float)d.hmin; d.hmax_f = (float)d.hmax;
         d.rtol_f = (float)d.rtol; d.atol_f = (float)d.atol;
+        d.atol78_f = (float)std::fmax(d.atol, 1e-9 * d.M);
+        d.cert_capture = !d.disk_on || d.rin > d.r_plus + kHorizonBand * d.M;
         d.island_batch = g_tune.island_batch;
         d.cross_batch = g_tune.cross_batch;
     }
@@ -407,7 +412,12 @@ __device__ __forceinline__ void load_ray(const InitSoA& soa, long long i, MRay<f
 // overlaps the FP32 work of the rest of the grid); every warp then traces
 // FP32 rays from the shared counter, lanes refilling independently and
 // parked island steps executed in batches.
-template <int MINB>
+// Integrator families of the mixed tracer (one kernel instantiation each, so
+// the 7(8) stage storage does not raise the register count of the RK4 loop).
+constexpr int kFamRk4 = 0;   // fixed RK4 and step doubling
+constexpr int kFam78 = 1;    // embedded 7(8)
+
+template <int MINB, int FAM>
 __global__ void __launch_bounds__(kBlock, MINB)
 render_mixed_kernel(const SceneDev s, const InitSoA soa, float* __restrict__ srgb, float* __restrict__ rcross,
                     float* __restrict__ inv3, Counters* __restrict__ ctr, int chunk) {
@@ -421,7 +431,7 @@ render_mixed_kernel(const SceneDev s, const InitSoA soa, float* __restrict__ srg
     if ((threadIdx.x >> 5) == 0 && (int)blockIdx.x < nd) {
         WarpQueue q{0, 0};
         bool drained = false, have = false;
-        DRay<false> R;
+        typename std::conditional<FAM == kFam78, DRay78<false>, DRay<false>>::type R;
         long long item = 0, p = 0;
         int sl = 0;
         float cam_y = 0.0f;
@@ -436,16 +446,28 @@ render_mixed_kernel(const SceneDev s, const InitSoA soa, float* __restrict__ srg
                     ray_coords(s, item, p, sl, x, y, sid);
                     float4 a = soa.a[item], b = soa.b[item];
                     cam_y = soa.cy[item];
-                    dray_start(R, s, (double)b.x + (double)b.y, (double)b.z + (double)b.w,
-                               (double)a.x + (double)a.y, (double)a.z + (double)a.w);
+                    if constexpr (FAM == kFam78)
+                        dray78_start(R, s, (double)b.x + (double)b.y, (double)b.z + (double)b.w,
+                                     (double)a.x + (double)a.y, (double)a.z + (double)a.w);
+                    else
+                        dray_start(R, s, (double)b.x + (double)b.y, (double)b.z + (double)b.w,
+                                   (double)a.x + (double)a.y, (double)a.z + (double)a.w);
                     have = true;
                     n_rays++;
                 }
             }
             if (!__any_sync(FULL, have)) break;
             if (have) {
-                bool done = dray_step(R, s);
-                n_steps++; n_f64++; n_evals += 4;
+                bool done;
+                if constexpr (FAM == kFam78) {
+                    bool acc;
+                    done = dray78_step(R, s, acc);
+                    if (acc) { n_steps++; n_f64++; }
+                    n_evals += 12;
+                } else {
+                    done = dray_step(R, s);
+                    n_steps++; n_f64++; n_evals += 4;
+                }
                 if (done) {
                     float col[3];
                     sample_colour(s, R.status == 1, R.orders, R.disk, (float)R.min_r, cam_y, col);
@@ -474,6 +496,7 @@ render_mixed_kernel(const SceneDev s, const InitSoA soa, float* __restrict__ srg
                 ray_coords(s, idx, p, sl, x, y, sid);
                 load_ray(soa, idx, R, cam_y);
                 mray_start(R, s, k);
+                if constexpr (FAM == kFam78) mray_set_k78(R, k);
                 have = true;
                 n_rays++;
                 n_evals++;
@@ -488,17 +511,31 @@ render_mixed_kernel(const SceneDev s, const InitSoA soa, float* __restrict__ srg
         bool done = false;
         if (pend && ((int)__popc(pend) >= T || !act)) {
             if (have && R.pending) {
-                done = mray_island(R, s, k);
-                n_steps++; n_f64++; n_evals += 5;
+                if constexpr (FAM == kFam78) {
+                    int att;
+                    done = mray_island78(R, s, k, att);
+                    n_steps++; n_f64++; n_evals += 13 * (att + 1);
+                } else {
+                    done = mray_island(R, s, k);
+                    n_steps++; n_f64++; n_evals += 5;
+                }
             }
         } else if (have && !R.pending) {
-            // kStepsPerTurn FP32 steps per pass of the scheduling loop: the
-            // ballots and queue checks above are paid once per pass; a lane
-            // that ends or parks early idles for the rest of the pass
+            // kStepsPerTurn FP32 steps (7(8): attempts) per pass of the
+            // scheduling loop: the ballots and queue checks above are paid
+            // once per pass; a lane that ends or parks early idles for the
+            // rest of the pass
 #pragma unroll 1
             for (int j = 0; j < kStepsPerTurn; ++j) {
-                int r = s.integrator == NP_INTEG_ADAPTIVE ? mray_step32_adaptive(R, s, k) : mray_step32(R, s, k);
-                if (r != STEP_PARK) { n_steps++; n_evals += s.integrator == NP_INTEG_ADAPTIVE ? 11 : 4; }
+                int r;
+                if constexpr (FAM == kFam78) {
+                    bool acc;
+                    r = mray_step78(R, s, k, acc);
+                    if (r != STEP_PARK) { n_steps += acc ? 1 : 0; n_evals += 13; }
+                } else {
+                    r = s.integrator == NP_INTEG_ADAPTIVE ? mray_step32_adaptive(R, s, k) : mray_step32(R, s, k);
+                    if (r != STEP_PARK) { n_steps++; n_evals += s.integrator == NP_INTEG_ADAPTIVE ? 11 : 4; }
+                }
                 done = r == STEP_DONE;
                 if (r != STEP_CONT) break;
             }
@@ -554,10 +591,33 @@ __global__ void trace_rays_kernel(const SceneDev s, int precision, int n, const 
         for (int j = 0; j < 4; ++j) { xr[j] = R.xr[j]; xphi[j] = R.xphi[j]; }
         ncross = R.crossings; st = R.status;
     } else if ((s.islands & kIslandCritical) && near_critical(E, L, Q, s.a, s.M, s.r_plus, kCriticalDb)) {
-        DRay<true> R;
-        dray_start(R, s, E, L, m.pr, m.pth);
-        while (!dray_step(R, s)) {}
-        for (int j = 0; j < 4; ++j) { xr[j] = R.xr[j]; xphi[j] = R.xphi[j]; }
+        if (s.integrator == NP_INTEG_RKF78) {
+            DRay78<true> R;
+            dray78_start(R, s, E, L, m.pr, m.pth);
+            bool acc;
+            while (!dray78_step(R, s, acc)) {}
+            for (int j = 0; j < 4; ++j) { xr[j] = R.xr[j]; xphi[j] = R.xphi[j]; }
+            ncross = R.crossings; st = R.status;
+        } else {
+            DRay<true> R;
+            dray_start(R, s, E, L, m.pr, m.pth);
+            while (!dray_step(R, s)) {}
+            for (int j = 0; j < 4; ++j) { xr[j] = R.xr[j]; xphi[j] = R.xphi[j]; }
+            ncross = R.crossings; st = R.status;
+        }
+    } else if (s.integrator == NP_INTEG_RKF78) {
+        const SpaceK k{(float)s.a, (float)(s.a * s.a), (float)s.M, (float)s.r_plus, (float)s.r_minus};
+        MRay<true> R;
+        R.pr = d_hl(m.pr); R.pth = d_hl(m.pth); R.E = d_hl(E); R.L = d_hl(L);
+        mray_start(R, s, k);
+        mray_set_k78(R, k);
+        while (true) {
+            bool acc;
+            int r = mray_step78(R, s, k, acc);
+            if (r == STEP_PARK) { int att; r = mray_island78(R, s, k, att) ? STEP_DONE : STEP_CONT; }
+            if (r == STEP_DONE) break;
+        }
+        for (int j = 0; j < 4; ++j) { xr[j] = R.xr_d[j]; xphi[j] = R.xphi[j]; }
         ncross = R.crossings; st = R.status;
     } else {
         const SpaceK k{(float)s.a, (float)(s.a * s.a), (float)s.M, (float)s.r_plus, (float)s.r_minus};
@@ -692,10 +752,10 @@ void launch_fp64(const SceneDev& s, float* srgb, float* rcross, float* inv3, Cou
     }
 }
 
-template <int MINB>
+template <int MINB, int FAM>
 void launch_mixed_t(const SceneDev& s, const InitSoA& soa, float* srgb, float* rc, float* inv3, Counters* ctr,
                     int chunk, cudaStream_t st) {
-    render_mixed_kernel<MINB><<<grid_for((const void*)render_mixed_kernel<MINB>), kBlock, 0, st>>>(
+    render_mixed_kernel<MINB, FAM><<<grid_for((const void*)render_mixed_kernel<MINB, FAM>), kBlock, 0, st>>>(
         s, soa, srgb, rc, inv3, ctr, chunk);
 }
 
@@ -703,12 +763,18 @@ void launch_mixed_t(const SceneDev& s, const InitSoA& soa, float* srgb, float* r
 // the compiler must fit: 3 -> 170 registers, 4 -> 128, 5 -> 102, 6 -> 85, 8 -> 64).
 void launch_mixed(int minb, const SceneDev& s, const InitSoA& soa, float* srgb, float* rc, float* inv3,
                   Counters* ctr, int chunk, cudaStream_t st) {
+    if (s.integrator == NP_INTEG_RKF78) {
+        // the 7(8) loop holds about nine stage vectors: caps of 3 and 4 blocks only
+        if (g_tune.min_blocks78 == 4) launch_mixed_t<4, kFam78>(s, soa, srgb, rc, inv3, ctr, chunk, st);
+        else launch_mixed_t<3, kFam78>(s, soa, srgb, rc, inv3, ctr, chunk, st);
+        return;
+    }
     switch (minb) {
-        case 3: launch_mixed_t<3>(s, soa, srgb, rc, inv3, ctr, chunk, st); break;
-        case 5: launch_mixed_t<5>(s, soa, srgb, rc, inv3, ctr, chunk, st); break;
-        case 6: launch_mixed_t<6>(s, soa, srgb, rc, inv3, ctr, chunk, st); break;
-        case 8: launch_mixed_t<8>(s, soa, srgb, rc, inv3, ctr, chunk, st); break;
-        default: launch_mixed_t<4>(s, soa, srgb, rc, inv3, ctr, chunk, st); break;
+        case 3: launch_mixed_t<3, kFamRk4>(s, soa, srgb, rc, inv3, ctr, chunk, st); break;
+        case 5: launch_mixed_t<5, kFamRk4>(s, soa, srgb, rc, inv3, ctr, chunk, st); break;
+        case 6: launch_mixed_t<6, kFamRk4>(s, soa, srgb, rc, inv3, ctr, chunk, st); break;
+        case 8: launch_mixed_t<8, kFamRk4>(s, soa, srgb, rc, inv3, ctr, chunk, st); break;
+        default: launch_mixed_t<4, kFamRk4>(s, soa, srgb, rc, inv3, ctr, chunk, st); break;
     }
 }
 
@@ -791,6 +857,7 @@ int np_scene_validate(const np_scene_t* s) {
     if (s->crossing != NP_CROSS_LINEAR && s->crossing != NP_CROSS_HERMITE && s->crossing != NP_CROSS_ROOT)
         return fail(NP_ERR_INVALID, "Invalid crossing mode.");
     if (!(s->inv_gate >= 0.0 && s->inv_gate < 1.0)) return fail(NP_ERR_INVALID, "Invalid invariant gate.");
+    if (!(s->rtol_fp64 < 1.0) || !std::isfinite(s->rtol_fp64)) return fail(NP_ERR_INVALID, "Invalid FP64 tolerance.");
     // non-finite values in any other field would only surface as NaN images
     auto fin = [](double v) { return std::isfinite(v); };
     if (!fin(s->theta_deg) || !fin(s->phi_deg)) return fail(NP_ERR_INVALID, "Invalid camera angle.");
@@ -805,12 +872,12 @@ int np_scene_validate(const np_scene_t* s) {
     return NP_OK;
 }
 
-// The embedded 7(8) integrator and root-found crossings exist on the FP64
-// path only.
+// Root-found crossings on the mixed path exist for the embedded 7(8)
+// integrator (Henon steps); the invariant gate exists on the FP64 path.
 static int check_path(const np_scene_t& sc, int precision) {
     if (precision != NP_PREC_FP64 && precision != NP_PREC_MIXED) return fail(NP_ERR_INVALID, "Invalid precision.");
-    if (precision == NP_PREC_MIXED && (sc.integrator == NP_INTEG_RKF78 || sc.crossing == NP_CROSS_ROOT))
-        return fail(NP_ERR_INVALID, "The rkf78 integrator and root crossings need precision fp64.");
+    if (precision == NP_PREC_MIXED && sc.crossing == NP_CROSS_ROOT && sc.integrator != NP_INTEG_RKF78)
+        return fail(NP_ERR_INVALID, "Root crossings on precision mixed need the rkf78 integrator.");
     return NP_OK;
 }
 
@@ -950,6 +1017,10 @@ int np_tune(int param, int value) {
         case NP_TUNE_CHUNK:
             if (value < 1 || value > 4096) return fail(NP_ERR_INVALID, "chunk must be in [1, 4096]");
             g_tune.chunk = value;
+            return NP_OK;
+        case NP_TUNE_MIN_BLOCKS78:
+            if (value != 3 && value != 4) return fail(NP_ERR_INVALID, "min blocks of the 7(8) tracer must be 3 or 4");
+            g_tune.min_blocks78 = value;
             return NP_OK;
         default:
             return fail(NP_ERR_INVALID, "unknown tuning parameter %d", param);

@@ -20,6 +20,10 @@
 //   --mode research     FP64, rkf78 at rtol 1e-12 / atol 1e-14, root-found
 //                       crossings, invariant gate 1e-12, ZAMO camera and
 //                       invariant tracking (explicit flags take precedence)
+//   --mode precise      mixed precision, rkf78 at rtol 1e-8 / atol 1e-9 in
+//                       compensated FP32, crossings landed on the equator
+//                       (Henon steps), FP64 islands (explicit flags take
+//                       precedence)
 //   --islands N         FP64 island mask of the mixed path (NP_ISLAND_*)
 //   --benchmark         the 1280x720, a=0.9 benchmark scene (other flags may follow)
 //   --out-raw FILE      float32 mean RGB [3][H][W] and first-crossing radius [H][W]
@@ -263,9 +267,23 @@ int main(int argc, char** argv) {
         if (!c.gate_set) s.inv_gate = 1e-12;
         s.camera = NP_CAMERA_ZAMO;
         s.check_invariants = 1;
+    } else if (mode == "precise") {
+        if (!c.precision_set) c.precision = NP_PREC_MIXED;
+        if (!c.integrator_set) s.integrator = NP_INTEG_RKF78;
+        if (!c.rtol_set) s.rtol = 1e-8;
+        if (!c.atol_set) s.atol = 1e-9;
+        if (!c.crossing_set) s.crossing = NP_CROSS_ROOT;
     }
-    if (c.precision == NP_PREC_MIXED && (s.integrator == NP_INTEG_RKF78 || s.crossing == NP_CROSS_ROOT)) {
-        std::fprintf(stderr, "The rkf78 integrator and root crossings need --precision fp64.\n");
+    if (c.precision == NP_PREC_MIXED && mode == "research") {
+        std::fprintf(stderr, "Research mode needs --precision fp64.\n");
+        return 1;
+    }
+    if (c.precision == NP_PREC_MIXED && s.inv_gate > 0.0) {
+        std::fprintf(stderr, "The invariant gate needs --precision fp64.\n");
+        return 1;
+    }
+    if (c.precision == NP_PREC_MIXED && s.crossing == NP_CROSS_ROOT && s.integrator != NP_INTEG_RKF78) {
+        std::fprintf(stderr, "Root crossings on --precision mixed need --integrator rkf78.\n");
         return 1;
     }
     s.background = lower(c.bg) == "point" ? NP_BG_POINT : NP_BG_GRADIENT;

@@ -686,4 +686,618 @@ __device__ __forceinline__ bool dray_step(DRay<REC>& R, const SceneDev& s) {
     return false;
 }
 
+// ===========================================================================
+// Embedded 7(8) integration in compensated FP32 (the mixed path's
+// NP_INTEG_RKF78), with crossings landed on the equator by Henon's method.
+//
+// Fehlberg's 7(8) pair (E. Fehlberg, NASA TR R-287, 1968): 13 stages, the
+// 8th-order solution propagated, local error estimate h 41/840 (k1 + k11 -
+// k12 - k13).  Error control (one attempt per call): the weighted max norm of
+// that estimate over r, theta, p_r, p_theta with the scene's rtol / atol,
+// never below the FP32 rounding of the step's own increment; the step factor
+// 0.9 e^(-1/8), clamped to [0.2, 5] after an accepted step and to [0.1, 0.9]
+// after a rejected one.  The state stays an unevaluated (hi, lo) pair per
+// component, and theta reaches sin/cos as (hi, lo) too: near the equator
+// cos(theta) = -sin(theta - pi/2) is then exact to the pair's precision
+// instead of to the FP32 ulp of theta (6e-8 rad), which is what the disk
+// crossing radius is most sensitive to.
+//
+// Henon's method (M. Henon, Physica D 5, 1982): when an accepted step crosses
+// theta = pi/2, one more 7(8) step is taken from the step's start with theta
+// as the independent variable, dy/dtheta = f(y) / f_theta(y), of size
+// pi/2 - theta_0.  It lands on the equator exactly, so the crossing radius
+// carries the integrator's own error and no interpolant error.
+
+// sin and cos of the angle hi + lo (|lo| well below ulp(hi)), folded as
+// sincos_polar does but with the low part kept in the folded argument.
+__host__ __device__ __forceinline__ void sincos_polar_hl(float th, float lo, float& sn, float& cs) {
+    const float PI_HI = 3.14159274101257324f, PI_LO = -8.74227766e-8f;
+    const float PI2_HI = 1.57079637050628662f, PI2_LO = -4.37113883e-8f;
+    const bool mid = th >= 0.785398163f, top = th > 2.35619449f;
+    float z = top ? add_rn(sub_rn(PI_HI, th), sub_rn(PI_LO, lo))
+                  : (mid ? add_rn(sub_rn(th, PI2_HI), sub_rn(lo, PI2_LO)) : add_rn(th, lo));
+    float z2 = z * z;
+    float ps = fmaf(z2, -1.0f / 39916800.0f, 1.0f / 362880.0f);
+    ps = fmaf(z2, ps, -1.0f / 5040.0f);
+    ps = fmaf(z2, ps, 1.0f / 120.0f);
+    ps = fmaf(z2, ps, -1.0f / 6.0f);
+    ps = z * fmaf(z2, ps, 1.0f);
+    float pc = fmaf(z2, -1.0f / 3628800.0f, 1.0f / 40320.0f);
+    pc = fmaf(z2, pc, -1.0f / 720.0f);
+    pc = fmaf(z2, pc, 1.0f / 24.0f);
+    pc = fmaf(z2, pc, -0.5f);
+    pc = fmaf(z2, pc, 1.0f);
+    const bool mid_only = mid && !top;
+    sn = mid_only ? pc : ps;
+    cs = mid_only ? -ps : (top ? -pc : pc);
+}
+
+// rhs_f with theta given as (hi, lo).
+template <bool PHI>
+__device__ __forceinline__ F5 rhs_fhl(float r, float th, float tlo, float pr, float pth, const RayK& c,
+                                      const SpaceK& k) {
+    float sn, cs;
+    sincos_polar_hl(th, tlo, sn, cs);
+    float s2 = fmaxf(sn * sn, 1e-30f);
+    float is2 = rcp_approx(s2);
+    float r2 = r * r;
+    float Sig = fmaf(k.a2, cs * cs, r2);
+    float iS = rcp_approx(Sig);
+    float Del = (r - k.rp) * (r - k.rm);
+    float iD = rcp_approx(Del);
+    float P = fmaf(r2 + k.a2, c.E, -c.aL);
+    float PiD = P * iD;
+    float W = fmaf(c.L2, is2, fmaf(c.a2E2, s2, -c.twoaEL));
+    float F = fmaf(Del * pr, pr, fmaf(pth, pth, fmaf(-P, PiD, W)));
+    float Del_r = 2.0f * (r - k.M);
+    float F_r = fmaf(Del_r, fmaf(pr, pr, PiD * PiD), -4.0f * r * c.E * PiD);
+    float sc2 = 2.0f * sn * cs;
+    float F_t = sc2 * fmaf(-c.L2 * is2, is2, c.a2E2);
+    F5 d;
+    d.r = Del * pr * iS;
+    d.th = pth * iS;
+    d.pr = -0.5f * iS * fmaf(-2.0f * r * iS, F, F_r);
+    d.pth = -0.5f * iS * fmaf(k.a2 * sc2 * iS, F, F_t);
+    d.ph = PHI ? iS * fmaf(k.a, PiD, fmaf(c.L, is2, -k.a * c.E)) : 0.0f;
+    return d;
+}
+
+template <typename T> struct V5 { T r, th, pr, pth, ph; };
+template <typename T> struct V4 { T r, th, pr, pth; };
+
+template <typename T>
+__device__ __forceinline__ V4<T> v4(const V5<T>& k) { return V4<T>{k.r, k.th, k.pr, k.pth}; }
+
+// One Fehlberg 7(8) combination.  ev(S) returns f at the stage input y0 +
+// h S (the caller forms it from its own state representation); k1 = f(y0)
+// is given.  Outputs the increments d = h sum b_i k_i and the error estimate
+// err = h 41/840 (k1 + k11 - k12 - k13) of (r, theta, p_r, p_theta).
+template <typename T, bool PHI, class Ev>
+__device__ __forceinline__ void f78_combine(const V5<T>& K1, T h, Ev ev, V5<T>& d, V4<T>& err) {
+    const V4<T> k1 = v4(K1);
+#define NP78_S(expr) V4<T>{expr(r), expr(th), expr(pr), expr(pth)}
+#define NP78_E2(c) (T(2.0 / 27) * k1.c)
+    V5<T> f = ev(NP78_S(NP78_E2));
+    const V4<T> k2 = v4(f);
+#define NP78_E3(c) (T(1.0 / 36) * k1.c + T(1.0 / 12) * k2.c)
+    f = ev(NP78_S(NP78_E3));
+    const V4<T> k3 = v4(f);
+#define NP78_E4(c) (T(1.0 / 24) * k1.c + T(1.0 / 8) * k3.c)
+    f = ev(NP78_S(NP78_E4));
+    const V4<T> k4 = v4(f);
+#define NP78_E5(c) (T(5.0 / 12) * k1.c + T(-25.0 / 16) * k3.c + T(25.0 / 16) * k4.c)
+    f = ev(NP78_S(NP78_E5));
+    const V4<T> k5 = v4(f);
+#define NP78_E6(c) (T(1.0 / 20) * k1.c + T(1.0 / 4) * k4.c + T(1.0 / 5) * k5.c)
+    f = ev(NP78_S(NP78_E6));
+    const V4<T> k6 = v4(f);
+    V5<T> sb{T(34.0 / 105) * f.r, T(34.0 / 105) * f.th, T(34.0 / 105) * f.pr, T(34.0 / 105) * f.pth,
+             PHI ? T(34.0 / 105) * f.ph : T(0)};
+#define NP78_ACC(w)                                                                                      \
+    sb.r += T(w) * f.r; sb.th += T(w) * f.th; sb.pr += T(w) * f.pr; sb.pth += T(w) * f.pth;              \
+    if (PHI) sb.ph += T(w) * f.ph;
+#define NP78_E7(c) (T(-25.0 / 108) * k1.c + T(125.0 / 108) * k4.c + T(-65.0 / 27) * k5.c + T(125.0 / 54) * k6.c)
+    f = ev(NP78_S(NP78_E7));
+    const V4<T> k7 = v4(f);
+    NP78_ACC(9.0 / 35)
+#define NP78_E8(c) (T(31.0 / 300) * k1.c + T(61.0 / 225) * k5.c + T(-2.0 / 9) * k6.c + T(13.0 / 900) * k7.c)
+    f = ev(NP78_S(NP78_E8));
+    const V4<T> k8 = v4(f);
+    NP78_ACC(9.0 / 35)
+#define NP78_E9(c) (T(2.0) * k1.c + T(-53.0 / 6) * k4.c + T(704.0 / 45) * k5.c + T(-107.0 / 9) * k6.c + \
+                    T(67.0 / 90) * k7.c + T(3.0) * k8.c)
+    f = ev(NP78_S(NP78_E9));
+    const V4<T> k9 = v4(f);
+    NP78_ACC(9.0 / 280)
+#define NP78_E10(c) (T(-91.0 / 108) * k1.c + T(23.0 / 108) * k4.c + T(-976.0 / 135) * k5.c + T(311.0 / 54) * k6.c + \
+                     T(-19.0 / 60) * k7.c + T(17.0 / 6) * k8.c + T(-1.0 / 12) * k9.c)
+    f = ev(NP78_S(NP78_E10));
+    const V4<T> k10 = v4(f);
+    NP78_ACC(9.0 / 280)
+#define NP78_E11(c) (T(2383.0 / 4100) * k1.c + T(-341.0 / 164) * k4.c + T(4496.0 / 1025) * k5.c +                \
+                     T(-301.0 / 82) * k6.c + T(2133.0 / 4100) * k7.c + T(45.0 / 82) * k8.c + T(45.0 / 164) * k9.c + \
+                     T(18.0 / 41) * k10.c)
+    f = ev(NP78_S(NP78_E11));
+    const V4<T> k11 = v4(f);
+#define NP78_E12(c) (T(3.0 / 205) * k1.c + T(-6.0 / 41) * k6.c + T(-3.0 / 205) * k7.c + T(-3.0 / 41) * k8.c + \
+                     T(3.0 / 41) * k9.c + T(6.0 / 41) * k10.c)
+    f = ev(NP78_S(NP78_E12));
+    const V4<T> k12 = v4(f);
+    NP78_ACC(41.0 / 840)
+#define NP78_E13(c) (T(-1777.0 / 4100) * k1.c + T(-341.0 / 164) * k4.c + T(4496.0 / 1025) * k5.c +                \
+                     T(-289.0 / 82) * k6.c + T(2193.0 / 4100) * k7.c + T(51.0 / 82) * k8.c + T(33.0 / 164) * k9.c + \
+                     T(12.0 / 41) * k10.c + k12.c)
+    f = ev(NP78_S(NP78_E13));
+    NP78_ACC(41.0 / 840)
+    d = V5<T>{h * sb.r, h * sb.th, h * sb.pr, h * sb.pth, PHI ? h * sb.ph : T(0)};
+    const T e1 = T(41.0 / 840) * h;
+    err = V4<T>{e1 * ((k1.r + k11.r) - (k12.r + f.r)), e1 * ((k1.th + k11.th) - (k12.th + f.th)),
+                e1 * ((k1.pr + k11.pr) - (k12.pr + f.pr)), e1 * ((k1.pth + k11.pth) - (k12.pth + f.pth))};
+#undef NP78_S
+#undef NP78_ACC
+#undef NP78_E2
+#undef NP78_E3
+#undef NP78_E4
+#undef NP78_E5
+#undef NP78_E6
+#undef NP78_E7
+#undef NP78_E8
+#undef NP78_E9
+#undef NP78_E10
+#undef NP78_E11
+#undef NP78_E12
+#undef NP78_E13
+}
+
+// Weighted max norm of a 7(8) error estimate: scale atol + rtol max(|y0|,
+// |y0 + d|) per component, never below `floor_rel` |d| (the rounding of the
+// increment itself in the arithmetic at hand).  A non-finite increment or
+// estimate (a stage that left the domain, e.g. inside the horizon) gives an
+// infinite norm: fmax alone would drop a NaN and accept the step.
+template <typename T>
+__device__ __forceinline__ T f78_norm(const V4<T>& y0, const V5<T>& d, const V4<T>& err, T rtol, T atol, T floor_rel) {
+    T e = T(0);
+    const T y[4] = {y0.r, y0.th, y0.pr, y0.pth};
+    const T dd[4] = {d.r, d.th, d.pr, d.pth};
+    const T ee[4] = {err.r, err.th, err.pr, err.pth};
+    bool finite = true;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        T sc = atol + rtol * fmax(fabs(y[i]), fabs(y[i] + dd[i]));
+        sc = fmax(sc, floor_rel * fabs(dd[i]));
+        e = fmax(e, fabs(ee[i]) / fmax(sc, T(1e-30)));
+        finite = finite && isfinite(dd[i]) && isfinite(ee[i]);
+    }
+    return finite ? e : T(INFINITY);
+}
+
+// Step-size factor after an attempt with error norm e.
+__device__ __forceinline__ float f78_factor(float e, bool accepted) {
+    const float f = 0.9f * __powf(fmaxf(e, 1e-12f), -0.125f);
+    return accepted ? fminf(5.0f, fmaxf(0.2f, f)) : fminf(0.9f, fmaxf(0.1f, f));
+}
+
+// An ingoing ray (p_r < 0) at radius r is certainly captured when the radial
+// potential R(r') = P(r')^2 - Delta(r') K, P = (r'^2 + a^2) E - a L,
+// K = Q + (L - a E)^2, stays positive on [r_+, r]: it has no turning point
+// left.  P increases with r' (E > 0) and Delta increases on [r_+, r], so
+// min P^2 > Delta(r) K over the interval is sufficient.  FP64, a few
+// operations; used once per ray entering the horizon band.
+__device__ __forceinline__ bool capture_certified(double r, double th, double pr, double pth, double E, double L,
+                                                  double a, double M, double rp, double rm) {
+    if (!(pr < 0.0) || !(E > 0.0)) return false;
+    double sn, cs;
+    sincos(th, &sn, &cs);
+    const double Q = pth * pth + cs * cs * (L * L / fmax(sn * sn, 1e-300) - a * a * E * E);
+    const double K = Q + (L - a * E) * (L - a * E);
+    const double Pp = (rp * rp + a * a) * E - a * L, Pr = (r * r + a * a) * E - a * L;
+    const double minP = Pp > 0.0 ? Pp : (Pr < 0.0 ? -Pr : 0.0);
+    const double Del = (r - rp) * (r - rm);
+    return K >= 0.0 && minP * minP > Del * K * (1.0 + 1e-9) + 1e-300;
+}
+
+// A step whose theta starts moving towards the equator and ends moving
+// away from it on the same side has crossed the equator twice (the polar
+// motion of a ray with Q > 0 oscillates symmetrically about it): such a
+// step is rejected, so that no crossing pair is missed.
+__host__ __device__ __forceinline__ bool double_crossing(float dth0, float pth0, float dth1, float pth1) {
+    const bool same = (dth0 > 0.0f) == (dth1 > 0.0f);
+    const bool toward = (pth0 > 0.0f) == (dth0 < 0.0f);
+    const bool away = (pth1 > 0.0f) == (dth1 > 0.0f);
+    return same && toward && away;
+}
+
+// FP32 evaluation at the stage y0 + h S of a (hi, lo) state.
+template <bool PHI>
+struct Ev78f {
+    const HiLo &r, &th, &pr, &pth;
+    float h;
+    const RayK& c;
+    const SpaceK& k;
+    __device__ __forceinline__ V5<float> operator()(const V4<float>& S) const {
+        F5 f = rhs_fhl<PHI>(r.hi + fmaf(h, S.r, r.lo), th.hi, fmaf(h, S.th, th.lo), pr.hi + fmaf(h, S.pr, pr.lo),
+                            pth.hi + fmaf(h, S.pth, pth.lo), c, k);
+        return V5<float>{f.r, f.th, f.pr, f.pth, f.ph};
+    }
+};
+
+// The same with theta as the independent variable (Henon): returns
+// (dr, 1, dp_r, dp_theta, dphi) / dtheta at the stage theta0 + dth S.
+template <bool PHI>
+struct Ev78fHenon {
+    const HiLo &r, &th, &pr, &pth;
+    float dth;
+    const RayK& c;
+    const SpaceK& k;
+    __device__ __forceinline__ V5<float> operator()(const V4<float>& S) const {
+        F5 f = rhs_fhl<PHI>(r.hi + fmaf(dth, S.r, r.lo), th.hi, fmaf(dth, S.th, th.lo), pr.hi + fmaf(dth, S.pr, pr.lo),
+                            pth.hi + fmaf(dth, S.pth, pth.lo), c, k);
+        const float it = 1.0f / f.th;
+        return V5<float>{f.r * it, 1.0f, f.pr * it, f.pth * it, PHI ? f.ph * it : 0.0f};
+    }
+};
+
+// Crossing of theta = pi/2 inside an accepted FP32 step from (r0, th0, pr0,
+// pth0, ph0) with f(y0) = k0: Henon step of size -dtheta_eq(th0).  Returns
+// the crossing radius (hi, lo) and azimuth; false when the step is
+// ill-conditioned (f_theta ~ 0 somewhere: a grazing ray), in which case the
+// caller falls back to the Hermite interpolant.
+template <bool PHI>
+__device__ __forceinline__ bool henon78_f(const HiLo& r0, const HiLo& th0, const HiLo& pr0, const HiLo& pth0,
+                                          const HiLo& ph0, const float k0[5], const RayK& c, const SpaceK& k,
+                                          HiLo& rc, float& phc) {
+    const float dth = -dtheta_eq(th0);
+    const float it = 1.0f / k0[1];
+    const V5<float> g1{k0[0] * it, 1.0f, k0[2] * it, k0[3] * it, PHI ? k0[4] * it : 0.0f};
+    V5<float> d;
+    V4<float> err;
+    f78_combine<float, PHI>(g1, dth, Ev78fHenon<PHI>{r0, th0, pr0, pth0, dth, c, k}, d, err);
+    if (!isfinite(d.r) || !(fabsf(d.r) < 1e4f)) return false;
+    rc = r0;
+    hl_add(rc, d.r);
+    if (PHI) phc = (float)((double)ph0.hi + (double)(ph0.lo + d.ph));
+    return true;
+}
+
+// FP64 stage evaluation of the Carter system (islands and near-critical
+// rays): sin/cos of the stage angle by angle addition from those of theta0.
+struct Ev78d {
+    const D5& y;
+    double sn0, cs0, h, E, L, a, M, rp, rm;
+    __device__ __forceinline__ V5<double> operator()(const V4<double>& S) const {
+        double sn, cs;
+        stage_sincos_d(y.th, sn0, cs0, h * S.th, sn, cs);
+        D5 z{y.r + h * S.r, y.th + h * S.th, y.pr + h * S.pr, y.pth + h * S.pth, 0.0};
+        D5 f = rhs_dsc(z, sn, cs, E, L, a, M, rp, rm);
+        return V5<double>{f.r, f.th, f.pr, f.pth, f.ph};
+    }
+};
+
+struct Ev78dHenon {
+    const D5& y;
+    double sn0, cs0, dth, E, L, a, M, rp, rm;
+    __device__ __forceinline__ V5<double> operator()(const V4<double>& S) const {
+        double sn, cs;
+        stage_sincos_d(y.th, sn0, cs0, dth * S.th, sn, cs);
+        D5 z{y.r + dth * S.r, y.th + dth * S.th, y.pr + dth * S.pr, y.pth + dth * S.pth, 0.0};
+        D5 f = rhs_dsc(z, sn, cs, E, L, a, M, rp, rm);
+        const double it = 1.0 / f.th;
+        return V5<double>{f.r * it, 1.0, f.pr * it, f.pth * it, f.ph * it};
+    }
+};
+
+// FP64 Henon crossing from y0 (sin/cos sn0, cs0, f(y0) = f0); false when
+// ill-conditioned.
+__device__ __forceinline__ bool henon78_d(const D5& y0, double sn0, double cs0, const D5& f0, double E, double L,
+                                          double a, double M, double rp, double rm, double& rc, double& phc) {
+    const double dth = kPi * 0.5 - y0.th;
+    const double it = 1.0 / f0.th;
+    const V5<double> g1{f0.r * it, 1.0, f0.pr * it, f0.pth * it, f0.ph * it};
+    V5<double> d;
+    V4<double> err;
+    f78_combine<double, true>(g1, dth, Ev78dHenon{y0, sn0, cs0, dth, E, L, a, M, rp, rm}, d, err);
+    if (!isfinite(d.r) || !(fabs(d.r) < 1e4)) return false;
+    rc = y0.r + d.r;
+    phc = y0.ph + d.ph;
+    return true;
+}
+
+// Records one equatorial crossing at radius rc (FP32 ray): per-ray report and
+// disk shading.
+template <bool PHI>
+__device__ __forceinline__ void mray_record_crossing(MRay<PHI>& R, const SceneDev& s, const SpaceK& k, float rc,
+                                                     double rc_d, float phc) {
+    if (PHI && R.crossings < 4) {
+        R.xr[R.crossings] = rc;
+        R.xr_d[R.crossings] = rc_d;
+        R.xphi[R.crossings] = phc;
+    }
+    R.crossings++;
+    if (R.orders < s.max_orders && rc >= s.rin_f && rc <= s.rout_f) {
+        float g = doppler_g_f(rc, R.E.hi, R.L.hi, k.M, k.a);
+        shade_disk(rc, g, s.qf, s.gain, R.disk);
+        if (R.orders == 0) R.first_r = rc;
+        R.orders++;
+    }
+}
+
+// f(y) of the current state with theta as (hi, lo) (first stage of the next 7(8) step).
+template <bool PHI>
+__device__ __forceinline__ void mray_set_k78(MRay<PHI>& R, const SpaceK& k) {
+    F5 f = rhs_fhl<PHI>(R.r.hi, R.th.hi, R.th.lo, R.pr.hi, R.pth.hi, R.c, k);
+    R.k[0] = f.r; R.k[1] = f.th; R.k[2] = f.pr; R.k[3] = f.pth; R.k[4] = f.ph;
+}
+
+// Tail of an accepted 7(8) step (FP32 or island): termination, next k1,
+// crossing (Henon, Hermite fallback), escape.  y0 / k0 describe the start
+// of the step; h is the step taken.
+template <bool PHI>
+__device__ __forceinline__ bool mray_finish78(MRay<PHI>& R, const SceneDev& s, const SpaceK& k, float h,
+                                              const HiLo& r0, const HiLo& th0, const HiLo& pr0, const HiLo& pth0,
+                                              const HiLo& ph0, const float k0[5]) {
+    R.step++;
+    bool ok = R.r.hi > s.r_plus_f + 1e-6f * s.r_plus_f && R.th.hi > 1e-7f && R.th.hi < s.pi_lim_f;
+    if (!ok) { R.status = 1; return true; }
+    mray_set_k78(R, k);
+    R.min_r = fminf(R.min_r, R.r.hi);
+    const float dp = dtheta_eq(th0), dc = dtheta_eq(R.th);
+    if ((dp > 0.0f && dc < 0.0f) || (dp < 0.0f && dc > 0.0f)) {
+        HiLo rc;
+        float phc = 0.0f;
+        if (!(s.crossing == NP_CROSS_ROOT && henon78_f<PHI>(r0, th0, pr0, pth0, ph0, k0, R.c, k, rc, phc))) {
+            // cubic Hermite in lambda over the step (also the fallback of a
+            // grazing crossing), or linear in theta
+            const float lin = fabsf(dp) / (fabsf(dp) + fabsf(dc));
+            float u = s.crossing == NP_CROSS_LINEAR ? lin : hermite_root_f(dp, dc, h * k0[1], h * R.k[1], lin);
+            float dr = (R.r.hi - r0.hi) + (R.r.lo - r0.lo);
+            float u2 = u * u, u3 = u2 * u;
+            const bool lin_only = s.crossing == NP_CROSS_LINEAR;
+            rc = r0;
+            hl_add(rc, lin_only ? u * dr
+                                : (3.0f * u2 - 2.0f * u3) * dr + (u3 - 2.0f * u2 + u) * (h * k0[0]) + (u3 - u2) * (h * R.k[0]));
+            if (PHI) {
+                float dph = (R.ph.hi - ph0.hi) + (R.ph.lo - ph0.lo);
+                float cph = lin_only ? u * dph
+                                     : (3.0f * u2 - 2.0f * u3) * dph + (u3 - 2.0f * u2 + u) * (h * k0[4]) + (u3 - u2) * (h * R.k[4]);
+                phc = (float)((double)ph0.hi + (double)(ph0.lo + cph));
+            }
+        }
+        mray_record_crossing(R, s, k, rc.hi + rc.lo, hl_d(rc), phc);
+    }
+    if (R.r.hi > s.r_far_f && R.step > 11) { R.status = 0; return true; }
+    return false;
+}
+
+// One FP32 7(8) attempt.  Accepted: the state advances (STEP_CONT or
+// STEP_DONE).  Rejected: h shrinks and the lane returns STEP_CONT without a
+// step, so one lane's retries never stall its warp.  Island steps park the
+// lane with h_pend (horizon band; turning points when the mask asks).
+template <bool PHI>
+__device__ __forceinline__ int mray_step78(MRay<PHI>& R, const SceneDev& s, const SpaceK& k, bool& accepted) {
+    accepted = false;
+    if (R.step >= s.max_steps) { R.status = 2; return STEP_DONE; }
+    // a step moves r by about h (|dr/dlambda| ~ E): at most half the radius
+    float h = fminf(R.h_adapt > 0.0f ? R.h_adapt : mray_h(s, R.r.hi), 0.5f * R.r.hi);
+    if ((s.islands & kIslandHorizon) && R.r.hi < s.r_band_f) {
+        // inside the band: a ray that provably falls in ends here (it reaches
+        // r_+ without another crossing of the disk, which lies outside the
+        // band); any other takes FP64 island steps
+        if (s.cert_capture &&
+            capture_certified(hl_d(R.r), hl_d(R.th), hl_d(R.pr), hl_d(R.pth), hl_d(R.E), hl_d(R.L), s.a, s.M,
+                              s.r_plus, s.r_minus)) {
+            R.step++; R.status = 1; R.min_r = s.r_plus_f;
+            return STEP_DONE;
+        }
+        R.pending = true; R.h_pend = h;
+        return STEP_PARK;
+    }
+    const V5<float> k1{R.k[0], R.k[1], R.k[2], R.k[3], R.k[4]};
+    V5<float> d;
+    V4<float> err;
+    f78_combine<float, PHI>(k1, h, Ev78f<PHI>{R.r, R.th, R.pr, R.pth, h, R.c, k}, d, err);
+    float e = f78_norm<float>(V4<float>{R.r.hi, R.th.hi, R.pr.hi, R.pth.hi}, d, err, s.rtol_f, s.atol78_f, 0.0f);
+    {
+        const float dth0 = dtheta_eq(R.th);
+        if (double_crossing(dth0, R.pth.hi, dth0 + d.th, R.pth.hi + d.pth)) e = fmaxf(e, 2.0f);
+    }
+    if (!(e <= 1.0f)) {
+        h *= isfinite(e) ? f78_factor(e, false) : 0.1f;
+        R.h_adapt = h;
+        if (h < s.hmin_f) { R.step++; R.status = 1; return STEP_DONE; }
+        return STEP_CONT;
+    }
+    accepted = true;
+    const HiLo r0 = R.r, th0 = R.th, pr0 = R.pr, pth0 = R.pth, ph0 = R.ph;
+    const float k0[5] = {R.k[0], R.k[1], R.k[2], R.k[3], R.k[4]};
+    hl_add(R.r, d.r); hl_add(R.th, d.th); hl_add(R.pr, d.pr); hl_add(R.pth, d.pth);
+    if (PHI) hl_add(R.ph, d.ph);
+    R.h_adapt = h * f78_factor(e, true);
+    if (s.islands & kIslandTurning) {
+        bool turn = ((pr0.hi > 0.0f) != (R.pr.hi > 0.0f)) || ((pth0.hi > 0.0f) != (R.pth.hi > 0.0f));
+        if (turn) {
+            R.r = r0; R.th = th0; R.pr = pr0; R.pth = pth0; R.ph = ph0;
+            R.pending = true; R.h_pend = h;
+            accepted = false;
+            return STEP_PARK;
+        }
+    }
+    return mray_finish78(R, s, k, h, r0, th0, pr0, pth0, ph0, k0) ? STEP_DONE : STEP_CONT;
+}
+
+// The parked FP64 7(8) step: a by-value core and the FP32-side
+// bookkeeping.  The core is inlined: a call would make the FP32 loop save
+// its live registers around it, which cost more than the FP64 stage storage
+// (islands are rare, and the FP32 stage vectors are dead while one runs).
+struct Isl78In { double r, th, pr, pth, ph, E, L, h, a, M, rp, rm, rtol, atol, hmin; int root; };
+struct Isl78Out { double r, th, pr, pth, ph, h_taken, h_next, rc, phc; int ok, crossed, attempts; };
+
+// Attempts from h until one is accepted (at most 24, h shrinking); an
+// accepted step that crosses the equator is landed on it by an FP64 Henon
+// step when `root` is set.
+__device__ __forceinline__ Isl78Out island78_core(const Isl78In in) {
+    Isl78Out o{};
+    const D5 y{in.r, in.th, in.pr, in.pth, in.ph};
+    double sn0, cs0;
+    sincos(y.th, &sn0, &cs0);
+    const D5 f0 = rhs_dsc(y, sn0, cs0, in.E, in.L, in.a, in.M, in.rp, in.rm);
+    const V5<double> k1{f0.r, f0.th, f0.pr, f0.pth, f0.ph};
+    double h = in.h, e = 0.0;
+    V5<double> d{};
+    int att = 0;
+    bool acc = false;
+#pragma unroll 1
+    for (; att < 24; ++att) {
+        V4<double> err;
+        f78_combine<double, true>(k1, h, Ev78d{y, sn0, cs0, h, in.E, in.L, in.a, in.M, in.rp, in.rm}, d, err);
+        e = f78_norm<double>(V4<double>{y.r, y.th, y.pr, y.pth}, d, err, in.rtol, in.atol, 1e-15);
+        if (double_crossing((float)(y.th - kPi * 0.5), (float)y.pth, (float)(y.th + d.th - kPi * 0.5),
+                            (float)(y.pth + d.pth)))
+            e = fmax(e, 2.0);
+        if (e <= 1.0) { acc = true; break; }
+        h *= isfinite(e) ? (double)f78_factor((float)e, false) : 0.1;
+        if (h < in.hmin) break;
+    }
+    o.attempts = att + 1;
+    if (!acc) return o;
+    o.ok = 1;
+    o.r = y.r + d.r; o.th = y.th + d.th; o.pr = y.pr + d.pr; o.pth = y.pth + d.pth; o.ph = y.ph + d.ph;
+    o.h_taken = h;
+    o.h_next = h * (double)f78_factor((float)e, true);
+    const double dp = y.th - kPi * 0.5, dc = o.th - kPi * 0.5;
+    if (in.root && ((dp > 0.0 && dc < 0.0) || (dp < 0.0 && dc > 0.0)))
+        o.crossed = henon78_d(y, sn0, cs0, f0, in.E, in.L, in.a, in.M, in.rp, in.rm, o.rc, o.phc) ? 1 : 0;
+    return o;
+}
+
+// The parked FP64 island step of an FP32 ray (h_pend): FP64 attempts at the
+// scene's FP64 tolerance, then the common tail.  `attempts` returns the
+// attempts taken.
+template <bool PHI>
+__device__ __forceinline__ bool mray_island78(MRay<PHI>& R, const SceneDev& s, const SpaceK& k, int& attempts) {
+    const HiLo r0 = R.r, th0 = R.th, pr0 = R.pr, pth0 = R.pth, ph0 = R.ph;
+    const float k0[5] = {R.k[0], R.k[1], R.k[2], R.k[3], R.k[4]};
+    Isl78In in;
+    in.r = hl_d(R.r); in.th = hl_d(R.th); in.pr = hl_d(R.pr); in.pth = hl_d(R.pth); in.ph = PHI ? hl_d(R.ph) : 0.0;
+    in.E = hl_d(R.E); in.L = hl_d(R.L); in.h = (double)R.h_pend;
+    in.a = s.a; in.M = s.M; in.rp = s.r_plus; in.rm = s.r_minus;
+    // the FP32 step's own tolerance: the island changes the arithmetic of
+    // the step, not its accuracy target (near-critical rays use rtol_fp64)
+    in.rtol = s.rtol; in.atol = (double)s.atol78_f; in.hmin = s.hmin; in.root = s.crossing == NP_CROSS_ROOT;
+    const Isl78Out o = island78_core(in);
+    attempts = o.attempts;
+    R.pending = false;
+    R.fp64_steps++;
+    if (!o.ok) { R.step++; R.status = 1; return true; }
+    R.r = d_hl(o.r); R.th = d_hl(o.th); R.pr = d_hl(o.pr); R.pth = d_hl(o.pth);
+    if (PHI) R.ph = d_hl(o.ph);
+    R.h_adapt = (float)o.h_next;
+    if (o.crossed) {
+        // landed on the equator in FP64: record here; the common tail below
+        // is not used, so it cannot count the crossing twice
+        R.step++;
+        bool ok = R.r.hi > s.r_plus_f + 1e-6f * s.r_plus_f && R.th.hi > 1e-7f && R.th.hi < s.pi_lim_f;
+        if (!ok) { R.status = 1; return true; }
+        mray_set_k78(R, k);
+        R.min_r = fminf(R.min_r, R.r.hi);
+        mray_record_crossing(R, s, k, (float)o.rc, o.rc, (float)o.phc);
+        if (R.r.hi > s.r_far_f && R.step > 11) { R.status = 0; return true; }
+        return false;
+    }
+    return mray_finish78(R, s, k, (float)o.h_taken, r0, th0, pr0, pth0, ph0, k0);
+}
+
+// ---------------------------------------------------------------------------
+// Near-critical rays traced whole in FP64 with the 7(8) pair at the
+// scene's FP64 tolerance and Henon crossings.
+template <bool REC>
+struct DRay78 {
+    D5 y, f;
+    double sn, cs, E, L, h;
+    double min_r, first_r;
+    float disk[3];
+    int step, orders, crossings, status;
+    double xr[REC ? 4 : 1], xphi[REC ? 4 : 1];
+};
+
+template <bool REC>
+__device__ __forceinline__ void dray78_start(DRay78<REC>& R, const SceneDev& s, double E, double L, double pr,
+                                             double pth) {
+    R.y = D5{s.r_cam, s.th_cam, pr, pth, s.ph_cam};
+    R.E = E; R.L = L;
+    sincos(R.y.th, &R.sn, &R.cs);
+    R.f = rhs_dsc(R.y, R.sn, R.cs, E, L, s.a, s.M, s.r_plus, s.r_minus);
+    R.h = s.h_unit * fmin(fmax(1.0, R.y.r / s.M), 100.0);
+    R.min_r = s.r_cam; R.first_r = 0.0;
+    R.disk[0] = R.disk[1] = R.disk[2] = 0.0f;
+    R.step = 0; R.orders = 0; R.crossings = 0; R.status = 2;
+    if (REC) for (int i = 0; i < 4; ++i) { R.xr[i] = 0.0; R.xphi[i] = 0.0; }
+}
+
+// One attempt; returns true when the ray is done.  `accepted` tells whether
+// a step was taken.
+template <bool REC>
+__device__ __forceinline__ bool dray78_step(DRay78<REC>& R, const SceneDev& s, bool& accepted) {
+    accepted = false;
+    if (R.step >= s.max_steps) { R.status = 2; return true; }
+    if (s.cert_capture && R.y.r < (double)s.r_band_f &&
+        capture_certified(R.y.r, R.y.th, R.y.pr, R.y.pth, R.E, R.L, s.a, s.M, s.r_plus, s.r_minus)) {
+        R.step++; R.status = 1; R.min_r = s.r_plus;
+        return true;
+    }
+    const V5<double> k1{R.f.r, R.f.th, R.f.pr, R.f.pth, R.f.ph};
+    V5<double> d;
+    V4<double> err;
+    f78_combine<double, true>(k1, R.h, Ev78d{R.y, R.sn, R.cs, R.h, R.E, R.L, s.a, s.M, s.r_plus, s.r_minus}, d, err);
+    double e = f78_norm<double>(V4<double>{R.y.r, R.y.th, R.y.pr, R.y.pth}, d, err, s.rtol64, s.atol, 1e-15);
+    if (double_crossing((float)(R.y.th - kPi * 0.5), (float)R.y.pth, (float)(R.y.th + d.th - kPi * 0.5),
+                        (float)(R.y.pth + d.pth)))
+        e = fmax(e, 2.0);
+    if (!(e <= 1.0)) {
+        R.h *= isfinite(e) ? (double)f78_factor((float)e, false) : 0.1;
+        if (R.h < s.hmin) { R.step++; R.status = 1; return true; }
+        return false;
+    }
+    accepted = true;
+    const D5 y0 = R.y, f0 = R.f;
+    const double sn0 = R.sn, cs0 = R.cs;
+    const double h_taken = R.h;
+    R.y = D5{y0.r + d.r, y0.th + d.th, y0.pr + d.pr, y0.pth + d.pth, y0.ph + d.ph};
+    R.h *= (double)f78_factor((float)e, true);
+    R.step++;
+    bool ok = R.y.r > s.r_plus + 1e-9 && R.y.th > 1e-9 && R.y.th < kPi - 1e-9;
+    if (!ok) { R.status = 1; return true; }
+    sincos(R.y.th, &R.sn, &R.cs);
+    R.f = rhs_dsc(R.y, R.sn, R.cs, R.E, R.L, s.a, s.M, s.r_plus, s.r_minus);
+    R.min_r = fmin(R.min_r, R.y.r);
+    const double dp = y0.th - kPi * 0.5, dc = R.y.th - kPi * 0.5;
+    if ((dp > 0 && dc < 0) || (dp < 0 && dc > 0)) {
+        double rc, phc;
+        if (!(s.crossing == NP_CROSS_ROOT &&
+              henon78_d(y0, sn0, cs0, f0, R.E, R.L, s.a, s.M, s.r_plus, s.r_minus, rc, phc))) {
+            // cubic Hermite in lambda over the step (also the fallback of a
+            // grazing crossing), or linear in theta
+            const double lin = fabs(dp) / (fabs(dp) + fabs(dc));
+            if (s.crossing == NP_CROSS_LINEAR) {
+                rc = y0.r + lin * (R.y.r - y0.r);
+                phc = y0.ph + lin * (R.y.ph - y0.ph);
+            } else {
+                const double hs = h_taken;
+                const double u = hermite_root(dp, dc, hs * f0.th, hs * R.f.th, lin);
+                rc = hermite_eval(y0.r, R.y.r, hs * f0.r, hs * R.f.r, u);
+                phc = hermite_eval(y0.ph, R.y.ph, hs * f0.ph, hs * R.f.ph, u);
+            }
+        }
+        if (REC && R.crossings < 4) { R.xr[R.crossings] = rc; R.xphi[R.crossings] = phc; }
+        R.crossings++;
+        if (R.orders < s.max_orders && rc >= s.rin && rc <= s.rout) {
+            float g = (float)doppler_g(rc, -R.E, R.L, s.M, s.a);
+            shade_disk((float)rc, g, s.qf, s.gain, R.disk);
+            if (R.orders == 0) R.first_r = rc;
+            R.orders++;
+        }
+    }
+    if (R.y.r > s.r_far && R.step > 11) { R.status = 0; return true; }
+    return false;
+}
+
 }  // namespace np

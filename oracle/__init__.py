@@ -35,6 +35,8 @@ def load():
         lib.npo_trace_invariants.restype = C.c_int
         lib.npo_rkf78_tableau.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
         lib.npo_rkf78_tableau.restype = None
+        lib.npo_frame_rays.argtypes = [S, C.c_int, C.c_int, C.c_void_p]
+        lib.npo_frame_rays.restype = C.c_int
         lib.npo_critical_curve.argtypes = [S, C.c_void_p]
         lib.npo_critical_curve.restype = C.c_int
         lib.npo_metric_inv.argtypes = [C.c_double] * 4 + [C.c_void_p]
@@ -106,6 +108,42 @@ def trace_rays(scene, px, py, threads=0):
                           _vp(steps), threads) != 0:
         raise RuntimeError("oracle trace failed")
     return {"consts": consts, "cross": cross, "status": status, "steps": steps}
+
+
+def frame_rays(scene, y0, y1):
+    """Camera momenta (p_t, p_phi, p_r, p_theta) of sample `sample_offset` of
+    every pixel of rows [y0, y1): array [y1 - y0, width, 4]."""
+    out = np.zeros((y1 - y0, scene.width, 4), np.float64)
+    if load().npo_frame_rays(C.byref(scene), y0, y1, _vp(out)) != 0:
+        raise RuntimeError("npo_frame_rays failed")
+    return out
+
+
+def frame_crossings(scene, y0, y1, K=4, threads=None):
+    """Equatorial crossing radii (Mino-time solver, GEOR with mu_f = 0) of
+    the rays of frame_rays(scene, y0, y1): array [y1 - y0, width, K], 0
+    where a ray has fewer crossings.  The solver stops at u = M / escape_r."""
+    import math
+    from concurrent.futures import ThreadPoolExecutor
+    c = frame_rays(scene, y0, y1).reshape(-1, 4)
+    M = scene.mass
+    lunit = M if scene.units == 1 else 2.0 * M
+    r_cam = scene.r_cam * lunit
+    th = math.radians(scene.theta_deg)
+    a = scene.spin * M
+    E, L, pr, pth = -c[:, 0], c[:, 1], c[:, 2], c[:, 3]
+    Q = pth * pth + math.cos(th) ** 2 * (L * L / math.sin(th) ** 2 - a * a * E * E)
+    l, q2 = L / (E * M), Q / (E * E * M * M)
+    su = np.where(pr < 0, 1.0, -1.0)
+    sm = np.where(pth > 0, -1.0, 1.0)
+    r_far = scene.escape_r if scene.escape_r > 0 else (scene.r_cam + 20.0) * lunit
+
+    def one(i):
+        n, xu, _ = geokerr_crossings(M / r_cam, math.cos(th), scene.spin, l[i], q2[i], su[i], sm[i], M / r_far, K)
+        return np.where(xu > 0, M / np.maximum(xu, 1e-300), 0.0)
+    with ThreadPoolExecutor(max_workers=threads or os.cpu_count()) as ex:
+        xr = list(ex.map(one, range(len(E))))
+    return np.array(xr).reshape(y1 - y0, scene.width, K)
 
 
 def trace_invariants(scene, px, py, threads=0):

@@ -970,6 +970,26 @@ int npo_trace_rays(const np_scene_t* sc, int n, const double* px, const double* 
 }
 
 // Conserved-quantity drift of explicit rays; layout as np_trace_invariants_device.
+// Camera momenta (p_t, p_phi, p_r, p_theta) of the rays of sample
+// `sample_offset` (the sample whose first crossing np_render_device reports
+// in rcross) of every pixel of rows [y_begin, y_end): consts[4 * ((y -
+// y_begin) * width + x) + 0..3].  The camera restatement of render.cu:137-170
+// as npo_render uses it.
+int npo_frame_rays(const np_scene_t* sc, int y_begin, int y_end, double* consts) {
+    if (!sc || !consts || y_begin < 0 || y_end > sc->height || y_begin > y_end) return NP_ERR_INVALID;
+    const np_scene_t s = *sc;
+    Frame f = make_frame(s);
+    for (int y = y_begin; y < y_end; ++y)
+        for (int x = 0; x < s.width; ++x) {
+            Dir d = camera_dir(f, s, x, y, (uint32_t)s.sample_offset, false, 0.0, 0.0);
+            State y0 = f.zamo ? camera_zamo(f.M, f.a, f.r_cam, f.th_cam, f.ph_cam, d.nr, d.nth, d.nph)
+                              : camera_static(f.M, f.a, f.r_cam, f.th_cam, f.ph_cam, d.nr, d.nth, d.nph);
+            double* c = consts + 4 * ((size_t)(y - y_begin) * s.width + x);
+            c[0] = y0.pt; c[1] = y0.pph; c[2] = y0.pr; c[3] = y0.pth;
+        }
+    return NP_OK;
+}
+
 int npo_trace_invariants(const np_scene_t* sc, int n, const double* px, const double* py, double* drift,
                          int32_t* steps, int nthreads) {
     if (!sc || n < 0 || !px || !py || !drift) return NP_ERR_INVALID;

@@ -39,17 +39,18 @@ def test_no_device_reported(built):
     assert rc == 1 and "No CUDA devices found." in err
 
 
-@pytest.mark.parametrize("args", [
-    ["--precision", "mixed", "--integrator", "rkf78"],
-    ["--precision", "mixed", "--crossing", "root"],
-    ["--mode", "research", "--precision", "mixed"],
+@pytest.mark.parametrize("args,msg", [
+    (["--precision", "mixed", "--crossing", "root"], "Root crossings on --precision mixed need --integrator rkf78."),
+    (["--mode", "research", "--precision", "mixed"], "Research mode needs --precision fp64."),
+    (["--precision", "mixed", "--integrator", "rkf78", "--inv-gate", "1e-12"],
+     "The invariant gate needs --precision fp64."),
 ])
-def test_research_settings_need_fp64(built, args):
-    """The embedded 7(8) integrator and root-found crossings run on the FP64
-    path only; the CLI refuses them with --precision mixed before touching a
-    device."""
+def test_research_settings_need_fp64(built, args, msg):
+    """Research mode and the invariant gate run on the FP64 path only, and
+    root crossings on the mixed path are Henon steps of its 7(8) integrator;
+    the CLI refuses the other combinations before touching a device."""
     rc, out, err = _run("--w", "8", "--h", "8", *args)
-    assert rc == 1 and err.strip() == "The rkf78 integrator and root crossings need --precision fp64."
+    assert rc == 1 and err.strip() == msg
 
 
 @pytest.mark.parametrize("args,msg", [

@@ -138,13 +138,17 @@ def test_scene_validation_and_path_checks(built):
                 dict(inv_gate=1.0)):
         t = s.replace(**bad)
         assert lib.np_scene_validate(C.byref(t)) == NP_ERR_INVALID, bad
+    for bad in (dict(rtol_fp64=float("nan")), dict(rtol_fp64=1.0)):
+        t = s.replace(**bad)
+        assert lib.np_scene_validate(C.byref(t)) == NP_ERR_INVALID, bad
     rgb = (C.c_float * (3 * 64 * 36))()
-    # the 7(8) integrator and root crossings exist on the FP64 path only: the
-    # mixed path refuses them before looking for a device
-    for kw in (dict(integrator=NP_INTEG_RKF78), dict(crossing=NP_CROSS_ROOT)):
+    # root crossings on the mixed path are Henon steps of the 7(8) integrator:
+    # with RK4 or step doubling the mixed path refuses them before looking for
+    # a device
+    for kw in (dict(crossing=NP_CROSS_ROOT), dict(crossing=NP_CROSS_ROOT, integrator=1)):
         t = _scene(**kw)
         assert lib.np_render_host(C.byref(t), NP_PREC_MIXED, rgb, None, None, None) == NP_ERR_INVALID
-        assert b"fp64" in lib.np_last_error()
+        assert b"rkf78" in lib.np_last_error()
 
 
 def test_cli_research_mode_refuses_mixed(built):
@@ -190,3 +194,13 @@ def test_research_in_reference_units_and_zamo(built):
                 errs.append(abs(o["cross"][i, j, 0] - r_ref) / r_ref)
         bar = 1e-6 if sc.units == 0 else 1e-10
         assert len(errs) > 20 and max(errs) < bar, (sc.units, len(errs), max(errs))
+
+
+def test_cli_mixed_root_needs_rkf78(built):
+    cli = os.path.join(os.path.dirname(npx.lib_path()), "render")
+    p = subprocess.run([cli, "--precision", "mixed", "--crossing", "root", "--w", "8", "--h", "8"],
+                       capture_output=True, text=True, timeout=60)
+    assert p.returncode == 1 and "--integrator rkf78" in p.stderr
+    p = subprocess.run([cli, "--precision", "mixed", "--inv-gate", "1e-12", "--w", "8", "--h", "8"],
+                       capture_output=True, text=True, timeout=60)
+    assert p.returncode == 1 and "precision fp64" in p.stderr
