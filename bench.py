@@ -73,9 +73,10 @@ def _clock_summary(path, gpu_index):
             "reasons": reasons, "samples": len(rows)}
 
 
-def cpu_baseline(threads=None, rows_every=45):
+def cpu_baseline(threads=None, rows_every=45, timing=None):
     """Oracle FP64 render of every `rows_every`-th row of the benchmark frame
-    on the host cores; returns (rays/s, cores, sample description)."""
+    on the host cores; returns (rays/s, cores, sample description).  `timing`
+    (a dict) receives the rays and seconds of the sample."""
     import oracle
     from nullpath_gb300._abi import benchmark_scene
     sc = benchmark_scene()
@@ -88,6 +89,9 @@ def cpu_baseline(threads=None, rows_every=45):
     rays = len(rows) * sc.width * sc.spp
     desc = "%d of %d rows (every %dth) x %d px x %d spp = %d rays, FP64 oracle, %.1f s" % (
         len(rows), sc.height, rows_every, sc.width, sc.spp, rays, dt)
+    if timing is not None:
+        timing["rays"] = rays
+        timing["seconds"] = dt
     return rays / dt, threads, desc
 
 
@@ -186,37 +190,32 @@ def batch_leg(n_scenes=256, seed=1, passes=3):
 
 def critical_leg(W=2048, spp=16, spin=0.998, n_acc=8000):
     """2048x2048 at a = 0.998 with 16 spp, half the rays within +-2 % of the
-    critical curve (NP_JITTER_CRITICAL), every FP64 island on; fixed RK4 and
-    adaptive step doubling at rtol 1e-7; crossing error against the Mino-time
-    solver on critical-sampled rays."""
+    critical curve (NP_JITTER_CRITICAL).  The mixed 7(8) path with its islands
+    off, with the default islands (horizon band, near-critical rays traced
+    whole in FP64) and with every island; the reference step law's RK4 with
+    every island for comparison.  Crossing error against the Mino-time solver
+    on critical-sampled rays beside each."""
     import torch
     import nullpath_gb300 as npx
-    sc = npx.benchmark_scene(width=W, height=W, spp=spp, spin=spin).replace(jitter=npx.NP_JITTER_CRITICAL,
-                                                                           islands=npx.NP_ISLANDS_ALL)
     from nullpath_gb300 import accuracy
-    from nullpath_gb300._abi import NP_INTEG_ADAPTIVE
+    base = npx.benchmark_scene(width=W, height=W, spp=spp, spin=spin).replace(jitter=npx.NP_JITTER_CRITICAL)
     rays = W * W * spp
     out = {"rays": rays}
     rgb = torch.zeros((3, W, W), dtype=torch.float32, device="cuda")
     rc = torch.zeros((W, W), dtype=torch.float32, device="cuda")
     cache = {}
-    for name, scn, precs in (("rk4", sc, ("mixed", "fp64")),
-                             ("adaptive_rtol_1e-7", sc.replace(integrator=NP_INTEG_ADAPTIVE, rtol=1e-7), ("mixed",))):
+    for name, scn in (("rkf78_islands_none", npx.accurate_scene(base).replace(islands=0)),
+                      ("rkf78_islands_default", npx.accurate_scene(base).replace(islands=npx.NP_ISLANDS_DEFAULT)),
+                      ("rkf78_islands_all", npx.accurate_scene(base).replace(islands=npx.NP_ISLANDS_ALL)),
+                      ("rk4_islands_all", base.replace(islands=npx.NP_ISLANDS_ALL))):
         npx.render(scn, "mixed", rgb=rgb, rcross=rc)
         _, _, st = npx.render(scn, "mixed", rgb=rgb, rcross=rc, stats=True)
         leg = {"rays_per_s": rays / ((st.kernel_ms + st.init_ms) * 1e-3), "kernel_ms": st.kernel_ms + st.init_ms,
                "mean_steps_per_ray": st.steps / max(1, st.rays), "fp64_steps_frac": st.fp64_steps / max(1, st.steps),
-               "deferred_rays": int(st.deferred_rays)}
-        for prec in precs:
-            leg["error_vs_geokerr_" + prec] = accuracy.crossing_error(scn, n=n_acc, precision=prec, seed=3,
-                                                                      critical=True, cache=cache)
+               "deferred_rays": int(st.deferred_rays),
+               "error_vs_geokerr": accuracy.crossing_error(scn, n=n_acc, precision="mixed", seed=3, critical=True,
+                                                           cache=cache)}
         out[name] = leg
-    # without FP64 islands: the same crossings, for the cost of the islands
-    bare = sc.replace(islands=0)
-    _, _, st = npx.render(bare, "mixed", rgb=rgb, rcross=rc, stats=True)
-    out["rk4_no_islands"] = {"rays_per_s": rays / ((st.kernel_ms + st.init_ms) * 1e-3),
-                             "error_vs_geokerr_mixed": accuracy.crossing_error(bare, n=n_acc, precision="mixed", seed=3,
-                                                                               critical=True, cache=cache)}
     return out
 
 
@@ -297,27 +296,63 @@ def adjoint_leg(Ks=(16, 64, 256)):
     return out
 
 
+def headline_scene(path):
+    """The timed workload: the 1280x720x4, a = 0.9 benchmark frame.
+      rkf78  mixed path, compensated FP32 7(8) under error control at rtol
+             1e-8 with Henon crossings; the horizon band (a certified capture
+             test, FP64 steps otherwise) and near-critical rays (|b - b_crit|
+             < 1e-3 M, traced whole in FP64) as islands.  Turning-point
+             islands are measured beside it (islands_all): they cost about 5x
+             and do not change the crossing error of this formulation.
+      rk4    the reference's step law h = 0.01 clamp(r, 1, 100) and RK4 with
+             Hermite crossings, every FP64 island on."""
+    import nullpath_gb300 as npx
+    base = npx.benchmark_scene(seed=0)
+    if path == "rk4":
+        return base.replace(islands=npx.NP_ISLANDS_ALL)
+    return npx.accurate_scene(base).replace(islands=npx.NP_ISLANDS_DEFAULT)
+
+
+def path_flops(oc, path, precision, st):
+    """Algorithmic FP32 (or FP64) flops of one render's tracer kernel from its
+    statistics and the op counts of nullpath_gb300/opcount.json."""
+    if precision == "fp64":
+        return oc["fp64_step_flops"] * st.steps
+    if path == "rk4":
+        return oc["mixed_step_flops"] * (st.steps - st.fp64_steps)
+    steps32 = st.steps - st.fp64_steps
+    # 13 evaluations per 7(8) attempt (FP32 or island), one per ray start
+    attempts32 = max(steps32, (st.rhs_evals - st.rays) / 13.0 - st.fp64_steps)
+    return oc["mixed78_step_flops"] * steps32 + oc["mixed78_rejected_attempt_flops"] * (attempts32 - steps32)
+
+
 def run_reference(args):
     ws, rank = _dist()
     if rank != 0:
         return
-    per_step = []
     desc = None
     cores = os.cpu_count()
+    rays = secs = 0.0
     for i in range(args.warmup + args.steps):
-        v, cores, desc = cpu_baseline(rows_every=args.ref_rows_every)
+        t = {}
+        v, cores, desc = cpu_baseline(rows_every=args.ref_rows_every, timing=t)
         if i >= args.warmup:
-            per_step.append(v)
-    val = statistics.mean(per_step)
+            rays += t["rays"]
+            secs += t["seconds"]
+    # one step is the sampled work actually executed (a row sample of the
+    # frame): ms_per_step is its measured time, value the rays of all timed
+    # steps over their time
+    val = rays / secs
     cpu = {"value": val, "unit": "rays/s", "cores": cores, "kind": "port",
            "sample": desc + "; restatement bit-identical to the reference headers in reference mode"}
-    full_rays = 1280 * 720 * 4
     out = {"impl": "reference", "metric": METRIC, "value": val, "unit": "rays/s", "n_gpus": ws,
-           "steps": args.steps, "warmup": args.warmup, "ms_per_step": full_rays / val * 1e3,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": secs / args.steps * 1e3,
            "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
            "config": {"workload": WORKLOAD, "sample": desc, "device": "host cpu",
-                      "ms_per_step": "time of one full 1280x720x4 pass at the sampled rate"},
+                      "rays_per_step": int(rays / args.steps),
+                      "step": "the row sample above of the 1280x720x4 frame (FP64 RK4 at the reference step "
+                              "law, the reference renderer's arithmetic)"},
            "cpu_baseline": cpu,
            "e2e": {"value": val, "unit": "rays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
@@ -339,10 +374,12 @@ def run_ours(args):
             dist.barrier()
 
     lib = npx.load()
-    # FP64 within 0.1 M of the horizon, at turning points and for near-critical
-    # impact parameters: every island of the mixed path
     from nullpath_gb300 import replicas
-    sc = replicas.rank_scene(npx.benchmark_scene(seed=0).replace(islands=npx.NP_ISLANDS_ALL), rank)
+    sc = replicas.rank_scene(headline_scene(args.path), rank)
+    if args.frame:
+        # a smaller frame of the same scene (profiling captures); not the benchmark workload
+        fw, fh = (int(v) for v in args.frame.lower().split("x"))
+        sc = sc.replace(width=fw, height=fh)
     H, W = sc.height, sc.width
     rays_per_step = W * H * sc.spp
     rgb = torch.zeros((3, H, W), dtype=torch.float32, device="cuda")
@@ -400,32 +437,42 @@ def run_ours(args):
     if rank == 0:
         oc = _opcount()
         st = stats[-1]
-        flop_step = oc["mixed_step_flops"] if args.precision == "mixed" else oc["fp64_step_flops"]
         kern_ms = statistics.mean(s.kernel_ms for s in stats)
-        steps_main = st.steps - (st.fp64_steps if args.precision == "mixed" else 0)
-        achieved = flop_step * steps_main / (kern_ms * 1e-3) / 1e12
+        achieved = path_flops(oc, args.path, args.precision, st) / (kern_ms * 1e-3) / 1e12
         peak = ctypes_peak(lib, 0 if args.precision == "mixed" else 1)
+        tkey = "dram_bytes_per_ray_rkf78" if args.path == "rkf78" else "dram_bytes_per_ray"
+        traffic = oc.get(tkey)
         out = {
             "metric": METRIC, "value": replicas.aggregate_rays_per_s(rays_per_step, ms, ws), "unit": "rays/s",
             "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32+f64" if args.precision == "mixed" else "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "width": W, "height": H, "spp": sc.spp, "spin": sc.spin,
-                       "precision": args.precision, "rays_per_step": rays_per_step,
-                       "fp64_islands": "horizon band 0.1 M, radial/polar turning points, |b-b_crit| < 1e-3 M",
+            "config": {"workload": WORKLOAD if not args.frame else "kerr_render_%s_a0.9_4spp" % args.frame,
+                       "width": W, "height": H, "spp": sc.spp, "spin": sc.spin,
+                       "precision": args.precision, "path": args.path,
+                       "integrator": "compensated FP32 Fehlberg 7(8), rtol %g, atol %g, Henon crossings" % (
+                           sc.rtol, sc.atol) if args.path == "rkf78" else "RK4, h = 0.01 clamp(r, 1, 100), Hermite",
+                       "rays_per_step": rays_per_step,
+                       "fp64_islands": ("horizon band 0.1 M (certified capture, FP64 steps otherwise), "
+                                        "|b-b_crit| < 1e-3 M" if args.path == "rkf78" else
+                                        "horizon band 0.1 M, radial/polar turning points, |b-b_crit| < 1e-3 M"),
                        "l2": "256 MiB buffer written between timed steps (outside the step events)",
                        "parallelism": "replicas" if ws > 1 else "single"},
             "steps_per_s": ws * st.steps / (ms * 1e-3),
             "mean_steps_per_ray": st.steps / max(1, st.rays),
+            "rhs_evals_per_ray": st.rhs_evals / max(1, st.rays),
             "fp64_island_steps_frac": st.fp64_steps / max(1, st.steps),
             "deferred_rays": st.deferred_rays,
             "kernel_ms": {"tracer": kern_ms, "ray_init": statistics.mean(s.init_ms for s in stats)},
             "roofline": {"bound": "fp32" if args.precision == "mixed" else "fp64", "achieved": achieved,
                          "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
-                         "traffic": oc["dram_bytes_per_ray"] * rays_per_step,
-                         "traffic_source": "ncu DRAM bytes per ray of render_mixed_kernel (640x360x4 capture) "
-                                           "scaled to the rays of one launch",
-                         "peak_source": "measured in this run by np_measure_fma_peak (register FMA loop)"},
+                         "traffic": traffic * rays_per_step if traffic else None,
+                         "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per ray of the tracer "
+                                           "kernel (nullpath_gb300/opcount.json), scaled to the rays of one launch",
+                         "achieved_source": "algorithmic flops (nullpath_gb300/opcount.json) of the accepted steps "
+                                            "and rejected attempts of the timed launches over their CUDA-event time",
+                         "peak_source": "measured in this run by np_measure_fma_peak (register FMA loop); "
+                                        "MEASURED_PEAKS.json holds HBM and bf16 figures only"},
             "e2e": {"value": replicas.aggregate_rays_per_s(rays_per_step, e2e, ws), "unit": "rays/s",
                     "h2d_bytes_per_step": C.sizeof(sc),
                     "d2h_bytes_per_step": 4 * H * W * 4},
@@ -433,18 +480,27 @@ def run_ours(args):
             "clocks": clocks,
             "wall_s": wall,
         }
-        if args.precision == "mixed":
-            # the library's default island mask (horizon and near-critical)
-            dsc = sc.replace(islands=npx.NP_ISLANDS_DEFAULT)
-            dms = []
-            for i in range(3):
+
+        def timed(scn, prec="mixed", n=3):
+            best = None
+            for i in range(n + 1):
                 flush.fill_(float(i))
-                _, _, sd = npx.render(dsc, "mixed", rgb=rgb, rcross=rc, stats=True)
-                dms.append(sd.kernel_ms + sd.init_ms)
-            out["default_islands"] = {"islands": "horizon band + near-critical", "rays_per_s":
-                                      rays_per_step / (min(dms) * 1e-3), "kernel_ms": min(dms)}
+                _, _, sd = npx.render(scn, prec, rgb=rgb, rcross=rc, stats=True)
+                if i and (best is None or sd.kernel_ms + sd.init_ms < best.kernel_ms + best.init_ms):
+                    best = sd
+            t = best.kernel_ms + best.init_ms
+            return {"rays_per_s": rays_per_step / (t * 1e-3), "kernel_ms": t,
+                    "mean_steps_per_ray": best.steps / max(1, best.rays),
+                    "rhs_evals_per_ray": best.rhs_evals / max(1, best.rays),
+                    "fp64_island_steps_frac": best.fp64_steps / max(1, best.steps)}
+        if args.precision == "mixed" and args.path == "rkf78":
+            out["islands_all"] = timed(sc.replace(islands=npx.NP_ISLANDS_ALL))
+            out["islands_all"]["islands"] = "horizon band, turning points (FP64 7(8) steps), near-critical"
+            out["islands_none"] = timed(sc.replace(islands=0))
+            out["rk4_reference_step_law"] = timed(headline_scene("rk4"))
+            out["rk4_reference_step_law"]["islands"] = "all"
         if args.fp64_frame and args.precision == "mixed":
-            _, _, s64 = npx.render(sc, "fp64", stats=True)
+            _, _, s64 = npx.render(headline_scene("rk4"), "fp64", stats=True)
             out["fp64_path"] = {"rays_per_s": rays_per_step / (s64.kernel_ms * 1e-3), "kernel_ms": s64.kernel_ms,
                                 "mean_steps_per_ray": s64.steps / max(1, s64.rays),
                                 "roofline": {"bound": "fp64", "achieved": oc["fp64_step_flops"] * s64.steps /
@@ -455,19 +511,16 @@ def run_ours(args):
             out["mixed_over_fp64"] = out["value"] / ws / out["fp64_path"]["rays_per_s"]
         if args.accuracy:
             from nullpath_gb300 import accuracy
-            acc = {"reference_step_law": accuracy.crossing_error(sc, n=20000, precision=args.precision, seed=1)}
-            fine = sc.replace(step_scale=0.0025)
-            _, _, sf = npx.render(fine, args.precision, rgb=rgb, rcross=rc, stats=True)
-            _, _, sf = npx.render(fine, args.precision, rgb=rgb, rcross=rc, stats=True)
-            acc["step_0.0025"] = accuracy.crossing_error(fine, n=20000, precision=args.precision, seed=1)
-            acc["step_0.0025"]["rays_per_s"] = rays_per_step / ((sf.kernel_ms + sf.init_ms) * 1e-3)
-            from nullpath_gb300._abi import NP_INTEG_ADAPTIVE
-            adap = sc.replace(integrator=NP_INTEG_ADAPTIVE, rtol=1e-7)
-            _, _, sa = npx.render(adap, args.precision, rgb=rgb, rcross=rc, stats=True)
-            _, _, sa = npx.render(adap, args.precision, rgb=rgb, rcross=rc, stats=True)
-            acc["adaptive_rtol_1e-7"] = accuracy.crossing_error(adap, n=20000, precision=args.precision, seed=1)
-            acc["adaptive_rtol_1e-7"]["rays_per_s"] = rays_per_step / ((sa.kernel_ms + sa.init_ms) * 1e-3)
-            acc["adaptive_rtol_1e-7"]["mean_steps_per_ray"] = sa.steps / max(1, sa.rays)
+            cache = {}
+            acc = {"headline": accuracy.crossing_error(sc, n=50000, precision=args.precision, seed=21, cache=cache)}
+            if args.path == "rkf78":
+                acc["islands_all"] = accuracy.crossing_error(sc.replace(islands=npx.NP_ISLANDS_ALL), n=50000,
+                                                             precision=args.precision, seed=21, cache=cache)
+                acc["islands_none"] = accuracy.crossing_error(sc.replace(islands=0), n=50000,
+                                                              precision=args.precision, seed=21, cache=cache)
+                acc["rk4_reference_step_law"] = accuracy.crossing_error(headline_scene("rk4"), n=50000,
+                                                                        precision=args.precision, seed=21,
+                                                                        cache=cache)
             out["error_vs_geokerr"] = acc
             leg_s = {}
             for key, fn in (("geokerr_grid", geokerr_grid_leg), ("adjoint_256x256x4", adjoint_leg),
@@ -501,6 +554,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--frame", default=None, help="WxH: a smaller frame of the same scene (profiling only)")
+    ap.add_argument("--path", default="rkf78", choices=["rkf78", "rk4"],
+                    help="integrator of the timed frame (see headline_scene)")
     ap.add_argument("--no-fp64-frame", dest="fp64_frame", action="store_false")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--no-accuracy", dest="accuracy", action="store_false")

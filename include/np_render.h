@@ -90,6 +90,19 @@ typedef enum np_background { NP_BG_GRADIENT = 0, NP_BG_POINT = 1 } np_background
  *                  turning points and for near-critical impact parameters. */
 typedef enum np_precision { NP_PREC_FP64 = 0, NP_PREC_MIXED = 1 } np_precision;
 
+/* Arithmetic of the island steps and near-critical rays of the mixed 7(8)
+ * path (np_scene_t.island_arith; the RK4 and step-doubling mixed paths use
+ * native FP64).
+ *   NP_ISLAND_ARITH_FP64  native FP64 (default)
+ *   NP_ISLAND_ARITH_DF    double-float: unevaluated pairs of FP32 values, a
+ *                         48-bit significand, on the FP32 pipes (a double-
+ *                         float addition costs 20 FP32 operations, a product
+ *                         8).  On GB300 it measured slower than native FP64
+ *                         despite FP64's 1/64 rate: its long dependent
+ *                         operation chains leave the few island warps
+ *                         latency-bound. */
+typedef enum np_island_arith { NP_ISLAND_ARITH_FP64 = 0, NP_ISLAND_ARITH_DF = 1 } np_island_arith;
+
 /* FP64 islands of NP_PREC_MIXED (bit mask, np_scene_t.islands). */
 #define NP_ISLAND_HORIZON 1   /* steps within 0.1 M of the outer horizon */
 #define NP_ISLAND_TURNING 2   /* steps across a radial or polar turning point */
@@ -136,6 +149,9 @@ typedef struct np_scene {
     double rtol_fp64;             /* rtol of the near-critical rays the mixed 7(8) path traces
                                      whole in FP64; <= 0 means min(rtol, 1e-10) (its island steps
                                      keep rtol) */
+    int32_t island_arith;         /* np_island_arith: arithmetic of the FP64-class steps of the
+                                     mixed 7(8) path */
+    int32_t reserved0;            /* 0 */
 } np_scene_t;
 
 /* Per-call statistics, filled when the pointer is non-NULL. */
@@ -277,14 +293,16 @@ int np_render_device_noalloc(const np_scene_t* scene, int precision,
  *   NP_TUNE_CROSS_BATCH   lanes of a warp with a pending root-found crossing
  *                         (NP_CROSS_ROOT, FP64 path) that trigger the search
  *                         of all of them (1-32, default 12; 1 = at once)
- *   NP_TUNE_MIN_BLOCKS78  register cap of the mixed 7(8) tracer (3 or 4;
- *                         default 3: its FP32 loop, with the FP64 island
- *                         step inlined, needs about 168 registers) */
+ *   NP_TUNE_MIN_BLOCKS78  register cap of the mixed 7(8) tracer (3 or 4,
+ *                         default 4)
+ *   NP_TUNE_ISLAND_BATCH78 NP_TUNE_ISLAND_BATCH of the mixed 7(8) tracer
+ *                         (1..32, default 32) */
 #define NP_TUNE_ISLAND_BATCH 1
 #define NP_TUNE_MIN_BLOCKS 2
 #define NP_TUNE_CHUNK 3
 #define NP_TUNE_CROSS_BATCH 4
 #define NP_TUNE_MIN_BLOCKS78 5
+#define NP_TUNE_ISLAND_BATCH78 6
 int np_tune(int param, int value);
 
 /* Measures the sustained FMA throughput of this GPU's SIMT pipes with a

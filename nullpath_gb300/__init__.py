@@ -16,7 +16,8 @@ from ._abi import (Scene, RenderStats, isco_radius, reference_defaults, benchmar
                    NP_INTEG_RK4, NP_INTEG_ADAPTIVE, NP_INTEG_RKF78, NP_CROSS_LINEAR, NP_CROSS_HERMITE,
                    NP_CROSS_ROOT,
                    NP_BG_GRADIENT, NP_BG_POINT, NP_ISLAND_HORIZON, NP_ISLAND_TURNING,
-                   NP_ISLAND_CRITICAL, NP_ISLANDS_ALL, NP_ISLANDS_DEFAULT)
+                   NP_ISLAND_CRITICAL, NP_ISLANDS_ALL, NP_ISLANDS_DEFAULT, NP_ISLAND_ARITH_DF,
+                   NP_ISLAND_ARITH_FP64)
 from ._lib import load, lib_path, NullPathError
 from .render import render, render_host, trace_rays, trace_invariants, precision_code
 

@@ -57,6 +57,9 @@ struct SceneDev {
     double rtol64;             // rtol of the FP64 7(8) islands and near-critical rays of the mixed path
     float atol78_f;            // atol of the FP32 7(8) steps: the scene's, at least 1e-9 M (FP32 resolution)
     int cert_capture;          // 7(8) path: rays certified to fall in end at the horizon band (disk outside it)
+    int island_df;             // 7(8) path: FP64-class steps in double-float arithmetic
+    float a_hl[2], M_hl[2], rp_hl[2], rm_hl[2];   // a, M, r_+, r_- as double-float pairs
+    float rtol64_f, atol64_f;  // tolerances of the near-critical rays (double-float arithmetic)
     int island_batch;
     int cross_batch;           // pending root-found crossings that trigger a warp's search (FP64 tracer)
     // NP_JITTER_CRITICAL: tangent-plane radius of the critical curve at

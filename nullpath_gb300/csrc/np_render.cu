@@ -23,6 +23,7 @@
 #include "np_common.cuh"
 #include "tracer_fp64.cuh"
 #include "tracer_mixed.cuh"
+#include "tracer_df.cuh"
 
 using namespace np;
 
@@ -61,6 +62,10 @@ constexpr int kStepsPerTurn = 4;   // FP32 steps per pass of the mixed tracer's 
 // Tunables (set through np_tune; the autotuner searches them).
 struct Tuning {
     int island_batch = 8;   // parked lanes that trigger a batched FP64 island step
+    // The same for the 7(8) path, whose island steps (FP64 7(8)) cost about
+    // 80 FP32 steps: the warp waits until every lane with work is parked.
+    // 1280x720x4 frame, every island: 8 / 16 / 32 lanes gave 206 / 152 / 117 ms.
+    int island_batch78 = 32;
     // Lanes with a pending root-found crossing that trigger the warp's
     // search (FP64 tracer).  A search costs the warp about four single
     // steps; batching trades the stall of the other lanes against the wait
@@ -68,7 +73,12 @@ struct Tuning {
     // 12 lanes gave 329 / 367 / 393 / 402 k rays/s.
     int cross_batch = 12;
     int min_blocks = 4;     // register cap of the mixed tracer (blocks of 128 per SM)
-    int min_blocks78 = 3;   // the same for the mixed 7(8) tracer
+    // The same for the mixed 7(8) tracer.  Its FP32 loop alone needs 103
+    // registers; with the FP64 island step inlined, 168 fit without spills,
+    // while the 128 of 4 blocks spill around the island step.  Measured on the
+    // 1280x720x4 frame, 4 blocks are faster all the same: 17.5 vs 20.4 ms
+    // without islands, 201 vs 206 ms with every island.
+    int min_blocks78 = 4;
     int chunk = 64;         // ray indices a warp takes from the global counter at once
 };
 Tuning g_tune;
@@ -205,7 +215,11 @@ int prepare_scene(const np_scene_t& sc, SceneDev& d) {
         d.rtol_f = (float)d.rtol; d.atol_f = (float)d.atol;
         d.atol78_f = (float)std::fmax(d.atol, 1e-9 * d.M);
         d.cert_capture = !d.disk_on || d.rin > d.r_plus + kHorizonBand * d.M;
-        d.island_batch = g_tune.island_batch;
+        d.island_df = sc.island_arith == NP_ISLAND_ARITH_DF;
+        auto split = [](double x, float* o) { o[0] = (float)x; o[1] = (float)(x - (double)o[0]); };
+        split(d.a, d.a_hl); split(d.M, d.M_hl); split(d.r_plus, d.rp_hl); split(d.r_minus, d.rm_hl);
+        d.rtol64_f = (float)d.rtol64; d.atol64_f = (float)std::fmax(d.atol, 1e-14 * d.M);
+        d.island_batch = sc.integrator == NP_INTEG_RKF78 ? g_tune.island_batch78 : g_tune.island_batch;
         d.cross_batch = g_tune.cross_batch;
     }
     const double M = d.M, a = d.a, r = d.r_cam, th = d.th_cam;
@@ -415,7 +429,12 @@ __device__ __forceinline__ void load_ray(const InitSoA& soa, long long i, MRay<f
 // Integrator families of the mixed tracer (one kernel instantiation each, so
 // the 7(8) stage storage does not raise the register count of the RK4 loop).
 constexpr int kFamRk4 = 0;   // fixed RK4 and step doubling
-constexpr int kFam78 = 1;    // embedded 7(8)
+constexpr int kFam78 = 1;    // embedded 7(8), FP64 islands and near-critical rays
+constexpr int kFam78df = 2;  // embedded 7(8), the same in double-float arithmetic
+
+template <int FAM> struct CritRay { using type = DRay<false>; };
+template <> struct CritRay<kFam78> { using type = DRay78<false>; };
+template <> struct CritRay<kFam78df> { using type = DRay78df<false>; };
 
 template <int MINB, int FAM>
 __global__ void __launch_bounds__(kBlock, MINB)
@@ -431,7 +450,7 @@ render_mixed_kernel(const SceneDev s, const InitSoA soa, float* __restrict__ srg
     if ((threadIdx.x >> 5) == 0 && (int)blockIdx.x < nd) {
         WarpQueue q{0, 0};
         bool drained = false, have = false;
-        typename std::conditional<FAM == kFam78, DRay78<false>, DRay<false>>::type R;
+        typename CritRay<FAM>::type R;
         long long item = 0, p = 0;
         int sl = 0;
         float cam_y = 0.0f;
@@ -446,7 +465,9 @@ render_mixed_kernel(const SceneDev s, const InitSoA soa, float* __restrict__ srg
                     ray_coords(s, item, p, sl, x, y, sid);
                     float4 a = soa.a[item], b = soa.b[item];
                     cam_y = soa.cy[item];
-                    if constexpr (FAM == kFam78)
+                    if constexpr (FAM == kFam78df)
+                        dray78df_start(R, s, HiLo{b.x, b.y}, HiLo{b.z, b.w}, HiLo{a.x, a.y}, HiLo{a.z, a.w});
+                    else if constexpr (FAM == kFam78)
                         dray78_start(R, s, (double)b.x + (double)b.y, (double)b.z + (double)b.w,
                                      (double)a.x + (double)a.y, (double)a.z + (double)a.w);
                     else
@@ -459,11 +480,16 @@ render_mixed_kernel(const SceneDev s, const InitSoA soa, float* __restrict__ srg
             if (!__any_sync(FULL, have)) break;
             if (have) {
                 bool done;
-                if constexpr (FAM == kFam78) {
+                if constexpr (FAM == kFam78df) {
+                    bool acc;
+                    done = dray78df_step(R, s, acc);
+                    if (acc) { n_steps++; n_f64++; }
+                    n_evals += 13;
+                } else if constexpr (FAM == kFam78) {
                     bool acc;
                     done = dray78_step(R, s, acc);
                     if (acc) { n_steps++; n_f64++; }
-                    n_evals += 12;
+                    n_evals += 13;
                 } else {
                     done = dray_step(R, s);
                     n_steps++; n_f64++; n_evals += 4;
@@ -496,7 +522,7 @@ render_mixed_kernel(const SceneDev s, const InitSoA soa, float* __restrict__ srg
                 ray_coords(s, idx, p, sl, x, y, sid);
                 load_ray(soa, idx, R, cam_y);
                 mray_start(R, s, k);
-                if constexpr (FAM == kFam78) mray_set_k78(R, k);
+                if constexpr (FAM != kFamRk4) mray_set_k78(R, k);
                 have = true;
                 n_rays++;
                 n_evals++;
@@ -511,10 +537,14 @@ render_mixed_kernel(const SceneDev s, const InitSoA soa, float* __restrict__ srg
         bool done = false;
         if (pend && ((int)__popc(pend) >= T || !act)) {
             if (have && R.pending) {
-                if constexpr (FAM == kFam78) {
+                if constexpr (FAM == kFam78df) {
+                    int att;
+                    done = mray_island78_df(R, s, k, att);
+                    n_steps++; n_f64++; n_evals += 13 * att;
+                } else if constexpr (FAM == kFam78) {
                     int att;
                     done = mray_island78(R, s, k, att);
-                    n_steps++; n_f64++; n_evals += 13 * (att + 1);
+                    n_steps++; n_f64++; n_evals += 13 * att;
                 } else {
                     done = mray_island(R, s, k);
                     n_steps++; n_f64++; n_evals += 5;
@@ -528,7 +558,7 @@ render_mixed_kernel(const SceneDev s, const InitSoA soa, float* __restrict__ srg
 #pragma unroll 1
             for (int j = 0; j < kStepsPerTurn; ++j) {
                 int r;
-                if constexpr (FAM == kFam78) {
+                if constexpr (FAM != kFamRk4) {
                     bool acc;
                     r = mray_step78(R, s, k, acc);
                     if (r != STEP_PARK) { n_steps += acc ? 1 : 0; n_evals += 13; }
@@ -591,7 +621,14 @@ __global__ void trace_rays_kernel(const SceneDev s, int precision, int n, const 
         for (int j = 0; j < 4; ++j) { xr[j] = R.xr[j]; xphi[j] = R.xphi[j]; }
         ncross = R.crossings; st = R.status;
     } else if ((s.islands & kIslandCritical) && near_critical(E, L, Q, s.a, s.M, s.r_plus, kCriticalDb)) {
-        if (s.integrator == NP_INTEG_RKF78) {
+        if (s.integrator == NP_INTEG_RKF78 && s.island_df) {
+            DRay78df<true> R;
+            dray78df_start(R, s, d_hl(E), d_hl(L), d_hl(m.pr), d_hl(m.pth));
+            bool acc;
+            while (!dray78df_step(R, s, acc)) {}
+            for (int j = 0; j < 4; ++j) { xr[j] = R.xr[j]; xphi[j] = R.xphi[j]; }
+            ncross = R.crossings; st = R.status;
+        } else if (s.integrator == NP_INTEG_RKF78) {
             DRay78<true> R;
             dray78_start(R, s, E, L, m.pr, m.pth);
             bool acc;
@@ -614,7 +651,10 @@ __global__ void trace_rays_kernel(const SceneDev s, int precision, int n, const 
         while (true) {
             bool acc;
             int r = mray_step78(R, s, k, acc);
-            if (r == STEP_PARK) { int att; r = mray_island78(R, s, k, att) ? STEP_DONE : STEP_CONT; }
+            if (r == STEP_PARK) {
+                int att;
+                r = (s.island_df ? mray_island78_df(R, s, k, att) : mray_island78(R, s, k, att)) ? STEP_DONE : STEP_CONT;
+            }
             if (r == STEP_DONE) break;
         }
         for (int j = 0; j < 4; ++j) { xr[j] = R.xr_d[j]; xphi[j] = R.xphi[j]; }
@@ -765,7 +805,8 @@ void launch_mixed(int minb, const SceneDev& s, const InitSoA& soa, float* srgb, 
                   Counters* ctr, int chunk, cudaStream_t st) {
     if (s.integrator == NP_INTEG_RKF78) {
         // the 7(8) loop holds about nine stage vectors: caps of 3 and 4 blocks only
-        if (g_tune.min_blocks78 == 4) launch_mixed_t<4, kFam78>(s, soa, srgb, rc, inv3, ctr, chunk, st);
+        if (s.island_df) launch_mixed_t<4, kFam78df>(s, soa, srgb, rc, inv3, ctr, chunk, st);
+        else if (g_tune.min_blocks78 == 4) launch_mixed_t<4, kFam78>(s, soa, srgb, rc, inv3, ctr, chunk, st);
         else launch_mixed_t<3, kFam78>(s, soa, srgb, rc, inv3, ctr, chunk, st);
         return;
     }
@@ -858,6 +899,8 @@ int np_scene_validate(const np_scene_t* s) {
         return fail(NP_ERR_INVALID, "Invalid crossing mode.");
     if (!(s->inv_gate >= 0.0 && s->inv_gate < 1.0)) return fail(NP_ERR_INVALID, "Invalid invariant gate.");
     if (!(s->rtol_fp64 < 1.0) || !std::isfinite(s->rtol_fp64)) return fail(NP_ERR_INVALID, "Invalid FP64 tolerance.");
+    if (s->island_arith != NP_ISLAND_ARITH_DF && s->island_arith != NP_ISLAND_ARITH_FP64)
+        return fail(NP_ERR_INVALID, "Invalid island arithmetic.");
     // non-finite values in any other field would only surface as NaN images
     auto fin = [](double v) { return std::isfinite(v); };
     if (!fin(s->theta_deg) || !fin(s->phi_deg)) return fail(NP_ERR_INVALID, "Invalid camera angle.");
@@ -1017,6 +1060,10 @@ int np_tune(int param, int value) {
         case NP_TUNE_CHUNK:
             if (value < 1 || value > 4096) return fail(NP_ERR_INVALID, "chunk must be in [1, 4096]");
             g_tune.chunk = value;
+            return NP_OK;
+        case NP_TUNE_ISLAND_BATCH78:
+            if (value < 1 || value > 32) return fail(NP_ERR_INVALID, "island batch must be in [1, 32]");
+            g_tune.island_batch78 = value;
             return NP_OK;
         case NP_TUNE_MIN_BLOCKS78:
             if (value != 3 && value != 4) return fail(NP_ERR_INVALID, "min blocks of the 7(8) tracer must be 3 or 4");

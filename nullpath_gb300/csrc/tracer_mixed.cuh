@@ -868,7 +868,7 @@ __device__ __forceinline__ T f78_norm(const V4<T>& y0, const V5<T>& d, const V4<
         e = fmax(e, fabs(ee[i]) / fmax(sc, T(1e-30)));
         finite = finite && isfinite(dd[i]) && isfinite(ee[i]);
     }
-    return finite ? e : T(INFINITY);
+    return finite ? e : T(1e30);
 }
 
 // Step-size factor after an attempt with error norm e.
