@@ -393,7 +393,7 @@ __device__ __forceinline__ void init_one(const SceneDev& s, long long li, long l
     bool defer = false;
     if (s.islands & kIslandCritical) {
         double Q = m.pth * m.pth + s.cos_cam * s.cos_cam * (L * L / (s.sin_cam * s.sin_cam) - s.a * s.a * E * E);
-        defer = near_critical(E, L, Q, s.a, s.M, s.r_plus, kCriticalDb);
+        defer = near_critical_screened(E, L, Q, s.a, s.M, s.r_plus, kCriticalDb);
     }
     HiLo pr = d_hl(m.pr), pth = d_hl(m.pth), Eh = d_hl(E), Lh = d_hl(L);
     soa.a[gi] = make_float4(pr.hi, pr.lo, pth.hi, pth.lo);
@@ -620,7 +620,7 @@ __global__ void trace_rays_kernel(const SceneDev s, int precision, int n, const 
         }
         for (int j = 0; j < 4; ++j) { xr[j] = R.xr[j]; xphi[j] = R.xphi[j]; }
         ncross = R.crossings; st = R.status;
-    } else if ((s.islands & kIslandCritical) && near_critical(E, L, Q, s.a, s.M, s.r_plus, kCriticalDb)) {
+    } else if ((s.islands & kIslandCritical) && near_critical_screened(E, L, Q, s.a, s.M, s.r_plus, kCriticalDb)) {
         if (s.integrator == NP_INTEG_RKF78 && s.island_df) {
             DRay78df<true> R;
             dray78df_start(R, s, d_hl(E), d_hl(L), d_hl(m.pr), d_hl(m.pth));

@@ -523,6 +523,43 @@ __host__ __device__ __forceinline__ bool near_critical(double E, double L, doubl
     return g < 1e299 && fabs(g) < 0.385 * db_thr / M;
 }
 
+// near_critical with an FP32 screen: the FP32 gap (Newton on the same
+// cubic to 1e-6 relative, then the same ratio) is within about 1e-6 of the
+// FP64 one, so a ray whose FP32 gap is beyond 4x the threshold, or whose
+// photon-orbit radius lies clearly inside the horizon, is not near-critical;
+// every other ray takes the FP64 test.  The decisions equal near_critical's;
+// most rays skip its FP64 Newton iterations (GB300 runs FP64 at 1/64 rate).
+__device__ __forceinline__ bool near_critical_screened(double E, double L, double Q, double a, double M, double rp,
+                                                       double db_thr) {
+    const float Ef = (float)E, Lf = (float)L, Qf = (float)Q, af = (float)a, Mf = (float)M, rpf = (float)rp;
+    const float K = Qf + (Lf - af * Ef) * (Lf - af * Ef);
+    const float c3 = 4.0f * Ef * Ef;
+    const float c1 = 4.0f * af * af * Ef * Ef - 4.0f * af * Ef * Lf - 2.0f * K;
+    const float c0 = 2.0f * Mf * K;
+    float r = sqrtf(fmaxf(0.0f, -c1 / c3)) + 4.0f * Mf;
+    bool conv = false;
+#pragma unroll 1
+    for (int it = 0; it < 30; ++it) {
+        const float f = (c3 * r * r + c1) * r + c0;
+        const float fp = 3.0f * c3 * r * r + c1;
+        if (fp <= 0.0f) break;
+        const float dr = f / fp;
+        r -= dr;
+        if (fabsf(dr) < 1e-6f * r) { conv = true; break; }
+    }
+    if (conv && isfinite(r)) {
+        if (r < rpf * (1.0f - 1e-4f)) return false;
+        if (r > rpf * (1.0f + 1e-4f)) {
+            const float r2 = r * r;
+            const float P = (r2 + af * af) * Ef - af * Lf;
+            const float Del = r2 - 2.0f * Mf * r + af * af;
+            const float g = (P * P - Del * K) / (Ef * Ef * r2 * r2);
+            if (isfinite(g) && fabsf(g) > 4.0f * 0.385f * (float)(db_thr / M)) return false;
+        }
+    }
+    return near_critical(E, L, Q, a, M, rp, db_thr);
+}
+
 // RK4 increments d = h/6 (k1 + 2 k2 + 2 k3 + k4) of (r, theta, p_r, p_theta[, phi])
 // from a (hi, lo) state whose first stage k1 is known.
 template <bool PHI>
