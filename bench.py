@@ -137,17 +137,23 @@ def geokerr_grid_leg(n_side=128, nup=32, cpu_sample=1024):
             "max_rel_diff_gpu_vs_cpu": worst, "all_sampled": bool((got["n"] == nup).all())}
 
 
-def adjoint_headline_leg(K=64):
-    """Forward + adjoint on the 1280x720x4, a = 0.9 scene (FP32 adjoint,
-    checkpoint interval K): L2 loss against a render at (a = 0.7, theta =
-    74.5 deg, gain 1, q 3); rays/s of forward + backward and the production
-    forward render's rays/s on the same scene."""
+def adjoint_headline_leg(K=None):
+    """Forward + adjoint on the 1280x720x4, a = 0.9 scene (FP32 adjoint; the
+    checkpoint interval K chosen by diff.autotune_K unless given): L2 loss
+    against a render at (a = 0.7, theta = 74.5 deg, gain 1, q 3); rays/s of
+    forward + backward and the production forward render's rays/s on the
+    same scene."""
     import math
     import torch
     import nullpath_gb300 as npx
     from nullpath_gb300 import diff
     base = npx.benchmark_scene()
     rays = base.width * base.height * base.spp
+    tune = None
+    if K is None:
+        tune = diff.autotune_K(diff.scene_with(base, 0.9, math.radians(80.0), 1.0, 3.0), "mixed", Ks=(32, 64, 128),
+                               reps=1)
+        K = tune["K"]
     adj = diff.Adjoint()
     st = diff.AdjointStats()
     target = adj.forward(diff.scene_with(base, 0.7, 1.3, 1.0, 3.0), "mixed", K)
@@ -160,7 +166,7 @@ def adjoint_headline_leg(K=64):
     _, _, fst = npx.render(cur, "mixed", stats=True)
     fwd_ms = fst.kernel_ms + fst.init_ms
     tot = st.forward_ms + st.backward_ms
-    return {"K": K, "forward_ms": st.forward_ms, "backward_ms": st.backward_ms,
+    return {"K": K, "autotune": tune, "forward_ms": st.forward_ms, "backward_ms": st.backward_ms,
             "fwd_adj_rays_per_s": rays / (tot * 1e-3), "forward_render_rays_per_s": rays / (fwd_ms * 1e-3),
             "cost_vs_forward": tot / fwd_ms, "workspace_bytes": int(st.workspace_bytes), "gradient": g.tolist()}
 
@@ -257,9 +263,10 @@ def research_leg(n_acc=20000, n_drift=4000):
 def adjoint_leg(Ks=(16, 64, 256)):
     """Differentiable render, 256x256x4 from seed 2: target (0.7, 60 deg, 1, 3),
     current (0.5, 50 deg, 0.8, 2.5), L2 loss.  FP32 adjoint per K (forward +
-    reverse sweep timed with CUDA events), forward-only mixed render of the same
-    scene for the cost ratio, and the gradient error against the event-masked
-    central FP64 FD (h = 1e-4)."""
+    reverse sweep timed with CUDA events), the K the autotuner picks under its
+    memory cap, forward-only mixed render of the same scene for the cost
+    ratio, and the gradient error (every sample, and FD-resolved samples)
+    against the event-masked central FP64 FD (h = 1e-4)."""
     import math
     import numpy as np
     import torch
@@ -279,6 +286,8 @@ def adjoint_leg(Ks=(16, 64, 256)):
     out["gradient_check_fp32"] = diff.gradient_check(sc, np.array(p), target, precision="mixed", K=64, fd=fdr)
     out["gradient_check_fp64"] = diff.gradient_check(sc, np.array(p), target, precision="fp64", K=64, fd=fdr)
     del fdr
+    out["autotune"] = diff.autotune_K(cur, "mixed", Ks=(16, 32, 64, 128, 256), reps=2)
+    out["K_chosen"] = out["autotune"]["K"]
     for K in Ks:
         adj = diff.Adjoint()
         st = diff.AdjointStats()

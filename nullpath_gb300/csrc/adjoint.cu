@@ -7,7 +7,12 @@
 // Parameters differentiated: spin a, camera inclination theta_cam, disk gain,
 // emissivity index q.  The forward integrator is the Carter-form Hamiltonian
 // RK4 of the mixed path with the reference step law h = h0 clamp(r/M, 1, 100)
-// (render.cu:185,207) and cubic-Hermite crossing location, in FP32 or FP64.
+// (render.cu:185,207), shortened near the polar axis by the factor
+// sin(theta) / (sin(theta) + 0.05), and cubic-Hermite crossing location, in
+// FP32 or FP64.  The axis factor keeps the discrete map smooth for rays that
+// pass close to a pole (L ~ 0): there the theta equation's L^2/sin^3(theta)
+// term turns the ray within a few times theta_min, which the plain step law
+// steps over, so that the map's derivative is not that of its secant.
 //
 // Backward: the forward stores the state every K steps (checkpoints); the
 // reverse sweep walks the checkpoint segments from last to first, recomputes
@@ -54,6 +59,9 @@ struct AdjScene {
     double M, a, r_cam, th_cam, ph_cam, tan_half, aspect, h_unit, rin, rout, r_far, gain, q, r_plus, r_minus;
     int max_steps;
 };
+
+// Width of the step law's polar-axis factor sin(theta) / (sin(theta) + sigma).
+constexpr double kPoleSigma = 0.05;
 
 // ---------------------------------------------------------------------------
 // Forward-mode numbers with two tangents (d/da, d/dtheta_cam) for ray set-up.
@@ -296,14 +304,21 @@ __device__ __forceinline__ V4<R> axpy4(const V4<R>& y, R h, const V4<R>& k) {
     return V4<R>{y.r + h * k.r, y.th + h * k.th, y.pr + h * k.pr, y.pth + h * k.pth};
 }
 
-// Step size h = h0 clamp(r/M, 1, 100) and dh/dr.
+// Step size h = h0 clamp(r/M, 1, 100) sin(theta) / (sin(theta) + sigma) and
+// its partial derivatives dh/dr, dh/dtheta.
 template <typename R>
-__device__ __forceinline__ R step_h(const AdjScene& s, R r, R& dhdr) {
+__device__ __forceinline__ R step_h(const AdjScene& s, R r, R th, R& dhdr, R& dhdth) {
     R x = r / R(s.M);
-    if (x <= R(1)) { dhdr = R(0); return R(s.h_unit); }
-    if (x >= R(100)) { dhdr = R(0); return R(s.h_unit * 100.0); }
-    dhdr = R(s.h_unit / s.M);
-    return R(s.h_unit) * x;
+    R hr, dhr;
+    if (x <= R(1)) { hr = R(s.h_unit); dhr = R(0); }
+    else if (x >= R(100)) { hr = R(s.h_unit * 100.0); dhr = R(0); }
+    else { hr = R(s.h_unit) * x; dhr = R(s.h_unit / s.M); }
+    const R sn = sin(th), cs = cos(th);
+    const R den = sn + R(kPoleSigma);
+    const R f = sn / den;
+    dhdr = dhr * f;
+    dhdth = hr * R(kPoleSigma) * cs / (den * den);
+    return hr * f;
 }
 
 template <typename R>
@@ -431,8 +446,8 @@ __device__ void trace_fwd(const AdjScene& s, const V4<R>& y0, const Par<R>& p, V
     disk_sum = R(0);
     for (int n = 0; n < s.max_steps; ++n) {
         if (ck && n % s.K == 0) { ck[n / s.K] = y; ck_orders[n / s.K] = rec.orders; }
-        R dhdr;
-        R h = step_h<R>(s, y.r, dhdr);
+        R dhdr, dhdth;
+        R h = step_h<R>(s, y.r, y.th, dhdr, dhdth);
         V4<R> k1;
         V4<R> y1 = rk4_step(y, p, h, k1);
         rec.steps = n + 1;
@@ -474,8 +489,9 @@ struct AdjBuffers {
     float* srgb;            // [spp][3][npix] per-sample colours
     int32_t* sig;           // [spp][npix] event signature: status + 4 * orders
     unsigned char* ck;      // per-ray checkpoint slots
-    unsigned char* seg;     // per-ray segment buffers
+    unsigned char* seg;     // per-thread segment buffers of the reverse sweep
     double* grad;           // [total][4] per-sample gradients (a, theta, gain, q)
+    unsigned long long* work;   // next ray of the reverse sweep (zeroed before each sweep)
     size_t ck_stride, seg_stride;   // bytes per ray
 };
 
@@ -524,10 +540,15 @@ __global__ void adj_resolve_kernel(const float* srgb, float* img, long long npix
 
 // Reverse sweep.  gimg = dLoss/dimage [3][npix]; writes per-sample gradients
 // (d/da, d/dtheta_cam, d/dgain, d/dq) to b.grad.
+// A resident grid whose threads take rays one at a time from a global
+// counter (rays differ in length by orders of magnitude, so a static
+// assignment leaves a long tail); the segment buffer belongs to the thread,
+// so its memory scales with the grid, not with the rays.
 template <typename R>
 __global__ void adj_backward_kernel(const AdjScene s, AdjBuffers b, const float* __restrict__ gimg, int zamo) {
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < s.total;
-         i += (long long)gridDim.x * blockDim.x) {
+    const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    V4<R>* seg = (V4<R>*)(b.seg + (size_t)tid * b.seg_stride);
+    for (long long i = (long long)atomicAdd(b.work, 1ull); i < s.total; i = (long long)atomicAdd(b.work, 1ull)) {
         double* out = b.grad + (size_t)i * 4;
         out[0] = out[1] = out[2] = out[3] = 0.0;
         V4<R>* ck = (V4<R>*)(b.ck + (size_t)i * b.ck_stride);
@@ -545,7 +566,6 @@ __global__ void adj_backward_kernel(const AdjScene s, AdjBuffers b, const float*
         V4<R> gy{R(0), R(0), R(0), R(0)};
         R gE = R(0), gL = R(0), ga = R(0);
         double g_gain = 0.0, g_q = 0.0;
-        V4<R>* seg = (V4<R>*)(b.seg + (size_t)i * b.seg_stride);
         const R hp = R(1.5707963267948966);
         const int nseg = (N + s.K - 1) / s.K;
         for (int j = nseg - 1; j >= 0; --j) {
@@ -554,8 +574,8 @@ __global__ void adj_backward_kernel(const AdjScene s, AdjBuffers b, const float*
             seg[0] = ck[j];
             int hits_before = cko[j];
             for (int n = n0; n < n1; ++n) {
-                R dhdr;
-                R h = step_h<R>(s, seg[n - n0].r, dhdr);
+                R dhdr, dhdth;
+                R h = step_h<R>(s, seg[n - n0].r, seg[n - n0].th, dhdr, dhdth);
                 V4<R> k1;
                 seg[n - n0 + 1] = rk4_step(seg[n - n0], p, h, k1);
             }
@@ -570,8 +590,8 @@ __global__ void adj_backward_kernel(const AdjScene s, AdjBuffers b, const float*
                     if (n == N - 1 && status == 1) break;
                     R d0 = ya.th - hp, d1 = yb.th - hp;
                     if (!((d0 > R(0) && d1 < R(0)) || (d0 < R(0) && d1 > R(0)))) continue;
-                    R dhdr;
-                    R h = step_h<R>(s, ya.r, dhdr);
+                    R dhdr, dhdth;
+                    R h = step_h<R>(s, ya.r, ya.th, dhdr, dhdth);
                     V4<R> fa = rhs(ya, p), fb = rhs(yb, p);
                     R u = herm_root(d0, d1, h * fa.th, h * fb.th);
                     R u2 = u * u, u3 = u2 * u;
@@ -585,8 +605,8 @@ __global__ void adj_backward_kernel(const AdjScene s, AdjBuffers b, const float*
             for (int n = n1 - 1; n >= n0; --n) {
                 const V4<R> ya = seg[n - n0];
                 const V4<R> yb = seg[n - n0 + 1];
-                R dhdr;
-                R h = step_h<R>(s, ya.r, dhdr);
+                R dhdr, dhdth;
+                R h = step_h<R>(s, ya.r, ya.th, dhdr, dhdth);
                 R gh = R(0);
                 V4<R> gya{R(0), R(0), R(0), R(0)};
                 if (hcur >= 0 && hit_index[hcur] == n) {
@@ -627,6 +647,7 @@ __global__ void adj_backward_kernel(const AdjScene s, AdjBuffers b, const float*
                 // through the step y_{n+1} = Phi(y_n, h(r_n))
                 gh += rk4_step_vjp(ya, p, h, gy, gya, gE, gL, ga);
                 gya.r += gh * dhdr;
+                gya.th += gh * dhdth;
                 gy = gya;
             }
         }
@@ -653,6 +674,7 @@ struct np_adjoint {
     AdjScene s{};
     int zamo = 0;
     AdjBuffers b{};
+    int bwd_blocks = 1;      // grid of the reverse sweep (its threads own the segment buffers)
     size_t bytes = 0;
     void* base = nullptr;
     bool have_forward = false;
@@ -717,8 +739,22 @@ int np_adjoint_forward(np_adjoint_t* h, const np_scene_t* scene, int precision, 
     const size_t ck_stride = ((size_t)s.max_seg * (rsz + sizeof(int)) + 3 * sizeof(int) + 15) & ~(size_t)15;
     const size_t seg_stride = ((size_t)(K + 1) * rsz + 15) & ~(size_t)15;
     const size_t n = (size_t)s.total;
-    const size_t need = n * 3 * sizeof(float) + n * sizeof(int32_t) + n * ck_stride + n * seg_stride +
-                        n * 4 * sizeof(double) + 1024;
+    // reverse-sweep grid: the resident blocks of 64 threads, at most as many
+    // as the rays need, and few enough that the segment buffers stay within
+    // 256 MiB (at least one block per SM)
+    int dev = 0, sms = 1, occ = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (precision == NP_PREC_FP64)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, adj_backward_kernel<double>, 64, 0);
+    else
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, adj_backward_kernel<float>, 64, 0);
+    long long bwd = std::min<long long>((s.total + 63) / 64, (long long)sms * std::max(1, occ));
+    bwd = std::min<long long>(bwd, std::max<long long>(sms, (256ll << 20) / (long long)(seg_stride * 64)));
+    bwd = std::max<long long>(1, bwd);
+    const size_t nthreads = (size_t)bwd * 64;
+    const size_t need = n * 3 * sizeof(float) + n * sizeof(int32_t) + n * ck_stride + nthreads * seg_stride +
+                        n * 4 * sizeof(double) + 1024 + 256;
     cudaStream_t st = (cudaStream_t)stream_v;
     if (h->bytes < need) {
         if (h->base) { cudaStreamSynchronize(st); cudaFree(h->base); h->base = nullptr; h->bytes = 0; }
@@ -732,17 +768,20 @@ int np_adjoint_forward(np_adjoint_t* h, const np_scene_t* scene, int precision, 
     b.sig = d_sample_sig ? d_sample_sig : (int32_t*)p; p += n * sizeof(int32_t);
     p = (char*)(((uintptr_t)p + 255) & ~(uintptr_t)255);
     b.ck = (unsigned char*)p; p += n * ck_stride;
-    b.seg = (unsigned char*)p; p += n * seg_stride;
+    b.seg = (unsigned char*)p; p += nthreads * seg_stride;
     p = (char*)(((uintptr_t)p + 255) & ~(uintptr_t)255);
-    b.grad = (double*)p;
+    b.grad = (double*)p; p += n * 4 * sizeof(double);
+    p = (char*)(((uintptr_t)p + 255) & ~(uintptr_t)255);
+    b.work = (unsigned long long*)p;
     b.ck_stride = ck_stride; b.seg_stride = seg_stride;
     const int threads = 128;
-    const int blocks = (int)std::min<long long>((s.total + threads - 1) / threads, 152ll * 64);
+    const int blocks = (int)std::min<long long>((s.total + threads - 1) / threads, (long long)sms * 64);
     cudaEvent_t e0, e1;
     if (stats) { cudaEventCreate(&e0); cudaEventCreate(&e1); cudaEventRecord(e0, st); }
     if (precision == NP_PREC_FP64) adj_forward_kernel<double><<<blocks, threads, 0, st>>>(s, b, zamo, 1);
     else adj_forward_kernel<float><<<blocks, threads, 0, st>>>(s, b, zamo, 1);
-    adj_resolve_kernel<<<(int)std::min<long long>((3 * s.npix + 255) / 256, 152 * 16), 256, 0, st>>>(b.srgb, d_img, s.npix, s.spp);
+    adj_resolve_kernel<<<(int)std::min<long long>((3 * s.npix + 255) / 256, (long long)sms * 16), 256, 0, st>>>(
+        b.srgb, d_img, s.npix, s.spp);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return adj_fail(NP_ERR_KERNEL, "%s", cudaGetErrorString(e));
     if (stats) {
@@ -755,6 +794,7 @@ int np_adjoint_forward(np_adjoint_t* h, const np_scene_t* scene, int precision, 
         cudaEventDestroy(e0); cudaEventDestroy(e1);
     }
     h->s = s; h->zamo = zamo; h->b = b; h->precision = precision; h->have_forward = true;
+    h->bwd_blocks = (int)bwd;
     return NP_OK;
 }
 
@@ -765,9 +805,11 @@ int np_adjoint_backward(np_adjoint_t* h, const float* d_grad_img, double* h_grad
     cudaStream_t st = (cudaStream_t)stream_v;
     const AdjScene& s = h->s;
     const int threads = 64;
-    const int blocks = (int)std::min<long long>((s.total + threads - 1) / threads, 152ll * 128);
+    const int blocks = h->bwd_blocks;   // the grid the forward sized the segment buffers for
     cudaEvent_t e0, e1;
     if (stats) { cudaEventCreate(&e0); cudaEventCreate(&e1); cudaEventRecord(e0, st); }
+    if (cudaMemsetAsync(h->b.work, 0, sizeof(unsigned long long), st) != cudaSuccess)
+        return adj_fail(NP_ERR_KERNEL, "cudaMemsetAsync of the reverse-sweep counter failed");
     if (h->precision == NP_PREC_FP64) adj_backward_kernel<double><<<blocks, threads, 0, st>>>(s, h->b, d_grad_img, h->zamo);
     else adj_backward_kernel<float><<<blocks, threads, 0, st>>>(s, h->b, d_grad_img, h->zamo);
     cudaError_t e = cudaGetLastError();

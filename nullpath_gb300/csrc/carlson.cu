@@ -11,6 +11,15 @@
 #include "carlson.cuh"
 #include "mino_carlson.cuh"
 #include "geokerr_c_api.h"
+
+// Streaming multiprocessors of the current device (1 if it cannot be read).
+static int device_sms() {
+    int dev = 0, n = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        n <= 0)
+        return 1;
+    return n;
+}
 #include "np_render.h"
 
 void np_record_error(const char* msg);
@@ -76,7 +85,8 @@ int np_geokerr_equator_crossings_cf_device(int n, double a, const double* d_u0, 
     }
     if (n == 0) return NP_OK;
     const int threads = 128;
-    const int blocks = (n + threads - 1) / threads < 152 * 16 ? (n + threads - 1) / threads : 152 * 16;
+    const int cap = device_sms() * 16;
+    const int blocks = (n + threads - 1) / threads < cap ? (n + threads - 1) / threads : cap;
     crossings_cf_kernel<<<blocks, threads, 0, (cudaStream_t)stream>>>(n, a, d_u0, d_mu0, d_l, d_q2, d_su, d_sm, u_end, K,
                                                                      d_xu, d_nx);
     cudaError_t e = cudaGetLastError();
@@ -110,7 +120,8 @@ int np_geokerr_mu_of_lambda_device(int n, double a, const double* d_l, const dou
     }
     if (n == 0) return NP_OK;
     const int threads = 128;
-    const int blocks = (n + threads - 1) / threads < 152 * 16 ? (n + threads - 1) / threads : 152 * 16;
+    const int cap = device_sms() * 16;
+    const int blocks = (n + threads - 1) / threads < cap ? (n + threads - 1) / threads : cap;
     mu_of_lambda_kernel<<<blocks, threads, 0, (cudaStream_t)stream>>>(n, a, d_l, d_q2, d_mu0, d_sm, d_lam, d_mu);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
@@ -148,7 +159,8 @@ int np_geokerr_mino_times_device(int n, double a, const double* d_ua, const doub
     }
     if (n == 0) return NP_OK;
     const int threads = 128;
-    const int blocks = (n + threads - 1) / threads < 152 * 16 ? (n + threads - 1) / threads : 152 * 16;
+    const int cap = device_sms() * 16;
+    const int blocks = (n + threads - 1) / threads < cap ? (n + threads - 1) / threads : cap;
     mino_times_kernel<<<blocks, threads, 0, (cudaStream_t)stream>>>(n, a, d_ua, d_ub, d_mua, d_mub, d_l, d_q2, d_lam_u,
                                                                    d_lam_mu);
     cudaError_t e = cudaGetLastError();
@@ -180,7 +192,8 @@ int np_carlson_batch_device(int n, const char* d_types, const double* d_x, const
     }
     if (n == 0) return NP_OK;
     const int threads = 256;
-    const int blocks = (n + threads - 1) / threads < 152 * 16 ? (n + threads - 1) / threads : 152 * 16;
+    const int cap = device_sms() * 16;
+    const int blocks = (n + threads - 1) / threads < cap ? (n + threads - 1) / threads : cap;
     carlson_batch_kernel<<<blocks, threads, 0, (cudaStream_t)stream>>>(n, d_types, d_x, d_y, d_z, d_p, d_out);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {

@@ -9,6 +9,15 @@
 #include "np_kerr.h"
 #include "np_render.h"
 
+// Streaming multiprocessors of the current device (1 if it cannot be read).
+static int device_sms() {
+    int dev = 0, n = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        n <= 0)
+        return 1;
+    return n;
+}
+
 void np_record_error(const char* msg);
 
 namespace {
@@ -50,7 +59,8 @@ int np_kerr_integrate_device(int n, double M, double a, const double* d_cam, int
                              double* d_states, int* d_alive, void* stream) {
     int rc = check_args(n, M, a, d_cam, steps, d_states, d_alive);
     if (rc != NP_OK || n == 0) return rc;
-    const int threads = 128, blocks = (int)((n + threads - 1) / threads < 152 * 16 ? (n + threads - 1) / threads : 152 * 16);
+    const int threads = 128, cap = device_sms() * 16;
+    const int blocks = (int)((n + threads - 1) / threads < cap ? (n + threads - 1) / threads : cap);
     kerr_integrate_kernel<<<blocks, threads, 0, (cudaStream_t)stream>>>(n, M, a, d_cam, steps, h_scale, zamo, d_states,
                                                                        d_alive);
     cudaError_t e = cudaGetLastError();

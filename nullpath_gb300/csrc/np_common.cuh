@@ -10,6 +10,16 @@
 // Records the message np_last_error() returns (thread-local, np_render.cu).
 void np_record_error(const char* msg);
 
+// Streaming multiprocessors of the current device (1 if it cannot be read):
+// grid-stride launches cap their grids at a multiple of it.
+inline int np_device_sms() {
+    int dev = 0, n = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        n <= 0)
+        return 1;
+    return n;
+}
+
 namespace np {
 
 constexpr double kPi = 3.141592653589793238462643383279502884;

@@ -945,7 +945,7 @@ int np_render_device(const np_scene_t* scene, int precision, float* d_rgb, float
         if (stats) NP_CU(cudaEventRecord(sc->ev1, st), NP_ERR_KERNEL);
     } else {
         InitSoA soa{sc->soa_a, sc->soa_b, sc->soa_cy, sc->soa_flag, sc->list};
-        int ib = (int)std::min<long long>((s.total + 255) / 256, 152ll * 8);
+        int ib = (int)std::min<long long>((s.total + 255) / 256, (long long)np_device_sms() * 8);
         ray_init_kernel<<<ib, 256, 0, st>>>(s, soa, sc->ctr);
         NP_CU(cudaGetLastError(), NP_ERR_KERNEL);
         if (stats) NP_CU(cudaEventRecord(sc->ev1, st), NP_ERR_KERNEL);
@@ -955,7 +955,7 @@ int np_render_device(const np_scene_t* scene, int precision, float* d_rgb, float
     if (stats) NP_CU(cudaEventRecord(sc->ev2, st), NP_ERR_KERNEL);
     {
         long long n = 3 * s.npix;
-        int blocks = (int)std::min<long long>((n + 255) / 256, 152 * 16);
+        int blocks = (int)std::min<long long>((n + 255) / 256, (long long)np_device_sms() * 16);
         resolve_kernel<<<blocks, 256, 0, st>>>(sc->srgb, d_rgb, s.npix, s.spp, accumulate);
         NP_CU(cudaGetLastError(), NP_ERR_KERNEL);
     }
@@ -1168,14 +1168,14 @@ extern "C" int np_render_device_noalloc(const np_scene_t* scene, int precision, 
     } else {
         InitSoA soa{(float4*)(base + kNaA), (float4*)(base + kNaB), (float*)(base + kNaCy),
                     (unsigned char*)(base + kNaFlag), (long long*)(base + kNaList)};
-        int ib = (int)std::min<long long>((s.total + 255) / 256, 152ll * 8);
+        int ib = (int)std::min<long long>((s.total + 255) / 256, (long long)np_device_sms() * 8);
         ray_init_kernel<<<ib, 256, 0, st>>>(s, soa, ctr);
         NP_CU(cudaGetLastError(), NP_ERR_KERNEL);
         launch_mixed(g_tune.min_blocks, s, soa, srgb, d_rcross, nullptr, ctr, g_tune.chunk, st);
     }
     NP_CU(cudaGetLastError(), NP_ERR_KERNEL);
     long long n = 3 * s.npix;
-    int blocks = (int)std::min<long long>((n + 255) / 256, 152 * 16);
+    int blocks = (int)std::min<long long>((n + 255) / 256, (long long)np_device_sms() * 16);
     resolve_kernel<<<blocks, 256, 0, st>>>(srgb, d_rgb, s.npix, s.spp, accumulate);
     NP_CU(cudaGetLastError(), NP_ERR_KERNEL);
     return NP_OK;
@@ -1448,12 +1448,12 @@ int batch_enqueue(np_batch* b, const BatchTune& t, cudaStream_t st) {
     const BatchDev& B = b->B;
     NP_CU(cudaMemsetAsync(B.ctr, 0, sizeof(Counters), st), NP_ERR_KERNEL);
     NP_CU(cudaMemsetAsync(B.done, 0, (size_t)b->n * sizeof(unsigned), st), NP_ERR_KERNEL);
-    const int ib = (int)std::min<long long>((B.total + 255) / 256, 152ll * 8);
+    const int ib = (int)std::min<long long>((B.total + 255) / 256, (long long)np_device_sms() * 8);
     batch_init_kernel<<<ib, 256, 0, st>>>(B);
     NP_CU(cudaGetLastError(), NP_ERR_KERNEL);
     batch_launch(B, t, b->grid[t.shape], st);
     NP_CU(cudaGetLastError(), NP_ERR_KERNEL);
-    const int rb = (int)std::min<long long>((B.total_pix + 255) / 256, 152ll * 16);
+    const int rb = (int)std::min<long long>((B.total_pix + 255) / 256, (long long)np_device_sms() * 16);
     batch_resolve_kernel<<<rb, 256, 0, st>>>(B);
     NP_CU(cudaGetLastError(), NP_ERR_KERNEL);
     return NP_OK;
@@ -1840,7 +1840,7 @@ int np_frame_tonemap(np_frame_t* f, float exposure_ev, float gamma, int reinhard
     if (f->spp_done <= 0) return fail(NP_ERR_INVALID, "no pass rendered");
     const long long np_ = (long long)f->W * f->H;
     const float g = gamma <= 0.0f ? 1.0f : gamma;
-    const int blocks = (int)std::min<long long>((np_ + 255) / 256, 152ll * 16);
+    const int blocks = (int)std::min<long long>((np_ + 255) / 256, (long long)np_device_sms() * 16);
     tonemap_kernel<<<blocks, 256, 0, f->stream>>>(f->d_sum, np_, 1.0f / (float)f->spp_done, powf(2.0f, exposure_ev),
                                                   reinhard ? 1 : 0, g, f->d_u8);
     NP_CU(cudaGetLastError(), NP_ERR_KERNEL);
@@ -1889,7 +1889,7 @@ int np_frame_read(np_frame_t* f, float* h_rgb_mean, float* h_rcross, float* h_in
     if (f->spp_done <= 0) return fail(NP_ERR_INVALID, "no pass rendered");
     const long long np_ = (long long)f->W * f->H;
     if (h_rgb_mean) {
-        const int blocks = (int)std::min<long long>((3 * np_ + 255) / 256, 152ll * 16);
+        const int blocks = (int)std::min<long long>((3 * np_ + 255) / 256, (long long)np_device_sms() * 16);
         scale_kernel<<<blocks, 256, 0, f->stream>>>(f->d_sum, f->d_tmp, 3 * np_, 1.0f / (float)f->spp_done);
         NP_CU(cudaGetLastError(), NP_ERR_KERNEL);
         NP_CU(cudaMemcpyAsync(h_rgb_mean, f->d_tmp, 3 * (size_t)np_ * sizeof(float), cudaMemcpyDeviceToHost, f->stream),

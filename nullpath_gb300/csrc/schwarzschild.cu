@@ -16,6 +16,15 @@
 #include "np_kerr.h"
 #include "np_render.h"
 
+// Streaming multiprocessors of the current device (1 if it cannot be read).
+static int device_sms() {
+    int dev = 0, n = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        n <= 0)
+        return 1;
+    return n;
+}
+
 void np_record_error(const char* msg);
 
 namespace {
@@ -82,7 +91,8 @@ int np_schwarzschild_deflection_device(float mass, float r_start, int n, const f
     }
     if (n == 0) return NP_OK;
     const int threads = 128;
-    const int blocks = (n + threads - 1) / threads < 152 * 16 ? (n + threads - 1) / threads : 152 * 16;
+    const int cap = device_sms() * 16;
+    const int blocks = (n + threads - 1) / threads < cap ? (n + threads - 1) / threads : cap;
     deflection_kernel<<<blocks, threads, 0, (cudaStream_t)stream>>>(mass, r_start, n, d_b, d_deflection, d_rmin,
                                                                    (int*)d_status);
     cudaError_t e = cudaGetLastError();

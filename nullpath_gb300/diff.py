@@ -136,13 +136,11 @@ def fd_gradient(scene, params, target, h=1e-4, precision="fp64", per_sample=Fals
     With per_sample=True also returns the per-sample contributions
     [spp, H, W, 4] and a mask of the samples whose difference quotient is
     resolved: the central differences at h and h/16 agree to 1 % beyond the
-    rounding of the FP32 sample colours.  The fixed-step RK4 map is not smooth
-    at the scale h for every ray: rays with L close to 0 pass near the pole,
-    where the Boyer-Lindquist theta equation is stiff, and their step count
-    and crossings move by tens of steps within +-h.  The adjoint gives the
-    derivative of the discrete map at the point (a complex-step derivative
-    agrees with it); a secant over +-h does not, so a check compares the two
-    over the resolved samples."""
+    rounding of the FP32 sample colours.  The differentiable render's step law
+    shrinks near the polar axis, so that rays with L close to 0, which turn
+    within a few times their closest approach to the pole, are resolved and
+    the discrete map stays smooth at the scale h; the resolved mask then
+    leaves out only samples near rounding or interpolant switches."""
     import torch
     adj = Adjoint()
     p0 = np.asarray(params, dtype=np.float64)
@@ -189,7 +187,8 @@ def fd_gradient(scene, params, target, h=1e-4, precision="fp64", per_sample=Fals
 
 
 def gradient_check(scene, params, target, precision="mixed", K=16, h=1e-4, fd=None):
-    """Adjoint against the event-masked FD over the FD-resolved samples.
+    """Adjoint against the event-masked FD: over every sample (rel_err_all)
+    and over the FD-resolved samples (rel_err_resolved).
     `fd` may carry a previous fd_gradient(..., per_sample=True) result for the
     same scene, params and target.  Returns a dict with both gradients, the
     relative error per component and the share of samples (and of |gradient|)
@@ -206,8 +205,45 @@ def gradient_check(scene, params, target, precision="mixed", K=16, h=1e-4, fd=No
     g_res = (ps * resolved).sum(dim=(0, 1, 2)).cpu().numpy()
     f_res = (fd_ps * resolved).sum(dim=(0, 1, 2)).cpu().numpy()
     rel = np.abs(g_res - f_res) / np.maximum(np.abs(f_res), 1e-12)
+    rel_all = np.abs(np.asarray(g_all) - np.asarray(fd)) / np.maximum(np.abs(np.asarray(fd)), 1e-12)
     excl = (~resolved).float().mean(dim=(0, 1, 2)).cpu().numpy()
     excl_share = ((ps.abs() * (~resolved)).sum(dim=(0, 1, 2)) / ps.abs().sum(dim=(0, 1, 2)).clamp_min(1e-300))
     return {"adjoint": g_all.tolist(), "fd": fd.tolist(), "adjoint_resolved": g_res.tolist(),
-            "fd_resolved": f_res.tolist(), "rel_err_resolved": rel.tolist(),
+            "fd_resolved": f_res.tolist(), "rel_err_resolved": rel.tolist(), "rel_err_all": rel_all.tolist(),
             "excluded_sample_frac": excl.tolist(), "excluded_abs_grad_share": excl_share.cpu().numpy().tolist()}
+
+
+def autotune_K(scene, precision="mixed", Ks=(16, 32, 64, 128, 256), mem_cap=None, reps=2):
+    """Chooses the adjoint's checkpoint interval K by measured time under a
+    memory cap.  For each K of `Ks` it runs forward + backward `reps` times on
+    `scene` (with a unit image gradient) and records the best CUDA-event time
+    and the workspace; the fastest K whose workspace fits `mem_cap` bytes
+    (default: half of the device's free memory) wins.  Small K stores more
+    checkpoints; large K recomputes longer segments and holds a longer
+    segment buffer per reverse-sweep thread.  Returns a dict with the chosen
+    K and the per-K measurements."""
+    import torch
+    if mem_cap is None:
+        mem_cap = torch.cuda.mem_get_info()[0] // 2
+    rows = {}
+    ones = torch.ones((3, scene.height, scene.width), dtype=torch.float32, device="cuda")
+    for K in Ks:
+        best = None
+        ws = 0
+        for _ in range(reps):
+            adj = Adjoint()
+            st = AdjointStats()
+            try:
+                adj.forward(scene, precision, K, stats=st)
+                adj.backward(ones, stats=st)
+            finally:
+                adj.close()
+            t = st.forward_ms + st.backward_ms
+            ws = int(st.workspace_bytes)
+            best = t if best is None else min(best, t)
+        rows[K] = {"ms": best, "workspace_bytes": ws, "fits": ws <= mem_cap}
+    ok = [K for K in Ks if rows[K]["fits"]]
+    if not ok:
+        raise RuntimeError("no checkpoint interval fits %d bytes" % mem_cap)
+    K = min(ok, key=lambda k: rows[k]["ms"])
+    return {"K": K, "mem_cap_bytes": int(mem_cap), "per_K": {str(k): v for k, v in rows.items()}}

@@ -6,7 +6,8 @@ The sample map is the FP64 path of the differentiable render restated in
 plain Python: camera direction (stratified or wanghash jitter, render.cu:
 145-154), static-observer or ZAMO camera momentum (bh_kerr.h:781-826,
 910-967), Carter-form Kerr Hamiltonian right-hand side, RK4 with the step law
-h = h0 clamp(r/M, 1, 100) (render.cu:185,207), equator crossings located on
+h = h0 clamp(r/M, 1, 100) (render.cu:185,207) times the polar-axis factor
+sin(theta) / (sin(theta) + 0.05) of the differentiable render, equator crossings located on
 the cubic Hermite interpolant of the step, and the disk colour sum
 sum_k r_k^-q g_k^3 with the Keplerian redshift g (bh_kerr.h:833-862) over the
 first `disk_max_orders` crossings inside [rin, rout] (render.cu:229-231).
@@ -23,6 +24,9 @@ import math
 
 _M32 = 0xFFFFFFFF
 
+# Width of the polar-axis factor sin(theta) / (sin(theta) + sigma) of the
+# differentiable render's step law (csrc/adjoint.cu).
+POLE_SIGMA = 0.05
 
 def _mix32(x):
     x &= _M32
@@ -214,6 +218,8 @@ def trace(sc, a, th_cam, q, x, y, sl):
     for n in range(sc["max_steps"]):
         xr = yv[0] / M
         h = h0 if _re(xr) <= 1 else (h0 * 100 if _re(xr) >= 100 else h0 * xr)
+        sn = _sin(yv[1])
+        h = h * sn / (sn + POLE_SIGMA)          # the polar-axis factor of the differentiable step law
         y1 = _rk4(yv, E, L, a, M, h)
         if not (_re(y1[0]) > rp * 1.000001 and _re(y1[1]) > 1e-7 and _re(y1[1]) < 3.1415925):
             return 1, orders, n + 1, disk
