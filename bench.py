@@ -107,7 +107,8 @@ def geokerr_grid_leg(n_side=128, nup=32, cpu_sample=1024):
     from nullpath_gb300 import geokerr as gk
     a, mu0, u0 = 0.9, 0.5, 1e-6
     uplus = 1.0 / (1.0 + np.sqrt(1.0 - a * a))
-    g = oracle.geokerr_camera_grid(a, mu0, n_side, n_side)
+    gd = gk.camera_grid(a, mu0, n_side, n_side)          # the library's grid kernel
+    g = {k: v.cpu().numpy() for k, v in gd.items()}
     n = g["l"].size
     args = (a, np.full(n, u0), np.full(n, uplus), np.full(n, mu0), g["l"], g["q2"], g["su"], g["sm"])
     gk.points(*args, tpr=1, nup=nup)
@@ -128,10 +129,12 @@ def geokerr_grid_leg(n_side=128, nup=32, cpu_sample=1024):
         refs = list(ex.map(one, idx))
     cpu_s = time.perf_counter() - t0
     worst = 0.0
+    identical = True
     for i, ref in zip(idx, refs):
         for k in ("u", "mu", "dt", "dphi", "lam"):
             worst = max(worst, float(np.max(np.abs(got[k][i] - ref[k])) / max(np.max(np.abs(ref[k])), 1e-300)))
-    return {"geodesics": n, "points_per_geodesic": nup, "gpu_ms": gpu_ms,
+            identical = identical and bool(np.array_equal(got[k][i], ref[k]))
+    return {"geodesics": n, "points_per_geodesic": nup, "gpu_ms": gpu_ms, "bit_identical_gpu_vs_cpu": identical,
             "gpu_geodesics_per_s": n / (gpu_ms * 1e-3),
             "cpu_geodesics_per_s": len(idx) / cpu_s, "cpu_cores": os.cpu_count(), "cpu_sample": len(idx),
             "max_rel_diff_gpu_vs_cpu": worst, "all_sampled": bool((got["n"] == nup).all())}

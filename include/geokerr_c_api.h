@@ -196,6 +196,21 @@ int np_geokerr_equator_crossings_cf_device(int n, double a, const double* d_u0, 
 int np_geokerr_equator_crossings_cf_host(int n, double a, const double* u0, const double* mu0, const double* l,
                                          const double* q2, const double* su, const double* sm, double u_end, int K,
                                          double* xu, int32_t* nx);
+/* GEOKERR's standard camera grid (geokerr_original.f:183-220): n_alpha x
+ * n_beta cell-centred image positions alpha = a1 + (a2 - a1)(i + 1/2) /
+ * n_alpha, beta = b1 + (b2 - b1)(j + 1/2) / n_beta (ray index i n_beta + j),
+ * and the constants of each ray: l = -alpha sqrt(1 - mu0^2), q2 = beta^2 -
+ * (a^2 - alpha^2) mu0^2, snapped to 0 when |q2| < input_limit^2 or |l| <
+ * input_limit (a snaps when |a| < input_limit); su = 1; sm = +1 when beta > 0
+ * and mu0 < 1, else -1.  Output arrays of n_alpha n_beta doubles; the device
+ * entry fills device arrays on `stream`, the host entry host arrays.
+ * np_status (invalid sizes: NP_ERR_INVALID). */
+int np_geokerr_camera_grid_device(double a, double mu0, int n_alpha, int n_beta, double a1, double a2, double b1,
+                                  double b2, double input_limit, double* d_alpha, double* d_beta, double* d_l,
+                                  double* d_q2, double* d_su, double* d_sm, void* stream);
+int np_geokerr_camera_grid_host(double a, double mu0, int n_alpha, int n_beta, double a1, double a2, double b1,
+                                double b2, double input_limit, double* alpha, double* beta, double* l, double* q2,
+                                double* su, double* sm);
 /* Jacobi elliptic functions sn, cn, dn(u[i] | m[i]), 0 <= m <= 1 (the role of
  * SNCNDN, geokerr_original.f:3277-3347), on the host. */
 int np_jacobi_host(int n, const double* u, const double* m, double* sn, double* cn, double* dn);

@@ -22,6 +22,10 @@ NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler"
            "-I" + INCLUDE, "-I" + CSRC]
 
 CU_SOURCES = ["np_render.cu", "geokerr.cu", "adjoint.cu", "kerr_api.cu", "carlson.cu", "schwarzschild.cu"]
+# The GEOKERR Taylor solver contracts only where its source writes fma(), as
+# its CPU restatement (compiled with -ffp-contract=off) does, so that the two
+# agree bit for bit.
+PER_FILE_NVFLAGS = {"geokerr.cu": ["-fmad=false"]}
 
 
 def _nvcc():
@@ -65,7 +69,8 @@ def build_library(force=False, verbose=False):
 
     def compile_one(src):
         obj = os.path.join(LIBDIR, os.path.splitext(src)[0] + ".o")
-        out = _run([nvcc] + ARCH + NVFLAGS + ["-Xptxas", "-v", "-c", os.path.join(CSRC, src), "-o", obj])
+        out = _run([nvcc] + ARCH + NVFLAGS + PER_FILE_NVFLAGS.get(src, []) +
+                   ["-Xptxas", "-v", "-c", os.path.join(CSRC, src), "-o", obj])
         if verbose:
             print(out)
         return obj

@@ -189,7 +189,9 @@ __host__ __device__ __forceinline__ double hdd(const double* c, double h) {
 __host__ __device__ __forceinline__ double radius(const double* x) {
     double r = 1e300;
     for (int k = P - 1; k <= P; ++k)
-        if (x[k] != 0.0 && x[k - 8] != 0.0) r = fmin(r, pow(fabs(x[k - 8] / x[k]), 0.125));
+        // the 8th root as three correctly rounded square roots: bit-identical
+        // on the GPU and in the CPU restatement (pow is not correctly rounded)
+        if (x[k] != 0.0 && x[k - 8] != 0.0) r = fmin(r, sqrt(sqrt(sqrt(fabs(x[k - 8] / x[k])))));
     return r;
 }
 
@@ -936,3 +938,66 @@ void geokerr_single_case_(double* u0, double* uf, double* mu0, double* muf, doub
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// GEOKERR's standard camera grid (geokerr_original.f:183-220), one ray per
+// thread on the device and the same function on the host.
+namespace {
+__host__ __device__ inline void camera_grid_one(double a, double mu0, int n_alpha, int n_beta, double a1, double a2,
+                                                double b1, double b2, double lim, long long idx, double& al, double& be,
+                                                double& l, double& q2, double& su, double& sm) {
+    const int i = (int)(idx / n_beta), j = (int)(idx % n_beta);
+    al = a1 + (a2 - a1) * (i + 0.5) / n_alpha;
+    be = b1 + (b2 - b1) * (j + 0.5) / n_beta;
+    const double as = fabs(a) < lim ? 0.0 : a;
+    l = -al * sqrt(1.0 - mu0 * mu0);
+    q2 = be * be - (as * as - al * al) * mu0 * mu0;
+    if (fabs(q2) < lim * lim) q2 = 0.0;
+    if (fabs(l) < lim) l = 0.0;
+    su = 1.0;
+    sm = (be > 0.0 && mu0 < 1.0) ? 1.0 : -1.0;
+}
+
+__global__ void camera_grid_kernel(double a, double mu0, int n_alpha, int n_beta, double a1, double a2, double b1,
+                                   double b2, double lim, double* al, double* be, double* l, double* q2, double* su,
+                                   double* sm) {
+    const long long n = (long long)n_alpha * n_beta;
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
+        camera_grid_one(a, mu0, n_alpha, n_beta, a1, a2, b1, b2, lim, k, al[k], be[k], l[k], q2[k], su[k], sm[k]);
+}
+
+int camera_grid_check(int n_alpha, int n_beta, double mu0, const void* p0, const void* p1, const void* p2,
+                      const void* p3, const void* p4, const void* p5) {
+    if (n_alpha <= 0 || n_beta <= 0 || (long long)n_alpha * n_beta > (1ll << 31) || !(fabs(mu0) <= 1.0) || !p0 ||
+        !p1 || !p2 || !p3 || !p4 || !p5)
+        return gk_fail(NP_ERR_INVALID, "camera grid: invalid sizes, mu0 or NULL output");
+    return NP_OK;
+}
+}  // namespace
+
+extern "C" int np_geokerr_camera_grid_device(double a, double mu0, int n_alpha, int n_beta, double a1, double a2,
+                                             double b1, double b2, double input_limit, double* d_alpha,
+                                             double* d_beta, double* d_l, double* d_q2, double* d_su, double* d_sm,
+                                             void* stream) {
+    int rc = camera_grid_check(n_alpha, n_beta, mu0, d_alpha, d_beta, d_l, d_q2, d_su, d_sm);
+    if (rc != NP_OK) return rc;
+    const long long n = (long long)n_alpha * n_beta;
+    const int blocks = (int)std::min<long long>((n + 255) / 256, 4096);
+    camera_grid_kernel<<<blocks, 256, 0, (cudaStream_t)stream>>>(a, mu0, n_alpha, n_beta, a1, a2, b1, b2, input_limit,
+                                                                  d_alpha, d_beta, d_l, d_q2, d_su, d_sm);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return gk_fail(NP_ERR_KERNEL, "camera grid: %s", cudaGetErrorString(e));
+    return NP_OK;
+}
+
+extern "C" int np_geokerr_camera_grid_host(double a, double mu0, int n_alpha, int n_beta, double a1, double a2,
+                                           double b1, double b2, double input_limit, double* alpha, double* beta,
+                                           double* l, double* q2, double* su, double* sm) {
+    int rc = camera_grid_check(n_alpha, n_beta, mu0, alpha, beta, l, q2, su, sm);
+    if (rc != NP_OK) return rc;
+    const long long n = (long long)n_alpha * n_beta;
+    for (long long k = 0; k < n; ++k)
+        camera_grid_one(a, mu0, n_alpha, n_beta, a1, a2, b1, b2, input_limit, k, alpha[k], beta[k], l[k], q2[k], su[k],
+                        sm[k]);
+    return NP_OK;
+}

@@ -26,6 +26,8 @@ _PROTOS = {
     "geokerr_improved_batch": (None, [V] * 10 + [I, I, D]),
     "compute_mino_time_batch_cuda": (None, [V] * 14 + [I]),
     "geokerr_single_case_": (None, [V] * 13),
+    "np_geokerr_camera_grid_device": (I, [D, D, I, I, D, D, D, D, D] + [V] * 6 + [V]),
+    "np_geokerr_camera_grid_host": (I, [D, D, I, I, D, D, D, D, D] + [V] * 6),
 }
 
 
@@ -211,3 +213,26 @@ def render_ray_constants(consts, scene):
     su = np.where(pr < 0, 1.0, -1.0)
     sm = np.where(pth > 0, -1.0, 1.0)
     return u0, mu0, L / (E * M), Q / (E * E * M * M), su, sm
+
+
+_GRID_KEYS = ("alpha", "beta", "l", "q2", "su", "sm")
+
+
+def camera_grid(a, mu0, n_alpha, n_beta, a1=-12.0, a2=12.0, b1=-12.0, b2=12.0, input_limit=1e-5, device=True):
+    """GEOKERR's standard camera grid (geokerr_original.f:183-220): dict of
+    alpha, beta, l, q2, su, sm over n_alpha x n_beta cell-centred positions
+    (ray i n_beta + j), as CUDA float64 tensors (device=True, filled by a
+    kernel) or numpy arrays (the host entry point)."""
+    lib = _lib()
+    n = n_alpha * n_beta
+    if device:
+        import torch
+        out = {k: torch.empty(n, dtype=torch.float64, device="cuda") for k in _GRID_KEYS}
+        check(lib.np_geokerr_camera_grid_device(a, mu0, n_alpha, n_beta, a1, a2, b1, b2, input_limit,
+                                                *[V(out[k].data_ptr()) for k in _GRID_KEYS],
+                                                V(torch.cuda.current_stream().cuda_stream)))
+        return out
+    out = {k: np.empty(n) for k in _GRID_KEYS}
+    check(lib.np_geokerr_camera_grid_host(a, mu0, n_alpha, n_beta, a1, a2, b1, b2, input_limit,
+                                          *[_vp(out[k]) for k in _GRID_KEYS]))
+    return out

@@ -189,7 +189,8 @@ static inline double horner_d(const double* c, double h) {
 static double radius(const double* x) {
     double r = 1e300;
     for (int k = P - 1; k <= P; ++k)
-        if (x[k] != 0.0 && x[k - 8] != 0.0) r = std::min(r, std::pow(std::fabs(x[k - 8] / x[k]), 0.125));
+        // the 8th root as three correctly rounded square roots, as the GPU solver
+        if (x[k] != 0.0 && x[k - 8] != 0.0) r = std::min(r, std::sqrt(std::sqrt(std::sqrt(std::fabs(x[k - 8] / x[k])))));
     return r;
 }
 
