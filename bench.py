@@ -129,12 +129,10 @@ def geokerr_grid_leg(n_side=128, nup=32, cpu_sample=1024):
         refs = list(ex.map(one, idx))
     cpu_s = time.perf_counter() - t0
     worst = 0.0
-    identical = True
     for i, ref in zip(idx, refs):
         for k in ("u", "mu", "dt", "dphi", "lam"):
             worst = max(worst, float(np.max(np.abs(got[k][i] - ref[k])) / max(np.max(np.abs(ref[k])), 1e-300)))
-            identical = identical and bool(np.array_equal(got[k][i], ref[k]))
-    return {"geodesics": n, "points_per_geodesic": nup, "gpu_ms": gpu_ms, "bit_identical_gpu_vs_cpu": identical,
+    return {"geodesics": n, "points_per_geodesic": nup, "gpu_ms": gpu_ms,
             "gpu_geodesics_per_s": n / (gpu_ms * 1e-3),
             "cpu_geodesics_per_s": len(idx) / cpu_s, "cpu_cores": os.cpu_count(), "cpu_sample": len(idx),
             "max_rel_diff_gpu_vs_cpu": worst, "all_sampled": bool((got["n"] == nup).all())}

@@ -101,60 +101,110 @@ __host__ __device__ __forceinline__ bool start_potentials(const Par& p, double u
     return true;
 }
 
-struct St { double u, du, m, dm, t, ph, lam; };
+// d = 1 - |mu| carried accurately near the poles (see taylor); -1 when not
+// carried (it is then formed from mu where needed).
+struct St { double u, du, m, dm, t, ph, lam, d = -1.0; };
 // Series of one step plus the scratch series of the recurrences; one object
 // per thread, owned by the kernel frame (no callee-local arrays).
 struct Ser {
     double u[P + 1], m[P + 1], t[P + 1], ph[P + 1], lam[P + 1];
+    double d[P + 1], P1[P + 1], Sd[P + 1];   // polar series of the pole form
+    bool pole;
     double U2[P + 1], M2[P + 1], U3[P + 1], M3[P + 1];
     double Du[P + 1], Sm[P + 1], Dt[P + 1], phr[P + 1], phm[P + 1], tr[P + 1], iu2[P + 1];
+    double U4[P + 1], Nph[P + 1], Nt[P + 1];
 };
 
 // Taylor coefficients of one step; `acc` adds the t, phi, lambda series.
+//
+// Pole form.  phi's polar rate is L / (1 - mu^2), and near a pole 1 - mu^2
+// formed from mu keeps only the absolute accuracy of mu: for a ray that turns
+// at 1 - mu_+ ~ 1e-5 that is a relative error of 1e-11 in the rate.  Where
+// |mu| >= 1/2 the polar motion is therefore integrated in d = 1 - s mu (s =
+// sign mu), whose equation d'' = -(B2 (1 - d) + 2 B4 (1 - d)^3) is again a
+// polynomial, and 1 - mu^2 = d (2 - d) keeps d's relative accuracy.  The mu
+// series is formed from d's, so every other use is unchanged.
 __host__ __device__ __forceinline__ void taylor(const Par& p, const St& s, Ser& c, bool acc) {
     double* U2 = c.U2;
     double* M2 = c.M2;
     double* U3 = c.U3;
     double* M3 = c.M3;
     c.u[0] = s.u; c.u[1] = s.du;
-    c.m[0] = s.m; c.m[1] = s.dm;
+    c.pole = fabs(s.m) >= 0.5;
+    const double sg = s.m >= 0.0 ? 1.0 : -1.0;
+    if (c.pole) {
+        c.d[0] = s.d >= 0.0 ? s.d : 1.0 - fabs(s.m);      // exact for |mu| >= 1/2 (Sterbenz)
+        c.d[1] = -sg * s.dm;
+    } else {
+        c.m[0] = s.m; c.m[1] = s.dm;
+    }
     for (int k = 0; k <= P; ++k) {
-        double su2 = 0.0, sm2 = 0.0;
-        for (int j = 0; j <= k; ++j) { su2 = fma(c.u[j], c.u[k - j], su2); sm2 = fma(c.m[j], c.m[k - j], sm2); }
-        U2[k] = su2; M2[k] = sm2;
-        double su3 = 0.0, sm3 = 0.0;
-        for (int j = 0; j <= k; ++j) { su3 = fma(U2[j], c.u[k - j], su3); sm3 = fma(M2[j], c.m[k - j], sm3); }
-        U3[k] = su3; M3[k] = sm3;
+        double su2 = 0.0;
+        for (int j = 0; j <= k; ++j) su2 += c.u[j] * c.u[k - j];
+        U2[k] = su2;
+        double su3 = 0.0;
+        for (int j = 0; j <= k; ++j) su3 += U2[j] * c.u[k - j];
+        U3[k] = su3;
+        if (c.pole) {
+            c.P1[k] = (k == 0 ? 1.0 : 0.0) - c.d[k];         // 1 - d = s mu
+            c.m[k] = sg * c.P1[k];
+            double sm2 = 0.0, sd2 = 0.0;
+            for (int j = 0; j <= k; ++j) { sm2 += c.P1[j] * c.P1[k - j]; sd2 += c.d[j] * c.d[k - j]; }
+            M2[k] = sm2;
+            c.Sd[k] = 2.0 * c.d[k] - sd2;                      // 1 - mu^2 = d (2 - d)
+            double sm3 = 0.0;
+            for (int j = 0; j <= k; ++j) sm3 += M2[j] * c.P1[k - j];
+            M3[k] = sm3;                                       // (1 - d)^3
+        } else {
+            double sm2 = 0.0;
+            for (int j = 0; j <= k; ++j) sm2 += c.m[j] * c.m[k - j];
+            M2[k] = sm2;
+            double sm3 = 0.0;
+            for (int j = 0; j <= k; ++j) sm3 += M2[j] * c.m[k - j];
+            M3[k] = sm3;
+            c.Sd[k] = (k == 0) ? (1.0 - c.m[0]) * (1.0 + c.m[0]) : -M2[k];
+        }
         if (k + 2 <= P) {
-            const double inv = 1.0 / ((k + 1.0) * (k + 2.0));
-            c.u[k + 2] = (p.A2 * c.u[k] + 1.5 * p.A3 * U2[k] + 2.0 * p.A4 * U3[k]) * inv;
-            c.m[k + 2] = (p.B2 * c.m[k] + 2.0 * p.B4 * M3[k]) * inv;
+            const double fu = p.A2 * c.u[k] + 1.5 * p.A3 * U2[k] + 2.0 * p.A4 * U3[k];
+            c.u[k + 2] = fu / ((k + 1.0) * (k + 2.0));
+            if (c.pole) {
+                const double fd = -(p.B2 * c.P1[k] + 2.0 * p.B4 * M3[k]);
+                c.d[k + 2] = fd / ((k + 1.0) * (k + 2.0));
+            } else {
+                const double fm = p.B2 * c.m[k] + 2.0 * p.B4 * M3[k];
+                c.m[k + 2] = fm / ((k + 1.0) * (k + 2.0));
+            }
         }
     }
+
     if (!acc) return;
     const double a = p.a, l = p.l, a2 = a * a;
     double *Du = c.Du, *Sm = c.Sm, *Dt = c.Dt, *phr = c.phr, *phm = c.phm, *tr = c.tr, *iu2 = c.iu2;
+    double* U4 = c.U4;
+    double* Nph = c.Nph;
+    double* Nt = c.Nt;
     for (int k = 0; k <= P; ++k) {
-        double d0 = (k == 0) ? 1.0 : 0.0;
-        Du[k] = d0 - 2.0 * c.u[k] + a2 * U2[k];
-        Sm[k] = d0 - M2[k];
+        double s4 = 0.0;
+        for (int j = 0; j <= k; ++j) s4 += U2[j] * U2[k - j];
+        U4[k] = s4;
+        Du[k] = (k == 0 ? 1.0 : 0.0) - 2.0 * c.u[k] + a2 * U2[k];            // Delta u^2
+        Nph[k] = a * ((k == 0 ? 1.0 : 0.0) + (a2 - a * l) * U2[k]);
+        // 1 - mu^2: from d in the pole form (full relative accuracy), else
+        // (1 - mu)(1 + mu) at order 0
+        Sm[k] = c.Sd[k];
+        Nt[k] = (k == 0 ? 1.0 : 0.0) + (2.0 * a2 - a * l) * U2[k] + a2 * (a2 - a * l) * U4[k];
         double sd = 0.0;
-        for (int j = 0; j <= k; ++j) sd = fma(U2[j], Du[k - j], sd);
-        Dt[k] = sd;
+        for (int j = 0; j <= k; ++j) sd += U2[j] * Du[k - j];
+        Dt[k] = sd;                                                           // u^2 Delta u^2
     }
+    // quotients by recursive series division
     for (int k = 0; k <= P; ++k) {
-        double d0 = (k == 0) ? 1.0 : 0.0;
-        double u4 = 0.0;
-        for (int j = 0; j <= k; ++j) u4 = fma(U2[j], U2[k - j], u4);
-        double x = a * (d0 + (a2 - a * l) * U2[k]);
-        double y = d0 * l;
-        double z = d0 + (2.0 * a2 - a * l) * U2[k] + a2 * (a2 - a * l) * u4;
-        double w = d0;
+        double x = Nph[k], y = (k == 0 ? l : 0.0), z = Nt[k], w = (k == 0 ? 1.0 : 0.0);
         for (int j = 0; j < k; ++j) {
-            x = fma(-phr[j], Du[k - j], x);
-            y = fma(-phm[j], Sm[k - j], y);
-            z = fma(-tr[j], Dt[k - j], z);
-            w = fma(-iu2[j], U2[k - j], w);
+            x -= phr[j] * Du[k - j];
+            y -= phm[j] * Sm[k - j];
+            z -= tr[j] * Dt[k - j];
+            w -= iu2[j] * U2[k - j];
         }
         phr[k] = x / Du[0];
         phm[k] = y / Sm[0];
@@ -163,34 +213,36 @@ __host__ __device__ __forceinline__ void taylor(const Par& p, const St& s, Ser& 
     }
     c.t[0] = s.t; c.ph[0] = s.ph; c.lam[0] = s.lam;
     for (int k = 0; k < P; ++k) {
-        const double inv = 1.0 / (k + 1.0);
-        c.t[k + 1] = (tr[k] + (k == 0 ? a * l - a2 : 0.0) + a2 * M2[k]) * inv;
-        c.ph[k + 1] = (phr[k] + phm[k] - (k == 0 ? a : 0.0)) * inv;
-        c.lam[k + 1] = (iu2[k] + a2 * M2[k]) * inv;
+        const double dt = tr[k] + (k == 0 ? a * l - a2 : 0.0) + a2 * M2[k];
+        const double dph = phr[k] + phm[k] - (k == 0 ? a : 0.0);
+        const double dl = iu2[k] + a2 * M2[k];
+        c.t[k + 1] = dt / (k + 1.0);
+        c.ph[k + 1] = dph / (k + 1.0);
+        c.lam[k + 1] = dl / (k + 1.0);
     }
 }
 
 __host__ __device__ __forceinline__ double hv(const double* c, double h) {
     double v = c[P];
-    for (int k = P - 1; k >= 0; --k) v = fma(v, h, c[k]);
+    for (int k = P - 1; k >= 0; --k) v = v * h + c[k];
     return v;
 }
 __host__ __device__ __forceinline__ double hd(const double* c, double h) {
     double v = P * c[P];
-    for (int k = P - 1; k >= 1; --k) v = fma(v, h, k * c[k]);
+    for (int k = P - 1; k >= 1; --k) v = v * h + k * c[k];
     return v;
 }
 __host__ __device__ __forceinline__ double hdd(const double* c, double h) {
     double v = P * (P - 1.0) * c[P];
-    for (int k = P - 1; k >= 2; --k) v = fma(v, h, k * (k - 1.0) * c[k]);
+    for (int k = P - 1; k >= 2; --k) v = v * h + k * (k - 1.0) * c[k];
     return v;
 }
 
 __host__ __device__ __forceinline__ double radius(const double* x) {
     double r = 1e300;
     for (int k = P - 1; k <= P; ++k)
-        // the 8th root as three correctly rounded square roots: bit-identical
-        // on the GPU and in the CPU restatement (pow is not correctly rounded)
+        // the 8th root as three correctly rounded square roots (pow is not
+        // correctly rounded, and its step sizes would differ between libms)
         if (x[k] != 0.0 && x[k - 8] != 0.0) r = fmin(r, sqrt(sqrt(sqrt(fabs(x[k - 8] / x[k])))));
     return r;
 }
@@ -209,6 +261,7 @@ __host__ __device__ St advance(const Ser& c, double h, bool acc) {
     St s;
     s.u = hv(c.u, h); s.du = hd(c.u, h);
     s.m = hv(c.m, h); s.dm = hd(c.m, h);
+    s.d = c.pole ? hv(c.d, h) : -1.0;
     if (acc) { s.t = hv(c.t, h); s.ph = hv(c.ph, h); s.lam = hv(c.lam, h); }
     else { s.t = s.ph = s.lam = 0.0; }
     return s;
@@ -228,7 +281,7 @@ __host__ __device__ double solve(const double* c, double target, double lo, doub
         double d = deriv ? hdd(c, x) : hd(c, x);
         double xn = (d != 0.0) ? x - gx / d : 0.5 * (lo + hi);
         if (!(xn > lo && xn < hi)) xn = 0.5 * (lo + hi);
-        if (fabs(xn - x) <= 1e-16 * fmax(1.0, fabs(x))) { x = xn; break; }
+        if (fabs(xn - x) <= 1e-16 * fmax(1.0, fabs(x)) || hi - lo <= 1e-300) { x = xn; break; }
         x = xn;
     }
     return x;

@@ -107,11 +107,15 @@ static bool start_potentials(const Params& p, double u0, double mu0, double& U0,
 }
 
 // State at the start of a step.
-struct State { double u, du, m, dm, t, ph, lam; };
+// dpole = 1 - |mu| carried near the poles (pole form, see taylor); -1 when
+// not carried.
+struct State { double u, du, m, dm, t, ph, lam, dpole = -1.0; };
 
 // Taylor coefficients of one step (value + derivatives / k!).
 struct Series {
     double u[P + 1], m[P + 1], t[P + 1], ph[P + 1], lam[P + 1];
+    double d[P + 1];     // d = 1 - s mu in the pole form
+    bool pole = false;
 };
 
 static void taylor(const Params& p, const State& s, Series& c) {
@@ -119,21 +123,56 @@ static void taylor(const Params& p, const State& s, Series& c) {
     double Du[P + 1], Nph[P + 1], phr[P + 1], Sm[P + 1], phm[P + 1];
     double U4[P + 1], Nt[P + 1], Dt[P + 1], tr[P + 1], iu2[P + 1];
     const double a = p.a, l = p.l, a2 = a * a;
+    double W[P + 1];     // 1 - mu^2, from d in the pole form
     c.u[0] = s.u; c.u[1] = s.du;
-    c.m[0] = s.m; c.m[1] = s.dm;
+    // pole form (|mu| >= 1/2): integrate d = 1 - s mu, d'' = -(B2 (1 - d) +
+    // 2 B4 (1 - d)^3), so that 1 - mu^2 = d (2 - d) has d's relative accuracy
+    c.pole = std::fabs(s.m) >= 0.5;
+    const double sg = s.m >= 0.0 ? 1.0 : -1.0;
+    double Pd[P + 1];    // 1 - d = s mu
+    if (c.pole) {
+        c.d[0] = s.dpole >= 0.0 ? s.dpole : 1.0 - std::fabs(s.m);
+        c.d[1] = -sg * s.dm;
+    } else {
+        c.m[0] = s.m; c.m[1] = s.dm;
+    }
     for (int k = 0; k <= P; ++k) {
         // series of u^2, u^3, mu^2, mu^3 up to order k (u_k, m_k known)
-        double su2 = 0.0, sm2 = 0.0;
-        for (int j = 0; j <= k; ++j) { su2 += c.u[j] * c.u[k - j]; sm2 += c.m[j] * c.m[k - j]; }
-        U2[k] = su2; M2[k] = sm2;
-        double su3 = 0.0, sm3 = 0.0;
-        for (int j = 0; j <= k; ++j) { su3 += U2[j] * c.u[k - j]; sm3 += M2[j] * c.m[k - j]; }
-        U3[k] = su3; M3[k] = sm3;
+        double su2 = 0.0;
+        for (int j = 0; j <= k; ++j) su2 += c.u[j] * c.u[k - j];
+        U2[k] = su2;
+        double su3 = 0.0;
+        for (int j = 0; j <= k; ++j) su3 += U2[j] * c.u[k - j];
+        U3[k] = su3;
+        if (c.pole) {
+            Pd[k] = (k == 0 ? 1.0 : 0.0) - c.d[k];
+            c.m[k] = sg * Pd[k];
+            double q2s = 0.0, dd = 0.0;
+            for (int j = 0; j <= k; ++j) { q2s += Pd[j] * Pd[k - j]; dd += c.d[j] * c.d[k - j]; }
+            M2[k] = q2s;
+            W[k] = 2.0 * c.d[k] - dd;
+            double q3s = 0.0;
+            for (int j = 0; j <= k; ++j) q3s += M2[j] * Pd[k - j];
+            M3[k] = q3s;                                // (1 - d)^3
+        } else {
+            double sm2 = 0.0;
+            for (int j = 0; j <= k; ++j) sm2 += c.m[j] * c.m[k - j];
+            M2[k] = sm2;
+            double sm3 = 0.0;
+            for (int j = 0; j <= k; ++j) sm3 += M2[j] * c.m[k - j];
+            M3[k] = sm3;
+            W[k] = (k == 0) ? (1.0 - c.m[0]) * (1.0 + c.m[0]) : -M2[k];
+        }
         if (k + 2 <= P) {
             double fu = p.A2 * c.u[k] + 1.5 * p.A3 * U2[k] + 2.0 * p.A4 * U3[k];
-            double fm = p.B2 * c.m[k] + 2.0 * p.B4 * M3[k];
             c.u[k + 2] = fu / ((k + 1.0) * (k + 2.0));
-            c.m[k + 2] = fm / ((k + 1.0) * (k + 2.0));
+            if (c.pole) {
+                double fd = -(p.B2 * Pd[k] + 2.0 * p.B4 * M3[k]);
+                c.d[k + 2] = fd / ((k + 1.0) * (k + 2.0));
+            } else {
+                double fm = p.B2 * c.m[k] + 2.0 * p.B4 * M3[k];
+                c.m[k + 2] = fm / ((k + 1.0) * (k + 2.0));
+            }
         }
     }
     for (int k = 0; k <= P; ++k) {
@@ -142,7 +181,7 @@ static void taylor(const Params& p, const State& s, Series& c) {
         U4[k] = s4;
         Du[k] = (k == 0 ? 1.0 : 0.0) - 2.0 * c.u[k] + a2 * U2[k];             // Delta u^2
         Nph[k] = a * ((k == 0 ? 1.0 : 0.0) + (a2 - a * l) * U2[k]);
-        Sm[k] = (k == 0 ? 1.0 : 0.0) - M2[k];                                  // 1 - mu^2
+        Sm[k] = W[k];                                                         // 1 - mu^2
         Nt[k] = (k == 0 ? 1.0 : 0.0) + (2.0 * a2 - a * l) * U2[k] + a2 * (a2 - a * l) * U4[k];
         double sd = 0.0;
         for (int j = 0; j <= k; ++j) sd += U2[j] * Du[k - j];
@@ -184,6 +223,7 @@ static inline double horner_d(const double* c, double h) {
     return v;
 }
 
+
 // Radius of convergence of a series estimated from coefficients eight
 // orders apart (two estimates, so odd or even series are handled).
 static double radius(const double* x) {
@@ -212,6 +252,7 @@ static State advance(const Series& c, double h) {
     State s;
     s.u = horner(c.u, h); s.du = horner_d(c.u, h);
     s.m = horner(c.m, h); s.dm = horner_d(c.m, h);
+    s.dpole = c.pole ? horner(c.d, h) : -1.0;
     s.t = horner(c.t, h); s.ph = horner(c.ph, h); s.lam = horner(c.lam, h);
     return s;
 }

@@ -68,12 +68,14 @@ def test_camera_grid_matches_oracle(cuda):
     assert (z["l"][3:6] == 0.0).all() and (z["sm"] == -1.0).all()
 
 
-def test_grid_points_bit_identical_on_full_grid(cuda):
+def test_grid_points_full_grid_near_polar(cuda):
     """The 128 x 128 grid with 32 points per geodesic (a = 0.9, r_o = 1e6 M,
-    i = 60 deg): the GPU solver and its CPU restatement agree bit for bit on
-    300 sampled rays, near-polar ones included (the solver contracts only its
-    explicit fma() and takes its 8th roots as square roots, both correctly
-    rounded everywhere)."""
+    i = 60 deg): GPU solver against its CPU restatement on 300 rays, the 60
+    of smallest |l| included.  Those pass near a pole, where the sampled phi
+    has a condition number of ~3e4 in the potential's coefficients, so the
+    1e-12 bar needs the same rounding on both sides: the GPU build contracts
+    no multiply-add and follows the restatement's operation order, and the
+    results agree bit for bit."""
     a, mu0, u0 = 0.9, 0.5, 1e-6
     uplus = 1.0 / (1.0 + np.sqrt(1.0 - a * a))
     g = {k: v.cpu().numpy() for k, v in gk.camera_grid(a, mu0, 128, 128).items()}
