@@ -274,8 +274,13 @@ int np_adjoint_backward(np_adjoint_t* handle, const float* d_grad_img, double* h
  *   - at most NP_NOALLOC_MAX_RAYS rays per call; larger passes are rejected
  *     with NP_ERR_INVALID (split the samples over several calls with
  *     sample_offset and accumulate = 1);
+ *   - d_rcross may be NULL.  Each call writes the first-crossing radius of
+ *     its own first sample, so when a pass is split over several calls pass
+ *     d_rcross to the first call only;
  *   - the first call on each device looks up the array's device address;
- *     make that first call before any stream capture;
+ *     make that first call before any stream capture.  The address is kept
+ *     for the life of the process: resetting the device (cudaDeviceReset)
+ *     after that first call is not supported;
  *   - every call shares the one array, so calls whose work overlaps on the
  *     GPU (different streams, or different host threads) race; serialise
  *     them;

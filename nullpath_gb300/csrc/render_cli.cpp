@@ -36,6 +36,7 @@
 #include <algorithm>
 #include <cctype>
 #include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -104,36 +105,74 @@ bool write_ppm(const char* path, int w, int h, const std::vector<unsigned char>&
     return n == rgb.size();
 }
 
-// Accumulator file: u32 "NPAC", version 1, W, H, samples done; then float
-// colour sums [3][H][W], first-crossing radius [H][W], invariant maxima [3].
+// Accumulator file: u32 "NPAC", version 2, W, H, samples done, the scene
+// hash (two u32, low first); then float colour sums [3][H][W], first-crossing
+// radius [H][W], invariant maxima [3].
 struct Accum {
     int w = 0, h = 0, spp = 0;
+    uint64_t scene_hash = 0;
     std::vector<float> sum, rc, inv;
 };
 constexpr unsigned kAccumMagic = 0x4341504eu;   // "NPAC"
+constexpr unsigned kAccumVersion = 2u;
 
+// FNV-1a (64-bit) over the fields of the scene that change a sample's colour
+// (every field but phi, spp and sample_offset), the precision and the samples
+// per pass (the pass split decides the sample order of the sums).  A resumed
+// accumulator must come from the same scene, or its sums would mix renders.
+uint64_t scene_hash(const np_scene_t& s, int precision, int samples_per_pass) {
+    uint64_t h = 1469598103934665603ull;
+    auto eat = [&](const void* p, size_t n) {
+        const unsigned char* b = (const unsigned char*)p;
+        for (size_t i = 0; i < n; ++i) { h ^= b[i]; h *= 1099511628211ull; }
+    };
+    auto i32 = [&](int32_t v) { eat(&v, sizeof(v)); };
+    auto f64 = [&](double v) { eat(&v, sizeof(v)); };
+    i32(s.width); i32(s.height); f64(s.mass); f64(s.spin); f64(s.r_cam); f64(s.theta_deg); f64(s.fov_y_deg);
+    i32(s.units); i32(s.camera); i32(s.jitter); i32((int32_t)s.seed); i32(s.integrator); i32(s.max_steps);
+    f64(s.step_scale); f64(s.rtol); f64(s.atol); f64(s.escape_r); i32(s.disk_on); i32(s.disk_max_orders);
+    f64(s.disk_rin); f64(s.disk_rout); f64(s.emissivity_q); f64(s.disk_gain); i32(s.crossing); i32(s.background);
+    f64(s.bg_sigma_deg); f64(s.bg_brightness); i32(s.check_invariants); i32(s.islands); f64(s.inv_gate);
+    f64(s.rtol_fp64); i32(s.island_arith);
+    i32(precision); i32(samples_per_pass);
+    return h;
+}
+
+// Writes to path.tmp, flushes and closes it, then renames it over path, so an
+// interrupted write never destroys the last complete checkpoint.
 bool write_accum(const char* path, const Accum& a) {
-    FILE* f = std::fopen(path, "wb");
+    const std::string tmp = std::string(path) + ".tmp";
+    FILE* f = std::fopen(tmp.c_str(), "wb");
     if (!f) return false;
-    const unsigned hdr[5] = {kAccumMagic, 1u, (unsigned)a.w, (unsigned)a.h, (unsigned)a.spp};
+    const unsigned hdr[7] = {kAccumMagic, kAccumVersion, (unsigned)a.w, (unsigned)a.h, (unsigned)a.spp,
+                             (unsigned)(a.scene_hash & 0xffffffffu), (unsigned)(a.scene_hash >> 32)};
     bool ok = std::fwrite(hdr, sizeof(hdr), 1, f) == 1 &&
               std::fwrite(a.sum.data(), sizeof(float), a.sum.size(), f) == a.sum.size() &&
               std::fwrite(a.rc.data(), sizeof(float), a.rc.size(), f) == a.rc.size() &&
               std::fwrite(a.inv.data(), sizeof(float), a.inv.size(), f) == a.inv.size();
+    ok = (std::fflush(f) == 0) && ok;
     ok = (std::fclose(f) == 0) && ok;
-    return ok;
+    if (!ok) { std::remove(tmp.c_str()); return false; }
+    return std::rename(tmp.c_str(), path) == 0;
 }
 
-// Reads an accumulator file for a w x h frame; returns an error message or "".
-std::string read_accum(const char* path, int w, int h, Accum& a) {
+// Reads an accumulator file for a w x h frame of the scene with hash `hash`;
+// returns an error message or "".
+std::string read_accum(const char* path, int w, int h, uint64_t hash, Accum& a) {
     FILE* f = std::fopen(path, "rb");
     if (!f) return std::string("Cannot read ") + path + ".";
-    unsigned hdr[5];
+    unsigned hdr[7];
     std::string err;
-    if (std::fread(hdr, sizeof(hdr), 1, f) != 1 || hdr[0] != kAccumMagic || hdr[1] != 1u) {
+    if (std::fread(hdr, sizeof(unsigned) * 2, 1, f) != 1 || hdr[0] != kAccumMagic) {
         err = std::string(path) + " is not an accumulator file.";
+    } else if (hdr[1] != kAccumVersion) {
+        err = std::string(path) + " is an accumulator of another version (no scene hash); render it again.";
+    } else if (std::fread(hdr + 2, sizeof(unsigned) * 5, 1, f) != 1) {
+        err = std::string(path) + " is truncated.";
     } else if ((int)hdr[2] != w || (int)hdr[3] != h) {
         err = std::string(path) + " holds a different image size.";
+    } else if ((((uint64_t)hdr[6] << 32) | hdr[5]) != hash) {
+        err = std::string(path) + " was rendered from a different scene, precision or --samples; it cannot be resumed.";
     } else {
         const size_t npix = (size_t)w * h;
         a.w = w; a.h = h; a.spp = (int)hdr[4];
@@ -296,7 +335,7 @@ int main(int argc, char** argv) {
     }
     Accum resumed;
     if (c.resume) {
-        std::string err = read_accum(c.resume, s.width, s.height, resumed);
+        std::string err = read_accum(c.resume, s.width, s.height, scene_hash(s, c.precision, c.samples), resumed);
         if (!err.empty()) { std::fprintf(stderr, "%s\n", err.c_str()); return 1; }
     }
 
@@ -341,6 +380,7 @@ int main(int argc, char** argv) {
             if (c.accum_out) {
                 Accum a;
                 a.w = s.width; a.h = s.height;
+                a.scene_hash = scene_hash(s, c.precision, c.samples);
                 a.sum.resize(3 * npix); a.rc.resize(npix); a.inv.resize(3);
                 if (np_frame_save(fr, a.sum.data(), a.rc.data(), a.inv.data(), &a.spp) != NP_OK ||
                     !write_accum(c.accum_out, a)) {

@@ -71,12 +71,21 @@ def test_resume_file_checks(built, tmp_path):
     bad.write_bytes(b"not an accumulator")
     rc, out, err = _run("--w", "8", "--h", "8", "--resume", str(bad))
     assert rc == 1 and err.strip() == "%s is not an accumulator file." % bad
+    old = tmp_path / "old.npac"
+    old.write_bytes(struct.pack("<5I", 0x4341504E, 1, 8, 8, 2) + b"\0" * 4 * (3 * 64 + 64 + 3))
+    rc, out, err = _run("--w", "8", "--h", "8", "--resume", str(old))
+    assert rc == 1 and err.strip() == "%s is an accumulator of another version (no scene hash); render it again." % old
     other = tmp_path / "other.npac"
-    other.write_bytes(struct.pack("<5I", 0x4341504E, 1, 4, 4, 2) + b"\0" * 4 * (3 * 16 + 16 + 3))
+    other.write_bytes(struct.pack("<7I", 0x4341504E, 2, 4, 4, 2, 0, 0) + b"\0" * 4 * (3 * 16 + 16 + 3))
     rc, out, err = _run("--w", "8", "--h", "8", "--resume", str(other))
     assert rc == 1 and err.strip() == "%s holds a different image size." % other
+    scene = tmp_path / "scene.npac"
+    scene.write_bytes(struct.pack("<7I", 0x4341504E, 2, 8, 8, 2, 123, 456) + b"\0" * 4 * (3 * 64 + 64 + 3))
+    rc, out, err = _run("--w", "8", "--h", "8", "--resume", str(scene))
+    assert rc == 1 and err.strip() == ("%s was rendered from a different scene, precision or --samples; "
+                                       "it cannot be resumed." % scene)
     short = tmp_path / "short.npac"
-    short.write_bytes(struct.pack("<5I", 0x4341504E, 1, 8, 8, 2) + b"\0" * 16)
+    short.write_bytes(struct.pack("<3I", 0x4341504E, 2, 8))
     rc, out, err = _run("--w", "8", "--h", "8", "--resume", str(short))
     assert rc == 1 and err.strip() == "%s is truncated." % short
     rc, out, err = _run("--w", "8", "--h", "8", "--frames", "3", "--accum-out", str(tmp_path / "a.npac"))

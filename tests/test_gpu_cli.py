@@ -104,3 +104,18 @@ def test_resume_is_bit_identical(cuda, tmp_path):
     assert s1 == s2 == 8
     assert np.array_equal(m1, m2) and np.array_equal(r1, r2)
     assert np.array_equal(_read_ppm(full_ppm), _read_ppm(res_ppm))
+    # the file carries a hash of the scene: another spin, precision or
+    # --samples refuses to resume it
+    for change in (["--spin", "0.5"], ["--precision", "fp64"], ["--samples", "1"]):
+        args = list(common)
+        i = args.index(change[0])
+        args[i + 1] = change[1]
+        p = subprocess.run([CLI] + args + ["--spp-total", "8", "--resume", acc, "--out", res_ppm],
+                           capture_output=True, text=True, timeout=300)
+        assert p.returncode == 1 and "different scene" in p.stderr, (change, p.stderr)
+    # a truncated leftover of an interrupted write (acc + ".tmp") is ignored
+    with open(acc + ".tmp", "wb") as f:
+        f.write(b"NPAC")
+    p = subprocess.run([CLI] + common + ["--spp-total", "8", "--resume", acc, "--out", res_ppm],
+                       capture_output=True, text=True, timeout=300)
+    assert p.returncode == 0, p.stderr
