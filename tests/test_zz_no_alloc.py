@@ -79,10 +79,13 @@ def test_noalloc_rejects_oversize_and_takes_no_memory(cuda):
 def test_noalloc_split_pass_matches_one_pass(cuda):
     """A pass split over two calls (samples 0-1, then 2-3 with sample_offset
     2 and accumulate = 1, rcross on the first call only) equals one
-    four-sample np_render_device pass."""
+    four-sample np_render_device pass.  The wanghash jitter places a sample
+    by its index alone (stratified jitter lays its strata out by the call's
+    spp, so a split changes its pattern)."""
     import torch
+    from nullpath_gb300._abi import NP_JITTER_WANGHASH
     lib = npx.load()
-    sc = npx.benchmark_scene(width=64, height=36, spp=4)
+    sc = npx.benchmark_scene(width=64, height=36, spp=4).replace(jitter=NP_JITTER_WANGHASH)
     ref_rgb, ref_rc = npx.render(sc, NP_PREC_MIXED)
     rgb = torch.zeros((3, 36, 64), device="cuda")
     rc = torch.zeros((36, 64), device="cuda")
