@@ -102,8 +102,12 @@ def build_cli(force=False):
 
 
 def build_oracle(force=False):
-    """Builds oracle/liboracle.so (and oracle/_ref when the reference checkout exists)."""
+    """Builds oracle/liboracle.so, and oracle/_ref from the reference checkout
+    named by NP_REFERENCE_DIR (default /root/reference) when it exists."""
     args = ["make", "-s", "-C", ORACLE]
+    ref = os.environ.get("NP_REFERENCE_DIR", "/root/reference")
+    if os.path.isfile(os.path.join(ref, "include", "bh_kerr.h")):
+        args.append("REF_DIR=" + ref)
     if force:
         args.append("-B")
     _run(args)

@@ -27,7 +27,8 @@
 //   --islands N         FP64 island mask of the mixed path (NP_ISLAND_*)
 //   --benchmark         the 1280x720, a=0.9 benchmark scene (other flags may follow)
 //   --out-raw FILE      float32 mean RGB [3][H][W] and first-crossing radius [H][W]
-//   --json FILE         a sidecar with the scene, passes and timings
+//   --json FILE         a sidecar with the scene, passes, timings and the
+//                       camera azimuth of every frame
 //   --accum-out FILE    the accumulator (colour sums, first-crossing radius,
 //                       invariant maxima, samples done) at every checkpoint
 //   --resume FILE       continue from such a file to --spp-total; the result
@@ -414,6 +415,7 @@ int main(int argc, char** argv) {
     };
 
     int rc = 0;
+    std::vector<double> frame_phi;   // camera azimuth of each frame, for the sidecar
     if (c.frames <= 1) {
         if (!render_one(c.phi0_deg, c.out_path)) rc = 1;
         else std::printf("Wrote %s\n", c.out_path);
@@ -424,6 +426,7 @@ int main(int argc, char** argv) {
         for (int i = 0; i < c.frames && rc == 0; ++i) {
             const float t = (float)i / (float)c.frames;
             const double phi = c.phi0_deg + 360.0 * c.turns * t;
+            frame_phi.push_back(phi);
             char path[512];
             std::snprintf(path, sizeof(path), c.out_pat, i);
             if (!render_one(phi, path)) rc = 1;
@@ -440,7 +443,7 @@ int main(int argc, char** argv) {
                          "\"mode\": \"%s\", \"crossing\": \"%s\", \"rtol\": %.17g, \"atol\": %.17g, "
                          "\"inv_gate\": %.17g, \"camera\": \"%s\", \"seed\": %u, \"jitter\": %d, "
                          "\"rays\": %llu, \"steps\": %llu, "
-                         "\"kernel_ms\": %.6f, \"rays_per_s\": %.6g}\n",
+                         "\"kernel_ms\": %.6f, \"rays_per_s\": %.6g, \"frame_phi_deg\": [",
                          s.width, s.height, np_frame_spp(fr), c.frames, passes_done, s.mass, s.spin, s.r_cam, s.theta_deg,
                          s.fov_y_deg, s.units == NP_UNITS_M ? "M" : "Rs", c.precision == NP_PREC_MIXED ? "mixed" : "fp64",
                          s.integrator == NP_INTEG_ADAPTIVE ? "adaptive" : s.integrator == NP_INTEG_RKF78 ? "rkf78" : "rk4",
@@ -448,6 +451,9 @@ int main(int argc, char** argv) {
                          s.crossing == NP_CROSS_ROOT ? "root" : s.crossing == NP_CROSS_HERMITE ? "hermite" : "linear",
                          s.rtol, s.atol, s.inv_gate, s.camera == NP_CAMERA_ZAMO ? "zamo" : "static", s.seed, s.jitter,
                          rays, steps, kernel_ms, kernel_ms > 0 ? rays / (kernel_ms * 1e-3) : 0.0);
+            if (frame_phi.empty()) frame_phi.push_back(c.phi0_deg);
+            for (size_t i = 0; i < frame_phi.size(); ++i) std::fprintf(f, "%s%.17g", i ? ", " : "", frame_phi[i]);
+            std::fprintf(f, "]}\n");
             std::fclose(f);
         }
     }

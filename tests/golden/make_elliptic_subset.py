@@ -4,7 +4,7 @@ elliptic_inputs.dat and elliptic_reference.dat, the Fortran Carlson values to
 12 significant digits), as `kind x y z p value` lines.  R_J rows of those
 files are not valid references and are left out.
 
-    python tests/golden/make_elliptic_subset.py /root/reference
+    python tests/golden/make_elliptic_subset.py <reference checkout>
 """
 import os
 import sys
@@ -30,4 +30,6 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: %s <reference checkout>" % sys.argv[0])
+    main(sys.argv[1])

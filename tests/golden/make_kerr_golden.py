@@ -3,7 +3,7 @@ kerr_api_probe.cpp built against the reference's own physics headers
 (include/bh_common.h, bh_types.h, bh_kerr.h, bh_schwarzschild.h of the
 reference checkout), with the flags the tests use for the np_kerr.h build.
 
-    python tests/golden/make_kerr_golden.py /root/reference
+    python tests/golden/make_kerr_golden.py <reference checkout>
 """
 import os
 import subprocess
@@ -27,4 +27,6 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: %s <reference checkout>" % sys.argv[0])
+    main(sys.argv[1])

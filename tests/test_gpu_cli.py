@@ -68,15 +68,38 @@ def test_cli_passes_match_library_render(cuda, tmp_path):
 
 def test_cli_frames_and_pattern(cuda, tmp_path):
     pat = str(tmp_path / "f_%03d.ppm")
-    p = subprocess.run([CLI, "--w", "24", "--h", "16", "--frames", "3", "--turns", "0.5", "--outpat", pat,
+    side = str(tmp_path / "f.json")
+    p = subprocess.run([CLI, "--w", "24", "--h", "16", "--frames", "3", "--turns", "0.5", "--phi0", "20",
+                        "--outpat", pat, "--bg", "point", "--json", side,
                         "--precision", "mixed", "--benchmark", "--w", "24", "--h", "16"],
                        capture_output=True, text=True, timeout=300)
     assert p.returncode == 0, p.stderr
     files = [pat % i for i in range(3)]
     assert all(os.path.exists(f) for f in files)
     imgs = [_read_ppm(f) for f in files]
-    # the spacetime, disk and sky are axisymmetric: every azimuth gives the same image
+    # the spacetime, disk and both skies depend on no azimuth (render.cu:74-86,
+    # 312-359): every frame gives the same image, so the orbit is checked
+    # through the azimuth each frame was rendered at (render.cu:630-635)
     assert imgs[0].shape == (16, 24, 3) and np.array_equal(imgs[0], imgs[1]) and np.array_equal(imgs[0], imgs[2])
+    phis = json.load(open(side))["frame_phi_deg"]
+    want = [20.0 + 360.0 * 0.5 * float(np.float32(i) / np.float32(3)) for i in range(3)]
+    assert np.allclose(phis, want, rtol=0, atol=1e-9), phis
+
+
+def test_camera_azimuth_rotates_crossings(cuda):
+    """phi_deg enters the ray start: every equatorial crossing's azimuth moves
+    by exactly the camera's azimuth, and nothing else changes."""
+    sc = npx.benchmark_scene(width=32, height=18, spp=1)
+    rng = np.random.default_rng(4)
+    px, py = rng.uniform(0, 32, 400), rng.uniform(0, 18, 400)
+    a = {k: v.cpu().numpy() for k, v in npx.trace_rays(sc, px, py, precision="fp64").items()}
+    b = {k: v.cpu().numpy() for k, v in npx.trace_rays(sc.replace(phi_deg=37.0), px, py, precision="fp64").items()}
+    ca, cb = a["cross"], b["cross"]
+    assert np.array_equal(a["status"], b["status"]) and np.array_equal(ca[..., 0], cb[..., 0])
+    hit = ca[..., 0] > 0
+    assert hit.sum() > 100
+    d = np.angle(np.exp(1j * (cb[..., 1][hit] - ca[..., 1][hit] - np.radians(37.0))))
+    assert np.abs(d).max() < 1e-9
     bad = subprocess.run([CLI, "--w", "8", "--h", "8", "--frames", "2", "--outpat", str(tmp_path / "x_%d_%d.ppm")],
                          capture_output=True, text=True, timeout=120)
     assert bad.returncode == 1 and "Invalid --outpat" in bad.stderr
