@@ -95,11 +95,13 @@ def cpu_baseline(threads=None, rows_every=45, timing=None):
     return rays / dt, threads, desc
 
 
-def geokerr_grid_leg(n_side=128, nup=32, cpu_sample=1024):
+def geokerr_grid_leg(n_side=128, nup=32, cpu_sample=1024, reps=5):
     """GEOKERR standard grid: a=0.9, r_o=1e6 M, i=60 deg, [-12,12]^2 alpha/beta,
-    n_side^2 geodesics x nup points on the GPU; the CPU restatement times a
-    bounded sample on all host cores and is the parity reference (max
-    normwise relative difference over the sample)."""
+    n_side^2 geodesics x nup points on the GPU, every point evaluated in
+    closed form by its own thread (Taylor solver timed beside it).  CPU: the
+    same closed form built for the host, on every geodesic over all host
+    cores (max normwise relative difference GPU vs CPU), and the Taylor
+    restatement (oracle) on a bounded sample."""
     import numpy as np
     import torch
     from concurrent.futures import ThreadPoolExecutor
@@ -111,31 +113,64 @@ def geokerr_grid_leg(n_side=128, nup=32, cpu_sample=1024):
     g = {k: v.cpu().numpy() for k, v in gd.items()}
     n = g["l"].size
     args = (a, np.full(n, u0), np.full(n, uplus), np.full(n, mu0), g["l"], g["q2"], g["su"], g["sm"])
-    gk.points(*args, tpr=1, nup=nup)
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record()
-    out = gk.points(*args, tpr=1, nup=nup)
-    e1.record()
-    torch.cuda.synchronize()
-    gpu_ms = e0.elapsed_time(e1)
+    dargs = (a,) + tuple(torch.as_tensor(x, dtype=torch.float64, device="cuda") for x in args[1:])
+
+    def timed(method):
+        gk.points(*dargs, tpr=1, nup=nup, method=method)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            out = gk.points(*dargs, tpr=1, nup=nup, method=method)
+        e1.record()
+        torch.cuda.synchronize()
+        return out, e0.elapsed_time(e1) / reps
+    out, gpu_ms = timed("closed_form")
+    _, taylor_ms = timed("taylor")
     got = {k: v.cpu().numpy() for k, v in out.items()}
-    idx = np.linspace(0, n - 1, cpu_sample).astype(int)
+    # CPU: the host build of the same closed form, every geodesic
+    chunks = np.array_split(np.arange(n), os.cpu_count() or 1)
+
+    def host_chunk(idx):
+        return idx, gk.points_host(a, u0, uplus, mu0, g["l"][idx], g["q2"][idx], g["su"][idx], g["sm"][idx], 1, nup,
+                                   0.5)
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=os.cpu_count()) as ex:
+        parts = list(ex.map(host_chunk, chunks))
+    cpu_s = time.perf_counter() - t0
+    worst_cpu = 0.0
+    methods = np.zeros(3, int)
+    for idx, h in parts:
+        methods += np.bincount(h["method"], minlength=3)
+        for k in ("u", "mu", "dt", "dphi", "lam"):
+            d = np.abs(got[k][idx] - h[k]).max(axis=1) / np.maximum(np.abs(h[k]).max(axis=1), 1e-300)
+            worst_cpu = max(worst_cpu, float(d.max()))
+        for k in ("tpm", "tpr"):
+            if not np.array_equal(got[k][idx], h[k]):
+                worst_cpu = float("inf")
+    # the Taylor restatement (oracle) on a bounded sample
+    sample = np.linspace(0, n - 1, cpu_sample).astype(int)
 
     def one(i):
         return oracle.geokerr_points(u0, uplus, mu0, a, g["l"][i], g["q2"][i], 1.0, g["sm"][i], 1, nup, 0.5)
     t0 = time.perf_counter()
     with ThreadPoolExecutor(max_workers=os.cpu_count()) as ex:
-        refs = list(ex.map(one, idx))
-    cpu_s = time.perf_counter() - t0
-    worst = 0.0
-    for i, ref in zip(idx, refs):
+        refs = list(ex.map(one, sample))
+    oracle_s = time.perf_counter() - t0
+    worst_taylor = 0.0
+    for i, ref in zip(sample, refs):
         for k in ("u", "mu", "dt", "dphi", "lam"):
-            worst = max(worst, float(np.max(np.abs(got[k][i] - ref[k])) / max(np.max(np.abs(ref[k])), 1e-300)))
+            worst_taylor = max(worst_taylor,
+                               float(np.max(np.abs(got[k][i] - ref[k])) / max(np.max(np.abs(ref[k])), 1e-300)))
     return {"geodesics": n, "points_per_geodesic": nup, "gpu_ms": gpu_ms,
-            "gpu_geodesics_per_s": n / (gpu_ms * 1e-3),
-            "cpu_geodesics_per_s": len(idx) / cpu_s, "cpu_cores": os.cpu_count(), "cpu_sample": len(idx),
-            "max_rel_diff_gpu_vs_cpu": worst, "all_sampled": bool((got["n"] == nup).all())}
+            "gpu_geodesics_per_s": n / (gpu_ms * 1e-3), "gpu_points_per_s": n * nup / (gpu_ms * 1e-3),
+            "gpu_ms_taylor_solver": taylor_ms, "speedup_vs_taylor_solver": taylor_ms / gpu_ms,
+            "closed_form_rays": int(methods[1] + methods[2]), "taylor_fallback_rays": int(methods[0]),
+            "cpu_geodesics_per_s": n / cpu_s, "cpu_cores": os.cpu_count(), "cpu_kind": "host build, closed form",
+            "max_rel_diff_gpu_vs_cpu": worst_cpu,
+            "oracle_taylor_geodesics_per_s": len(sample) / oracle_s, "oracle_sample": len(sample),
+            "max_rel_diff_vs_taylor_restatement": worst_taylor,
+            "all_sampled": bool((got["n"] == nup).all())}
 
 
 def adjoint_headline_leg(K=None):

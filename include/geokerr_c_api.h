@@ -122,12 +122,33 @@ int np_geokerr_final_state_host(int n, const double* a, const double* u0, const 
  * su[i], sm[i] and the common spin a, TPR flag, nup and offset; outputs are
  * [n][nup] device arrays (u, mu, delta t, delta phi, affine lambda, mu and
  * u turning counts) and npts[i] = points written (0 when the ray could not
- * be sampled).  Device pointers; returns np_status. */
+ * be sampled).  Every point is evaluated in closed form by its own thread
+ * (the semi-analytic GEOR / GEOMU / GEOPHITIME route,
+ * geokerr_original.f:771-1187, 1648-2360); rays outside the closed forms
+ * (q2 <= 0, a = 0, a double radial root) are integrated by the order-24
+ * Taylor solver.  n * nup < 2^31.  Device pointers; the per-ray workspace
+ * comes from the stream-ordered allocator.  Returns np_status. */
 int np_geokerr_points_device(int n, double a, const double* u0, const double* uf, const double* mu0,
                              const double* l, const double* q2, const double* su, const double* sm,
                              int tpr, int nup, double offset,
                              double* u, double* mu, double* dt, double* dphi, double* lam,
                              int32_t* tpm, int32_t* tprv, int32_t* npts, void* stream);
+
+/* The same sampler with every ray on the Taylor solver (one thread per ray). */
+int np_geokerr_points_taylor_device(int n, double a, const double* u0, const double* uf, const double* mu0,
+                                    const double* l, const double* q2, const double* su, const double* sm,
+                                    int tpr, int nup, double offset,
+                                    double* u, double* mu, double* dt, double* dphi, double* lam,
+                                    int32_t* tpm, int32_t* tprv, int32_t* npts, void* stream);
+
+/* np_geokerr_points_device on the host (same arithmetic, same bits);
+ * method[i] (optional) = 1 four real radial roots, 2 two real roots and a
+ * complex pair, 0 Taylor solver or no points. */
+int np_geokerr_points_host(int n, double a, const double* u0, const double* uf, const double* mu0,
+                           const double* l, const double* q2, const double* su, const double* sm,
+                           int tpr, int nup, double offset,
+                           double* u, double* mu, double* dt, double* dphi, double* lam,
+                           int32_t* tpm, int32_t* tprv, int32_t* npts, int32_t* method);
 
 /* Batched geokerr_eval_lambda: ray i with u0[i], mu0[i], uf[i], Lz[i],
  * Q2[i], t0[i], lam0[i], dlam[i] and common a and S; outputs [n][S]

@@ -27,7 +27,9 @@ CU_SOURCES = ["np_render.cu", "geokerr.cu", "adjoint.cu", "kerr_api.cu", "carlso
 # restatement (oracle/geokerr_oracle.cpp, -ffp-contract=off): for rays that
 # pass near a pole the sampled phi has a condition number of ~3e4 in the
 # potential's coefficients, so the two agree to 1e-12 only with the same
-# rounding.
+# rounding.  The same holds between its device code and its host build
+# (np_geokerr_points_host): both evaluate the closed forms of geokerr_cf.cuh
+# with +, -, *, / and sqrt only, so they give the same bits.
 PER_FILE_NVFLAGS = {"geokerr.cu": ["-fmad=false"]}
 
 

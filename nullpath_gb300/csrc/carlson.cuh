@@ -25,6 +25,9 @@ namespace np {
 namespace carlson {
 
 constexpr double kTol = 1e-16;
+// (3 kTol)^(-1/6), (3 kTol)^(-1/8) and (kTol / 4)^(-1/6), correctly rounded: literal so
+// that the host and device builds stop their duplication loops at the same step
+constexpr double kQ_rf = 386.49729393434575, kQ_rc = 87.16855428717356, kQ_rdj = 584.803547642573;
 constexpr int kMaxIter = 64;    // each duplication shrinks the deviations by 4
 
 NP_CARLSON_HD double nan_() { return std::nan(""); }
@@ -34,7 +37,7 @@ NP_CARLSON_HD double rf(double x, double y, double z) {
     if (!(x >= 0.0 && y >= 0.0 && z >= 0.0) || (x + y == 0.0) || (x + z == 0.0) || (y + z == 0.0)) return nan_();
     const double A0 = (x + y + z) / 3.0;
     double A = A0;
-    double Q = std::pow(3.0 * kTol, -1.0 / 6.0) * std::fmax(std::fabs(A0 - x), std::fmax(std::fabs(A0 - y), std::fabs(A0 - z)));
+    double Q = kQ_rf * std::fmax(std::fabs(A0 - x), std::fmax(std::fabs(A0 - y), std::fabs(A0 - z)));
     double f = 1.0;     // 4^-m
     for (int m = 0; m < kMaxIter && Q * f >= std::fabs(A); ++m) {
         const double sx = std::sqrt(x), sy = std::sqrt(y), sz = std::sqrt(z);
@@ -61,7 +64,7 @@ NP_CARLSON_HD double rc(double x, double y) {
     }
     const double A0 = (x + 2.0 * y) / 3.0;
     double A = A0;
-    double Q = std::pow(3.0 * kTol, -1.0 / 8.0) * std::fabs(A0 - x);
+    double Q = kQ_rc * std::fabs(A0 - x);
     double f = 1.0;
     for (int m = 0; m < kMaxIter && Q * f >= std::fabs(A); ++m) {
         const double lam = 2.0 * std::sqrt(x) * std::sqrt(y) + y;
@@ -85,7 +88,7 @@ NP_CARLSON_HD double rd(double x, double y, double z) {
     if (!(x >= 0.0 && y >= 0.0 && z > 0.0) || (x + y == 0.0)) return nan_();
     const double A0 = (x + y + 3.0 * z) / 5.0;
     double A = A0;
-    double Q = std::pow(0.25 * kTol, -1.0 / 6.0) *
+    double Q = kQ_rdj *
                std::fmax(std::fabs(A0 - x), std::fmax(std::fabs(A0 - y), std::fabs(A0 - z)));
     double f = 1.0, sum = 0.0;
     for (int m = 0; m < kMaxIter && Q * f >= std::fabs(A); ++m) {
@@ -108,7 +111,7 @@ NP_CARLSON_HD double rj_pos(double x, double y, double z, double p) {
     const double A0 = (x + y + z + 2.0 * p) / 5.0;
     double A = A0;
     const double delta = (p - x) * (p - y) * (p - z);
-    double Q = std::pow(0.25 * kTol, -1.0 / 6.0) *
+    double Q = kQ_rdj *
                std::fmax(std::fmax(std::fabs(A0 - x), std::fabs(A0 - y)), std::fmax(std::fabs(A0 - z), std::fabs(A0 - p)));
     double f = 1.0, f3 = 1.0, sum = 0.0;
     for (int m = 0; m < kMaxIter && Q * f >= std::fabs(A); ++m) {

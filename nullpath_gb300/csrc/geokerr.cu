@@ -30,6 +30,7 @@
 #include <cuda_runtime.h>
 
 #include "geokerr_c_api.h"
+#include "geokerr_cf.cuh"
 #include "np_render.h"
 
 void np_record_error(const char* msg);
@@ -53,6 +54,7 @@ constexpr int P = 24;
 
 struct Par {
     double a, l, A2, A3, A4, Q0, B2, B4, uplus;
+    double mpos, a2mneg;   // polar roots in mu^2 (a^2 times the second)
 };
 
 // Constants of the motion and GEOKERR's polar potential (roots of M in mu^2
@@ -77,6 +79,8 @@ __host__ __device__ Par make_par(double a, double l, double q2, double mu0) {
         if (a2mneg > a2 * mu0 * mu0) a2mneg = a2 * mu0 * mu0;
         if (mu0 * mu0 > mpos) mpos = mu0 * mu0;
     }
+    p.mpos = mpos;
+    p.a2mneg = a2mneg;
     p.B4 = -a2;
     p.B2 = a2 * mpos + a2mneg;
     p.Q0 = -mpos * a2mneg;
@@ -384,20 +388,81 @@ __global__ void geokerr_points_kernel(int n, double a, const double* __restrict_
     if (npts) npts[i] = w;
 }
 
-// eval_lambda, step 1: GEOKERR points with the conventions of
-// geokerr_eval_lambda.f90:102-118 (SU from uf - u0, SM = -1 for mu0 > 0,
-// TPR = 1, OFFSET = 0.5, NUP = S).
-__global__ void eval_points_kernel(int n, double a, const double* __restrict__ u0, const double* __restrict__ mu0,
-                                   const double* __restrict__ uf, const double* __restrict__ Lz,
-                                   const double* __restrict__ Q2, int S, double* w_u, double* w_mu, double* w_dt,
-                                   double* w_dphi, double* w_lam, int32_t* w_tpm, int32_t* w_tpr, int32_t* w_n) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
+// Closed-form points (geokerr_cf.cuh): one thread per ray computes the
+// ray's constants, one thread per (ray, sample) evaluates a point, and the
+// rays outside the closed forms run the Taylor sampler above from a compacted
+// list.  mode 0 takes su, sm and tpr from the caller; mode 1 uses
+// geokerr_eval_lambda's conventions (su from uf - u0, sm = -1 for mu0 > 0,
+// tpr = 1; geokerr_eval_lambda.f90:102-118).
+__host__ __device__ inline void cf_signs(int mode, int i, const double* u0, const double* uf, const double* mu0,
+                                         const double* su, const double* sm, int tpr, double& sui, double& smi,
+                                         int& tpri) {
+    if (mode == 0) { sui = su[i]; smi = sm[i]; tpri = tpr; return; }
+    sui = (uf[i] - u0[i]) >= 0.0 ? 1.0 : -1.0;
+    smi = mu0[i] <= 0.0 ? 1.0 : -1.0;
+    tpri = 1;
+}
+
+// Returns false when the start is forbidden (no points, as sample_points).
+__host__ __device__ inline bool cf_ray(int mode, int i, double a, const double* u0, const double* uf,
+                                       const double* mu0, const double* l, const double* q2, const double* su,
+                                       const double* sm, int tpr, int nup, double offset, np::gkcf::CfRay& R) {
+    double sui, smi, U0, M0;
+    int tpri;
+    cf_signs(mode, i, u0, uf, mu0, su, sm, tpr, sui, smi, tpri);
+    const Par p = make_par(a, l[i], q2[i], mu0[i]);
+    if (!start_potentials(p, u0[i], mu0[i], U0, M0)) return false;
+    np::gkcf::setup(a, l[i], q2[i], u0[i], uf[i], mu0[i], sui, smi, tpri, nup, offset, p.mpos, p.a2mneg, R);
+    return true;
+}
+
+__global__ void cf_setup_kernel(int n, int mode, double a, const double* __restrict__ u0,
+                                const double* __restrict__ uf, const double* __restrict__ mu0,
+                                const double* __restrict__ l, const double* __restrict__ q2,
+                                const double* __restrict__ su, const double* __restrict__ sm, int tpr, int nup,
+                                double offset, np::gkcf::CfRay* rays, int32_t* npts, int32_t* fb, int32_t* nfb) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const double su = (uf[i] - u0[i]) >= 0.0 ? 1.0 : -1.0;
-    const double sm = mu0[i] <= 0.0 ? 1.0 : -1.0;
-    Par p = make_par(a, Lz[i], Q2[i], mu0[i]);
-    PointOut o{w_u, w_mu, w_dt, w_dphi, w_lam, w_tpm, w_tpr, (long long)i * S};
-    w_n[i] = sample_points(p, u0[i], uf[i], mu0[i], su, sm, 1, S, 0.5, o);
+    np::gkcf::CfRay R;
+    if (!cf_ray(mode, i, a, u0, uf, mu0, l, q2, su, sm, tpr, nup, offset, R)) {
+        R.kind = -1;
+        R.last = 0;
+    }
+    rays[i] = R;
+    if (R.kind == np::gkcf::kFallback) fb[atomicAdd(nfb, 1)] = i;
+    else if (npts) npts[i] = R.last;
+}
+
+__global__ void cf_points_kernel(int n, int nup, const np::gkcf::CfRay* __restrict__ rays, double* u, double* mu,
+                                 double* dt, double* dphi, double* lam, int32_t* tpm, int32_t* tprv) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const int i = (int)(t / nup), k = (int)(t % nup) + 1;
+    if (i >= n) return;
+    const np::gkcf::CfRay& R = rays[i];
+    if ((R.kind != np::gkcf::kR4 && R.kind != np::gkcf::kR2C) || k > R.last) return;
+    const np::gkcf::Point P = np::gkcf::sample(R, k);
+    const long long o = (long long)i * nup + (k - 1);
+    u[o] = P.u; mu[o] = P.mu; dt[o] = P.dt; dphi[o] = P.dphi; lam[o] = P.lam; tpm[o] = P.tpm; tprv[o] = P.tpr;
+}
+
+__global__ void cf_fallback_kernel(const int32_t* __restrict__ fb, const int32_t* __restrict__ nfb, int mode,
+                                   double a, const double* __restrict__ u0, const double* __restrict__ uf,
+                                   const double* __restrict__ mu0, const double* __restrict__ l,
+                                   const double* __restrict__ q2, const double* __restrict__ su,
+                                   const double* __restrict__ sm, int tpr, int nup, double offset, double* u,
+                                   double* mu, double* dt, double* dphi, double* lam, int32_t* tpm, int32_t* tprv,
+                                   int32_t* npts) {
+    const int count = *nfb;
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < count; idx += gridDim.x * blockDim.x) {
+        const int i = fb[idx];
+        double sui, smi;
+        int tpri;
+        cf_signs(mode, i, u0, uf, mu0, su, sm, tpr, sui, smi, tpri);
+        const Par p = make_par(a, l[i], q2[i], mu0[i]);
+        PointOut o{u, mu, dt, dphi, lam, tpm, tprv, (long long)i * nup};
+        const int w = sample_points(p, u0[i], uf[i], mu0[i], sui, smi, tpri, nup, offset, o);
+        if (npts) npts[i] = w;
+    }
 }
 
 // eval_lambda, step 2: linear resampling onto lam0 + k dlam
@@ -624,6 +689,39 @@ __global__ void final_state_kernel(int n, const double* __restrict__ a, const do
 
 int grid(int n, int b) { return (n + b - 1) / b; }
 
+// The closed-form pipeline on a stream: setup, points, Taylor fallback.  Its
+// per-ray workspace (n CfRay records and the fallback list) is taken from the
+// stream-ordered pool and released on the stream.
+int points_cf_launch(int n, int mode, double a, const double* u0, const double* uf, const double* mu0,
+                     const double* l, const double* q2, const double* su, const double* sm, int tpr, int nup,
+                     double offset, double* u, double* mu, double* dt, double* dphi, double* lam, int32_t* tpm,
+                     int32_t* tprv, int32_t* npts, cudaStream_t st) {
+    if ((long long)n * nup > (1ll << 31) - 1) return gk_fail(NP_ERR_INVALID, "n * nup exceeds 2^31 - 1");
+    const size_t bytes = (size_t)n * sizeof(np::gkcf::CfRay) + ((size_t)n + 1) * sizeof(int32_t);
+    void* w = nullptr;
+    if (cudaMallocAsync(&w, bytes, st) != cudaSuccess) {
+        cudaGetLastError();
+        return gk_fail(NP_ERR_ALLOC, "cudaMallocAsync of %zu bytes failed", bytes);
+    }
+    np::gkcf::CfRay* rays = (np::gkcf::CfRay*)w;
+    int32_t* fb = (int32_t*)(rays + n);
+    int32_t* nfb = fb + n;
+    cudaMemsetAsync(nfb, 0, sizeof(int32_t), st);
+    cf_setup_kernel<<<grid(n, 128), 128, 0, st>>>(n, mode, a, u0, uf, mu0, l, q2, su, sm, tpr, nup, offset, rays, npts,
+                                                  fb, nfb);
+    const long long total = (long long)n * nup;
+    cf_points_kernel<<<(unsigned)((total + 127) / 128), 128, 0, st>>>(n, nup, rays, u, mu, dt, dphi, lam, tpm, tprv);
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = 1;
+    const int fb_blocks = std::min(grid(n, 32), 4 * sms);
+    cf_fallback_kernel<<<fb_blocks, 32, 0, st>>>(fb, nfb, mode, a, u0, uf, mu0, l, q2, su, sm, tpr, nup, offset, u, mu,
+                                                 dt, dphi, lam, tpm, tprv, npts);
+    cudaError_t e = cudaGetLastError();
+    cudaFreeAsync(w, st);
+    return e == cudaSuccess ? NP_OK : gk_fail(NP_ERR_KERNEL, "%s", cudaGetErrorString(e));
+}
+
 // Host arrays in, final states out (geokerr_cuda_batch and friends): copies
 // n rays' inputs to the device, runs final_state_kernel, copies back.
 // Returns false when the device work failed.
@@ -697,10 +795,54 @@ int np_geokerr_points_device(int n, double a, const double* u0, const double* uf
     if (n < 0 || nup <= 0) return gk_fail(NP_ERR_INVALID, "bad sizes");
     if (n == 0) return NP_OK;
     if (!(fabs(a) < 1.0)) return gk_fail(NP_ERR_INVALID, "spin must satisfy |a| < 1");
+    return points_cf_launch(n, 0, a, u0, uf, mu0, l, q2, su, sm, tpr, nup, offset, u, mu, dt, dphi, lam, tpm, tprv,
+                            npts, (cudaStream_t)stream);
+}
+
+int np_geokerr_points_taylor_device(int n, double a, const double* u0, const double* uf, const double* mu0,
+                                    const double* l, const double* q2, const double* su, const double* sm, int tpr,
+                                    int nup, double offset, double* u, double* mu, double* dt, double* dphi,
+                                    double* lam, int32_t* tpm, int32_t* tprv, int32_t* npts, void* stream) {
+    if (n < 0 || nup <= 0) return gk_fail(NP_ERR_INVALID, "bad sizes");
+    if (n == 0) return NP_OK;
+    if (!(fabs(a) < 1.0)) return gk_fail(NP_ERR_INVALID, "spin must satisfy |a| < 1");
     geokerr_points_kernel<<<grid(n, 64), 64, 0, (cudaStream_t)stream>>>(n, a, u0, uf, mu0, l, q2, su, sm, tpr, nup,
                                                                         offset, u, mu, dt, dphi, lam, tpm, tprv, npts);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? NP_OK : gk_fail(NP_ERR_KERNEL, "%s", cudaGetErrorString(e));
+}
+
+int np_geokerr_points_host(int n, double a, const double* u0, const double* uf, const double* mu0, const double* l,
+                           const double* q2, const double* su, const double* sm, int tpr, int nup, double offset,
+                           double* u, double* mu, double* dt, double* dphi, double* lam, int32_t* tpm, int32_t* tprv,
+                           int32_t* npts, int32_t* method) {
+    if (n < 0 || nup <= 0) return gk_fail(NP_ERR_INVALID, "bad sizes");
+    if (!(fabs(a) < 1.0)) return gk_fail(NP_ERR_INVALID, "spin must satisfy |a| < 1");
+    if (!u0 || !uf || !mu0 || !l || !q2 || !su || !sm || !u || !mu || !dt || !dphi || !lam || !tpm || !tprv)
+        return gk_fail(NP_ERR_INVALID, "NULL argument");
+    for (int i = 0; i < n; ++i) {
+        np::gkcf::CfRay R;
+        int w = 0, how = 0;
+        if (cf_ray(0, i, a, u0, uf, mu0, l, q2, su, sm, tpr, nup, offset, R)) {
+            if (R.kind == np::gkcf::kFallback) {
+                const Par p = make_par(a, l[i], q2[i], mu0[i]);
+                PointOut o{u, mu, dt, dphi, lam, tpm, tprv, (long long)i * nup};
+                w = sample_points(p, u0[i], uf[i], mu0[i], su[i], sm[i], tpr, nup, offset, o);
+            } else {
+                how = R.kind;
+                for (int k = 1; k <= R.last; ++k) {
+                    const np::gkcf::Point P = np::gkcf::sample(R, k);
+                    const long long o = (long long)i * nup + (k - 1);
+                    u[o] = P.u; mu[o] = P.mu; dt[o] = P.dt; dphi[o] = P.dphi; lam[o] = P.lam;
+                    tpm[o] = P.tpm; tprv[o] = P.tpr;
+                }
+                w = R.last;
+            }
+        }
+        if (npts) npts[i] = w;
+        if (method) method[i] = how;
+    }
+    return NP_OK;
 }
 
 int np_geokerr_equator_crossings_device(int n, double a, const double* u0, const double* mu0, const double* l,
@@ -741,8 +883,12 @@ int np_geokerr_eval_lambda_device(int n, double a, const double* u0, const doubl
     double *w_u = wd, *w_mu = wd + m, *w_dt = wd + 2 * m, *w_dphi = wd + 3 * m, *w_lam = wd + 4 * m;
     int32_t* wi = (int32_t*)(wd + 5 * m);
     int32_t *w_tpm = wi, *w_tpr = wi + m, *w_n = wi + 2 * m;
-    eval_points_kernel<<<grid(n, 64), 64, 0, st>>>(n, a, u0, mu0, uf, Lz, Q2, S, w_u, w_mu, w_dt, w_dphi, w_lam,
-                                                  w_tpm, w_tpr, w_n);
+    int rc = points_cf_launch(n, 1, a, u0, uf, mu0, Lz, Q2, nullptr, nullptr, 1, S, 0.5, w_u, w_mu, w_dt, w_dphi,
+                              w_lam, w_tpm, w_tpr, w_n, st);
+    if (rc != NP_OK) {
+        if (own) { cudaStreamSynchronize(st); cudaFree(w); }
+        return rc;
+    }
     eval_resample_kernel<<<grid(n, 64), 64, 0, st>>>(n, S, u0, mu0, t0, lam0, dlam, w_u, w_mu, w_dt, w_dphi, w_lam,
                                                     w_tpm, w_tpr, w_n, u, mu, t, phi, affine, tpmi, tpri, info);
     cudaError_t e = cudaGetLastError();

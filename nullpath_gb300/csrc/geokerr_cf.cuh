@@ -1,0 +1,452 @@
+// geokerr_cf.cuh -- GEOKERR's sampled geodesic points in closed form: every
+// (ray, sample) pair is evaluated on its own (the role of GEOR / GEOMU /
+// GEOPHITIME, geokerr_original.f:771-1187, 1648-2360, 2672-3136), for host
+// and device.
+//
+// With E = M = 1, u = 1/r, mu = cos(theta) and Mino time lambda, the motion
+// separates (du/dlambda)^2 = U(u), (dmu/dlambda)^2 = M(mu), and
+//   dt/dlambda     = 1/u^2 + 2/u + c+/(1 - r+ u) + c-/(1 - r- u) + a^2 mu^2
+//   dphi/dlambda   = d+/(1 - r+ u) + d-/(1 - r- u) - l + l/(1 - mu^2)
+//   daffine/dlambda = 1/u^2 + a^2 mu^2
+// with r+- = 1 +- sqrt(1 - a^2), c+- = 2 (2 r+- - a l)/(r+- - r-+) and
+// d+- = a (2 r+- - a l)/(r+- (r+- - r-+)): the partial fractions of the
+// right-hand sides of the Taylor solver in geokerr.cu (the constant terms
+// a^2 - a l of the t equation cancel).  Every radial term is then an integral
+// of 1, 1/(u - p) or 1/u^2 against du/sqrt(U), and every polar term one of
+// mu^2 or 1/(1 - mu^2) against dmu/sqrt(M).
+//
+// Radial, four real roots u1 < u2 < u3 < u4, motion in [u1, u2] (U has the
+// sign of -a^2 q2 at infinity): the Legendre variable
+//   S = sin^2(phi) = (u3 - u1)(u2 - u) / ((u2 - u1)(u3 - u)),  S = 0 at u2,
+//   m = (u2 - u1)(u4 - u3) / ((u3 - u1)(u4 - u2)),
+//   int_u^{u2} du / sqrt(U) = g F(phi | m),  g = 2 / sqrt(|c4| (u3 - u1)(u4 - u2))
+// (the reduction of Byrd & Friedman 256.00 written from u2), and
+//   1/(u - p) = 1/(u2 - p) + K_p S / (1 - n_p S),
+//   n_p = (u3 - p)(u2 - u1) / ((u2 - p)(u3 - u1)),
+//   K_p = (u3 - u2)(u2 - u1) / ((u2 - p)^2 (u3 - u1)),
+//   1 - n_p S = (u - p)(u3 - u2) / ((u2 - p)(u3 - u))   (no cancellation).
+// Radial, two real roots u1 < u2 and a complex pair rho +- i sigma: Byrd &
+// Friedman 259.00 give cn(w) = X(u) with int_{u1}^u du/sqrt(U) = w /
+// sqrt(|c4| A B); its half argument S = sn^2(w/2) = (1 - X)/(1 + dn w) is a
+// monotone Legendre variable over all of [u1, u2], u is a ratio of quadratics
+// in S, and 1/(u - p) splits into two terms 1/(1 - n_j S) with real n_j.
+//
+// Legendre integrals of the amplitude (S = sin^2 phi, C = cos^2 phi,
+// Delta^2 = 1 - m S), all with Carlson's R-functions (DLMF 19.25):
+//   F  = s R_F(C, Delta^2, 1),           Sd = int sin^2/Delta = s^3/3 R_D(C, Delta^2, 1)
+//   J(n)  = int sin^2 / ((1 - n sin^2) Delta) = s^3/3 R_J(C, Delta^2, 1, 1 - n S)
+//   Pi(n) = F + n J(n); for n < -1 from the R_J transformation DLMF 19.21.12
+//           (p and q = y - (x - y)(z - y)/(p - y)), which keeps Pi accurate as
+//           n -> -inf; past the pole (n > 1, 1 - n S < 0) the principal value
+//           from Pi(n) + Pi(m/n) = F + s R_C(C Delta^2, (1 - n S)(1 - m S/n))
+//           (DLMF 19.7.8)
+//   Pi2(n) = int 1/((1 - n sin^2)^2 Delta), by differentiating
+//           s c d / (1 - n S) and eliminating Pi in favour of J (no 1/n terms).
+// Polar (q2 > 0, a != 0): mu = mu+ cn(omega lambda - s_mu F0 | k) as in
+// mino_carlson.cuh; the integrals over whole half periods are complete
+// values, so each sample needs the amplitude of one reduced argument.
+//
+// Only +, -, *, / and sqrt enter (the Jacobi functions come from a Newton
+// solve of F(s) = w, not from trigonometric functions), so with contraction
+// off the host and device builds give the same bits.
+#pragma once
+
+#include <cmath>
+#include <cstdint>
+
+#include "carlson.cuh"
+#include "mino_carlson.cuh"
+
+namespace np {
+namespace gkcf {
+
+namespace cr = ::np::carlson;
+
+#define GKCF_HD NP_CARLSON_HD
+
+// ---------------------------------------------------------------------------
+// Legendre integrals of one amplitude
+// m and its complement mc = 1 - m are both carried (mc from its own
+// cancellation-free expression: near m = 1, 1 - m would keep only the
+// absolute accuracy of m).
+struct Amp {
+    double S, C, m, mc, s, D2, F, Sd;
+};
+
+GKCF_HD Amp amp_make(double S, double C, double m, double mc) {
+    Amp A;
+    A.S = S; A.C = C; A.m = m; A.mc = mc;
+    A.s = std::sqrt(S);
+    A.D2 = C + mc * S;      // 1 - m S
+    if (S > 0.0) {
+        A.F = A.s * cr::rf(C, A.D2, 1.0);
+        A.Sd = A.s * S / 3.0 * cr::rd(C, A.D2, 1.0);
+    } else {
+        A.F = 0.0; A.Sd = 0.0;
+    }
+    return A;
+}
+
+// p = 1 - n S, formed by the caller without cancellation where it can be small
+GKCF_HD double amp_pi(const Amp& A, double n, double p) {
+    if (A.S == 0.0) return 0.0;
+    const double m = A.m, mc = A.mc, s = A.s, S = A.S, C = A.C, D2 = A.D2;
+    if (n < -1.0) {
+        const double q = D2 - mc * m * S / (m - n);
+        return s * cr::rf(C, D2, 1.0) * m / (m - n) - n * s / (m - n) * cr::rc(C / D2, p * q / D2) +
+               n * mc * m * s * S * cr::rj(C, D2, 1.0, q) / (3.0 * (m - n) * (m - n));
+    }
+    if (p > 0.0) return A.F + n * s * S / 3.0 * cr::rj(C, D2, 1.0, p);
+    const double nn = m / n;
+    const double pim = A.F + nn * s * S / 3.0 * cr::rj(C, D2, 1.0, 1.0 - nn * S);
+    return A.F + s * cr::rc(C * D2, p * (1.0 - nn * S)) - pim;
+}
+
+GKCF_HD double amp_j(const Amp& A, double n, double p) {
+    if (A.S == 0.0) return 0.0;
+    if (p > 0.0) return A.s * A.S / 3.0 * cr::rj(A.C, A.D2, 1.0, p);
+    return (amp_pi(A, n, p) - A.F) / n;
+}
+
+// e = n - 1 is passed exactly: the denominator (n - 1)(n - m) = e (e + mc)
+// vanishes as n -> 1 together with mc -> 0 (a near-double radial root)
+GKCF_HD double amp_pi2(const Amp& A, double n, double e, double p) {
+    if (A.S == 0.0) return 0.0;
+    const double m = A.m;
+    const double V = A.s * std::sqrt(A.C) * std::sqrt(A.D2) / p;
+    const double num = n * n * V - (2.0 * n + 2.0 * m * n - n * n - 2.0 * m) * A.F -
+                       n * (2.0 * n + 2.0 * m * n - n * n - 3.0 * m) * amp_j(A, n, p) + m * n * A.Sd;
+    return num / (2.0 * e * (e + A.mc));
+}
+
+// sn, cn, dn of w in [0, K(m)]: for w <= K/2 the amplitude's sine s solves
+// s R_F(1 - s^2, 1 - m s^2, 1) = w, found by Newton steps from s = min(w,
+// sn(K/2)) (F is convex in s, so they descend monotonically; a bisection
+// bracket guards them); beyond K/2 the complementary argument K - w is
+// solved and sn(w) = cd(K - w), cn(w) = k' sd(K - w), dn(w) = k' nd(K - w).
+// S2 = sn^2 and C2 = cn^2 are returned without forming 1 - sn^2.
+GKCF_HD void jacobi(double w, double m, double mc, double K, double& S2, double& C2, double& D2) {
+    const bool comp = w > 0.5 * K;
+    const double x = comp ? K - w : w;
+    double s = 0.0;
+    if (x > 0.0) {
+        double hi = 1.0 / std::sqrt(1.0 + std::sqrt(mc)), lo = 0.0;
+        s = std::fmin(x, hi);
+        for (int it = 0; it < 64; ++it) {
+            const double c2 = (1.0 - s) * (1.0 + s), d2 = c2 + mc * s * s;
+            const double f = s * cr::rf(c2, d2, 1.0) - x;
+            if (f == 0.0) break;
+            if (f > 0.0) hi = s; else lo = s;
+            double sn = s - f * std::sqrt(c2 * d2);
+            if (!(sn > lo && sn < hi)) sn = 0.5 * (lo + hi);
+            const bool done = std::fabs(sn - s) <= 1e-16 * s;
+            s = sn;
+            if (done) break;
+        }
+    }
+    const double ss = s * s, cc = (1.0 - s) * (1.0 + s), dd = cc + mc * ss;
+    if (!comp) { S2 = ss; C2 = cc; D2 = dd; return; }
+    S2 = cc / dd; C2 = mc * ss / dd; D2 = mc / dd;
+}
+
+// ---------------------------------------------------------------------------
+// Per-ray constants
+enum { kFallback = 0, kR4 = 1, kR2C = 2 };
+
+struct CfRay {
+    int32_t kind, tpr, kmax, last;
+    double a, l, u0, ub, du, offset, su;
+    double r[4];            // R4: u1..u4; R2C: u1, u2, A, B
+    double m, mc, g;        // radial parameter, 1 - m; scale (R4: g, R2C: 2 / sqrt(|c4| A B))
+    double pole[3];         // 0, 1/r+, 1/r- (R4: n_p)
+    double pc[3][6];        // R2C: e1, e2 (e_j = n_j - 1), al1, al2, cinf, a0 per pole
+    double pn[3][2];        // R2C: n1, n2 per pole
+    double rp, rm, cp, cm, dp, dm;
+    // polar
+    double mpos, omp, mp, om, mth, mcth, Kth, nth, w0, mu2K, invK, Ph0mu2, Ph0inv;
+    double G0[5], Gtop[5];  // 1, 1/u^2, 1/u, 1/(u - 1/r+), 1/(u - 1/r-) integrals
+};
+
+// Radial Legendre amplitude of u (and, for R2C, D(S) = the Moebius denominator)
+GKCF_HD Amp radial_amp(const CfRay& R, double u, double& Dfac) {
+    const double m = R.m, mc = R.mc;
+    if (R.kind == kR4) {
+        const double u1 = R.r[0], u2 = R.r[1], u3 = R.r[2];
+        const double den = (u2 - u1) * (u3 - u);
+        Dfac = 0.0;
+        return amp_make((u3 - u1) * (u2 - u) / den, (u - u1) * (u3 - u2) / den, m, mc);
+    }
+    const double u1 = R.r[0], u2 = R.r[1], A = R.r[2], B = R.r[3];
+    const double den = (u2 - u) * B + (u - u1) * A;
+    const double omx = 2.0 * (u - u1) * A / den;       // 1 - X
+    const double opx = 2.0 * (u2 - u) * B / den;       // 1 + X
+    const double X = 0.5 * (opx - omx);
+    const double dnw = std::sqrt(mc + m * X * X);
+    const double S = omx / (1.0 + dnw);
+    const double C = X > 0.0 ? (X + dnw) / (1.0 + dnw) : mc * omx * opx / ((dnw - X) * (1.0 + dnw));
+    Dfac = A * B * (u2 - u1) * (C * (1.0 + S) + mc * S * S) / den;   // A B (u2 - u1)(1 - m S^2) / den
+    return amp_make(S, C, m, mc);
+}
+
+// R2C: the two pole factors 1 - n_j S at u, the one near zero from their product
+GKCF_HD void r2c_factors(const CfRay& R, int ip, const Amp& A, double u, double Dfac, double& f1, double& f2) {
+    const double* c = R.pc[ip];
+    f1 = A.C - c[0] * A.S;      // 1 - n S = (1 - S) - e S
+    f2 = A.C - c[1] * A.S;
+    const double prod = (u - R.pole[ip]) * Dfac / c[5];
+    if (std::fabs(f1) < std::fabs(f2)) f1 = prod / f2;
+    else f2 = prod / f1;
+}
+
+// int dv / (1 - n S) = F + n J (Pi for n < -1)
+GKCF_HD double pole_term(const Amp& A, double n, double f) {
+    return n < -1.0 ? amp_pi(A, n, f) : A.F + n * amp_j(A, n, f);
+}
+
+// G(u): the five radial integrals against du/sqrt(U), increasing in u
+// (R4: minus the integral from u to u2; R2C: the integral from u1 to u).
+GKCF_HD void radial_G(const CfRay& R, double u, double* G) {
+    double Dfac;
+    const Amp A = radial_amp(R, u, Dfac);
+    if (R.kind == kR4) {
+        const double u1 = R.r[0], u2 = R.r[1], u3 = R.r[2], g = R.g;
+        G[0] = -g * A.F;
+        for (int ip = 0; ip < 3; ++ip) {
+            const double p = R.pole[ip], n = (u3 - p) * (u2 - u1) / ((u2 - p) * (u3 - u1));
+            const double e = (u3 - u2) * (p - u1) / ((u2 - p) * (u3 - u1));      // n - 1
+            const double f = (u - p) * (u3 - u2) / ((u2 - p) * (u3 - u));
+            double h;
+            if (n < -1.0) h = A.F / (u3 - p) + (u3 - u2) / ((u3 - p) * (u2 - p)) * amp_pi(A, n, f);
+            else h = A.F / (u2 - p) + (u3 - u2) * (u2 - u1) / ((u2 - p) * (u2 - p) * (u3 - u1)) * amp_j(A, n, f);
+            G[2 + ip] = -g * h;
+            if (ip == 0) {
+                // (1/u2 + K0 S/(1 - n S))^2, with int S^2/(1 - n S)^2 = (Pi2 - 2 Pi + F)/n^2
+                const double K0 = (u3 - u2) * (u2 - u1) / (u2 * u2 * (u3 - u1));
+                const double Q = (amp_pi2(A, n, e, f) - 2.0 * amp_pi(A, n, f) + A.F) / (n * n);
+                G[1] = -g * (A.F / (u2 * u2) + 2.0 * K0 / u2 * amp_j(A, n, f) + K0 * K0 * Q);
+            }
+        }
+        return;
+    }
+    const double g = R.g;
+    G[0] = g * A.F;
+    for (int ip = 0; ip < 3; ++ip) {
+        const double* c = R.pc[ip];
+        double f1, f2;
+        r2c_factors(R, ip, A, u, Dfac, f1, f2);
+        const double n1 = R.pn[ip][0], n2 = R.pn[ip][1];
+        const double t1 = pole_term(A, n1, f1), t2 = pole_term(A, n2, f2);
+        G[2 + ip] = g * (c[4] * A.F + c[2] * t1 + c[3] * t2);
+        if (ip == 0) {
+            const double cross = 2.0 * c[2] * c[3] / (c[0] - c[1]);
+            G[1] = g * (c[4] * c[4] * A.F + 2.0 * c[4] * (c[2] * t1 + c[3] * t2) + cross * (n1 * t1 - n2 * t2) +
+                        c[2] * c[2] * amp_pi2(A, n1, c[0], f1) + c[3] * c[3] * amp_pi2(A, n2, c[1], f2));
+        }
+    }
+}
+
+// Polar integrals Phi(w) = (int_0^w mu^2 dw', int_0^w dw'/(1 - mu^2)) with
+// mu = mu+ cn w'; also cn w and the half-period index j of w.
+GKCF_HD void polar_Phi(const CfRay& R, double w, double& mu2, double& inv, double& cn, double& jj) {
+    const double K = R.Kth, m = R.mth;
+    const double j = std::floor(w / (2.0 * K) + 0.5);
+    const double r = w - 2.0 * j * K;
+    double S2, C2, D2;
+    jacobi(std::fabs(r), m, R.mcth, K, S2, C2, D2);
+    const Amp A = amp_make(S2, C2, m, R.mcth);
+    const double sg = r >= 0.0 ? 1.0 : -1.0;
+    mu2 = 2.0 * j * R.mu2K + sg * R.mpos * (A.F - A.Sd);
+    inv = 0.0;
+    if (R.l != 0.0) inv = 2.0 * j * R.invK + sg * amp_pi(A, R.nth, (R.omp + R.mpos * S2) / R.omp) / R.omp;
+    const double par = j - 2.0 * std::floor(0.5 * j);
+    cn = (par != 0.0 ? -1.0 : 1.0) * std::sqrt(C2);
+    jj = j;
+}
+
+// Per-ray setup; kind = kFallback when the ray is outside the closed forms
+// (q2 <= 0, a = 0, roots of U not in the two cases above, a start outside
+// [u1, u2], a polar orbit through the pole with l != 0).
+GKCF_HD void setup(double a, double l, double q2, double u0, double uf, double mu0, double su, double sm, int tpr_in,
+                   int nup, double offset, double mpos, double a2mneg, CfRay& R) {
+    R.kind = kFallback;
+    R.tpr = 0; R.kmax = 0; R.last = 0;
+    R.a = a; R.l = l; R.u0 = u0; R.offset = offset; R.su = su;
+    if (!(q2 > 0.0) || a == 0.0 || !(a2mneg < 0.0) || nup <= 0) return;
+    if (!(1.0 - mpos > 1e-15) && l != 0.0) return;
+    const double B = a * a - l * l - q2, Kc = (l - a) * (l - a) + q2;
+    const double c[5] = {1.0, 0.0, B, 2.0 * Kc, -a * a * q2};
+    double rr[4], rho = 0.0, sigma = 0.0;
+    const int nr = ::np::mino::real_roots(c, 4, rr, &rho, &sigma);
+    const double sq = std::sqrt(1.0 - a * a);
+    R.rp = 1.0 + sq;
+    R.rm = a * a / R.rp;
+    R.pole[0] = 0.0; R.pole[1] = 1.0 / R.rp; R.pole[2] = 1.0 / R.rm;
+    const double uplus = 1.0 / R.rp;
+    double u1, u2;
+    if (nr == 4) {
+        u1 = rr[0]; u2 = rr[1];
+        const double u3 = rr[2], u4 = rr[3];
+        if (!(u1 < u0 && u0 <= u2) || !(u2 < u3)) return;
+        R.kind = kR4;
+        for (int i = 0; i < 4; ++i) R.r[i] = rr[i];
+        R.m = (u2 - u1) * (u4 - u3) / ((u3 - u1) * (u4 - u2));
+        R.mc = (u3 - u2) * (u4 - u1) / ((u3 - u1) * (u4 - u2));
+        R.g = 2.0 / std::sqrt(-c[4] * (u3 - u1) * (u4 - u2));
+    } else if (nr == 2 && sigma > 0.0) {
+        u1 = rr[0]; u2 = rr[1];
+        if (!(u1 < u0 && u0 <= u2)) return;
+        R.kind = kR2C;
+        const double A = std::sqrt((u2 - rho) * (u2 - rho) + sigma * sigma);
+        const double Bq = std::sqrt((u1 - rho) * (u1 - rho) + sigma * sigma);
+        R.r[0] = u1; R.r[1] = u2; R.r[2] = A; R.r[3] = Bq;
+        const double mdirect = ((u2 - u1) * (u2 - u1) - (A - Bq) * (A - Bq)) / (4.0 * A * Bq);
+        // 1 - m = (A + B - (u2 - u1))(A + B + u2 - u1) / (4 A B), with
+        // A - |u2 - rho| = sigma^2 / (A + |u2 - rho|) (likewise B)
+        // (|u2 - rho| + |rho - u1| - (u2 - u1) is 0 for rho in [u1, u2], and
+        // twice the distance to the interval outside it: set, not rounded)
+        const double d2 = std::fabs(u2 - rho), d1 = std::fabs(rho - u1);
+        const double outside = rho < u1 ? 2.0 * (u1 - rho) : (rho > u2 ? 2.0 * (rho - u2) : 0.0);
+        const double gap = sigma * sigma / (A + d2) + sigma * sigma / (Bq + d1) + outside;
+        R.mc = gap * (A + Bq + (u2 - u1)) / (4.0 * A * Bq);
+        R.m = R.mc < 0.5 ? 1.0 - R.mc : mdirect;
+        R.g = 2.0 / std::sqrt(-c[4] * A * Bq);
+        // Poles: 1/(u - p) = D(S) / N_p(S) with the Moebius denominator
+        // D(S) = (1 - S)(A + B S) + B mc S^2 and N_p(S) = a0 (1 - n1 S)(1 - n2 S);
+        // e = n - 1 solves a0 e^2 + ((u1 - p) A + (u2 - p) B) e + (u2 - p) B mc = 0
+        // (exact coefficients), and the residues are
+        //   al_j = D(1/n_j) n_j / (a0 (n_j - n_k)) = (e_j (A n_j + B) + B mc) / (n_j a0 (e_j - e_k)).
+        // Each root is taken from the form in which it has no cancellation:
+        // n from a0 n^2 + a1 n + a2 = 0 where |n - 1| >= 1/2, else n = 1 + e.
+        for (int ip = 0; ip < 3; ++ip) {
+            const double p = R.pole[ip];
+            const double a0 = (u1 - p) * A, b1 = (u1 - p) * A + (u2 - p) * Bq, c0 = (u2 - p) * Bq * R.mc;
+            const double a1 = (u2 - p) * Bq - (u1 - p) * A, a2 = -R.m * Bq * (u2 - p);
+            const double dn = std::sqrt(a1 * a1 - 4.0 * a0 * a2);
+            const double qn = -0.5 * (a1 + (a1 >= 0.0 ? dn : -dn));
+            double n1 = qn / a0, n2 = a2 / qn;
+            if (std::fabs(n2) > std::fabs(n1)) { const double t = n1; n1 = n2; n2 = t; }
+            const double de = std::sqrt(b1 * b1 - 4.0 * a0 * c0);
+            const double qe = -0.5 * (b1 + (b1 >= 0.0 ? de : -de));
+            const double ea = qe / a0, eb = c0 / qe;
+            double e1 = n1 - 1.0, e2 = n2 - 1.0;
+            const double ec1 = std::fabs(ea - e1) < std::fabs(eb - e1) ? ea : eb;
+            const double ec2 = std::fabs(ea - e2) < std::fabs(eb - e2) ? ea : eb;
+            if (std::fabs(ec1) < 0.5) { e1 = ec1; n1 = 1.0 + ec1; }
+            if (std::fabs(ec2) < 0.5) { e2 = ec2; n2 = 1.0 + ec2; }
+            double* pc = R.pc[ip];
+            pc[0] = e1; pc[1] = e2;
+            pc[2] = (e1 * (A * n1 + Bq) + Bq * R.mc) / (n1 * a0 * (e1 - e2));
+            pc[3] = (e2 * (A * n2 + Bq) + Bq * R.mc) / (n2 * a0 * (e2 - e1));
+            pc[4] = 1.0 / (u2 - p);
+            pc[5] = a0;
+            R.pn[ip][0] = n1; R.pn[ip][1] = n2;
+        }
+    } else {
+        return;
+    }
+    // coefficients of the partial fractions
+    R.cp = 2.0 * (2.0 * R.rp - a * l) / (R.rp - R.rm);
+    R.cm = 2.0 * (2.0 * R.rm - a * l) / (R.rm - R.rp);
+    R.dp = a * (2.0 * R.rp - a * l) / (R.rp * (R.rp - R.rm));
+    R.dm = a * (2.0 * R.rm - a * l) / (R.rm * (R.rm - R.rp));
+    // sampling, as the Taylor sampler: NUP points uniform in u from U0 to the
+    // turning point UB and back (geokerr_original.f:357-605)
+    double ub;
+    int tpr = 0;
+    if (su > 0.0 && u2 < uplus) { ub = u2; tpr = tpr_in; }
+    else ub = su > 0.0 ? uplus : 0.0;
+    double UF = uf;
+    if (tpr == 1 && ((su > 0.0 && UF > ub) || (su < 0.0 && UF < ub))) UF = ub;
+    if (tpr == 1 && UF == ub) UF = u0;
+    const double du = ((ub - u0) >= 0.0 ? 1.0 : -1.0) * su * ((ub - u0) + (2.0 * tpr - 1.0) * (ub - UF)) / (double)nup;
+    int kmax = (du == 0.0) ? 0 : (int)((ub - u0) / du + offset);
+    if (kmax > nup) kmax = nup;
+    R.ub = ub; R.tpr = tpr; R.du = du; R.kmax = kmax;
+    R.last = tpr == 1 ? nup : (kmax < nup ? kmax : nup);
+    if (R.last < 0) R.last = 0;
+    // A target the ray never reaches (at or inside the horizon before a
+    // turning point, at or beyond u = 0 on the way out) leaves the ray
+    // without points, as in the Taylor sampler.
+    if (R.last > 0) {
+        if (su > 0.0) {
+            const int kk = R.last < kmax ? R.last : kmax;
+            if (kk >= 1 && !(u0 + (kk - offset) * du < uplus)) R.last = 0;
+        } else if (!(u0 + (R.last - offset) * du > 0.0)) {
+            R.last = 0;
+        }
+    }
+    // polar constants
+    R.mpos = mpos;
+    // 1 - mu+^2 is the small root of a^2 y^2 - (a^2 + l^2 + q2) y + l^2 = 0,
+    // taken without the cancellation of 1 - mpos unless GEOKERR's rules
+    // moved the root (to mu0^2, or to 1 by clamping)
+    {
+        const double a2 = a * a, bb = a2 - (q2 + l * l);
+        const double yy = -0.5 * (bb + (bb >= 0.0 ? 1.0 : -1.0) * std::sqrt(bb * bb + 4.0 * q2 * a2));
+        const double m0 = bb < 0.0 ? q2 / yy : -yy / a2;
+        const double E = a2 + l * l + q2;
+        R.omp = (m0 == mpos) ? 2.0 * l * l / (E + std::sqrt((E - 2.0 * a * l) * (E + 2.0 * a * l))) : 1.0 - mpos;
+    }
+    R.mp = std::sqrt(mpos);
+    const double w2 = a * a * mpos - a2mneg;
+    R.om = std::sqrt(w2);
+    R.mth = a * a * mpos / w2;
+    R.mcth = -a2mneg / w2;
+    R.Kth = cr::rf(0.0, R.mcth, 1.0);
+    R.nth = -mpos / R.omp;
+    double c0 = mu0 / R.mp;
+    c0 = c0 > 1.0 ? 1.0 : (c0 < -1.0 ? -1.0 : c0);
+    const Amp A0 = amp_make((1.0 - c0) * (1.0 + c0), c0 * c0, R.mth, R.mcth);
+    const double F0 = c0 >= 0.0 ? A0.F : 2.0 * R.Kth - A0.F;
+    R.w0 = -(sm < 0.0 ? -1.0 : 1.0) * F0;
+    const Amp Ac = amp_make(1.0, 0.0, R.mth, R.mcth);
+    R.mu2K = mpos * (R.Kth - Ac.Sd);
+    R.invK = l != 0.0 ? amp_pi(Ac, R.nth, 1.0 / R.omp) / R.omp : 0.0;
+    double cn0, j0;
+    polar_Phi(R, R.w0, R.Ph0mu2, R.Ph0inv, cn0, j0);
+    // radial integrals at the start and at the turning point
+    radial_G(R, u0, R.G0);
+    if (tpr == 1 && R.kind == kR2C) radial_G(R, u2, R.Gtop);
+    else for (int i = 0; i < 5; ++i) R.Gtop[i] = 0.0;
+    bool ok = true;
+    for (int i = 0; i < 5; ++i) ok = ok && std::isfinite(R.G0[i]) && std::isfinite(R.Gtop[i]);
+    ok = ok && std::isfinite(R.Ph0mu2) && std::isfinite(R.Ph0inv) && std::isfinite(R.om) && R.om > 0.0;
+    if (!ok) R.kind = kFallback;
+}
+
+struct Point {
+    double u, mu, dt, dphi, lam;
+    int32_t tpm, tpr;
+};
+
+// Sample k (1-based, k <= R.last) of a ray set up above.
+GKCF_HD Point sample(const CfRay& R, int k) {
+    Point P;
+    const bool branch2 = k > R.kmax;
+    const double ut = branch2 ? 2.0 * R.ub - (R.u0 + (k - R.offset) * R.du) : R.u0 + (k - R.offset) * R.du;
+    double Gk[5], I[5];
+    radial_G(R, ut, Gk);
+    for (int i = 0; i < 5; ++i) {
+        if (R.su > 0.0) I[i] = branch2 ? 2.0 * R.Gtop[i] - R.G0[i] - Gk[i] : Gk[i] - R.G0[i];
+        else I[i] = R.G0[i] - Gk[i];
+    }
+    const double lam = I[0];
+    const double w = R.om * lam + R.w0;
+    double mu2, inv, cn, j;
+    polar_Phi(R, w, mu2, inv, cn, j);
+    const double Imu2 = (mu2 - R.Ph0mu2) / R.om, Iinv = (inv - R.Ph0inv) / R.om;
+    const double Ip = -I[3] / R.rp, Im = -I[4] / R.rm;
+    const double a2 = R.a * R.a;
+    P.u = ut;
+    P.mu = R.mp * cn;
+    P.dt = I[1] + 2.0 * I[2] + R.cp * Ip + R.cm * Im + a2 * Imu2;
+    P.dphi = R.dp * Ip + R.dm * Im - R.l * lam + R.l * Iinv;
+    P.lam = I[1] + a2 * Imu2;
+    const double K2 = 2.0 * R.Kth;
+    P.tpm = (int32_t)(std::floor(w / K2) - std::floor(R.w0 / K2));
+    P.tpr = branch2 ? 1 : 0;
+    return P;
+}
+
+}  // namespace gkcf
+}  // namespace np

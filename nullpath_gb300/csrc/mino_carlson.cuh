@@ -53,13 +53,25 @@ NP_CARLSON_HD int real_roots(const double* c, int n, double* r, double* rho = nu
     double R = 0.0;
     for (int k = 0; k < n; ++k) R = std::fmax(R, std::fabs(c[k] / c[n]));
     R = 1.0 + R;
+    // starting points on the circle of radius R at the angles 0.4 + 2 pi k / n,
+    // as literals (identical in host and device builds)
+    const double c4[4][2] = {{0.9210609940028851, 0.3894183423086505}, {-0.38941834230865036, 0.9210609940028851},
+                             {-0.9210609940028852, -0.3894183423086503}, {0.38941834230865063, -0.921060994002885}};
+    const double c3[3][2] = {{0.9210609940028851, 0.3894183423086505}, {-0.7977766741403581, 0.60295304808712},
+                             {-0.12328431986252686, -0.9923713903957702}};
     for (int k = 0; k < n; ++k) {
-        const double ang = 0.4 + 2.0 * 3.141592653589793 * k / n;
-        z[k] = Cx{R * std::cos(ang), R * std::sin(ang)};
+        const double* d = n == 4 ? c4[k] : (n == 3 ? c3[k] : c4[2 * k]);
+        z[k] = Cx{R * d[0], R * d[1]};
     }
+    // Converged when every correction is below 1e-15 relative, or when the
+    // largest has stalled below 1e-11 (roots of a close pair, real or
+    // complex, are only determined to the coefficients' rounding over their
+    // separation, and the corrections then stay at that noise level).
     bool conv = false;
+    double last = INFINITY;
     for (int it = 0; it < 200 && !conv; ++it) {
         conv = true;
+        double worst = 0.0;
         for (int k = 0; k < n; ++k) {
             Cx p{c[n], 0.0}, dp{0.0, 0.0};
             for (int j = n - 1; j >= 0; --j) {
@@ -73,9 +85,13 @@ NP_CARLSON_HD int real_roots(const double* c, int n, double* r, double* rho = nu
                 if (j != k) s = cadd(s, cdiv(Cx{1.0, 0.0}, csub(z[k], z[j])));
             const Cx step = cdiv(w, csub(Cx{1.0, 0.0}, cmul(w, s)));
             z[k] = csub(z[k], step);
-            if (std::fabs(step.re) + std::fabs(step.im) > 1e-15 * (1.0 + std::fabs(z[k].re) + std::fabs(z[k].im)))
-                conv = false;
+            const double rel = (std::fabs(step.re) + std::fabs(step.im)) /
+                               (1.0 + std::fabs(z[k].re) + std::fabs(z[k].im));
+            worst = std::fmax(worst, rel);
+            if (rel > 1e-15) conv = false;
         }
+        if (!conv && it >= 16 && worst < 1e-11 && worst > 0.25 * last) conv = true;
+        last = worst;
     }
     if (!conv) return -1;
     int m = 0;

@@ -18,6 +18,8 @@ _PROTOS = {
     "geokerr_complete_stream_cuda": (I, [D] * 8 + [I] + [V] * 5),
     "compute_geokerr_complete_cuda": (None, [V] * 12 + [I]),
     "np_geokerr_points_device": (I, [I, D] + [V] * 7 + [I, I, D] + [V] * 8 + [V]),
+    "np_geokerr_points_taylor_device": (I, [I, D] + [V] * 7 + [I, I, D] + [V] * 8 + [V]),
+    "np_geokerr_points_host": (I, [I, D] + [V] * 7 + [I, I, D] + [V] * 8 + [V]),
     "np_geokerr_eval_lambda_device": (I, [I, D] + [V] * 8 + [I] + [V] * 8 + [V, V]),
     "np_geokerr_eval_lambda_work_bytes": (C.c_size_t, [I, I]),
     "np_geokerr_equator_crossings_device": (I, [I, D] + [V] * 6 + [D, I] + [V] * 3 + [V]),
@@ -139,8 +141,11 @@ def _t(x):
     return C.c_void_p(x.data_ptr()) if x is not None else None
 
 
-def points(a, u0, uf, mu0, l, q2, su, sm, tpr=1, nup=32, offset=0.5):
-    """Batched GEOKERR sampler on CUDA tensors; returns a dict of [n, nup] tensors."""
+def points(a, u0, uf, mu0, l, q2, su, sm, tpr=1, nup=32, offset=0.5, method="closed_form"):
+    """Batched GEOKERR sampler on CUDA tensors; returns a dict of [n, nup]
+    tensors.  method "closed_form" evaluates every point on its own thread
+    (rays outside the closed forms on the Taylor solver); "taylor" integrates
+    every ray with the order-24 Taylor solver."""
     import torch
     lib = _lib()
     dev = torch.device("cuda")
@@ -151,9 +156,32 @@ def points(a, u0, uf, mu0, l, q2, su, sm, tpr=1, nup=32, offset=0.5):
     out["tpm"] = torch.zeros((n, nup), dtype=torch.int32, device=dev)
     out["tpr"] = torch.zeros((n, nup), dtype=torch.int32, device=dev)
     out["n"] = torch.zeros(n, dtype=torch.int32, device=dev)
-    check(lib.np_geokerr_points_device(n, a, *[_t(x) for x in ins], tpr, nup, offset,
-                                       *[_t(out[k]) for k in ("u", "mu", "dt", "dphi", "lam", "tpm", "tpr", "n")],
-                                       C.c_void_p(torch.cuda.current_stream().cuda_stream)))
+    if method not in ("closed_form", "taylor"):
+        raise ValueError("method must be 'closed_form' or 'taylor'")
+    fn = lib.np_geokerr_points_device if method == "closed_form" else lib.np_geokerr_points_taylor_device
+    check(fn(n, a, *[_t(x) for x in ins], tpr, nup, offset,
+             *[_t(out[k]) for k in ("u", "mu", "dt", "dphi", "lam", "tpm", "tpr", "n")],
+             C.c_void_p(torch.cuda.current_stream().cuda_stream)))
+    return out
+
+
+def points_host(a, u0, uf, mu0, l, q2, su, sm, tpr=1, nup=32, offset=0.5):
+    """The closed-form sampler run on the host (the device code's arithmetic,
+    the same bits); numpy in and out, plus method[n] (1: four real radial
+    roots, 2: two real roots and a complex pair, 0: Taylor solver or no
+    points)."""
+    lib = _lib()
+    cv = lambda x: np.ascontiguousarray(np.broadcast_to(np.asarray(x, dtype=np.float64), np.shape(l)))
+    ins = [cv(x) for x in (u0, uf, mu0, l, q2, su, sm)]
+    n = ins[0].size
+    out = {k: np.zeros((n, nup), dtype=np.float64) for k in ("u", "mu", "dt", "dphi", "lam")}
+    out["tpm"] = np.zeros((n, nup), dtype=np.int32)
+    out["tpr"] = np.zeros((n, nup), dtype=np.int32)
+    out["n"] = np.zeros(n, dtype=np.int32)
+    out["method"] = np.zeros(n, dtype=np.int32)
+    check(lib.np_geokerr_points_host(n, a, *[x.ctypes.data for x in ins], tpr, nup, offset,
+                                     *[out[k].ctypes.data for k in ("u", "mu", "dt", "dphi", "lam", "tpm", "tpr", "n",
+                                                                    "method")]))
     return out
 
 

@@ -16,8 +16,9 @@ Cases (kernel names in parentheses):
     adjoint         differentiable render 128x128x2, FP32, K = 64
                     (adj_forward_kernel<float>, adj_backward_kernel<float>)
     batch           16 uneven scenes in one persistent launch (batch_mixed_kernel)
-    geokerr         GEOKERR camera grid 128x128, 32 points per geodesic
-                    (geokerr_points_kernel)
+    geokerr         GEOKERR camera grid 128x128, 32 points per geodesic, closed
+                    form (cf_setup_kernel, cf_points_kernel, cf_fallback_kernel)
+    geokerr_taylor  the same grid on the Taylor solver (geokerr_points_kernel)
     carlson         2^20 Carlson R_F / R_D / R_J cases (carlson_batch_kernel)
 """
 import argparse
@@ -70,7 +71,7 @@ def _batch(reps):
     b.close()
 
 
-def _geokerr(reps):
+def _geokerr(reps, method="closed_form"):
     from nullpath_gb300 import geokerr as gk
     a, mu0, u0 = 0.9, 0.5, 1e-6
     uplus = 1.0 / (1.0 + math.sqrt(1.0 - a * a))
@@ -78,7 +79,7 @@ def _geokerr(reps):
     n = g["l"].size
     for _ in range(reps + 1):
         gk.points(a, np.full(n, u0), np.full(n, uplus), np.full(n, mu0), g["l"], g["q2"], g["su"], g["sm"],
-                  tpr=1, nup=32, offset=0.5)
+                  tpr=1, nup=32, offset=0.5, method=method)
 
 
 def _carlson(reps):
@@ -93,7 +94,8 @@ def _carlson(reps):
 
 CASES = {"fp64_rk4": _fp64_rk4, "fp64_research": _fp64_research,
          "mixed_rk4": lambda r: _mixed(r, "rk4"), "mixed_rkf78": lambda r: _mixed(r, "rkf78"),
-         "adjoint": _adjoint, "batch": _batch, "geokerr": _geokerr, "carlson": _carlson}
+         "adjoint": _adjoint, "batch": _batch, "geokerr": _geokerr,
+         "geokerr_taylor": lambda r: _geokerr(r, "taylor"), "carlson": _carlson}
 
 
 def main():

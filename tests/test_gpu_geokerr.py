@@ -70,18 +70,17 @@ def test_camera_grid_matches_oracle(cuda):
 
 def test_grid_points_full_grid_near_polar(cuda):
     """The 128 x 128 grid with 32 points per geodesic (a = 0.9, r_o = 1e6 M,
-    i = 60 deg): GPU solver against its CPU restatement on 300 rays, the 60
-    of smallest |l| included.  Those pass near a pole, where the sampled phi
-    has a condition number of ~3e4 in the potential's coefficients, so the
-    1e-12 bar needs the same rounding on both sides: the GPU build contracts
-    no multiply-add and follows the restatement's operation order, and the
-    results agree bit for bit."""
+    i = 60 deg).  Taylor solver: GPU against its CPU restatement on 300
+    rays, the 60 of smallest |l| included; those pass near a pole, where
+    phi has a condition number of ~3e4 in the potential's coefficients, so
+    the GPU build contracts no multiply-add and follows the restatement's
+    operation order, and the two agree bit for bit."""
     a, mu0, u0 = 0.9, 0.5, 1e-6
     uplus = 1.0 / (1.0 + np.sqrt(1.0 - a * a))
     g = {k: v.cpu().numpy() for k, v in gk.camera_grid(a, mu0, 128, 128).items()}
     n = g["l"].size
     out = gk.points(a, np.full(n, u0), np.full(n, uplus), np.full(n, mu0), g["l"], g["q2"], g["su"], g["sm"],
-                    tpr=1, nup=32, offset=0.5)
+                    tpr=1, nup=32, offset=0.5, method="taylor")
     got = {k: v.cpu().numpy() for k, v in out.items()}
     rng = np.random.default_rng(1)
     near_pole = np.argsort(np.abs(g["l"]))[:60]
@@ -89,6 +88,41 @@ def test_grid_points_full_grid_near_polar(cuda):
         ref = oracle.geokerr_points(u0, uplus, mu0, a, g["l"][i], g["q2"][i], 1.0, g["sm"][i], 1, 32, 0.5)
         for k in ("u", "mu", "dt", "dphi", "lam"):
             assert np.array_equal(got[k][i], ref[k]), (int(i), k, _rel(got[k][i], ref[k]))
+
+
+@pytest.mark.parametrize("a", [0.9, 0.5, 0.998])
+def test_closed_form_device_equals_host(cuda, a):
+    """The closed-form sampler (one thread per point) on the GPU and its
+    host build give the same bits on the whole 128 x 128 grid: only +, -,
+    *, / and sqrt enter, and neither side contracts a multiply-add."""
+    mu0, u0 = 0.5, 1e-6
+    uplus = 1.0 / (1.0 + np.sqrt(1.0 - a * a))
+    g = {k: v.cpu().numpy() for k, v in gk.camera_grid(a, mu0, 128, 128).items()}
+    n = g["l"].size
+    args = (a, np.full(n, u0), np.full(n, uplus), np.full(n, mu0), g["l"], g["q2"], g["su"], g["sm"])
+    dev = {k: v.cpu().numpy() for k, v in gk.points(*args, tpr=1, nup=32, offset=0.5).items()}
+    host = gk.points_host(*args, tpr=1, nup=32, offset=0.5)
+    assert (host["method"] > 0).mean() > 0.99
+    assert np.array_equal(dev["n"], host["n"]) and (dev["n"] == 32).all()
+    for k in ("u", "mu", "dt", "dphi", "lam", "tpm", "tpr"):
+        assert np.array_equal(dev[k], host[k]), (k, _rel(dev[k], host[k]))
+
+
+def test_closed_form_device_matches_truth(cuda):
+    """The GPU closed form against the 40-digit truth (near-polar, shadow
+    edge and random rays at four spins): 2e-12."""
+    t = np.load(os.path.join(HERE, "golden", "geokerr_cf_truth.npz"))
+    for a in np.unique(t["a"]):
+        sel = np.flatnonzero(t["a"] == a)
+        uplus = 1.0 / (1.0 + np.sqrt(1.0 - a * a))
+        n = sel.size
+        out = gk.points(float(a), np.full(n, 1e-6), np.full(n, uplus), np.full(n, 0.5), t["l"][sel], t["q2"][sel],
+                        t["su"][sel], t["sm"][sel], tpr=1, nup=32, offset=0.5)
+        got = {k: v.cpu().numpy() for k, v in out.items()}
+        for j, i in enumerate(sel):
+            for k, key in enumerate(("u", "mu", "dt", "dphi", "lam")):
+                assert _rel(got[key][j], t["pts"][i, k]) < 2e-12, (a, int(i), key)
+            assert np.array_equal(got["tpm"][j], t["tpm"][i])
 
 
 def test_eval_lambda_batch_matches_single(cuda):
