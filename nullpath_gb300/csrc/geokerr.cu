@@ -439,7 +439,7 @@ __global__ void cf_points_kernel(int n, int nup, const np::gkcf::CfRay* __restri
     const int i = (int)(t / nup), k = (int)(t % nup) + 1;
     if (i >= n) return;
     const np::gkcf::CfRay& R = rays[i];
-    if ((R.kind != np::gkcf::kR4 && R.kind != np::gkcf::kR2C) || k > R.last) return;
+    if (R.kind <= np::gkcf::kFallback || k > R.last) return;
     const np::gkcf::Point P = np::gkcf::sample(R, k);
     const long long o = (long long)i * nup + (k - 1);
     u[o] = P.u; mu[o] = P.mu; dt[o] = P.dt; dphi[o] = P.dphi; lam[o] = P.lam; tpm[o] = P.tpm; tprv[o] = P.tpr;
@@ -709,16 +709,36 @@ int points_cf_launch(int n, int mode, double a, const double* u0, const double* 
     cudaMemsetAsync(nfb, 0, sizeof(int32_t), st);
     cf_setup_kernel<<<grid(n, 128), 128, 0, st>>>(n, mode, a, u0, uf, mu0, l, q2, su, sm, tpr, nup, offset, rays, npts,
                                                   fb, nfb);
-    const long long total = (long long)n * nup;
-    cf_points_kernel<<<(unsigned)((total + 127) / 128), 128, 0, st>>>(n, nup, rays, u, mu, dt, dphi, lam, tpm, tprv);
+    // The Taylor rays (a few serial integrations) run on a side stream
+    // beside the per-point kernel; the caller's stream waits for both.
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_setup = nullptr, ev_fb = nullptr;
+    const bool overlap = cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking) == cudaSuccess &&
+                         cudaEventCreateWithFlags(&ev_setup, cudaEventDisableTiming) == cudaSuccess &&
+                         cudaEventCreateWithFlags(&ev_fb, cudaEventDisableTiming) == cudaSuccess;
+    cudaStream_t fb_stream = st;
+    if (overlap) {
+        cudaEventRecord(ev_setup, st);
+        cudaStreamWaitEvent(side, ev_setup, 0);
+        fb_stream = side;
+    }
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = 1;
     const int fb_blocks = std::min(grid(n, 32), 4 * sms);
-    cf_fallback_kernel<<<fb_blocks, 32, 0, st>>>(fb, nfb, mode, a, u0, uf, mu0, l, q2, su, sm, tpr, nup, offset, u, mu,
-                                                 dt, dphi, lam, tpm, tprv, npts);
+    cf_fallback_kernel<<<fb_blocks, 32, 0, fb_stream>>>(fb, nfb, mode, a, u0, uf, mu0, l, q2, su, sm, tpr, nup, offset,
+                                                        u, mu, dt, dphi, lam, tpm, tprv, npts);
+    const long long total = (long long)n * nup;
+    cf_points_kernel<<<(unsigned)((total + 127) / 128), 128, 0, st>>>(n, nup, rays, u, mu, dt, dphi, lam, tpm, tprv);
+    if (overlap) {
+        cudaEventRecord(ev_fb, side);
+        cudaStreamWaitEvent(st, ev_fb, 0);
+    }
     cudaError_t e = cudaGetLastError();
     cudaFreeAsync(w, st);
+    if (ev_setup) cudaEventDestroy(ev_setup);
+    if (ev_fb) cudaEventDestroy(ev_fb);
+    if (side) cudaStreamDestroy(side);
     return e == cudaSuccess ? NP_OK : gk_fail(NP_ERR_KERNEL, "%s", cudaGetErrorString(e));
 }
 

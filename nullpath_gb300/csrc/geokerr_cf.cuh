@@ -151,7 +151,9 @@ GKCF_HD void jacobi(double w, double m, double mc, double K, double& S2, double&
 
 // ---------------------------------------------------------------------------
 // Per-ray constants
-enum { kFallback = 0, kR4 = 1, kR2C = 2 };
+// kR2O: two real roots r1 < r2 below the motion and a complex pair (q2 < 0),
+// motion in u > r2; it shares the kR2C code with (u1, u2, A, B) -> (r2, r1, B, -A).
+enum { kFallback = 0, kR4 = 1, kR2C = 2, kR2O = 3 };
 
 struct CfRay {
     int32_t kind, tpr, kmax, last;
@@ -163,8 +165,10 @@ struct CfRay {
     double pn[3][2];        // R2C: n1, n2 per pole
     double rp, rm, cp, cm, dp, dm;
     // polar
-    double mpos, omp, mp, om, mth, mcth, Kth, nth, w0, mu2K, invK, Ph0mu2, Ph0inv;
-    double G0[5], Gtop[5];  // 1, 1/u^2, 1/u, 1/(u - 1/r+), 1/(u - 1/r-) integrals
+    // pkind 0: mu = mu+ cn (q2 > 0); 1: mu = s0 mu+ dn (q2 < 0, vortical)
+    int32_t pkind, pad;
+    double mpos, omp, mp, om, mth, mcth, Kth, nth, pq, s0, w0, mu2K, invK, Ph0mu2, Ph0inv;
+    double G0[7], Gtop[7];  // 1, 1/u^2, 1/u, 1/(u - 1/r+), 1/(u - 1/r-), u/(u - 1/r+), u/(u - 1/r-) integrals
 };
 
 // Radial Legendre amplitude of u (and, for R2C, D(S) = the Moebius denominator)
@@ -198,13 +202,12 @@ GKCF_HD void r2c_factors(const CfRay& R, int ip, const Amp& A, double u, double 
     else f2 = prod / f1;
 }
 
-// int dv / (1 - n S) = F + n J (Pi for n < -1)
-GKCF_HD double pole_term(const Amp& A, double n, double f) {
-    return n < -1.0 ? amp_pi(A, n, f) : A.F + n * amp_j(A, n, f);
-}
-
-// G(u): the five radial integrals against du/sqrt(U), increasing in u
+// G(u): the seven radial integrals against du/sqrt(U), increasing in u
 // (R4: minus the integral from u to u2; R2C: the integral from u1 to u).
+// u/(u - p) = 1 + p/(u - p) is integrated with the constant written as the
+// anchor's value (u2/(u2 - p), u3/(u3 - p), u1/(u1 - p)): the radial phi rate
+// d+ r+ u/(1 - r+ u) + d- r- u/(1 - r- u) is then free of the cancellation
+// between the O(l) terms of its partial fractions at small u.
 GKCF_HD void radial_G(const CfRay& R, double u, double* G) {
     double Dfac;
     const Amp A = radial_amp(R, u, Dfac);
@@ -215,10 +218,18 @@ GKCF_HD void radial_G(const CfRay& R, double u, double* G) {
             const double p = R.pole[ip], n = (u3 - p) * (u2 - u1) / ((u2 - p) * (u3 - u1));
             const double e = (u3 - u2) * (p - u1) / ((u2 - p) * (u3 - u1));      // n - 1
             const double f = (u - p) * (u3 - u2) / ((u2 - p) * (u3 - u));
-            double h;
-            if (n < -1.0) h = A.F / (u3 - p) + (u3 - u2) / ((u3 - p) * (u2 - p)) * amp_pi(A, n, f);
-            else h = A.F / (u2 - p) + (u3 - u2) * (u2 - u1) / ((u2 - p) * (u2 - p) * (u3 - u1)) * amp_j(A, n, f);
+            double h, x;
+            if (n < -1.0) {
+                const double Cp = (u3 - u2) / ((u3 - p) * (u2 - p)), T = amp_pi(A, n, f);
+                h = A.F / (u3 - p) + Cp * T;
+                x = u3 / (u3 - p) * A.F + p * Cp * T;
+            } else {
+                const double Kp = (u3 - u2) * (u2 - u1) / ((u2 - p) * (u2 - p) * (u3 - u1)), T = amp_j(A, n, f);
+                h = A.F / (u2 - p) + Kp * T;
+                x = u2 / (u2 - p) * A.F + p * Kp * T;
+            }
             G[2 + ip] = -g * h;
+            if (ip > 0) G[4 + ip] = -g * x;
             if (ip == 0) {
                 // (1/u2 + K0 S/(1 - n S))^2, with int S^2/(1 - n S)^2 = (Pi2 - 2 Pi + F)/n^2
                 const double K0 = (u3 - u2) * (u2 - u1) / (u2 * u2 * (u3 - u1));
@@ -235,8 +246,20 @@ GKCF_HD void radial_G(const CfRay& R, double u, double* G) {
         double f1, f2;
         r2c_factors(R, ip, A, u, Dfac, f1, f2);
         const double n1 = R.pn[ip][0], n2 = R.pn[ip][1];
-        const double t1 = pole_term(A, n1, f1), t2 = pole_term(A, n2, f2);
+        // int dv / (1 - n S) = F + n J, or Pi for n < -1
+        const bool pi1 = n1 < -1.0, pi2 = n2 < -1.0;
+        const double j1 = pi1 ? 0.0 : amp_j(A, n1, f1), j2 = pi2 ? 0.0 : amp_j(A, n2, f2);
+        const double t1 = pi1 ? amp_pi(A, n1, f1) : A.F + n1 * j1;
+        const double t2 = pi2 ? amp_pi(A, n2, f2) : A.F + n2 * j2;
         G[2 + ip] = g * (c[4] * A.F + c[2] * t1 + c[3] * t2);
+        if (ip > 0) {
+            // u/(u - p): constant u1/(u1 - p) less p al_j of the Pi-form terms
+            const double p = R.pole[ip];
+            double k0 = R.r[0] / (R.r[0] - p), x = 0.0;
+            if (pi1) { k0 -= p * c[2]; x += p * c[2] * t1; } else x += p * c[2] * n1 * j1;
+            if (pi2) { k0 -= p * c[3]; x += p * c[3] * t2; } else x += p * c[3] * n2 * j2;
+            G[4 + ip] = g * (k0 * A.F + x);
+        }
         if (ip == 0) {
             const double cross = 2.0 * c[2] * c[3] / (c[0] - c[1]);
             G[1] = g * (c[4] * c[4] * A.F + 2.0 * c[4] * (c[2] * t1 + c[3] * t2) + cross * (n1 * t1 - n2 * t2) +
@@ -255,23 +278,64 @@ GKCF_HD void polar_Phi(const CfRay& R, double w, double& mu2, double& inv, doubl
     jacobi(std::fabs(r), m, R.mcth, K, S2, C2, D2);
     const Amp A = amp_make(S2, C2, m, R.mcth);
     const double sg = r >= 0.0 ? 1.0 : -1.0;
-    mu2 = 2.0 * j * R.mu2K + sg * R.mpos * (A.F - A.Sd);
+    // mu^2 = mu+^2 cn^2 = mu+^2 (1 - S), or mu+^2 dn^2 = mu+^2 (1 - m S)
+    mu2 = 2.0 * j * R.mu2K + sg * R.mpos * (A.F - (R.pkind ? m : 1.0) * A.Sd);
     inv = 0.0;
-    if (R.l != 0.0) inv = 2.0 * j * R.invK + sg * amp_pi(A, R.nth, (R.omp + R.mpos * S2) / R.omp) / R.omp;
-    const double par = j - 2.0 * std::floor(0.5 * j);
-    cn = (par != 0.0 ? -1.0 : 1.0) * std::sqrt(C2);
+    // 1 - mu^2 = (1 - mu+^2)(1 - nth S), 1 - nth S = (1 - mu+^2 + pq S) / (1 - mu+^2)
+    if (R.l != 0.0) inv = 2.0 * j * R.invK + sg * amp_pi(A, R.nth, (R.omp + R.pq * S2) / R.omp) / R.omp;
+    if (R.pkind) {
+        cn = R.s0 * std::sqrt(D2);                 // mu / mu+ = s0 dn, even with period 2K
+    } else {
+        const double par = j - 2.0 * std::floor(0.5 * j);
+        cn = (par != 0.0 ? -1.0 : 1.0) * std::sqrt(C2);
+    }
     jj = j;
 }
 
+// Complex-pair poles: 1/(u - p) = D(S) / N_p(S) with the Moebius denominator
+// D(S) = (1 - S)(A + B S) + B mc S^2 and N_p(S) = a0 (1 - n1 S)(1 - n2 S);
+// e = n - 1 solves a0 e^2 + ((u1 - p) A + (u2 - p) B) e + (u2 - p) B mc = 0
+// (exact coefficients), and the residues are
+//   al_j = D(1/n_j) n_j / (a0 (n_j - n_k)) = (e_j (A n_j + B) + B mc) / (n_j a0 (e_j - e_k)).
+// Each root is taken from the form in which it has no cancellation: n from
+// a0 n^2 + a1 n + a2 = 0 where |n - 1| >= 1/2, else n = 1 + e.
+GKCF_HD void complex_poles(CfRay& R) {
+    const double u1 = R.r[0], u2 = R.r[1], A = R.r[2], Bq = R.r[3];
+    for (int ip = 0; ip < 3; ++ip) {
+        const double p = R.pole[ip];
+        const double a0 = (u1 - p) * A, b1 = (u1 - p) * A + (u2 - p) * Bq, c0 = (u2 - p) * Bq * R.mc;
+        const double a1 = (u2 - p) * Bq - (u1 - p) * A, a2 = -R.m * Bq * (u2 - p);
+        const double dn = std::sqrt(a1 * a1 - 4.0 * a0 * a2);
+        const double qn = -0.5 * (a1 + (a1 >= 0.0 ? dn : -dn));
+        double n1 = qn / a0, n2 = a2 / qn;
+        if (std::fabs(n2) > std::fabs(n1)) { const double t = n1; n1 = n2; n2 = t; }
+        const double de = std::sqrt(b1 * b1 - 4.0 * a0 * c0);
+        const double qe = -0.5 * (b1 + (b1 >= 0.0 ? de : -de));
+        const double ea = qe / a0, eb = c0 / qe;
+        double e1 = n1 - 1.0, e2 = n2 - 1.0;
+        const double ec1 = std::fabs(ea - e1) < std::fabs(eb - e1) ? ea : eb;
+        const double ec2 = std::fabs(ea - e2) < std::fabs(eb - e2) ? ea : eb;
+        if (std::fabs(ec1) < 0.5) { e1 = ec1; n1 = 1.0 + ec1; }
+        if (std::fabs(ec2) < 0.5) { e2 = ec2; n2 = 1.0 + ec2; }
+        double* pc = R.pc[ip];
+        pc[0] = e1; pc[1] = e2;
+        pc[2] = (e1 * (A * n1 + Bq) + Bq * R.mc) / (n1 * a0 * (e1 - e2));
+        pc[3] = (e2 * (A * n2 + Bq) + Bq * R.mc) / (n2 * a0 * (e2 - e1));
+        pc[4] = 1.0 / (u2 - p);
+        pc[5] = a0;
+        R.pn[ip][0] = n1; R.pn[ip][1] = n2;
+    }
+}
+
 // Per-ray setup; kind = kFallback when the ray is outside the closed forms
-// (q2 <= 0, a = 0, roots of U not in the two cases above, a start outside
-// [u1, u2], a polar orbit through the pole with l != 0).
+// (q2 = 0, a = 0, U without real roots or with a motion between middle
+// roots, a polar orbit through the pole with l != 0).
 GKCF_HD void setup(double a, double l, double q2, double u0, double uf, double mu0, double su, double sm, int tpr_in,
                    int nup, double offset, double mpos, double a2mneg, CfRay& R) {
     R.kind = kFallback;
     R.tpr = 0; R.kmax = 0; R.last = 0;
     R.a = a; R.l = l; R.u0 = u0; R.offset = offset; R.su = su;
-    if (!(q2 > 0.0) || a == 0.0 || !(a2mneg < 0.0) || nup <= 0) return;
+    if (q2 == 0.0 || a == 0.0 || a2mneg == 0.0 || !(mpos > 0.0) || nup <= 0) return;
     if (!(1.0 - mpos > 1e-15) && l != 0.0) return;
     const double B = a * a - l * l - q2, Kc = (l - a) * (l - a) + q2;
     const double c[5] = {1.0, 0.0, B, 2.0 * Kc, -a * a * q2};
@@ -282,18 +346,18 @@ GKCF_HD void setup(double a, double l, double q2, double u0, double uf, double m
     R.rm = a * a / R.rp;
     R.pole[0] = 0.0; R.pole[1] = 1.0 / R.rp; R.pole[2] = 1.0 / R.rm;
     const double uplus = 1.0 / R.rp;
-    double u1, u2;
-    if (nr == 4) {
-        u1 = rr[0]; u2 = rr[1];
-        const double u3 = rr[2], u4 = rr[3];
+    double uturn = INFINITY;      // radial turning point ahead of an ingoing ray
+    if (nr == 4 && c[4] < 0.0) {
+        const double u1 = rr[0], u2 = rr[1], u3 = rr[2], u4 = rr[3];
         if (!(u1 < u0 && u0 <= u2) || !(u2 < u3)) return;
         R.kind = kR4;
         for (int i = 0; i < 4; ++i) R.r[i] = rr[i];
         R.m = (u2 - u1) * (u4 - u3) / ((u3 - u1) * (u4 - u2));
         R.mc = (u3 - u2) * (u4 - u1) / ((u3 - u1) * (u4 - u2));
         R.g = 2.0 / std::sqrt(-c[4] * (u3 - u1) * (u4 - u2));
-    } else if (nr == 2 && sigma > 0.0) {
-        u1 = rr[0]; u2 = rr[1];
+        uturn = u2;
+    } else if (nr == 2 && sigma > 0.0 && c[4] < 0.0) {
+        const double u1 = rr[0], u2 = rr[1];
         if (!(u1 < u0 && u0 <= u2)) return;
         R.kind = kR2C;
         const double A = std::sqrt((u2 - rho) * (u2 - rho) + sigma * sigma);
@@ -310,37 +374,31 @@ GKCF_HD void setup(double a, double l, double q2, double u0, double uf, double m
         R.mc = gap * (A + Bq + (u2 - u1)) / (4.0 * A * Bq);
         R.m = R.mc < 0.5 ? 1.0 - R.mc : mdirect;
         R.g = 2.0 / std::sqrt(-c[4] * A * Bq);
-        // Poles: 1/(u - p) = D(S) / N_p(S) with the Moebius denominator
-        // D(S) = (1 - S)(A + B S) + B mc S^2 and N_p(S) = a0 (1 - n1 S)(1 - n2 S);
-        // e = n - 1 solves a0 e^2 + ((u1 - p) A + (u2 - p) B) e + (u2 - p) B mc = 0
-        // (exact coefficients), and the residues are
-        //   al_j = D(1/n_j) n_j / (a0 (n_j - n_k)) = (e_j (A n_j + B) + B mc) / (n_j a0 (e_j - e_k)).
-        // Each root is taken from the form in which it has no cancellation:
-        // n from a0 n^2 + a1 n + a2 = 0 where |n - 1| >= 1/2, else n = 1 + e.
-        for (int ip = 0; ip < 3; ++ip) {
-            const double p = R.pole[ip];
-            const double a0 = (u1 - p) * A, b1 = (u1 - p) * A + (u2 - p) * Bq, c0 = (u2 - p) * Bq * R.mc;
-            const double a1 = (u2 - p) * Bq - (u1 - p) * A, a2 = -R.m * Bq * (u2 - p);
-            const double dn = std::sqrt(a1 * a1 - 4.0 * a0 * a2);
-            const double qn = -0.5 * (a1 + (a1 >= 0.0 ? dn : -dn));
-            double n1 = qn / a0, n2 = a2 / qn;
-            if (std::fabs(n2) > std::fabs(n1)) { const double t = n1; n1 = n2; n2 = t; }
-            const double de = std::sqrt(b1 * b1 - 4.0 * a0 * c0);
-            const double qe = -0.5 * (b1 + (b1 >= 0.0 ? de : -de));
-            const double ea = qe / a0, eb = c0 / qe;
-            double e1 = n1 - 1.0, e2 = n2 - 1.0;
-            const double ec1 = std::fabs(ea - e1) < std::fabs(eb - e1) ? ea : eb;
-            const double ec2 = std::fabs(ea - e2) < std::fabs(eb - e2) ? ea : eb;
-            if (std::fabs(ec1) < 0.5) { e1 = ec1; n1 = 1.0 + ec1; }
-            if (std::fabs(ec2) < 0.5) { e2 = ec2; n2 = 1.0 + ec2; }
-            double* pc = R.pc[ip];
-            pc[0] = e1; pc[1] = e2;
-            pc[2] = (e1 * (A * n1 + Bq) + Bq * R.mc) / (n1 * a0 * (e1 - e2));
-            pc[3] = (e2 * (A * n2 + Bq) + Bq * R.mc) / (n2 * a0 * (e2 - e1));
-            pc[4] = 1.0 / (u2 - p);
-            pc[5] = a0;
-            R.pn[ip][0] = n1; R.pn[ip][1] = n2;
-        }
+        complex_poles(R);
+        uturn = u2;
+    } else if (nr == 2 && sigma > 0.0 && c[4] > 0.0) {
+        // Motion above both real roots (Byrd & Friedman 260.00):
+        // cn w = ((u - r1) A - (u - r2) B) / ((u - r1) A + (u - r2) B),
+        // int_{r2}^u du / sqrt(U) = w / sqrt(c4 A B), m = ((A + B)^2 - (r2 - r1)^2) / (4 A B);
+        // the same half-argument algebra as kR2C with (u1, u2, A, B) = (r2, r1, B, -A).
+        const double r1 = rr[0], r2 = rr[1];
+        if (!(r2 < u0)) return;
+        R.kind = kR2O;
+        const double A = std::sqrt((r2 - rho) * (r2 - rho) + sigma * sigma);
+        const double Bq = std::sqrt((r1 - rho) * (r1 - rho) + sigma * sigma);
+        R.r[0] = r2; R.r[1] = r1; R.r[2] = Bq; R.r[3] = -A;
+        // 1 - m = ((r2 - r1) - |A - B|)((r2 - r1) + |A - B|) / (4 A B); for rho
+        // outside [r1, r2], (r2 - r1) - |A - B| = sigma^2 (1/(A' + d') - 1/(B' + d''))
+        // with the nearer root first (no cancellation)
+        const double d2 = std::fabs(rho - r2), d1 = std::fabs(rho - r1), w = r2 - r1;
+        double gap;
+        if (rho >= r2) gap = sigma * sigma / (A + d2) - sigma * sigma / (Bq + d1);
+        else if (rho <= r1) gap = sigma * sigma / (Bq + d1) - sigma * sigma / (A + d2);
+        else gap = w - std::fabs(A - Bq);
+        R.mc = gap * (w + std::fabs(A - Bq)) / (4.0 * A * Bq);
+        R.m = R.mc < 0.5 ? 1.0 - R.mc : ((A + Bq) * (A + Bq) - w * w) / (4.0 * A * Bq);
+        R.g = 2.0 / std::sqrt(c[4] * A * Bq);
+        complex_poles(R);
     } else {
         return;
     }
@@ -353,7 +411,7 @@ GKCF_HD void setup(double a, double l, double q2, double u0, double uf, double m
     // turning point UB and back (geokerr_original.f:357-605)
     double ub;
     int tpr = 0;
-    if (su > 0.0 && u2 < uplus) { ub = u2; tpr = tpr_in; }
+    if (su > 0.0 && uturn < uplus) { ub = uturn; tpr = tpr_in; }
     else ub = su > 0.0 ? uplus : 0.0;
     double UF = uf;
     if (tpr == 1 && ((su > 0.0 && UF > ub) || (su < 0.0 && UF < ub))) UF = ub;
@@ -388,28 +446,56 @@ GKCF_HD void setup(double a, double l, double q2, double u0, double uf, double m
         R.omp = (m0 == mpos) ? 2.0 * l * l / (E + std::sqrt((E - 2.0 * a * l) * (E + 2.0 * a * l))) : 1.0 - mpos;
     }
     R.mp = std::sqrt(mpos);
-    const double w2 = a * a * mpos - a2mneg;
-    R.om = std::sqrt(w2);
-    R.mth = a * a * mpos / w2;
-    R.mcth = -a2mneg / w2;
-    R.Kth = cr::rf(0.0, R.mcth, 1.0);
-    R.nth = -mpos / R.omp;
-    double c0 = mu0 / R.mp;
-    c0 = c0 > 1.0 ? 1.0 : (c0 < -1.0 ? -1.0 : c0);
-    const Amp A0 = amp_make((1.0 - c0) * (1.0 + c0), c0 * c0, R.mth, R.mcth);
-    const double F0 = c0 >= 0.0 ? A0.F : 2.0 * R.Kth - A0.F;
-    R.w0 = -(sm < 0.0 ? -1.0 : 1.0) * F0;
+    double F0;
+    if (a2mneg < 0.0) {
+        // mu = mu+ cn(omega lambda + w0 | k), omega^2 = a^2 mu+^2 - a^2 mneg,
+        // k^2 = a^2 mu+^2 / omega^2
+        R.pkind = 0;
+        const double w2 = a * a * mpos - a2mneg;
+        R.om = std::sqrt(w2);
+        R.mth = a * a * mpos / w2;
+        R.mcth = -a2mneg / w2;
+        R.pq = mpos;
+        R.s0 = 1.0;
+        double c0 = mu0 / R.mp;
+        c0 = c0 > 1.0 ? 1.0 : (c0 < -1.0 ? -1.0 : c0);
+        R.Kth = cr::rf(0.0, R.mcth, 1.0);
+        const Amp A0 = amp_make((1.0 - c0) * (1.0 + c0), c0 * c0, R.mth, R.mcth);
+        F0 = c0 >= 0.0 ? A0.F : 2.0 * R.Kth - A0.F;
+        R.w0 = -(sm < 0.0 ? -1.0 : 1.0) * F0;
+    } else {
+        // vortical (q2 < 0): mu^2 between mneg and mu+^2 (Byrd & Friedman 218.00),
+        // mu = s0 mu+ dn(omega lambda + w0 | k), omega = a mu+,
+        // k^2 = (mu+^2 - mneg) / mu+^2; dn(w0) = |mu0| / mu+
+        R.pkind = 1;
+        const double a2mp = a * a * mpos, diff = a2mp - a2mneg;     // a^2 (mu+^2 - mneg)
+        if (!(diff > 0.0) || mu0 == 0.0) { R.kind = kFallback; return; }
+        R.om = std::sqrt(a2mp);
+        R.mth = diff / a2mp;
+        R.mcth = a2mneg / a2mp;
+        R.pq = diff / (a * a);
+        R.s0 = mu0 > 0.0 ? 1.0 : -1.0;
+        R.Kth = cr::rf(0.0, R.mcth, 1.0);
+        const double am0 = a * a * mu0 * mu0;
+        double S0 = (a2mp - am0) / diff, C0 = (am0 - a2mneg) / diff;
+        S0 = S0 < 0.0 ? 0.0 : (S0 > 1.0 ? 1.0 : S0);
+        C0 = C0 < 0.0 ? 0.0 : (C0 > 1.0 ? 1.0 : C0);
+        F0 = amp_make(S0, C0, R.mth, R.mcth).F;
+        // d mu / d lambda = -s0 mu+ k^2 sn cn omega: negative times s0 on (0, K)
+        R.w0 = (sm * R.s0 < 0.0) ? F0 : -F0;
+    }
+    R.nth = -R.pq / R.omp;
     const Amp Ac = amp_make(1.0, 0.0, R.mth, R.mcth);
-    R.mu2K = mpos * (R.Kth - Ac.Sd);
-    R.invK = l != 0.0 ? amp_pi(Ac, R.nth, 1.0 / R.omp) / R.omp : 0.0;
+    R.mu2K = mpos * (R.Kth - (R.pkind ? R.mth : 1.0) * Ac.Sd);
+    R.invK = l != 0.0 ? amp_pi(Ac, R.nth, 1.0 - R.nth) / R.omp : 0.0;
     double cn0, j0;
     polar_Phi(R, R.w0, R.Ph0mu2, R.Ph0inv, cn0, j0);
     // radial integrals at the start and at the turning point
     radial_G(R, u0, R.G0);
-    if (tpr == 1 && R.kind == kR2C) radial_G(R, u2, R.Gtop);
-    else for (int i = 0; i < 5; ++i) R.Gtop[i] = 0.0;
+    if (tpr == 1 && R.kind == kR2C) radial_G(R, uturn, R.Gtop);
+    else for (int i = 0; i < 7; ++i) R.Gtop[i] = 0.0;
     bool ok = true;
-    for (int i = 0; i < 5; ++i) ok = ok && std::isfinite(R.G0[i]) && std::isfinite(R.Gtop[i]);
+    for (int i = 0; i < 7; ++i) ok = ok && std::isfinite(R.G0[i]) && std::isfinite(R.Gtop[i]);
     ok = ok && std::isfinite(R.Ph0mu2) && std::isfinite(R.Ph0inv) && std::isfinite(R.om) && R.om > 0.0;
     if (!ok) R.kind = kFallback;
 }
@@ -424,9 +510,9 @@ GKCF_HD Point sample(const CfRay& R, int k) {
     Point P;
     const bool branch2 = k > R.kmax;
     const double ut = branch2 ? 2.0 * R.ub - (R.u0 + (k - R.offset) * R.du) : R.u0 + (k - R.offset) * R.du;
-    double Gk[5], I[5];
+    double Gk[7], I[7];
     radial_G(R, ut, Gk);
-    for (int i = 0; i < 5; ++i) {
+    for (int i = 0; i < 7; ++i) {
         if (R.su > 0.0) I[i] = branch2 ? 2.0 * R.Gtop[i] - R.G0[i] - Gk[i] : Gk[i] - R.G0[i];
         else I[i] = R.G0[i] - Gk[i];
     }
@@ -440,10 +526,13 @@ GKCF_HD Point sample(const CfRay& R, int k) {
     P.u = ut;
     P.mu = R.mp * cn;
     P.dt = I[1] + 2.0 * I[2] + R.cp * Ip + R.cm * Im + a2 * Imu2;
-    P.dphi = R.dp * Ip + R.dm * Im - R.l * lam + R.l * Iinv;
+    // d+ + d- = l: phi' = d+ (1/(1 - r+ u) - 1) + d- (1/(1 - r- u) - 1) + l/(1 - mu^2),
+    // with 1/(1 - r u) - 1 = -u/(u - 1/r)
+    P.dphi = -R.dp * I[5] - R.dm * I[6] + R.l * Iinv;
     P.lam = I[1] + a2 * Imu2;
-    const double K2 = 2.0 * R.Kth;
-    P.tpm = (int32_t)(std::floor(w / K2) - std::floor(R.w0 / K2));
+    // turning points of mu: cn = +-1 at multiples of 2K; dn at multiples of K
+    const double Kt = R.pkind ? R.Kth : 2.0 * R.Kth;
+    P.tpm = (int32_t)(std::floor(w / Kt) - std::floor(R.w0 / Kt));
     P.tpr = branch2 ? 1 : 0;
     return P;
 }

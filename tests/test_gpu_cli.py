@@ -84,6 +84,9 @@ def test_cli_frames_and_pattern(cuda, tmp_path):
     phis = json.load(open(side))["frame_phi_deg"]
     want = [20.0 + 360.0 * 0.5 * float(np.float32(i) / np.float32(3)) for i in range(3)]
     assert np.allclose(phis, want, rtol=0, atol=1e-9), phis
+    bad = subprocess.run([CLI, "--w", "8", "--h", "8", "--frames", "2", "--outpat", str(tmp_path / "x_%d_%d.ppm")],
+                         capture_output=True, text=True, timeout=120)
+    assert bad.returncode == 1 and "Invalid --outpat" in bad.stderr
 
 
 def test_camera_azimuth_rotates_crossings(cuda):
@@ -100,9 +103,6 @@ def test_camera_azimuth_rotates_crossings(cuda):
     assert hit.sum() > 100
     d = np.angle(np.exp(1j * (cb[..., 1][hit] - ca[..., 1][hit] - np.radians(37.0))))
     assert np.abs(d).max() < 1e-9
-    bad = subprocess.run([CLI, "--w", "8", "--h", "8", "--frames", "2", "--outpat", str(tmp_path / "x_%d_%d.ppm")],
-                         capture_output=True, text=True, timeout=120)
-    assert bad.returncode == 1 and "Invalid --outpat" in bad.stderr
 
 
 def test_resume_is_bit_identical(cuda, tmp_path):
