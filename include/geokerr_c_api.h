@@ -125,8 +125,7 @@ int np_geokerr_final_state_host(int n, const double* a, const double* u0, const 
  * be sampled).  Every point is evaluated in closed form by its own thread
  * (the semi-analytic GEOR / GEOMU / GEOPHITIME route,
  * geokerr_original.f:771-1187, 1648-2360); rays outside the closed forms
- * (q2 = 0, a = 0, a radial potential without real roots, a double radial
- * root) are integrated by the order-24
+ * (q2 = 0, a = 0, a double radial root) are integrated by the order-24
  * Taylor solver.  n * nup < 2^31.  Device pointers; the per-ray workspace
  * comes from the stream-ordered allocator.  Returns np_status. */
 int np_geokerr_points_device(int n, double a, const double* u0, const double* uf, const double* mu0,
@@ -145,7 +144,8 @@ int np_geokerr_points_taylor_device(int n, double a, const double* u0, const dou
 /* np_geokerr_points_device on the host (same arithmetic, same bits);
  * method[i] (optional) = 1 four real radial roots, 2 two real roots and a
  * complex pair around the motion, 3 two real roots below it and a complex
- * pair (q2 < 0), 0 Taylor solver or no points. */
+ * pair (q2 < 0), 4 two complex pairs (q2 < 0), 0 Taylor solver or no
+ * points. */
 int np_geokerr_points_host(int n, double a, const double* u0, const double* uf, const double* mu0,
                            const double* l, const double* q2, const double* su, const double* sm,
                            int tpr, int nup, double offset,

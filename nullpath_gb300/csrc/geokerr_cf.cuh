@@ -42,9 +42,14 @@
 //           (DLMF 19.7.8)
 //   Pi2(n) = int 1/((1 - n sin^2)^2 Delta), by differentiating
 //           s c d / (1 - n S) and eliminating Pi in favour of J (no 1/n terms).
-// Polar (q2 > 0, a != 0): mu = mu+ cn(omega lambda - s_mu F0 | k) as in
-// mino_carlson.cuh; the integrals over whole half periods are complete
-// values, so each sample needs the amplitude of one reduced argument.
+// Radial, q2 < 0: two real roots below the motion and a complex pair (Byrd &
+// Friedman 260.00, the same half-argument algebra), or two complex pairs (a
+// rotated form of B&F 267.00: u = rho1 + sigma1 tan(theta' + theta0), whose
+// pole terms add odd parts integrated in closed form with R_C).
+// Polar: mu = mu+ cn(omega lambda - s_mu F0 | k) for q2 > 0, and
+// mu = s0 mu+ dn(omega lambda + w0 | k) for q2 < 0 (B&F 213.00, 218.00); the
+// integrals over whole half periods are complete values, so each sample
+// needs the amplitude of one reduced argument.
 //
 // Only +, -, *, / and sqrt enter (the Jacobi functions come from a Newton
 // solve of F(s) = w, not from trigonometric functions), so with contraction
@@ -153,16 +158,19 @@ GKCF_HD void jacobi(double w, double m, double mc, double K, double& S2, double&
 // Per-ray constants
 // kR2O: two real roots r1 < r2 below the motion and a complex pair (q2 < 0),
 // motion in u > r2; it shares the kR2C code with (u1, u2, A, B) -> (r2, r1, B, -A).
-enum { kFallback = 0, kR4 = 1, kR2C = 2, kR2O = 3 };
+// kC4: two complex pairs (q2 < 0), every u allowed.
+enum { kFallback = 0, kR4 = 1, kR2C = 2, kR2O = 3, kC4 = 4 };
 
 struct CfRay {
     int32_t kind, tpr, kmax, last;
     double a, l, u0, ub, du, offset, su;
-    double r[4];            // R4: u1..u4; R2C: u1, u2, A, B
+    double r[4];            // R4: u1..u4; R2C: u1, u2, A, B; C4: rho1, sigma1, cos th0, sin th0
     double m, mc, g;        // radial parameter, 1 - m; scale (R4: g, R2C: 2 / sqrt(|c4| A B))
     double pole[3];         // 0, 1/r+, 1/r- (R4: n_p)
-    double pc[3][6];        // R2C: e1, e2 (e_j = n_j - 1), al1, al2, cinf, a0 per pole
-    double pn[3][2];        // R2C: n1, n2 per pole
+    double pc[3][6];        // R2C: e1, e2 (e_j = n_j - 1), al1, al2, cinf, a0 per pole;
+                            // C4: Dc, Ds, a, e-coefficient, kappa, u/(u - p) constant
+    double pn[3][2];        // R2C: n1, n2; C4: n, n - 1 per pole
+    double comp[6];         // C4: complete F, J(n_p) x 3, Pi(n_0), Pi2(n_0)
     double rp, rm, cp, cm, dp, dm;
     // polar
     // pkind 0: mu = mu+ cn (q2 > 0); 1: mu = s0 mu+ dn (q2 < 0, vortical)
@@ -171,9 +179,65 @@ struct CfRay {
     double G0[7], Gtop[7];  // 1, 1/u^2, 1/u, 1/(u - 1/r+), 1/(u - 1/r-), u/(u - 1/r+), u/(u - 1/r-) integrals
 };
 
+// atanh(z) = z R_C(1, 1 - z^2), |z| < 1, with 1 - z^2 supplied exactly
+GKCF_HD double atanh_rc(double z, double one_minus_z2) { return z * cr::rc(1.0, one_minus_z2); }
+
+// W(S) = 1/2 int_0^S ds / ((1 - n s) sqrt(1 - m s)), n >= 1 > m, q = 1 - n S
+// exact (principal value past s = 1/n).  With y = sqrt(1 - m s) and
+// c = (n - m)/n it is (1/(2 n sqrt c)) [2 ln((y_S + sqrt c)/(1 + sqrt c)) - ln|q|];
+// both logarithms as atanh through R_C (no log call, no cancellation as m -> 0).
+GKCF_HD double w_odd(double S, double n, double m, double q) {
+    if (S == 0.0) return 0.0;
+    const double sc = std::sqrt((n - m) / n);
+    const double y = std::sqrt(1.0 - m * S);
+    const double x = m * S / ((1.0 + y) * (1.0 + sc));       // 1 - (y + sc)/(1 + sc)
+    const double t1 = -4.0 * atanh_rc(x / (2.0 - x), 4.0 * (1.0 - x) / ((2.0 - x) * (2.0 - x)));
+    const double aq = std::fabs(q);
+    const double t2 = -2.0 * atanh_rc((aq - 1.0) / (aq + 1.0), 4.0 * aq / ((aq + 1.0) * (aq + 1.0)));
+    return (t1 + t2) / (2.0 * n * sc);
+}
+
+// W2(S) = 1/2 int_0^S ds / ((1 - n s)^2 sqrt(1 - m s)), from
+// d/ds [y / (1 - n s)] = (m/2) / ((1 - n s) y) + (n - m) / ((1 - n s)^2 y).
+GKCF_HD double w2_odd(double S, double n, double m, double q, double w) {
+    const double y = std::sqrt(1.0 - m * S);
+    const double top = (n * S - m * S / (1.0 + y)) / q;      // y/(1 - n S) - 1
+    return (top - m * w) / (2.0 * (n - m));
+}
+
+// An odd, quasi-periodic Legendre integral at amplitude theta' in (-pi, pi)
+// from its value on [0, pi/2] and its complete value.
+GKCF_HD double quadrant(double base, double complete, double cp, double sp) {
+    const double b = cp >= 0.0 ? base : 2.0 * complete - base;
+    return sp >= 0.0 ? b : -b;
+}
+
+// C4 (two complex pairs, Byrd & Friedman 267.00 in rotated form): with
+// u = rho1 + sigma1 tan(theta), U du^2 = c4 (alpha cos^2 + 2 beta sin cos +
+// gamma sin^2) dtheta^2 / cos^4 ..., and the rotation theta = theta' + theta0
+// onto the eigenvectors of [[alpha, beta], [beta, gamma]] (alpha = (rho1 -
+// rho2)^2 + sigma2^2, beta = (rho1 - rho2) sigma1, gamma = sigma1^2), so
+// that int du / sqrt(U) = F(theta' | m) / sqrt(c4 l1), m = 1 - l2/l1.  A
+// pole term is 1/(u - p) = a + e S/(1 - n S) + kappa sin cos/(1 - n S) with
+// n = 1 + Ds^2/Dc^2: an even part (F, J) and an odd part (W).
+GKCF_HD void c4_angle(const CfRay& R, double u, double& ct, double& cp, double& sp) {
+    const double t = u - R.r[0];
+    const double h = std::sqrt(t * t + R.r[1] * R.r[1]);
+    ct = R.r[1] / h;
+    const double st = t / h;
+    cp = ct * R.r[2] + st * R.r[3];
+    sp = st * R.r[2] - ct * R.r[3];
+}
+
 // Radial Legendre amplitude of u (and, for R2C, D(S) = the Moebius denominator)
 GKCF_HD Amp radial_amp(const CfRay& R, double u, double& Dfac) {
     const double m = R.m, mc = R.mc;
+    if (R.kind == kC4) {
+        double ct, cp, sp;
+        c4_angle(R, u, ct, cp, sp);
+        Dfac = 0.0;
+        return amp_make(sp * sp, cp * cp, m, mc);
+    }
     if (R.kind == kR4) {
         const double u1 = R.r[0], u2 = R.r[1], u3 = R.r[2];
         const double den = (u2 - u1) * (u3 - u);
@@ -211,6 +275,36 @@ GKCF_HD void r2c_factors(const CfRay& R, int ip, const Amp& A, double u, double 
 GKCF_HD void radial_G(const CfRay& R, double u, double* G) {
     double Dfac;
     const Amp A = radial_amp(R, u, Dfac);
+    if (R.kind == kC4) {
+        double ct, cp, sp;
+        c4_angle(R, u, ct, cp, sp);
+        const double g = R.g, m = R.m, S = A.S;
+        const double F = quadrant(A.F, R.comp[0], cp, sp);
+        G[0] = g * F;
+        for (int ip = 0; ip < 3; ++ip) {
+            const double* c = R.pc[ip];
+            const double p = R.pole[ip], Dc = c[0], Ds = c[1], n = R.pn[ip][0];
+            // 1 - n S = (u - p) cos(theta) (Dc cos theta' - Ds sin theta') / Dc^2
+            const double q = (u - p) * ct * (Dc * cp - Ds * sp) / (Dc * Dc);
+            const double J = quadrant(amp_j(A, n, q), R.comp[1 + ip], cp, sp);
+            const double w = w_odd(S, n, m, q);
+            G[2 + ip] = g * (c[2] * F + c[3] * J + c[4] * w);
+            if (ip > 0) G[4 + ip] = g * (c[5] * F + p * (c[3] * J + c[4] * w));
+            if (ip == 0) {
+                // (a + e S/(1 - nS) + kappa sc/(1 - nS))^2: even part with
+                // int S/(1 - nS)^2 = (Pi2 - Pi)/n, int S^2/(1 - nS)^2 = (Pi2 - 2 Pi + F)/n^2,
+                // odd part 2 kappa (a W + e (W2 - W)/n)
+                const double Pi = quadrant(amp_pi(A, n, q), R.comp[4], cp, sp);
+                const double P2 = quadrant(amp_pi2(A, n, R.pn[0][1], q), R.comp[5], cp, sp);
+                const double Q1 = (P2 - Pi) / n, Q2 = (P2 - 2.0 * Pi + F) / (n * n);
+                const double w2 = w2_odd(S, n, m, q, w);
+                const double a0 = c[2], e0 = c[3], k0 = c[4];
+                G[1] = g * (a0 * a0 * F + 2.0 * a0 * e0 * J + e0 * e0 * Q2 + k0 * k0 * (Q1 - Q2) +
+                            2.0 * k0 * (a0 * w + e0 * (w2 - w) / n));
+            }
+        }
+        return;
+    }
     if (R.kind == kR4) {
         const double u1 = R.r[0], u2 = R.r[1], u3 = R.r[2], g = R.g;
         G[0] = -g * A.F;
@@ -328,8 +422,8 @@ GKCF_HD void complex_poles(CfRay& R) {
 }
 
 // Per-ray setup; kind = kFallback when the ray is outside the closed forms
-// (q2 = 0, a = 0, U without real roots or with a motion between middle
-// roots, a polar orbit through the pole with l != 0).
+// (q2 = 0, a = 0, a motion between the middle roots of four real ones, a
+// double root, a polar orbit through the pole with l != 0).
 GKCF_HD void setup(double a, double l, double q2, double u0, double uf, double mu0, double su, double sm, int tpr_in,
                    int nup, double offset, double mpos, double a2mneg, CfRay& R) {
     R.kind = kFallback;
@@ -399,6 +493,53 @@ GKCF_HD void setup(double a, double l, double q2, double u0, double uf, double m
         R.m = R.mc < 0.5 ? 1.0 - R.mc : ((A + Bq) * (A + Bq) - w * w) / (4.0 * A * Bq);
         R.g = 2.0 / std::sqrt(c[4] * A * Bq);
         complex_poles(R);
+    } else if (nr == 0 && c[4] > 0.0) {
+        ::np::mino::Cx z[4];
+        double r0[4], rh, sg;
+        if (::np::mino::real_roots(c, 4, r0, &rh, &sg, z) != 0) return;
+        // the two roots in the upper half plane; the wider pair is the tan centre
+        int i1 = -1, i2 = -1;
+        for (int k = 0; k < 4; ++k)
+            if (z[k].im > 0.0) { if (i1 < 0) i1 = k; else i2 = k; }
+        if (i1 < 0 || i2 < 0) return;
+        if (z[i2].im > z[i1].im) { const int t = i1; i1 = i2; i2 = t; }
+        const double rho1 = z[i1].re, s1 = z[i1].im, rho2 = z[i2].re, s2 = z[i2].im;
+        const double d = rho1 - rho2;
+        const double al = d * d + s2 * s2, be = d * s1, ga = s1 * s1, hd = 0.5 * (al - ga);
+        const double l1 = 0.5 * (al + ga) + std::sqrt(hd * hd + be * be);
+        const double l2 = s1 * s1 * s2 * s2 / l1;                 // det / l1
+        // unit eigenvector of l1, from the better-conditioned of two forms
+        double vx = be, vy = l1 - al;
+        const double wx = l1 - ga, wy = be;
+        if (wx * wx + wy * wy > vx * vx + vy * vy) { vx = wx; vy = wy; }
+        const double nv = std::sqrt(vx * vx + vy * vy);
+        double c0 = vx / nv, s0 = vy / nv;
+        if (c0 < 0.0) { c0 = -c0; s0 = -s0; }
+        R.kind = kC4;
+        R.r[0] = rho1; R.r[1] = s1; R.r[2] = c0; R.r[3] = s0;
+        R.m = (l1 - l2) / l1;
+        R.mc = l2 / l1;
+        R.g = 1.0 / std::sqrt(c[4] * l1);
+        const Amp AK = amp_make(1.0, 0.0, R.m, R.mc);
+        R.comp[0] = AK.F;
+        for (int ip = 0; ip < 3; ++ip) {
+            const double p = R.pole[ip], t1 = rho1 - p;
+            const double Dc = t1 * c0 + s1 * s0, Ds = s1 * c0 - t1 * s0;
+            const double e = Ds * Ds / (Dc * Dc), n = 1.0 + e;
+            if (!(std::fabs(Dc) > 0.0) || !(e > 1e-12)) { R.kind = kFallback; return; }
+            double* pc = R.pc[ip];
+            pc[0] = Dc; pc[1] = Ds;
+            pc[2] = c0 / Dc;
+            pc[3] = Ds * (c0 * Ds + s0 * Dc) / (Dc * Dc * Dc);
+            pc[4] = -(c0 * Ds + s0 * Dc) / (Dc * Dc);
+            pc[5] = (rho1 * c0 + s1 * s0) / Dc;                    // 1 + p a
+            R.pn[ip][0] = n; R.pn[ip][1] = e;
+            R.comp[1 + ip] = amp_j(AK, n, -e);                     // 1 - n = -e
+            if (ip == 0) {
+                R.comp[4] = amp_pi(AK, n, -e);
+                R.comp[5] = amp_pi2(AK, n, e, -e);
+            }
+        }
     } else {
         return;
     }

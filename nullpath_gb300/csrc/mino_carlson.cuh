@@ -47,8 +47,10 @@ NP_CARLSON_HD Cx cdiv(Cx a, Cx b) {
 // Roots of sum_{k<=n} c[k] x^k (c[n] != 0, n <= 4) by Aberth-Ehrlich.
 // Returns the number of roots found real (stored sorted in r) or -1 when the
 // iteration did not converge; a complex pair is returned in (rho, sigma)
-// (rho +- i sigma, sigma > 0) when there is one.
-NP_CARLSON_HD int real_roots(const double* c, int n, double* r, double* rho = nullptr, double* sigma = nullptr) {
+// (rho +- i sigma, sigma > 0) when there is one; `all` (optional) receives
+// every root as found.
+NP_CARLSON_HD int real_roots(const double* c, int n, double* r, double* rho = nullptr, double* sigma = nullptr,
+                             Cx* all = nullptr) {
     Cx z[4];
     double R = 0.0;
     for (int k = 0; k < n; ++k) R = std::fmax(R, std::fabs(c[k] / c[n]));
@@ -94,6 +96,8 @@ NP_CARLSON_HD int real_roots(const double* c, int n, double* r, double* rho = nu
         last = worst;
     }
     if (!conv) return -1;
+    if (all)
+        for (int k = 0; k < n; ++k) all[k] = z[k];
     int m = 0;
     for (int k = 0; k < n; ++k) {
         if (std::fabs(z[k].im) > 1e-7 * (1.0 + std::fabs(z[k].re))) {

@@ -169,7 +169,8 @@ def points_host(a, u0, uf, mu0, l, q2, su, sm, tpr=1, nup=32, offset=0.5):
     """The closed-form sampler run on the host (the device code's arithmetic,
     the same bits); numpy in and out, plus method[n] (1: four real radial
     roots, 2: two real roots and a complex pair around the motion, 3: two
-    real roots below it and a complex pair, 0: Taylor solver or no points)."""
+    real roots below it and a complex pair, 4: two complex pairs, 0: Taylor
+    solver or no points)."""
     lib = _lib()
     cv = lambda x: np.ascontiguousarray(np.broadcast_to(np.asarray(x, dtype=np.float64), np.shape(l)))
     ins = [cv(x) for x in (u0, uf, mu0, l, q2, su, sm)]

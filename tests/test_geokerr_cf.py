@@ -95,52 +95,46 @@ def test_grid_closed_form_vs_taylor(a):
             assert _rel(h[key][i, :k], ref[key][:k]) < 3e-11, (i, key)
 
 
-def test_vortical_rays_closed_form():
-    """q2 < 0 (vortical) rays of the 128 x 128 grid whose radial potential
-    has two real roots below the motion run in closed form (mu = s0 mu+ dn,
-    Byrd & Friedman 218.00 and 260.00) and agree with the Taylor restatement
-    to 1e-13, turning counts included."""
+@pytest.mark.parametrize("method", [3, 4])
+def test_vortical_rays_closed_form(method):
+    """q2 < 0 (vortical) rays of the 128 x 128 grid run in closed form
+    (mu = s0 mu+ dn, Byrd & Friedman 218.00): with two real roots below the
+    motion (method 3, B&F 260.00) or none (method 4, two complex pairs, the
+    rotated form of B&F 267.00).  They agree with the Taylor restatement to
+    3e-14, turning counts included."""
     a, mu0, u0 = 0.9, 0.5, 1e-6
     uplus = 1.0 / (1.0 + math.sqrt(1.0 - a * a))
     g = oracle.geokerr_camera_grid(a, mu0, 128, 128)
     sel = np.flatnonzero(g["q2"] < 0)
     h = gk.points_host(a, u0, uplus, mu0, g["l"][sel], g["q2"][sel], g["su"][sel], g["sm"][sel], 1, 32, 0.5)
-    assert (h["method"] == 3).sum() >= 20
+    assert (h["method"] > 0).all()
+    assert (h["method"] == method).sum() >= 8
     for j, i in enumerate(sel):
-        if h["method"][j] != 3:
+        if h["method"][j] != method:
             continue
         ref = oracle.geokerr_points(u0, uplus, mu0, a, g["l"][i], g["q2"][i], g["su"][i], g["sm"][i], 1, 32, 0.5)
         k = ref["n"]
         assert h["n"][j] == k == 32
         assert np.array_equal(h["tpm"][j], ref["tpm"]) and np.array_equal(h["tpr"][j], ref["tpr"])
         for key in KEYS:
-            assert _rel(h[key][j], ref[key]) < 1e-13, (int(i), key)
+            assert _rel(h[key][j], ref[key]) < 3e-14, (int(i), key)
 
 
 def test_taylor_fallback_is_the_restatement():
-    """Rays outside the closed forms (q2 < 0 with a radial potential without
-    real roots, q2 = 0 equatorial orbits) run the Taylor solver, bit for bit
-    the restatement's."""
-    a, mu0, u0 = 0.9, 0.5, 1e-6
-    uplus = 1.0 / (1.0 + math.sqrt(1.0 - a * a))
-    g = oracle.geokerr_camera_grid(a, mu0, 128, 128)
-    neg = np.flatnonzero(g["q2"] < 0)
-    hn = gk.points_host(a, u0, uplus, mu0, g["l"][neg], g["q2"][neg], g["su"][neg], g["sm"][neg], 1, 32, 0.5)
-    sel = neg[hn["method"] == 0]
-    assert sel.size >= 2
-    l = np.concatenate([g["l"][sel], [2.5, -3.0]])
-    q2 = np.concatenate([g["q2"][sel], [0.0, 0.0]])
-    su = np.concatenate([g["su"][sel], [1.0, 1.0]])
-    sm = np.concatenate([g["sm"][sel], [1.0, -1.0]])
-    mu0v = np.concatenate([np.full(sel.size, mu0), [0.0, 0.0]])
-    h = gk.points_host(a, u0, uplus, mu0v, l, q2, su, sm, 1, 32, 0.5)
-    assert (h["method"] == 0).all()
-    for i in range(l.size):
-        ref = oracle.geokerr_points(u0, uplus, mu0v[i], a, l[i], q2[i], su[i], sm[i], 1, 32, 0.5)
+    """Rays outside the closed forms (q2 = 0 equatorial orbits, a = 0) run
+    the Taylor solver, bit for bit the restatement's."""
+    u0 = 1e-6
+    for a, l, q2, mu0, sm in ((0.9, 2.5, 0.0, 0.0, 1.0), (0.9, -3.0, 0.0, 0.0, -1.0),
+                              (0.0, 4.0, 10.0, 0.3, 1.0), (0.0, -2.0, 25.0, -0.2, -1.0)):
+        uplus = 1.0 / (1.0 + math.sqrt(1.0 - a * a))
+        h = gk.points_host(a, u0, uplus, mu0, np.array([l]), np.array([q2]), np.array([1.0]), np.array([sm]),
+                           1, 32, 0.5)
+        assert h["method"][0] == 0
+        ref = oracle.geokerr_points(u0, uplus, mu0, a, l, q2, 1.0, sm, 1, 32, 0.5)
         k = ref["n"]
-        assert h["n"][i] == k
+        assert h["n"][0] == k and k > 0
         for key in KEYS:
-            assert np.array_equal(h[key][i, :k], ref[key][:k]), (i, key)
+            assert np.array_equal(h[key][0, :k], ref[key][:k]), (a, l, key)
 
 
 def test_outgoing_rays_and_sampling_options():
