@@ -139,9 +139,9 @@ def geokerr_grid_leg(n_side=128, nup=32, cpu_sample=1024, reps=5):
         parts = list(ex.map(host_chunk, chunks))
     cpu_s = time.perf_counter() - t0
     worst_cpu = 0.0
-    methods = np.zeros(3, int)
+    methods = np.zeros(5, int)
     for idx, h in parts:
-        methods += np.bincount(h["method"], minlength=3)
+        methods += np.bincount(h["method"], minlength=5)
         for k in ("u", "mu", "dt", "dphi", "lam"):
             d = np.abs(got[k][idx] - h[k]).max(axis=1) / np.maximum(np.abs(h[k]).max(axis=1), 1e-300)
             worst_cpu = max(worst_cpu, float(d.max()))
@@ -165,7 +165,9 @@ def geokerr_grid_leg(n_side=128, nup=32, cpu_sample=1024, reps=5):
     return {"geodesics": n, "points_per_geodesic": nup, "gpu_ms": gpu_ms,
             "gpu_geodesics_per_s": n / (gpu_ms * 1e-3), "gpu_points_per_s": n * nup / (gpu_ms * 1e-3),
             "gpu_ms_taylor_solver": taylor_ms, "speedup_vs_taylor_solver": taylor_ms / gpu_ms,
-            "closed_form_rays": int(methods[1] + methods[2]), "taylor_fallback_rays": int(methods[0]),
+            "closed_form_rays": int(methods[1:].sum()), "taylor_fallback_rays": int(methods[0]),
+            "closed_form_cases": {"four_real_roots": int(methods[1]), "complex_pair_around": int(methods[2]),
+                                  "complex_pair_above_two_roots": int(methods[3]), "two_complex_pairs": int(methods[4])},
             "cpu_geodesics_per_s": n / cpu_s, "cpu_cores": os.cpu_count(), "cpu_kind": "host build, closed form",
             "max_rel_diff_gpu_vs_cpu": worst_cpu,
             "oracle_taylor_geodesics_per_s": len(sample) / oracle_s, "oracle_sample": len(sample),
