@@ -115,12 +115,13 @@ GKCF_HD double amp_j(const Amp& A, double n, double p) {
 
 // e = n - 1 is passed exactly: the denominator (n - 1)(n - m) = e (e + mc)
 // vanishes as n -> 1 together with mc -> 0 (a near-double radial root)
-GKCF_HD double amp_pi2(const Amp& A, double n, double e, double p) {
+// J = amp_j(A, n, p), computed once by the caller and shared with Pi = F + n J
+GKCF_HD double amp_pi2(const Amp& A, double n, double e, double p, double J) {
     if (A.S == 0.0) return 0.0;
     const double m = A.m;
     const double V = A.s * std::sqrt(A.C) * std::sqrt(A.D2) / p;
     const double num = n * n * V - (2.0 * n + 2.0 * m * n - n * n - 2.0 * m) * A.F -
-                       n * (2.0 * n + 2.0 * m * n - n * n - 3.0 * m) * amp_j(A, n, p) + m * n * A.Sd;
+                       n * (2.0 * n + 2.0 * m * n - n * n - 3.0 * m) * J + m * n * A.Sd;
     return num / (2.0 * e * (e + A.mc));
 }
 
@@ -286,7 +287,8 @@ GKCF_HD void radial_G(const CfRay& R, double u, double* G) {
             const double p = R.pole[ip], Dc = c[0], Ds = c[1], n = R.pn[ip][0];
             // 1 - n S = (u - p) cos(theta) (Dc cos theta' - Ds sin theta') / Dc^2
             const double q = (u - p) * ct * (Dc * cp - Ds * sp) / (Dc * Dc);
-            const double J = quadrant(amp_j(A, n, q), R.comp[1 + ip], cp, sp);
+            const double Jb = amp_j(A, n, q);
+            const double J = quadrant(Jb, R.comp[1 + ip], cp, sp);
             const double w = w_odd(S, n, m, q);
             G[2 + ip] = g * (c[2] * F + c[3] * J + c[4] * w);
             if (ip > 0) G[4 + ip] = g * (c[5] * F + p * (c[3] * J + c[4] * w));
@@ -294,8 +296,8 @@ GKCF_HD void radial_G(const CfRay& R, double u, double* G) {
                 // (a + e S/(1 - nS) + kappa sc/(1 - nS))^2: even part with
                 // int S/(1 - nS)^2 = (Pi2 - Pi)/n, int S^2/(1 - nS)^2 = (Pi2 - 2 Pi + F)/n^2,
                 // odd part 2 kappa (a W + e (W2 - W)/n)
-                const double Pi = quadrant(amp_pi(A, n, q), R.comp[4], cp, sp);
-                const double P2 = quadrant(amp_pi2(A, n, R.pn[0][1], q), R.comp[5], cp, sp);
+                const double Pi = quadrant(A.F + n * Jb, R.comp[4], cp, sp);      // n >= 1
+                const double P2 = quadrant(amp_pi2(A, n, R.pn[0][1], q, Jb), R.comp[5], cp, sp);
                 const double Q1 = (P2 - Pi) / n, Q2 = (P2 - 2.0 * Pi + F) / (n * n);
                 const double w2 = w2_odd(S, n, m, q, w);
                 const double a0 = c[2], e0 = c[3], k0 = c[4];
@@ -312,23 +314,26 @@ GKCF_HD void radial_G(const CfRay& R, double u, double* G) {
             const double p = R.pole[ip], n = (u3 - p) * (u2 - u1) / ((u2 - p) * (u3 - u1));
             const double e = (u3 - u2) * (p - u1) / ((u2 - p) * (u3 - u1));      // n - 1
             const double f = (u - p) * (u3 - u2) / ((u2 - p) * (u3 - u));
-            double h, x;
+            double h, x, T;
             if (n < -1.0) {
-                const double Cp = (u3 - u2) / ((u3 - p) * (u2 - p)), T = amp_pi(A, n, f);
+                const double Cp = (u3 - u2) / ((u3 - p) * (u2 - p));
+                T = amp_pi(A, n, f);
                 h = A.F / (u3 - p) + Cp * T;
                 x = u3 / (u3 - p) * A.F + p * Cp * T;
             } else {
-                const double Kp = (u3 - u2) * (u2 - u1) / ((u2 - p) * (u2 - p) * (u3 - u1)), T = amp_j(A, n, f);
+                const double Kp = (u3 - u2) * (u2 - u1) / ((u2 - p) * (u2 - p) * (u3 - u1));
+                T = amp_j(A, n, f);
                 h = A.F / (u2 - p) + Kp * T;
                 x = u2 / (u2 - p) * A.F + p * Kp * T;
             }
             G[2 + ip] = -g * h;
             if (ip > 0) G[4 + ip] = -g * x;
             if (ip == 0) {
-                // (1/u2 + K0 S/(1 - n S))^2, with int S^2/(1 - n S)^2 = (Pi2 - 2 Pi + F)/n^2
+                // (1/u2 + K0 S/(1 - n S))^2, with int S^2/(1 - n S)^2 = (Pi2 - 2 Pi + F)/n^2;
+                // n > 1 here (the pole u = 0 lies inside [u1, u2]), so T = J and Pi = F + n J
                 const double K0 = (u3 - u2) * (u2 - u1) / (u2 * u2 * (u3 - u1));
-                const double Q = (amp_pi2(A, n, e, f) - 2.0 * amp_pi(A, n, f) + A.F) / (n * n);
-                G[1] = -g * (A.F / (u2 * u2) + 2.0 * K0 / u2 * amp_j(A, n, f) + K0 * K0 * Q);
+                const double Q = (amp_pi2(A, n, e, f, T) - 2.0 * (A.F + n * T) + A.F) / (n * n);
+                G[1] = -g * (A.F / (u2 * u2) + 2.0 * K0 / u2 * T + K0 * K0 * Q);
             }
         }
         return;
@@ -356,8 +361,9 @@ GKCF_HD void radial_G(const CfRay& R, double u, double* G) {
         }
         if (ip == 0) {
             const double cross = 2.0 * c[2] * c[3] / (c[0] - c[1]);
+            const double jj1 = pi1 ? amp_j(A, n1, f1) : j1, jj2 = pi2 ? amp_j(A, n2, f2) : j2;
             G[1] = g * (c[4] * c[4] * A.F + 2.0 * c[4] * (c[2] * t1 + c[3] * t2) + cross * (n1 * t1 - n2 * t2) +
-                        c[2] * c[2] * amp_pi2(A, n1, c[0], f1) + c[3] * c[3] * amp_pi2(A, n2, c[1], f2));
+                        c[2] * c[2] * amp_pi2(A, n1, c[0], f1, jj1) + c[3] * c[3] * amp_pi2(A, n2, c[1], f2, jj2));
         }
     }
 }
@@ -536,8 +542,8 @@ GKCF_HD void setup(double a, double l, double q2, double u0, double uf, double m
             R.pn[ip][0] = n; R.pn[ip][1] = e;
             R.comp[1 + ip] = amp_j(AK, n, -e);                     // 1 - n = -e
             if (ip == 0) {
-                R.comp[4] = amp_pi(AK, n, -e);
-                R.comp[5] = amp_pi2(AK, n, e, -e);
+                R.comp[4] = AK.F + n * R.comp[1];
+                R.comp[5] = amp_pi2(AK, n, e, -e, R.comp[1]);
             }
         }
     } else {
