@@ -436,6 +436,70 @@ template <int FAM> struct CritRay { using type = DRay<false>; };
 template <> struct CritRay<kFam78> { using type = DRay78<false>; };
 template <> struct CritRay<kFam78df> { using type = DRay78df<false>; };
 
+// Near-critical rays from the deferred list, traced whole in FP64 by one
+// warp until the list is drained (rays taken four at a time from work2).
+template <int FAM>
+__device__ __forceinline__ void trace_deferred(const SceneDev& s, const InitSoA& soa, float* __restrict__ srgb,
+                                               float* __restrict__ rcross, Counters* __restrict__ ctr, long long D,
+                                               unsigned long long& n_rays, unsigned long long& n_steps,
+                                               unsigned long long& n_f64, unsigned long long& n_evals) {
+    const unsigned FULL = 0xffffffffu;
+    WarpQueue q{0, 0};
+    bool drained = false, have = false;
+    typename CritRay<FAM>::type R;
+    long long item = 0, p = 0;
+    int sl = 0;
+    float cam_y = 0.0f;
+    while (true) {
+        unsigned need = __ballot_sync(FULL, !have);
+        if (need && !drained) {
+            long long idx = warp_take(q, need, &ctr->work2, D, 4);
+            drained = q.base >= D;
+            if (!have && idx >= 0) {
+                item = soa.list[idx];
+                int x, y; uint32_t sid;
+                ray_coords(s, item, p, sl, x, y, sid);
+                float4 a = soa.a[item], b = soa.b[item];
+                cam_y = soa.cy[item];
+                if constexpr (FAM == kFam78df)
+                    dray78df_start(R, s, HiLo{b.x, b.y}, HiLo{b.z, b.w}, HiLo{a.x, a.y}, HiLo{a.z, a.w});
+                else if constexpr (FAM == kFam78)
+                    dray78_start(R, s, (double)b.x + (double)b.y, (double)b.z + (double)b.w,
+                                 (double)a.x + (double)a.y, (double)a.z + (double)a.w);
+                else
+                    dray_start(R, s, (double)b.x + (double)b.y, (double)b.z + (double)b.w,
+                               (double)a.x + (double)a.y, (double)a.z + (double)a.w);
+                have = true;
+                n_rays++;
+            }
+        }
+        if (!__any_sync(FULL, have)) break;
+        if (have) {
+            bool done;
+            if constexpr (FAM == kFam78df) {
+                bool acc;
+                done = dray78df_step(R, s, acc);
+                if (acc) { n_steps++; n_f64++; }
+                n_evals += 13;
+            } else if constexpr (FAM == kFam78) {
+                bool acc;
+                done = dray78_step(R, s, acc);
+                if (acc) { n_steps++; n_f64++; }
+                n_evals += 13;
+            } else {
+                done = dray_step(R, s);
+                n_steps++; n_f64++; n_evals += 4;
+            }
+            if (done) {
+                float col[3];
+                sample_colour(s, R.status == 1, R.orders, R.disk, (float)R.min_r, cam_y, col);
+                write_sample(s, srgb, rcross, p, sl, col, R.first_r);
+                have = false;
+            }
+        }
+    }
+}
+
 template <int MINB, int FAM>
 __global__ void __launch_bounds__(kBlock, MINB)
 render_mixed_kernel(const SceneDev s, const InitSoA soa, float* __restrict__ srgb, float* __restrict__ rcross,
@@ -444,65 +508,13 @@ render_mixed_kernel(const SceneDev s, const InitSoA soa, float* __restrict__ srg
     const SpaceK k{(float)s.a, (float)(s.a * s.a), (float)s.M, (float)s.r_plus, (float)s.r_minus};
     unsigned long long n_rays = 0, n_steps = 0, n_f64 = 0, n_evals = 0;
 
-    // ---- FP64 warps: near-critical rays
+    // ---- FP64 warps: near-critical rays.  Warp 0 of the first blocks starts
+    // on them; every other warp joins once the FP32 queue is drained, so the
+    // FP64 tail of a frame with many near-critical rays uses the whole grid.
     const long long D = (long long)ctr->deferred;
     const int nd = D > 0 ? (int)min((long long)gridDim.x, (D + 3) / 4) : 0;
-    if ((threadIdx.x >> 5) == 0 && (int)blockIdx.x < nd) {
-        WarpQueue q{0, 0};
-        bool drained = false, have = false;
-        typename CritRay<FAM>::type R;
-        long long item = 0, p = 0;
-        int sl = 0;
-        float cam_y = 0.0f;
-        while (true) {
-            unsigned need = __ballot_sync(FULL, !have);
-            if (need && !drained) {
-                long long idx = warp_take(q, need, &ctr->work2, D, 4);
-                drained = q.base >= D;
-                if (!have && idx >= 0) {
-                    item = soa.list[idx];
-                    int x, y; uint32_t sid;
-                    ray_coords(s, item, p, sl, x, y, sid);
-                    float4 a = soa.a[item], b = soa.b[item];
-                    cam_y = soa.cy[item];
-                    if constexpr (FAM == kFam78df)
-                        dray78df_start(R, s, HiLo{b.x, b.y}, HiLo{b.z, b.w}, HiLo{a.x, a.y}, HiLo{a.z, a.w});
-                    else if constexpr (FAM == kFam78)
-                        dray78_start(R, s, (double)b.x + (double)b.y, (double)b.z + (double)b.w,
-                                     (double)a.x + (double)a.y, (double)a.z + (double)a.w);
-                    else
-                        dray_start(R, s, (double)b.x + (double)b.y, (double)b.z + (double)b.w,
-                                   (double)a.x + (double)a.y, (double)a.z + (double)a.w);
-                    have = true;
-                    n_rays++;
-                }
-            }
-            if (!__any_sync(FULL, have)) break;
-            if (have) {
-                bool done;
-                if constexpr (FAM == kFam78df) {
-                    bool acc;
-                    done = dray78df_step(R, s, acc);
-                    if (acc) { n_steps++; n_f64++; }
-                    n_evals += 13;
-                } else if constexpr (FAM == kFam78) {
-                    bool acc;
-                    done = dray78_step(R, s, acc);
-                    if (acc) { n_steps++; n_f64++; }
-                    n_evals += 13;
-                } else {
-                    done = dray_step(R, s);
-                    n_steps++; n_f64++; n_evals += 4;
-                }
-                if (done) {
-                    float col[3];
-                    sample_colour(s, R.status == 1, R.orders, R.disk, (float)R.min_r, cam_y, col);
-                    write_sample(s, srgb, rcross, p, sl, col, R.first_r);
-                    have = false;
-                }
-            }
-        }
-    }
+    if ((threadIdx.x >> 5) == 0 && (int)blockIdx.x < nd)
+        trace_deferred<FAM>(s, soa, srgb, rcross, ctr, D, n_rays, n_steps, n_f64, n_evals);
 
     // ---- FP32 rays
     WarpQueue q{0, 0};
@@ -577,6 +589,7 @@ render_mixed_kernel(const SceneDev s, const InitSoA soa, float* __restrict__ srg
             have = false;
         }
     }
+    if (D > 0) trace_deferred<FAM>(s, soa, srgb, rcross, ctr, D, n_rays, n_steps, n_f64, n_evals);
     flush_counters(ctr, n_rays, n_steps, n_f64, n_evals);
 }
 
