@@ -147,8 +147,7 @@ typedef struct np_scene {
     int32_t islands;              /* NP_ISLAND_* mask of the mixed path */
     double inv_gate;              /* NP_INTEG_RKF78 invariant gate; <= 0 disables */
     double rtol_fp64;             /* rtol of the near-critical rays the mixed 7(8) path traces
-                                     whole in FP64; <= 0 means min(rtol, 1e-10) (its island steps
-                                     keep rtol) */
+                                     whole in FP64; <= 0 means rtol (as its island steps) */
     int32_t island_arith;         /* np_island_arith: arithmetic of the FP64-class steps of the
                                      mixed 7(8) path */
     int32_t reserved0;            /* 0 */

@@ -65,7 +65,7 @@ def test_random_rays_order1_meets_bar(cuda):
 
 def test_crossing_modes_and_islands(cuda):
     """Henon crossings beat the Hermite interpolant over the same 7(8) steps,
-    and the islands (FP64 7(8) steps at 1e-10) do not worsen the bar."""
+    and the islands (FP64 7(8) steps) do not worsen the bar."""
     from nullpath_gb300 import accuracy
     base = npx.accurate_scene(npx.benchmark_scene())
     henon = accuracy.crossing_error(base.replace(islands=0), n=20000, precision="mixed", seed=5)["order1"]
