@@ -264,3 +264,88 @@ def points(u0, uf, mu0, a, l, q2, su, sm, tpr=1, nup=32, offset=0.5):
         out["tpm"].append(int(mp.floor(w / (2 * Kth)) - mp.floor(w0 / (2 * Kth))))
         out["tpr"].append(1 if branch2 else 0)
     return out
+
+
+def points_vortical(u0, uf, mu0, a, l, q2, su, sm, tpr=1, nup=32, offset=0.5):
+    """Truth for q2 < 0 (vortical) rays, independent of any Legendre
+    reduction: the polar motion mu = s0 mu+ dn(a mu+ lambda + w0 | k) with
+    mpmath's Jacobi functions (Byrd & Friedman 218.00), the polar integrals
+    by quadrature in w, and the radial integrals by quadrature in u (these
+    rays meet no radial turning point: U > 0 from u0 to the horizon).
+    Returns None outside that case."""
+    a, l, q2, u0, uf, mu0 = (mp.mpf(x) for x in (a, l, q2, u0, uf, mu0))
+    if not (q2 < 0) or a == 0 or mu0 == 0:
+        return None
+    Bc, Kc = a * a - l * l - q2, (l - a) ** 2 + q2
+    c = [mp.mpf(1), mp.mpf(0), Bc, 2 * Kc, -a * a * q2]
+    U = lambda u: c[0] + c[2] * u ** 2 + c[3] * u ** 3 + c[4] * u ** 4
+    roots = mp.polyroots(c[::-1], maxsteps=400, extraprec=400)
+    if any(abs(mp.im(r)) < mp.mpf(10) ** -30 and mp.re(r) > 0 for r in roots):
+        return None                      # a positive real root: not this case
+    sq = mp.sqrt(1 - a * a)
+    rp, rm = 1 + sq, a * a / (1 + sq)
+    uplus = 1 / rp
+    if su > 0:
+        ub, tp = uplus, 0
+    else:
+        ub, tp = mp.mpf(0), 0
+    du = (1 if ub - u0 >= 0 else -1) * su * ((ub - u0) - (ub - uf)) / nup
+    kmax = 0 if du == 0 else min(int(mp.floor((ub - u0) / du + offset)), nup)
+    last = max(0, min(kmax, nup))
+    if last > 0 and ((su > 0 and not (u0 + (last - offset) * du < uplus)) or
+                     (su < 0 and not (u0 + (last - offset) * du > 0))):
+        last = 0
+    mpos, a2mneg = _polar_roots(a, l, q2, mu0)
+    if not (a2mneg > 0):
+        return None
+    mp_ = mp.sqrt(mpos)
+    om = a * mp_
+    mth = (a * a * mpos - a2mneg) / (a * a * mpos)
+    s0 = 1 if mu0 > 0 else -1
+    # dn(w0) = |mu0| / mu+; d mu / d lambda = -s0 mu+ k^2 sn cn omega
+    S0 = (a * a * mpos - a * a * mu0 * mu0) / (a * a * mpos - a2mneg)
+    F0 = mp.ellipf(mp.asin(mp.sqrt(max(mp.mpf(0), min(mp.mpf(1), S0)))), mth)
+    w0 = F0 if sm * s0 < 0 else -F0
+    Kth = mp.ellipk(mth)
+    dn = lambda w: mp.ellipfun('dn', w, m=mth)
+
+    def wquad(f, wa, wb):
+        pts = [wa] + [mp.mpf(k) * Kth for k in range(int(mp.floor(min(wa, wb) / Kth)) + 1,
+                                                     int(mp.floor(max(wa, wb) / Kth)) + 1)] + [wb]
+        pts = sorted(set(pts))
+        v = mp.quad(f, pts)
+        return v if wb >= wa else -v
+
+    def uquad(f, ua, ub_):
+        lo, hi = min(ua, ub_), max(ua, ub_)
+        pts = [lo]
+        x = lo
+        while x * 10 < hi:
+            x = x * 10
+            pts.append(x)
+        pts.append(hi)
+        return mp.quad(lambda x: f(x) / mp.sqrt(U(x)), pts)
+
+    cp = 2 * (2 * rp - a * l) / (rp - rm)
+    cm = 2 * (2 * rm - a * l) / (rm - rp)
+    dp = a * (2 * rp - a * l) / (rp * (rp - rm))
+    dm = a * (2 * rm - a * l) / (rm * (rm - rp))
+    out = {k: [] for k in ("u", "mu", "dt", "dphi", "lam", "tpm", "tpr")}
+    for k in range(1, last + 1):
+        ut = u0 + (k - offset) * du
+        lam = uquad(lambda x: 1, u0, ut)
+        i2 = uquad(lambda x: 1 / (x * x), u0, ut)
+        i1 = uquad(lambda x: 1 / x, u0, ut)
+        ip = uquad(lambda x: 1 / (1 - rp * x), u0, ut)
+        im = uquad(lambda x: 1 / (1 - rm * x), u0, ut)
+        w = om * lam + w0
+        mu2 = wquad(lambda v: mpos * dn(v) ** 2, w0, w) / om
+        inv = wquad(lambda v: 1 / (1 - mpos * dn(v) ** 2), w0, w) / om
+        out["u"].append(ut)
+        out["mu"].append(s0 * mp_ * dn(w))
+        out["dt"].append(i2 + 2 * i1 + cp * ip + cm * im + a * a * mu2)
+        out["dphi"].append(dp * ip + dm * im - l * lam + l * inv)
+        out["lam"].append(i2 + a * a * mu2)
+        out["tpm"].append(int(mp.floor(w / Kth) - mp.floor(w0 / Kth)))
+        out["tpr"].append(0)
+    return out

@@ -57,6 +57,25 @@ def test_closed_form_matches_truth():
         assert np.array_equal(h["tpm"][0], t["tpm"][j]) and np.array_equal(h["tpr"][0], t["tpr"][j]), j
 
 
+def test_vortical_closed_form_matches_quadrature_truth():
+    """q2 < 0 rays (two real radial roots below the motion, or two complex
+    pairs; dn-form polar motion) against a 40-digit truth built by
+    quadrature, independent of the Legendre reductions
+    (tests/golden/geokerr_cf_truth_vortical.npz): 5e-14."""
+    t = np.load(os.path.join(HERE, "golden", "geokerr_cf_truth_vortical.npz"))
+    seen = set()
+    for j in range(len(t["a"])):
+        a = float(t["a"][j])
+        uplus = 1.0 / (1.0 + math.sqrt(1.0 - a * a))
+        h = gk.points_host(a, 1e-6, uplus, 0.5, t["l"][j:j + 1], t["q2"][j:j + 1], t["su"][j:j + 1],
+                           t["sm"][j:j + 1], 1, 32, 0.5)
+        seen.add(int(h["method"][0]))
+        for k, key in enumerate(KEYS):
+            assert _rel(h[key][0], t["pts"][j, k]) < 5e-14, (j, key)
+        assert np.array_equal(h["tpm"][0], t["tpm"][j])
+    assert seen == {3, 4}
+
+
 def test_taylor_oracle_matches_truth():
     """The Taylor restatement on the same rays: 3e-11, its phi losing
     digits on near-polar orbits (the potential's coefficients carry 1 - mu+^2
