@@ -707,8 +707,10 @@ int points_cf_launch(int n, int mode, double a, const double* u0, const double* 
     int32_t* fb = (int32_t*)(rays + n);
     int32_t* nfb = fb + n;
     cudaMemsetAsync(nfb, 0, sizeof(int32_t), st);
-    cf_setup_kernel<<<grid(n, 128), 128, 0, st>>>(n, mode, a, u0, uf, mu0, l, q2, su, sm, tpr, nup, offset, rays, npts,
-                                                  fb, nfb);
+    // one ray per thread; warp-sized blocks spread a grid of a few thousand
+    // rays over every SM (the kernel is FP64-bound once resident)
+    cf_setup_kernel<<<grid(n, 32), 32, 0, st>>>(n, mode, a, u0, uf, mu0, l, q2, su, sm, tpr, nup, offset, rays, npts,
+                                                fb, nfb);
     // The Taylor rays (a few serial integrations) run on a side stream
     // beside the per-point kernel; the caller's stream waits for both.
     cudaStream_t side = nullptr;
