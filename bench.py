@@ -235,8 +235,9 @@ def batch_leg(n_scenes=256, seed=1, passes=3):
 def critical_leg(W=2048, spp=16, spin=0.998, n_acc=8000):
     """2048x2048 at a = 0.998 with 16 spp, half the rays within +-2 % of the
     critical curve (NP_JITTER_CRITICAL).  The mixed 7(8) path with its islands
-    off, with the default islands (horizon band, near-critical rays traced
-    whole in FP64) and with every island; the reference step law's RK4 with
+    off, with the default islands (horizon band; near-critical rays in FP64
+    closed form) and with every island, both also with the near-critical
+    rays integrated whole in FP64 7(8); the reference step law's RK4 with
     every island for comparison.  Crossing error against the Mino-time solver
     on critical-sampled rays beside each."""
     import torch
@@ -248,15 +249,20 @@ def critical_leg(W=2048, spp=16, spin=0.998, n_acc=8000):
     rgb = torch.zeros((3, W, W), dtype=torch.float32, device="cuda")
     rc = torch.zeros((W, W), dtype=torch.float32, device="cuda")
     cache = {}
+    integ = npx.NP_CRITICAL_INTEGRATE
     for name, scn in (("rkf78_islands_none", npx.accurate_scene(base).replace(islands=0)),
                       ("rkf78_islands_default", npx.accurate_scene(base).replace(islands=npx.NP_ISLANDS_DEFAULT)),
                       ("rkf78_islands_all", npx.accurate_scene(base).replace(islands=npx.NP_ISLANDS_ALL)),
+                      ("rkf78_islands_default_near_critical_integrated",
+                       npx.accurate_scene(base).replace(islands=npx.NP_ISLANDS_DEFAULT, critical_solver=integ)),
+                      ("rkf78_islands_all_near_critical_integrated",
+                       npx.accurate_scene(base).replace(islands=npx.NP_ISLANDS_ALL, critical_solver=integ)),
                       ("rk4_islands_all", base.replace(islands=npx.NP_ISLANDS_ALL))):
         npx.render(scn, "mixed", rgb=rgb, rcross=rc)
         _, _, st = npx.render(scn, "mixed", rgb=rgb, rcross=rc, stats=True)
         leg = {"rays_per_s": rays / ((st.kernel_ms + st.init_ms) * 1e-3), "kernel_ms": st.kernel_ms + st.init_ms,
                "mean_steps_per_ray": st.steps / max(1, st.rays), "fp64_steps_frac": st.fp64_steps / max(1, st.steps),
-               "deferred_rays": int(st.deferred_rays),
+               "deferred_rays": int(st.deferred_rays), "closed_form_rays": int(st.closed_form_rays),
                "error_vs_geokerr": accuracy.crossing_error(scn, n=n_acc, precision="mixed", seed=3, critical=True,
                                                            cache=cache)}
         out[name] = leg
@@ -500,9 +506,11 @@ def run_ours(args):
                        "integrator": "compensated FP32 Fehlberg 7(8), rtol %g, atol %g, Henon crossings" % (
                            sc.rtol, sc.atol) if args.path == "rkf78" else "RK4, h = 0.01 clamp(r, 1, 100), Hermite",
                        "rays_per_step": rays_per_step,
-                       "fp64_islands": ("horizon band 0.1 M (certified capture, FP64 steps otherwise), "
-                                        "|b-b_crit| < 1e-3 M" if args.path == "rkf78" else
-                                        "horizon band 0.1 M, radial/polar turning points, |b-b_crit| < 1e-3 M"),
+                       "fp64_islands": ("horizon band 0.1 M (certified capture, FP64 steps otherwise)" if
+                                        args.path == "rkf78" else
+                                        "horizon band 0.1 M, radial/polar turning points"),
+                       "near_critical": "|b-b_crit| < 1e-3 M: FP64 closed form (Mino-time solution, "
+                                        "crossings by Jacobi amplitude, Carlson R_F)",
                        "l2": "256 MiB buffer written between timed steps (outside the step events)",
                        "parallelism": "replicas" if ws > 1 else "single"},
             "steps_per_s": ws * st.steps / (ms * 1e-3),
@@ -510,6 +518,7 @@ def run_ours(args):
             "rhs_evals_per_ray": st.rhs_evals / max(1, st.rays),
             "fp64_island_steps_frac": st.fp64_steps / max(1, st.steps),
             "deferred_rays": st.deferred_rays,
+            "closed_form_rays": st.closed_form_rays,
             "kernel_ms": {"tracer": kern_ms, "ray_init": statistics.mean(s.init_ms for s in stats)},
             "roofline": {"bound": "fp32" if args.precision == "mixed" else "fp64", "achieved": achieved,
                          "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
@@ -523,7 +532,7 @@ def run_ours(args):
             "e2e": {"value": replicas.aggregate_rays_per_s(rays_per_step, e2e, ws), "unit": "rays/s",
                     "h2d_bytes_per_step": C.sizeof(sc),
                     "d2h_bytes_per_step": 4 * H * W * 4},
-            "gpu_launches": 3 * args.steps,
+            "gpu_launches": (4 if args.precision == "mixed" else 2) * args.steps,
             "clocks": clocks,
             "wall_s": wall,
         }
@@ -539,11 +548,14 @@ def run_ours(args):
             return {"rays_per_s": rays_per_step / (t * 1e-3), "kernel_ms": t,
                     "mean_steps_per_ray": best.steps / max(1, best.rays),
                     "rhs_evals_per_ray": best.rhs_evals / max(1, best.rays),
-                    "fp64_island_steps_frac": best.fp64_steps / max(1, best.steps)}
+                    "fp64_island_steps_frac": best.fp64_steps / max(1, best.steps),
+                    "closed_form_rays": best.closed_form_rays}
         if args.precision == "mixed" and args.path == "rkf78":
             out["islands_all"] = timed(sc.replace(islands=npx.NP_ISLANDS_ALL))
             out["islands_all"]["islands"] = "horizon band, turning points (FP64 7(8) steps), near-critical"
             out["islands_none"] = timed(sc.replace(islands=0))
+            out["near_critical_integrated"] = timed(sc.replace(critical_solver=npx.NP_CRITICAL_INTEGRATE))
+            out["near_critical_integrated"]["near_critical"] = "traced whole in FP64 7(8) at rtol"
             out["rk4_reference_step_law"] = timed(headline_scene("rk4"))
             out["rk4_reference_step_law"]["islands"] = "all"
         if args.fp64_frame and args.precision == "mixed":
@@ -565,6 +577,9 @@ def run_ours(args):
                                                              precision=args.precision, seed=21, cache=cache)
                 acc["islands_none"] = accuracy.crossing_error(sc.replace(islands=0), n=50000,
                                                               precision=args.precision, seed=21, cache=cache)
+                acc["near_critical_integrated"] = accuracy.crossing_error(
+                    sc.replace(critical_solver=npx.NP_CRITICAL_INTEGRATE), n=50000, precision=args.precision,
+                    seed=21, cache=cache)
                 acc["rk4_reference_step_law"] = accuracy.crossing_error(headline_scene("rk4"), n=50000,
                                                                         precision=args.precision, seed=21,
                                                                         cache=cache)

@@ -219,6 +219,25 @@ int np_geokerr_equator_crossings_cf_device(int n, double a, const double* d_u0, 
 int np_geokerr_equator_crossings_cf_host(int n, double a, const double* u0, const double* mu0, const double* l,
                                          const double* q2, const double* su, const double* sm, double u_end, int K,
                                          double* xu, int32_t* nx);
+/* Equatorial crossings in closed form by Jacobi amplitude: the polar motion
+ * mu = mu+ cn(omega lambda + w0 | k) gives the Mino time of each crossing,
+ * the radial motion's Legendre variable S = sn^2(F | m) its u, one amplitude
+ * per crossing (the crossings of GEOR with muf = 0, geokerr_original.f:
+ * 2672-3136, without integration).  Per ray: the first K (1..16) crossings
+ * with u in [u_lo, u_hi] along the ray to its end (the horizon, or u_far
+ * after its radial turning point): u in xu[n][K], the azimuth change from
+ * the start in xphi[n][K] (NULL to skip; NaN for a polar orbit through the
+ * pole with l != 0), the count in nx[i] and in status[i] (NULL to skip) 0
+ * (leaves through u_far), 1 (falls into the horizon) or -1 (outside the
+ * closed forms: a = 0, q2 = 0, a start inside the photon region or inside
+ * u_far).  q2 < 0 rays have no crossing.  np_status. */
+int np_geokerr_disk_crossings_device(int n, double a, const double* d_u0, const double* d_mu0, const double* d_l,
+                                     const double* d_q2, const double* d_su, const double* d_sm, double u_far,
+                                     double u_lo, double u_hi, int K, double* d_xu, double* d_xphi, int32_t* d_nx,
+                                     int32_t* d_status, void* stream);
+int np_geokerr_disk_crossings_host(int n, double a, const double* u0, const double* mu0, const double* l,
+                                   const double* q2, const double* su, const double* sm, double u_far, double u_lo,
+                                   double u_hi, int K, double* xu, double* xphi, int32_t* nx, int32_t* status);
 /* GEOKERR's standard camera grid (geokerr_original.f:183-220): n_alpha x
  * n_beta cell-centred image positions alpha = a1 + (a2 - a1)(i + 1/2) /
  * n_alpha, beta = b1 + (b2 - b1)(j + 1/2) / n_beta (ray index i n_beta + j),

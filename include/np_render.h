@@ -36,7 +36,7 @@
 extern "C" {
 #endif
 
-#define NP_ABI_VERSION 3
+#define NP_ABI_VERSION 4
 
 typedef enum np_status {
     NP_OK = 0,
@@ -103,6 +103,23 @@ typedef enum np_precision { NP_PREC_FP64 = 0, NP_PREC_MIXED = 1 } np_precision;
  *                         latency-bound. */
 typedef enum np_island_arith { NP_ISLAND_ARITH_FP64 = 0, NP_ISLAND_ARITH_DF = 1 } np_island_arith;
 
+/* Near-critical rays of NP_PREC_MIXED (np_scene_t.critical_solver; used
+ * when NP_ISLAND_CRITICAL is set).
+ *   NP_CRITICAL_CLOSED_FORM  the FP64 Mino-time solution (default): the
+ *                            Mino time of each equatorial crossing from the
+ *                            polar motion mu = mu+ cn(omega lambda + w0 | k),
+ *                            its radius from one Jacobi amplitude of the
+ *                            radial motion (Carlson's R_F), capture or escape
+ *                            from the roots of the radial potential; no
+ *                            integration steps.  Rays outside the closed
+ *                            forms (a = 0, Carter's Q = 0, a camera inside
+ *                            the photon region or beyond the escape radius)
+ *                            are integrated as below.
+ *   NP_CRITICAL_INTEGRATE    traced whole in FP64 (island_arith) by the
+ *                            integrator family of the scene: 7(8) at
+ *                            rtol_fp64, RK4 with the reference step law. */
+typedef enum np_critical_solver { NP_CRITICAL_CLOSED_FORM = 0, NP_CRITICAL_INTEGRATE = 1 } np_critical_solver;
+
 /* FP64 islands of NP_PREC_MIXED (bit mask, np_scene_t.islands). */
 #define NP_ISLAND_HORIZON 1   /* steps within 0.1 M of the outer horizon */
 #define NP_ISLAND_TURNING 2   /* steps across a radial or polar turning point */
@@ -150,7 +167,7 @@ typedef struct np_scene {
                                      whole in FP64; <= 0 means rtol (as its island steps) */
     int32_t island_arith;         /* np_island_arith: arithmetic of the FP64-class steps of the
                                      mixed 7(8) path */
-    int32_t reserved0;            /* 0 */
+    int32_t critical_solver;      /* np_critical_solver: near-critical rays of the mixed path */
 } np_scene_t;
 
 /* Per-call statistics, filled when the pointer is non-NULL. */
@@ -159,9 +176,11 @@ typedef struct np_render_stats {
     uint64_t steps;               /* accepted integration steps */
     uint64_t fp64_steps;          /* steps taken in FP64 by the mixed path */
     uint64_t rhs_evals;           /* right-hand-side evaluations */
-    uint64_t deferred_rays;       /* near-critical rays traced whole in FP64 (mixed path) */
+    uint64_t deferred_rays;       /* near-critical rays (mixed path) */
     double kernel_ms;             /* device time of the tracer kernel */
-    double init_ms;               /* device time of the ray-generation kernel (mixed path) */
+    double init_ms;               /* device time of ray generation and the near-critical
+                                     rays' closed form (mixed path) */
+    uint64_t closed_form_rays;    /* near-critical rays solved in closed form (mixed path) */
 } np_render_stats_t;
 
 /* ABI version compiled into the library. */

@@ -17,7 +17,7 @@ from ._abi import (Scene, RenderStats, isco_radius, reference_defaults, benchmar
                    NP_CROSS_ROOT,
                    NP_BG_GRADIENT, NP_BG_POINT, NP_ISLAND_HORIZON, NP_ISLAND_TURNING,
                    NP_ISLAND_CRITICAL, NP_ISLANDS_ALL, NP_ISLANDS_DEFAULT, NP_ISLAND_ARITH_DF,
-                   NP_ISLAND_ARITH_FP64)
+                   NP_ISLAND_ARITH_FP64, NP_CRITICAL_CLOSED_FORM, NP_CRITICAL_INTEGRATE)
 from ._lib import load, lib_path, NullPathError
 from .render import render, render_host, trace_rays, trace_invariants, precision_code
 

@@ -23,6 +23,7 @@ NP_ISLAND_HORIZON, NP_ISLAND_TURNING, NP_ISLAND_CRITICAL = 1, 2, 4
 NP_ISLANDS_ALL = 7
 NP_ISLANDS_DEFAULT = NP_ISLAND_HORIZON | NP_ISLAND_CRITICAL
 NP_ISLAND_ARITH_FP64, NP_ISLAND_ARITH_DF = 0, 1
+NP_CRITICAL_CLOSED_FORM, NP_CRITICAL_INTEGRATE = 0, 1
 
 
 class Scene(C.Structure):
@@ -44,7 +45,7 @@ class Scene(C.Structure):
         ("bg_sigma_deg", C.c_double), ("bg_brightness", C.c_double),
         ("check_invariants", C.c_int32), ("islands", C.c_int32),
         ("inv_gate", C.c_double), ("rtol_fp64", C.c_double),
-        ("island_arith", C.c_int32), ("reserved0", C.c_int32),
+        ("island_arith", C.c_int32), ("critical_solver", C.c_int32),
     ]
 
     def copy(self):
@@ -66,7 +67,7 @@ class RenderStats(C.Structure):
     _fields_ = [
         ("rays", C.c_uint64), ("steps", C.c_uint64), ("fp64_steps", C.c_uint64),
         ("rhs_evals", C.c_uint64), ("deferred_rays", C.c_uint64),
-        ("kernel_ms", C.c_double), ("init_ms", C.c_double),
+        ("kernel_ms", C.c_double), ("init_ms", C.c_double), ("closed_form_rays", C.c_uint64),
     ]
 
 
@@ -90,7 +91,7 @@ def reference_defaults():
                  disk_on=1, disk_max_orders=1, disk_rin=0.0, disk_rout=0.0,
                  emissivity_q=2.0, disk_gain=1.0, crossing=NP_CROSS_LINEAR,
                  background=NP_BG_GRADIENT, bg_sigma_deg=1.0, bg_brightness=3.0,
-                 check_invariants=0, islands=NP_ISLANDS_DEFAULT, inv_gate=0.0, rtol_fp64=0.0, island_arith=NP_ISLAND_ARITH_FP64, reserved0=0)
+                 check_invariants=0, islands=NP_ISLANDS_DEFAULT, inv_gate=0.0, rtol_fp64=0.0, island_arith=NP_ISLAND_ARITH_FP64, critical_solver=NP_CRITICAL_CLOSED_FORM)
 
 
 def benchmark_scene(width=1280, height=720, spp=4, spin=0.9, seed=0):
@@ -105,7 +106,7 @@ def benchmark_scene(width=1280, height=720, spp=4, spin=0.9, seed=0):
                  disk_on=1, disk_max_orders=3, disk_rin=isco_radius(1.0, spin), disk_rout=20.0,
                  emissivity_q=3.0, disk_gain=1.0, crossing=NP_CROSS_HERMITE,
                  background=NP_BG_GRADIENT, bg_sigma_deg=1.0, bg_brightness=3.0,
-                 check_invariants=0, islands=NP_ISLANDS_DEFAULT, inv_gate=0.0, rtol_fp64=0.0, island_arith=NP_ISLAND_ARITH_FP64, reserved0=0)
+                 check_invariants=0, islands=NP_ISLANDS_DEFAULT, inv_gate=0.0, rtol_fp64=0.0, island_arith=NP_ISLAND_ARITH_FP64, critical_solver=NP_CRITICAL_CLOSED_FORM)
 
 
 def accurate_scene(scene, rtol=1e-8, atol=1e-9, islands=None):

@@ -31,6 +31,7 @@
 
 #include "geokerr_c_api.h"
 #include "geokerr_cf.cuh"
+#include "equator_cf.cuh"
 #include "np_render.h"
 
 void np_record_error(const char* msg);
@@ -67,18 +68,9 @@ __host__ __device__ Par make_par(double a, double l, double q2, double mu0) {
     p.A3 = 2.0 * ((a - l) * (a - l) + q2);
     p.A4 = -a * a * q2;
     p.uplus = 1.0 / (1.0 + sqrt(1.0 - a * a));
-    const double a2 = a * a, b = a2 - (q2 + l * l);
-    const double yy = -0.5 * (b + (b >= 0.0 ? 1.0 : -1.0) * sqrt(b * b + 4.0 * q2 * a2));
+    const double a2 = a * a;
     double mpos, a2mneg;
-    if (b < 0.0) { a2mneg = -yy; mpos = q2 / yy; }
-    else { a2mneg = a2 * q2 / yy; mpos = -yy / a2; }
-    if (mpos > 1.0) mpos = 1.0;
-    if (a2mneg < 0.0 || a2 == 0.0) {
-        if (sqrt(mpos) < mu0) mpos = mu0 * mu0;
-    } else {
-        if (a2mneg > a2 * mu0 * mu0) a2mneg = a2 * mu0 * mu0;
-        if (mu0 * mu0 > mpos) mpos = mu0 * mu0;
-    }
+    np::gkcf::polar_roots(a, l, q2, mu0, mpos, a2mneg);
     p.mpos = mpos;
     p.a2mneg = a2mneg;
     p.B4 = -a2;
@@ -1220,5 +1212,73 @@ extern "C" int np_geokerr_camera_grid_host(double a, double mu0, int n_alpha, in
     for (long long k = 0; k < n; ++k)
         camera_grid_one(a, mu0, n_alpha, n_beta, a1, a2, b1, b2, input_limit, k, alpha[k], beta[k], l[k], q2[k], su[k],
                         sm[k]);
+    return NP_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Equatorial crossings by Jacobi amplitude (equator_cf.cuh), one ray per
+// thread on the device and the same function on the host.
+namespace {
+constexpr int kDiskXMax = 16;
+
+__host__ __device__ inline void disk_crossings_one(int i, double a, const double* u0, const double* mu0,
+                                                   const double* l, const double* q2, const double* su,
+                                                   const double* sm, double u_far, double u_lo, double u_hi, int K,
+                                                   double* xu, double* xphi, int32_t* nx, int32_t* status) {
+    double u[kDiskXMax];
+    int32_t br[kDiskXMax];
+    const np::gkcf::EqX o = np::gkcf::equator_crossings(a, l[i], q2[i], u0[i], mu0[i], su[i], sm[i], u_far, u_lo,
+                                                         u_hi, K, u, nullptr, br);
+    for (int k = 0; k < K; ++k) xu[(long long)i * K + k] = k < o.n ? u[k] : 0.0;
+    if (xphi) {
+        double ph[kDiskXMax];
+        if (o.n > 0) np::gkcf::crossing_phi(a, l[i], q2[i], u0[i], mu0[i], su[i], sm[i], u_far, o.n, u, br, ph);
+        for (int k = 0; k < K; ++k) xphi[(long long)i * K + k] = k < o.n ? ph[k] : 0.0;
+    }
+    nx[i] = o.n;
+    if (status) status[i] = o.status;
+}
+
+__global__ void disk_crossings_kernel(int n, double a, const double* u0, const double* mu0, const double* l,
+                                      const double* q2, const double* su, const double* sm, double u_far, double u_lo,
+                                      double u_hi, int K, double* xu, double* xphi, int32_t* nx, int32_t* status) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) disk_crossings_one(i, a, u0, mu0, l, q2, su, sm, u_far, u_lo, u_hi, K, xu, xphi, nx, status);
+}
+
+int disk_crossings_check(int n, double a, double u_far, double u_lo, double u_hi, int K, const void* p0,
+                         const void* p1, const void* p2, const void* p3, const void* p4, const void* p5,
+                         const void* p6, const void* p7) {
+    if (n < 0 || K <= 0 || K > kDiskXMax) return gk_fail(NP_ERR_INVALID, "disk crossings: bad sizes (1 <= K <= 16)");
+    if (!(fabs(a) < 1.0)) return gk_fail(NP_ERR_INVALID, "spin must satisfy |a| < 1");
+    if (!(u_far >= 0.0) || !(u_lo <= u_hi)) return gk_fail(NP_ERR_INVALID, "disk crossings: bad u window");
+    if (n > 0 && (!p0 || !p1 || !p2 || !p3 || !p4 || !p5 || !p6 || !p7))
+        return gk_fail(NP_ERR_INVALID, "NULL argument");
+    return NP_OK;
+}
+}  // namespace
+
+extern "C" int np_geokerr_disk_crossings_device(int n, double a, const double* d_u0, const double* d_mu0,
+                                                const double* d_l, const double* d_q2, const double* d_su,
+                                                const double* d_sm, double u_far, double u_lo, double u_hi, int K,
+                                                double* d_xu, double* d_xphi, int32_t* d_nx, int32_t* d_status,
+                                                void* stream) {
+    int rc = disk_crossings_check(n, a, u_far, u_lo, u_hi, K, d_u0, d_mu0, d_l, d_q2, d_su, d_sm, d_xu, d_nx);
+    if (rc != NP_OK || n == 0) return rc;
+    disk_crossings_kernel<<<(n + 63) / 64, 64, 0, (cudaStream_t)stream>>>(n, a, d_u0, d_mu0, d_l, d_q2, d_su, d_sm,
+                                                                          u_far, u_lo, u_hi, K, d_xu, d_xphi, d_nx,
+                                                                          d_status);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return gk_fail(NP_ERR_KERNEL, "disk crossings: %s", cudaGetErrorString(e));
+    return NP_OK;
+}
+
+extern "C" int np_geokerr_disk_crossings_host(int n, double a, const double* u0, const double* mu0, const double* l,
+                                              const double* q2, const double* su, const double* sm, double u_far,
+                                              double u_lo, double u_hi, int K, double* xu, double* xphi, int32_t* nx,
+                                              int32_t* status) {
+    int rc = disk_crossings_check(n, a, u_far, u_lo, u_hi, K, u0, mu0, l, q2, su, sm, xu, nx);
+    if (rc != NP_OK) return rc;
+    for (int i = 0; i < n; ++i) disk_crossings_one(i, a, u0, mu0, l, q2, su, sm, u_far, u_lo, u_hi, K, xu, xphi, nx, status);
     return NP_OK;
 }

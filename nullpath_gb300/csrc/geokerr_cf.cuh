@@ -427,6 +427,61 @@ GKCF_HD void complex_poles(CfRay& R) {
     }
 }
 
+// Radial reductions of q2 > 0 (c4 = -a^2 q2 < 0), motion in [u1, u2] holding
+// u0 with the turning point u2 ahead of an ingoing ray: kind, roots, m, mc
+// and g of R; false when u0 is outside that interval.
+// Four real roots u1 < u2 < u3 < u4:
+GKCF_HD bool reduce_r4(const double* rr, double c4, double u0, CfRay& R) {
+    const double u1 = rr[0], u2 = rr[1], u3 = rr[2], u4 = rr[3];
+    if (!(u1 < u0 && u0 <= u2) || !(u2 < u3)) return false;
+    R.kind = kR4;
+    for (int i = 0; i < 4; ++i) R.r[i] = rr[i];
+    R.m = (u2 - u1) * (u4 - u3) / ((u3 - u1) * (u4 - u2));
+    R.mc = (u3 - u2) * (u4 - u1) / ((u3 - u1) * (u4 - u2));
+    R.g = 2.0 / std::sqrt(-c4 * (u3 - u1) * (u4 - u2));
+    return true;
+}
+
+// two real roots u1 < u2 and the complex pair rho +- i sigma:
+GKCF_HD bool reduce_r2c(const double* rr, double rho, double sigma, double c4, double u0, CfRay& R) {
+    const double u1 = rr[0], u2 = rr[1];
+    if (!(u1 < u0 && u0 <= u2)) return false;
+    R.kind = kR2C;
+    const double A = std::sqrt((u2 - rho) * (u2 - rho) + sigma * sigma);
+    const double Bq = std::sqrt((u1 - rho) * (u1 - rho) + sigma * sigma);
+    R.r[0] = u1; R.r[1] = u2; R.r[2] = A; R.r[3] = Bq;
+    const double mdirect = ((u2 - u1) * (u2 - u1) - (A - Bq) * (A - Bq)) / (4.0 * A * Bq);
+    // 1 - m = (A + B - (u2 - u1))(A + B + u2 - u1) / (4 A B), with
+    // A - |u2 - rho| = sigma^2 / (A + |u2 - rho|) (likewise B)
+    // (|u2 - rho| + |rho - u1| - (u2 - u1) is 0 for rho in [u1, u2], and
+    // twice the distance to the interval outside it: set, not rounded)
+    const double d2 = std::fabs(u2 - rho), d1 = std::fabs(rho - u1);
+    const double outside = rho < u1 ? 2.0 * (u1 - rho) : (rho > u2 ? 2.0 * (rho - u2) : 0.0);
+    const double gap = sigma * sigma / (A + d2) + sigma * sigma / (Bq + d1) + outside;
+    R.mc = gap * (A + Bq + (u2 - u1)) / (4.0 * A * Bq);
+    R.m = R.mc < 0.5 ? 1.0 - R.mc : mdirect;
+    R.g = 2.0 / std::sqrt(-c4 * A * Bq);
+    return true;
+}
+
+// Roots of GEOKERR's polar potential M(mu) = q2 + (a^2 - l^2 - q2) mu^2 -
+// a^2 mu^4 in mu^2, by the stable quadratic formula: mpos = mu+^2 and a2mneg
+// = a^2 mu-^2 (carried with its factor a^2 so that a = 0 needs no special
+// case); a root that the start violates by rounding moves to mu0^2.
+GKCF_HD void polar_roots(double a, double l, double q2, double mu0, double& mpos, double& a2mneg) {
+    const double a2 = a * a, b = a2 - (q2 + l * l);
+    const double yy = -0.5 * (b + (b >= 0.0 ? 1.0 : -1.0) * std::sqrt(b * b + 4.0 * q2 * a2));
+    if (b < 0.0) { a2mneg = -yy; mpos = q2 / yy; }
+    else { a2mneg = a2 * q2 / yy; mpos = -yy / a2; }
+    if (mpos > 1.0) mpos = 1.0;
+    if (a2mneg < 0.0 || a2 == 0.0) {
+        if (std::sqrt(mpos) < mu0) mpos = mu0 * mu0;
+    } else {
+        if (a2mneg > a2 * mu0 * mu0) a2mneg = a2 * mu0 * mu0;
+        if (mu0 * mu0 > mpos) mpos = mu0 * mu0;
+    }
+}
+
 // Per-ray setup; kind = kFallback when the ray is outside the closed forms
 // (q2 = 0, a = 0, a motion between the middle roots of four real ones, a
 // double root, a polar orbit through the pole with l != 0).
@@ -448,34 +503,12 @@ GKCF_HD void setup(double a, double l, double q2, double u0, double uf, double m
     const double uplus = 1.0 / R.rp;
     double uturn = INFINITY;      // radial turning point ahead of an ingoing ray
     if (nr == 4 && c[4] < 0.0) {
-        const double u1 = rr[0], u2 = rr[1], u3 = rr[2], u4 = rr[3];
-        if (!(u1 < u0 && u0 <= u2) || !(u2 < u3)) return;
-        R.kind = kR4;
-        for (int i = 0; i < 4; ++i) R.r[i] = rr[i];
-        R.m = (u2 - u1) * (u4 - u3) / ((u3 - u1) * (u4 - u2));
-        R.mc = (u3 - u2) * (u4 - u1) / ((u3 - u1) * (u4 - u2));
-        R.g = 2.0 / std::sqrt(-c[4] * (u3 - u1) * (u4 - u2));
-        uturn = u2;
+        if (!reduce_r4(rr, c[4], u0, R)) return;
+        uturn = R.r[1];
     } else if (nr == 2 && sigma > 0.0 && c[4] < 0.0) {
-        const double u1 = rr[0], u2 = rr[1];
-        if (!(u1 < u0 && u0 <= u2)) return;
-        R.kind = kR2C;
-        const double A = std::sqrt((u2 - rho) * (u2 - rho) + sigma * sigma);
-        const double Bq = std::sqrt((u1 - rho) * (u1 - rho) + sigma * sigma);
-        R.r[0] = u1; R.r[1] = u2; R.r[2] = A; R.r[3] = Bq;
-        const double mdirect = ((u2 - u1) * (u2 - u1) - (A - Bq) * (A - Bq)) / (4.0 * A * Bq);
-        // 1 - m = (A + B - (u2 - u1))(A + B + u2 - u1) / (4 A B), with
-        // A - |u2 - rho| = sigma^2 / (A + |u2 - rho|) (likewise B)
-        // (|u2 - rho| + |rho - u1| - (u2 - u1) is 0 for rho in [u1, u2], and
-        // twice the distance to the interval outside it: set, not rounded)
-        const double d2 = std::fabs(u2 - rho), d1 = std::fabs(rho - u1);
-        const double outside = rho < u1 ? 2.0 * (u1 - rho) : (rho > u2 ? 2.0 * (rho - u2) : 0.0);
-        const double gap = sigma * sigma / (A + d2) + sigma * sigma / (Bq + d1) + outside;
-        R.mc = gap * (A + Bq + (u2 - u1)) / (4.0 * A * Bq);
-        R.m = R.mc < 0.5 ? 1.0 - R.mc : mdirect;
-        R.g = 2.0 / std::sqrt(-c[4] * A * Bq);
+        if (!reduce_r2c(rr, rho, sigma, c[4], u0, R)) return;
         complex_poles(R);
-        uturn = u2;
+        uturn = R.r[1];
     } else if (nr == 2 && sigma > 0.0 && c[4] > 0.0) {
         // Motion above both real roots (Byrd & Friedman 260.00):
         // cn w = ((u - r1) A - (u - r2) B) / ((u - r1) A + (u - r2) B),
@@ -652,11 +685,10 @@ struct Point {
     int32_t tpm, tpr;
 };
 
-// Sample k (1-based, k <= R.last) of a ray set up above.
-GKCF_HD Point sample(const CfRay& R, int k) {
+// The point at u = ut of a ray set up above, before (branch2 = false) or
+// after its radial turning point.
+GKCF_HD Point point_at(const CfRay& R, double ut, bool branch2) {
     Point P;
-    const bool branch2 = k > R.kmax;
-    const double ut = branch2 ? 2.0 * R.ub - (R.u0 + (k - R.offset) * R.du) : R.u0 + (k - R.offset) * R.du;
     double Gk[7], I[7];
     radial_G(R, ut, Gk);
     for (int i = 0; i < 7; ++i) {
@@ -682,6 +714,13 @@ GKCF_HD Point sample(const CfRay& R, int k) {
     P.tpm = (int32_t)(std::floor(w / Kt) - std::floor(R.w0 / Kt));
     P.tpr = branch2 ? 1 : 0;
     return P;
+}
+
+// Sample k (1-based, k <= R.last) of a ray set up above.
+GKCF_HD Point sample(const CfRay& R, int k) {
+    const bool branch2 = k > R.kmax;
+    const double ut = branch2 ? 2.0 * R.ub - (R.u0 + (k - R.offset) * R.du) : R.u0 + (k - R.offset) * R.du;
+    return point_at(R, ut, branch2);
 }
 
 }  // namespace gkcf

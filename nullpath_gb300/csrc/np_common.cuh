@@ -68,6 +68,7 @@ struct SceneDev {
     float atol78_f;            // atol of the FP32 7(8) steps: the scene's, at least 1e-9 M (FP32 resolution)
     int cert_capture;          // 7(8) path: rays certified to fall in end at the horizon band (disk outside it)
     int island_df;             // 7(8) path: FP64-class steps in double-float arithmetic
+    int crit_cf;               // mixed path: near-critical rays in closed form (Mino-time solution)
     float a_hl[2], M_hl[2], rp_hl[2], rm_hl[2];   // a, M, r_+, r_- as double-float pairs
     float rtol64_f, atol64_f;  // tolerances of the near-critical rays (double-float arithmetic)
     int island_batch;

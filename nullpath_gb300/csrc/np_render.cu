@@ -24,6 +24,7 @@
 #include "tracer_fp64.cuh"
 #include "tracer_mixed.cuh"
 #include "tracer_df.cuh"
+#include "equator_cf.cuh"
 
 using namespace np;
 
@@ -89,6 +90,7 @@ struct Counters {
     unsigned long long work2;       // next deferred-list index
     unsigned long long deferred;    // deferred-list length
     unsigned long long rays, steps, fp64_steps, evals;
+    unsigned long long closed_form;  // near-critical rays solved in closed form
 };
 
 // ---------------------------------------------------------------------------
@@ -220,6 +222,7 @@ int prepare_scene(const np_scene_t& sc, SceneDev& d) {
         d.atol78_f = (float)std::fmax(d.atol, 1e-9 * d.M);
         d.cert_capture = !d.disk_on || d.rin > d.r_plus + kHorizonBand * d.M;
         d.island_df = sc.island_arith == NP_ISLAND_ARITH_DF;
+        d.crit_cf = sc.critical_solver == NP_CRITICAL_CLOSED_FORM;
         auto split = [](double x, float* o) { o[0] = (float)x; o[1] = (float)(x - (double)o[0]); };
         split(d.a, d.a_hl); split(d.M, d.M_hl); split(d.r_plus, d.rp_hl); split(d.r_minus, d.rm_hl);
         d.rtol64_f = (float)d.rtol64; d.atol64_f = (float)std::fmax(d.atol, 1e-14 * d.M);
@@ -459,7 +462,7 @@ __device__ __forceinline__ void trace_deferred(const SceneDev& s, const InitSoA&
         if (need && !drained) {
             long long idx = warp_take(q, need, &ctr->work2, D, 4);
             drained = q.base >= D;
-            if (!have && idx >= 0) {
+            if (!have && idx >= 0 && soa.flag[soa.list[idx]] == 1) {
                 item = soa.list[idx];
                 int x, y; uint32_t sid;
                 ray_coords(s, item, p, sl, x, y, sid);
@@ -501,6 +504,82 @@ __device__ __forceinline__ void trace_deferred(const SceneDev& s, const InitSoA&
                 have = false;
             }
         }
+    }
+}
+
+// A near-critical ray in closed form (equator_cf.cuh): Carter's constants of
+// the camera momentum in the units E = M = 1, the disk crossings of the
+// Mino-time solution (radii in [rin, rout], at most max_orders), capture or
+// escape, and the closest approach.  false when the ray is outside the
+// closed forms (it is then integrated).
+struct CritCF {
+    int status, orders;
+    float disk[3];
+    double first_r, min_r;
+};
+
+__device__ __forceinline__ bool crit_constants(const SceneDev& s, const Momentum& m, double& l, double& q2,
+                                               double& su, double& sm) {
+    const double E = -m.pt, L = m.pph;
+    const double Q = m.pth * m.pth + s.cos_cam * s.cos_cam * (L * L / (s.sin_cam * s.sin_cam) - s.a * s.a * E * E);
+    l = L / (E * s.M);
+    q2 = Q / (E * E * s.M * s.M);
+    su = m.pr < 0.0 ? 1.0 : -1.0;
+    sm = m.pth > 0.0 ? -1.0 : 1.0;
+    return E > 0.0;
+}
+
+__device__ __forceinline__ bool crit_cf_solve(const SceneDev& s, const Momentum& m, CritCF& o) {
+    double l, q2, su, sm;
+    if (!crit_constants(s, m, l, q2, su, sm)) return false;
+    double xu[8];
+    const int kmax = s.disk_on ? min(s.max_orders, 8) : 0;
+    const gkcf::EqX x = gkcf::equator_crossings(s.a / s.M, l, q2, s.M / s.r_cam, s.cos_cam, su, sm, s.M / s.r_far,
+                                                s.M / s.rout, s.M / s.rin, kmax, xu, nullptr, nullptr);
+    if (x.status < 0) return false;
+    o.status = x.status;
+    o.orders = 0;
+    o.disk[0] = o.disk[1] = o.disk[2] = 0.0f;
+    o.first_r = 0.0;
+    for (int k = 0; k < x.n; ++k) {
+        const double rc = s.M / xu[k];
+        const float g = (float)doppler_g(rc, m.pt, m.pph, s.M, s.a);
+        shade_disk((float)rc, g, s.qf, s.gain, o.disk);
+        if (o.orders == 0) o.first_r = rc;
+        o.orders++;
+    }
+    o.min_r = x.status == 1 ? s.r_plus : (x.u_turn > 0.0 ? s.M / x.u_turn : s.r_cam);
+    return true;
+}
+
+// Near-critical rays of the deferred list in closed form, one ray per thread
+// (the FP64 work of a ray is a few hundred operations and a few Carlson
+// integrals, against thousands of FP64 integration steps).  A solved ray
+// gets flag 2 and is passed over by the tracer's FP64 warps; a ray outside
+// the closed forms keeps flag 1 and is integrated there.
+__global__ void __launch_bounds__(128)
+critical_cf_kernel(const SceneDev s, InitSoA soa, float* __restrict__ srgb, float* __restrict__ rcross,
+                   Counters* __restrict__ ctr, unsigned long long list_cap) {
+    const long long D = (long long)min(ctr->deferred, list_cap);
+    unsigned long long solved = 0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < D;
+         i += (long long)gridDim.x * blockDim.x) {
+        const long long item = soa.list[i];
+        long long p; int sl, x, y; uint32_t sid;
+        ray_coords(s, item, p, sl, x, y, sid);
+        const CamDir dir = camera_dir(s, x, y, sid, false, 0.0, 0.0);
+        CritCF o;
+        if (!crit_cf_solve(s, camera_momentum(s, dir), o)) continue;
+        float col[3];
+        sample_colour(s, o.status == 1, o.orders, o.disk, (float)o.min_r, dir.cam_y, col);
+        write_sample(s, srgb, rcross, p, sl, col, o.first_r);
+        soa.flag[item] = 2;
+        solved++;
+    }
+    for (int o = 16; o > 0; o >>= 1) solved += __shfl_down_sync(0xffffffffu, solved, o);
+    if ((threadIdx.x & 31) == 0 && solved) {
+        atomicAdd(&ctr->closed_form, solved);
+        atomicAdd(&ctr->rays, solved);
     }
 }
 
@@ -609,6 +688,25 @@ __global__ void resolve_kernel(const float* __restrict__ srgb, float* __restrict
     }
 }
 
+// The first four equatorial crossings of a near-critical ray (any radius,
+// up to the ray's end) in closed form, with their azimuths: the report of
+// trace_rays_kernel for the rays the renderer solves in closed form.
+__device__ __forceinline__ bool crit_cf_cross(const SceneDev& s, const Momentum& m, double* xr, double* xphi,
+                                              int& ncross, int& st) {
+    double l, q2, su, sm;
+    if (!crit_constants(s, m, l, q2, su, sm)) return false;
+    double xu[4], ph[4];
+    int32_t xb[4];
+    const double a = s.a / s.M, u0 = s.M / s.r_cam, uf = s.M / s.r_far;
+    const gkcf::EqX x = gkcf::equator_crossings(a, l, q2, u0, s.cos_cam, su, sm, uf, 0.0, 1e300, 4, xu, nullptr, xb);
+    if (x.status < 0) return false;
+    if (x.n > 0) gkcf::crossing_phi(a, l, q2, u0, s.cos_cam, su, sm, uf, x.n, xu, xb, ph);
+    for (int j = 0; j < x.n; ++j) { xr[j] = s.M / xu[j]; xphi[j] = s.ph_cam + ph[j]; }
+    ncross = x.n;
+    st = x.status;
+    return true;
+}
+
 // Explicit rays (positions in continuous pixel coordinates), one per thread.
 // The mixed path takes its island steps immediately (no batching) and
 // traces near-critical rays with the FP64 Carter tracer, as the renderer does.
@@ -637,6 +735,9 @@ __global__ void trace_rays_kernel(const SceneDev s, int precision, int n, const 
         }
         for (int j = 0; j < 4; ++j) { xr[j] = R.xr[j]; xphi[j] = R.xphi[j]; }
         ncross = R.crossings; st = R.status;
+    } else if ((s.islands & kIslandCritical) && near_critical_screened(E, L, Q, s.a, s.M, s.r_plus, kCriticalDb) &&
+               s.crit_cf && crit_cf_cross(s, m, xr, xphi, ncross, st)) {
+        // solved in closed form
     } else if ((s.islands & kIslandCritical) && near_critical_screened(E, L, Q, s.a, s.M, s.r_plus, kCriticalDb)) {
         if (s.integrator == NP_INTEG_RKF78 && s.island_df) {
             DRay78df<true> R;
@@ -836,6 +937,14 @@ void launch_mixed(int minb, const SceneDev& s, const InitSoA& soa, float* srgb, 
     }
 }
 
+// The near-critical rays listed by ray_init_kernel, in closed form (a fixed
+// grid over the device-side list length).
+void launch_critical(const SceneDev& s, const InitSoA& soa, float* srgb, float* rc, Counters* ctr,
+                     unsigned long long list_cap, cudaStream_t st) {
+    if (!(s.islands & kIslandCritical) || !s.crit_cf) return;
+    critical_cf_kernel<<<np_device_sms() * 4, 128, 0, st>>>(s, soa, srgb, rc, ctr, list_cap);
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -918,6 +1027,8 @@ int np_scene_validate(const np_scene_t* s) {
     if (!(s->rtol_fp64 < 1.0) || !std::isfinite(s->rtol_fp64)) return fail(NP_ERR_INVALID, "Invalid FP64 tolerance.");
     if (s->island_arith != NP_ISLAND_ARITH_DF && s->island_arith != NP_ISLAND_ARITH_FP64)
         return fail(NP_ERR_INVALID, "Invalid island arithmetic.");
+    if (s->critical_solver != NP_CRITICAL_CLOSED_FORM && s->critical_solver != NP_CRITICAL_INTEGRATE)
+        return fail(NP_ERR_INVALID, "Invalid near-critical solver.");
     // non-finite values in any other field would only surface as NaN images
     auto fin = [](double v) { return std::isfinite(v); };
     if (!fin(s->theta_deg) || !fin(s->phi_deg)) return fail(NP_ERR_INVALID, "Invalid camera angle.");
@@ -965,6 +1076,8 @@ int np_render_device(const np_scene_t* scene, int precision, float* d_rgb, float
         int ib = (int)std::min<long long>((s.total + 255) / 256, (long long)np_device_sms() * 8);
         ray_init_kernel<<<ib, 256, 0, st>>>(s, soa, sc->ctr);
         NP_CU(cudaGetLastError(), NP_ERR_KERNEL);
+        launch_critical(s, soa, sc->srgb, d_rcross, sc->ctr, (unsigned long long)s.total, st);
+        NP_CU(cudaGetLastError(), NP_ERR_KERNEL);
         if (stats) NP_CU(cudaEventRecord(sc->ev1, st), NP_ERR_KERNEL);
         launch_mixed(g_tune.min_blocks, s, soa, sc->srgb, d_rcross, d_inv3, sc->ctr, g_tune.chunk, st);
         NP_CU(cudaGetLastError(), NP_ERR_KERNEL);
@@ -991,6 +1104,7 @@ int np_render_device(const np_scene_t* scene, int precision, float* d_rgb, float
         stats->fp64_steps = sc->h_ctr->fp64_steps;
         stats->rhs_evals = sc->h_ctr->evals;
         stats->deferred_rays = precision == NP_PREC_MIXED ? sc->h_ctr->deferred : 0;
+        stats->closed_form_rays = sc->h_ctr->closed_form;
         stats->kernel_ms = ms;
         stats->init_ms = ms2;
     }
@@ -1187,6 +1301,8 @@ extern "C" int np_render_device_noalloc(const np_scene_t* scene, int precision, 
                     (unsigned char*)(base + kNaFlag), (long long*)(base + kNaList)};
         int ib = (int)std::min<long long>((s.total + 255) / 256, (long long)np_device_sms() * 8);
         ray_init_kernel<<<ib, 256, 0, st>>>(s, soa, ctr);
+        NP_CU(cudaGetLastError(), NP_ERR_KERNEL);
+        launch_critical(s, soa, srgb, d_rcross, ctr, (unsigned long long)s.total, st);
         NP_CU(cudaGetLastError(), NP_ERR_KERNEL);
         launch_mixed(g_tune.min_blocks, s, soa, srgb, d_rcross, nullptr, ctr, g_tune.chunk, st);
     }

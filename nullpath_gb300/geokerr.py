@@ -30,6 +30,8 @@ _PROTOS = {
     "geokerr_single_case_": (None, [V] * 13),
     "np_geokerr_camera_grid_device": (I, [D, D, I, I, D, D, D, D, D] + [V] * 6 + [V]),
     "np_geokerr_camera_grid_host": (I, [D, D, I, I, D, D, D, D, D] + [V] * 6),
+    "np_geokerr_disk_crossings_device": (I, [I, D] + [V] * 6 + [D, D, D, I] + [V] * 4 + [V]),
+    "np_geokerr_disk_crossings_host": (I, [I, D] + [V] * 6 + [D, D, D, I] + [V] * 4),
 }
 
 
@@ -183,6 +185,43 @@ def points_host(a, u0, uf, mu0, l, q2, su, sm, tpr=1, nup=32, offset=0.5):
     check(lib.np_geokerr_points_host(n, a, *[x.ctypes.data for x in ins], tpr, nup, offset,
                                      *[out[k].ctypes.data for k in ("u", "mu", "dt", "dphi", "lam", "tpm", "tpr", "n",
                                                                     "method")]))
+    return out
+
+
+def disk_crossings(a, u0, mu0, l, q2, su, sm, u_far, u_lo=0.0, u_hi=float("inf"), K=4, device=False, phi=True):
+    """Equatorial crossings by Jacobi amplitude (np_geokerr_disk_crossings_*):
+    the first K crossings with u in [u_lo, u_hi] up to the ray's end (the
+    horizon, or u_far after its turning point).  Returns dict xu[n][K],
+    xphi[n][K] (azimuth change from the start; when phi), nx[n] and
+    status[n] (0 leaves, 1 captured, -1 outside the closed forms), numpy
+    arrays on the host, CUDA tensors with device=True."""
+    lib = _lib()
+    if device:
+        import torch
+        dev = torch.device("cuda")
+        cv = lambda x: torch.as_tensor(np.broadcast_to(np.asarray(x, dtype=np.float64), np.shape(l)).copy(),
+                                       device=dev).contiguous()
+        ins = [cv(x) for x in (u0, mu0, l, q2, su, sm)]
+        n = ins[0].numel()
+        out = {"xu": torch.zeros((n, K), dtype=torch.float64, device=dev),
+               "nx": torch.zeros(n, dtype=torch.int32, device=dev),
+               "status": torch.zeros(n, dtype=torch.int32, device=dev)}
+        if phi:
+            out["xphi"] = torch.zeros((n, K), dtype=torch.float64, device=dev)
+        ptr = lambda t: V(t.data_ptr()) if t is not None else None
+        check(lib.np_geokerr_disk_crossings_device(n, a, *[ptr(x) for x in ins], u_far, u_lo, u_hi, K,
+                                                   ptr(out["xu"]), ptr(out.get("xphi")), ptr(out["nx"]),
+                                                   ptr(out["status"]), V(torch.cuda.current_stream().cuda_stream)))
+        return out
+    cv = lambda x: np.ascontiguousarray(np.broadcast_to(np.asarray(x, dtype=np.float64), np.shape(l)))
+    ins = [cv(x) for x in (u0, mu0, l, q2, su, sm)]
+    n = ins[0].size
+    out = {"xu": np.zeros((n, K)), "nx": np.zeros(n, dtype=np.int32), "status": np.zeros(n, dtype=np.int32)}
+    if phi:
+        out["xphi"] = np.zeros((n, K))
+    check(lib.np_geokerr_disk_crossings_host(n, a, *[x.ctypes.data for x in ins], u_far, u_lo, u_hi, K,
+                                             out["xu"].ctypes.data, out["xphi"].ctypes.data if phi else None,
+                                             out["nx"].ctypes.data, out["status"].ctypes.data))
     return out
 
 

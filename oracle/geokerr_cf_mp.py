@@ -349,3 +349,164 @@ def points_vortical(u0, uf, mu0, a, l, q2, su, sm, tpr=1, nup=32, offset=0.5):
         out["tpm"].append(int(mp.floor(w / Kth) - mp.floor(w0 / Kth)))
         out["tpr"].append(0)
     return out
+
+
+def crossings(u0, mu0, a, l, q2, su, sm, u_far, K=6, guess=None):
+    """Truth for the equatorial crossings of a q2 > 0 ray, independent of the
+    Legendre reductions: the Mino times lambda_j = ((2j + 1) K(k) - w0) /
+    omega of mu = mu+ cn(omega lambda + w0 | k) with mpmath's elliptic
+    functions; the radial Mino time lambda(u) = int du / sqrt(U) by
+    quadrature (u = u2 - t^2 near the turning point u2, breakpoints
+    geometric towards it), inverted at each lambda_j by Newton steps
+    (dlambda/du = 1/sqrt(U)) from `guess` (a list of u, one per crossing)
+    or from bisection; the azimuth change
+    dphi = d+ Ip + d- Im - l lambda + l int dw / (1 - mu^2) / omega by the same
+    quadratures.  The ray ends at the horizon (ingoing, no turning point
+    outside it) or at u_far after its turning point.  Returns
+    (status, [u_j], [dphi_j]) for the first K crossings (status 0: leaves,
+    1: captured), or None outside this case."""
+    a, l, q2, u0, mu0, u_far = (mp.mpf(x) for x in (a, l, q2, u0, mu0, u_far))
+    if not (q2 > 0) or a == 0:
+        return None
+    Bc, Kc = a * a - l * l - q2, (l - a) ** 2 + q2
+    c = [mp.mpf(1), mp.mpf(0), Bc, 2 * Kc, -a * a * q2]
+    U = lambda u: c[0] + c[2] * u ** 2 + c[3] * u ** 3 + c[4] * u ** 4
+    roots = mp.polyroots(c[::-1], maxsteps=400, extraprec=400)
+    real = sorted(mp.re(r) for r in roots if abs(mp.im(r)) < mp.mpf(10) ** -30)
+    above = [r for r in real if r >= u0]
+    below = [r for r in real if r < u0]
+    if not below:
+        return None
+    u2 = above[0] if above else mp.inf
+    sq = mp.sqrt(1 - a * a)
+    rp, rm = 1 + sq, a * a / (1 + sq)
+    uplus = 1 / rp
+    turns = su > 0 and u2 < uplus
+    # the nearest complex root or the second real root bounds the peak of
+    # 1/sqrt(U) at u2: breakpoints geometric in the distance to u2
+    near = [abs(r - u2) for r in roots if abs(r - u2) > mp.mpf(10) ** -30] if turns else []
+    width = min(near) if near else mp.mpf(1)
+    # U(u) = (u - u2) Q(u), Q by synthetic division
+    b3 = c[4]
+    b2 = c[3] + u2 * b3 if turns else 0
+    b1 = c[2] + u2 * b2 if turns else 0
+    b0 = c[1] + u2 * b1 if turns else 0
+    Q = lambda u: ((b3 * u + b2) * u + b1) * u + b0
+
+    cplx = [r for r in roots if mp.im(r) > mp.mpf(10) ** -30]
+
+    def open_int(f, ua, ub):
+        """int_ua^ub f(u) du / sqrt(U) away from real roots: breakpoints
+        geometric towards the real part of a complex pair inside the range
+        (1/sqrt(U) peaks there with width of its imaginary part)."""
+        pts = [ua, ub]
+        for z in cplx:
+            rho, sig = mp.re(z), mp.im(z)
+            if ua < rho < ub:
+                pts.append(rho)
+                s = sig / 4
+                while rho - s > ua or rho + s < ub:
+                    for x in (rho - s, rho + s):
+                        if ua < x < ub:
+                            pts.append(x)
+                    s *= 4
+        return mp.quad(lambda x: f(x) / mp.sqrt(U(x)), sorted(set(pts)))
+
+    def lam_int(f, ua, ub):
+        """int_ua^ub f(u) du / sqrt(U), ua <= ub <= u2."""
+        if ub <= ua:
+            return mp.mpf(0)
+        if not turns:
+            return open_int(f, ua, ub)
+        # u = u2 - t^2 removes the square-root zero of U = (u - u2) Q(u) at u2
+        ta, tb = mp.sqrt(u2 - ub), mp.sqrt(u2 - ua)
+        g = lambda t: 2 * f(u2 - t * t) / mp.sqrt(-Q(u2 - t * t))
+        pts = [ta]
+        s = mp.sqrt(width) / 4
+        while s < tb:
+            if s > ta:
+                pts.append(s)
+            s *= 4
+        pts.append(tb)
+        return mp.quad(g, pts)
+
+    one = lambda x: mp.mpf(1)
+    fp = lambda x: 1 / (1 - rp * x)
+    fm = lambda x: 1 / (1 - rm * x)
+    if su > 0:
+        if turns:
+            lam_t = lam_int(one, u0, u2)
+            lam_end = lam_t + lam_int(one, u_far, u2)
+            status = 0
+        else:
+            lam_t = None
+            lam_end = open_int(one, u0, uplus)
+            status = 1
+    else:
+        lam_t, status = None, 0
+        lam_end = open_int(one, u_far, u0)
+    # polar motion
+    mpos, a2mneg = _polar_roots(a, l, q2, mu0)
+    mp_ = mp.sqrt(mpos)
+    om = mp.sqrt(a * a * mpos - a2mneg)
+    mth = a * a * mpos / (om * om)
+    Kth = mp.ellipk(mth)
+    c0 = max(mp.mpf(-1), min(mp.mpf(1), mu0 / mp_))
+    w0 = -(1 if sm >= 0 else -1) * mp.ellipf(mp.acos(c0), mth)
+    cn = lambda w: mp.ellipfun('cn', w, m=mth)
+
+    def lam_of(u, out):
+        """Mino time at u on the branch before (out = False) or after the
+        turning point, and its derivative in u."""
+        if su > 0 and not out:
+            return lam_int(one, u0, u)
+        if su > 0:
+            return lam_t + lam_int(one, u, u2)
+        return open_int(one, u, u0)
+
+    xs, phis = [], []
+    j = -2
+    while len(xs) < K and j < 256:
+        lam = ((2 * j + 1) * Kth - w0) / om
+        j += 1
+        if not (lam > 0):
+            continue
+        if not (lam < lam_end):
+            break
+        out = turns and lam > lam_t
+        lo, hi = ((u0, u2) if not out else (u_far, u2)) if su > 0 and turns else \
+            ((u0, uplus) if su > 0 else (u_far, u0))
+        sgn = 1 if (su > 0 and not out) else -1          # dlambda/du sign
+        u = mp.mpf(guess[len(xs)]) if guess is not None and len(xs) < len(guess) else (lo + hi) / 2
+        for _ in range(60):
+            f = lam_of(u, out) - lam
+            if (f > 0) == (sgn > 0):
+                hi = u
+            else:
+                lo = u
+            un = u - sgn * f * mp.sqrt(U(u))
+            if not (lo < un < hi):
+                un = (lo + hi) / 2
+            done = abs(un - u) < mp.mpf(10) ** -32 * abs(u)
+            u = un
+            if done:
+                break
+        xs.append(u)
+        # azimuth: radial parts by quadrature along the path, polar by quadrature in w
+        if su > 0 and not out and turns:
+            ip, im = lam_int(fp, u0, u), lam_int(fm, u0, u)
+        elif su > 0 and not out:
+            ip, im = open_int(fp, u0, u), open_int(fm, u0, u)
+        elif su > 0:
+            ip = lam_int(fp, u0, u2) + lam_int(fp, u, u2)
+            im = lam_int(fm, u0, u2) + lam_int(fm, u, u2)
+        else:
+            ip, im = open_int(fp, u, u0), open_int(fm, u, u0)
+        w = om * lam + w0
+        pts = sorted(set([w0] + [k * Kth for k in range(int(mp.floor(w0 / Kth)) + 1, int(mp.floor(w / Kth)) + 1)] +
+                         [w]))
+        inv = mp.quad(lambda v: 1 / (1 - mpos * cn(v) ** 2), pts) / om
+        dp = a * (2 * rp - a * l) / (rp * (rp - rm))
+        dm = a * (2 * rm - a * l) / (rm * (rm - rp))
+        phis.append(dp * ip + dm * im - l * lam + l * inv)
+    return status, xs, phis

@@ -104,7 +104,8 @@ def test_double_float_islands_match_fp64_islands(cuda):
     sequences, so they differ at the FP32 rounding floor of the path), and
     the bar against the Mino-time solver holds for both."""
     from nullpath_gb300 import accuracy
-    sc = npx.accurate_scene(npx.benchmark_scene()).replace(islands=npx.NP_ISLANDS_ALL)
+    sc = npx.accurate_scene(npx.benchmark_scene()).replace(islands=npx.NP_ISLANDS_ALL,
+                                                           critical_solver=npx.NP_CRITICAL_INTEGRATE)
     rng = np.random.default_rng(9)
     px, py = rng.uniform(0, sc.width, 6000), rng.uniform(0, sc.height, 6000)
     a = npx.trace_rays(sc, px, py, "mixed")["cross"].cpu().numpy()[:, 0, 0]
