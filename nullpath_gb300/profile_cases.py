@@ -16,6 +16,9 @@ Cases (kernel names in parentheses):
     adjoint         differentiable render 128x128x2, FP32, K = 64
                     (adj_forward_kernel<float>, adj_backward_kernel<float>)
     batch           16 uneven scenes in one persistent launch (batch_mixed_kernel)
+    critical        near-critical rays in closed form: 512x512x16 at a = 0.998
+                    with critical-curve sampling, mixed 7(8) path, default
+                    islands (critical_cf_kernel; render_mixed_kernel<4, 1>)
     geokerr         GEOKERR camera grid 128x128, 32 points per geodesic, closed
                     form (cf_setup_kernel, cf_points_kernel, cf_fallback_kernel)
     geokerr_taylor  the same grid on the Taylor solver (geokerr_points_kernel)
@@ -45,6 +48,14 @@ def _mixed(reps, path):
     import nullpath_gb300 as npx
     base = npx.benchmark_scene(width=640, height=360, spp=4)
     sc = npx.accurate_scene(base) if path == "rkf78" else base.replace(islands=npx.NP_ISLANDS_ALL)
+    for _ in range(reps + 1):
+        npx.render(sc, "mixed")
+
+
+def _critical(reps):
+    import nullpath_gb300 as npx
+    base = npx.benchmark_scene(width=512, height=512, spp=16, spin=0.998).replace(jitter=npx.NP_JITTER_CRITICAL)
+    sc = npx.accurate_scene(base)
     for _ in range(reps + 1):
         npx.render(sc, "mixed")
 
@@ -92,7 +103,7 @@ def _carlson(reps):
         carlson.evaluate(kinds, x, y, z, p)
 
 
-CASES = {"fp64_rk4": _fp64_rk4, "fp64_research": _fp64_research,
+CASES = {"fp64_rk4": _fp64_rk4, "fp64_research": _fp64_research, "critical": _critical,
          "mixed_rk4": lambda r: _mixed(r, "rk4"), "mixed_rkf78": lambda r: _mixed(r, "rkf78"),
          "adjoint": _adjoint, "batch": _batch, "geokerr": _geokerr,
          "geokerr_taylor": lambda r: _geokerr(r, "taylor"), "carlson": _carlson}
