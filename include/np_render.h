@@ -178,8 +178,7 @@ typedef struct np_render_stats {
     uint64_t rhs_evals;           /* right-hand-side evaluations */
     uint64_t deferred_rays;       /* near-critical rays (mixed path) */
     double kernel_ms;             /* device time of the tracer kernel */
-    double init_ms;               /* device time of ray generation and the near-critical
-                                     rays' closed form (mixed path) */
+    double init_ms;               /* device time of the ray-generation kernel (mixed path) */
     uint64_t closed_form_rays;    /* near-critical rays solved in closed form (mixed path) */
 } np_render_stats_t;
 
@@ -339,7 +338,10 @@ int np_measure_fma_peak(int which, double* tflops);
  * orders traced by one persistent launch of the mixed path over one device
  * ray queue; the pass (counter reset, ray generation, tracing, resolve) is
  * captured into a CUDA graph on the first np_batch_run with use_graph = 1
- * and replayed afterwards.  Only NP_PREC_MIXED is accepted.  Outputs stay in
+ * and replayed afterwards.  Only NP_PREC_MIXED with the RK4 and step-doubling
+ * integrators is accepted (NP_INTEG_RKF78 scenes are refused: the embedded
+ * 7(8) tracer runs one scene per launch); near-critical rays follow each
+ * scene's critical_solver.  Outputs stay in
  * the batch: np_batch_scene_output returns device pointers to scene i's
  * planar [3][H][W] image and [H][W] first-crossing radii. */
 typedef struct np_batch np_batch_t;
@@ -350,6 +352,7 @@ typedef struct np_batch_stats {
     double total_ms;            /* CUDA-event time of the whole pass */
     double scene_ms_p50, scene_ms_p99, scene_ms_max;   /* scene completion after ray generation starts */
     int32_t block, min_blocks, chunk, island_batch;    /* launch setting used */
+    uint64_t closed_form_rays;  /* near-critical rays solved in closed form */
 } np_batch_stats_t;
 
 typedef struct np_batch_tune {

@@ -22,7 +22,8 @@ class BatchStats(C.Structure):
     _fields_ = [("scenes", C.c_int32), ("rays", C.c_uint64), ("steps", C.c_uint64), ("fp64_steps", C.c_uint64),
                 ("deferred_rays", C.c_uint64), ("total_ms", C.c_double), ("scene_ms_p50", C.c_double),
                 ("scene_ms_p99", C.c_double), ("scene_ms_max", C.c_double), ("block", C.c_int32),
-                ("min_blocks", C.c_int32), ("chunk", C.c_int32), ("island_batch", C.c_int32)]
+                ("min_blocks", C.c_int32), ("chunk", C.c_int32), ("island_batch", C.c_int32),
+                ("closed_form_rays", C.c_uint64)]
 
     def as_dict(self):
         return {f[0]: getattr(self, f[0]) for f in self._fields_}

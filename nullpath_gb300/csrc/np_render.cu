@@ -5,8 +5,9 @@
 //                        persistent, one ray per lane with per-lane refill.
 //   render_mixed_kernel  FP32/compensated Carter-form integrator with FP64
 //                        islands; near-critical rays are appended to a
-//                        deferred list and traced whole in FP64 by the
-//                        first warps of the same launch.
+//                        deferred list and solved by the first warps of the
+//                        same launch, in FP64 closed form (equator_cf.cuh)
+//                        or traced whole in FP64.
 //   resolve_kernel       sums the per-sample colours of a pass in sample
 //                        order into the planar image (progressive spp).
 //   trace_rays_kernel    explicit rays, per-ray crossing report.
@@ -302,18 +303,21 @@ __device__ __forceinline__ void write_sample(const SceneDev& s, float* srgb, flo
 }
 
 __device__ __forceinline__ void flush_counters(Counters* ctr, unsigned long long rays, unsigned long long steps,
-                                               unsigned long long f64, unsigned long long evals) {
+                                               unsigned long long f64, unsigned long long evals,
+                                               unsigned long long cf = 0) {
     for (int o = 16; o > 0; o >>= 1) {
         rays += __shfl_down_sync(0xffffffffu, rays, o);
         steps += __shfl_down_sync(0xffffffffu, steps, o);
         f64 += __shfl_down_sync(0xffffffffu, f64, o);
         evals += __shfl_down_sync(0xffffffffu, evals, o);
+        cf += __shfl_down_sync(0xffffffffu, cf, o);
     }
     if ((threadIdx.x & 31) == 0) {
         atomicAdd(&ctr->rays, rays);
         atomicAdd(&ctr->steps, steps);
         atomicAdd(&ctr->fp64_steps, f64);
         atomicAdd(&ctr->evals, evals);
+        if (cf) atomicAdd(&ctr->closed_form, cf);
     }
 }
 
@@ -443,13 +447,64 @@ template <int FAM> struct CritRay { using type = DRay<false>; };
 template <> struct CritRay<kFam78> { using type = DRay78<false>; };
 template <> struct CritRay<kFam78df> { using type = DRay78df<false>; };
 
-// Near-critical rays from the deferred list, traced whole in FP64 by one
-// warp until the list is drained (rays taken four at a time from work2).
+// A near-critical ray in closed form (equator_cf.cuh): Carter's constants of
+// the camera momentum in the units E = M = 1, the disk crossings of the
+// Mino-time solution (radii in [rin, rout], at most max_orders), capture or
+// escape, and the closest approach.  false when the ray is outside the
+// closed forms (it is then integrated).
+struct CritCF {
+    int status, orders;
+    float disk[3];
+    double first_r, min_r;
+};
+
+__device__ __forceinline__ bool crit_constants(const SceneDev& s, const Momentum& m, double& l, double& q2,
+                                               double& su, double& sm) {
+    const double E = -m.pt, L = m.pph;
+    const double Q = m.pth * m.pth + s.cos_cam * s.cos_cam * (L * L / (s.sin_cam * s.sin_cam) - s.a * s.a * E * E);
+    l = L / (E * s.M);
+    q2 = Q / (E * E * s.M * s.M);
+    su = m.pr < 0.0 ? 1.0 : -1.0;
+    sm = m.pth > 0.0 ? -1.0 : 1.0;
+    return E > 0.0;
+}
+
+// Not inlined: the single-scene and batched kernels call the same function,
+// so a ray gets the same bits from both, and the FP32 loops around the call
+// sites keep their own register allocation.
+__device__ __noinline__ bool crit_cf_solve(const SceneDev& s, const Momentum& m, CritCF& o) {
+    double l, q2, su, sm;
+    if (!crit_constants(s, m, l, q2, su, sm)) return false;
+    double xu[8];
+    const int kmax = s.disk_on ? min(s.max_orders, 8) : 0;
+    const gkcf::EqX x = gkcf::equator_crossings(s.a / s.M, l, q2, s.M / s.r_cam, s.cos_cam, su, sm, s.M / s.r_far,
+                                                s.M / s.rout, s.M / s.rin, kmax, xu, nullptr, nullptr);
+    if (x.status < 0) return false;
+    o.status = x.status;
+    o.orders = 0;
+    o.disk[0] = o.disk[1] = o.disk[2] = 0.0f;
+    o.first_r = 0.0;
+    for (int k = 0; k < x.n; ++k) {
+        const double rc = s.M / xu[k];
+        const float g = (float)doppler_g(rc, m.pt, m.pph, s.M, s.a);
+        shade_disk((float)rc, g, s.qf, s.gain, o.disk);
+        if (o.orders == 0) o.first_r = rc;
+        o.orders++;
+    }
+    o.min_r = x.status == 1 ? s.r_plus : (x.u_turn > 0.0 ? s.M / x.u_turn : s.r_cam);
+    return true;
+}
+
+// Near-critical rays from the deferred list, one per lane until the list is
+// drained (rays taken four at a time from work2): solved in closed form
+// (crit_cf_solve) when the scene asks for it and the ray is inside the
+// closed forms, else traced whole in FP64.
 template <int FAM>
 __device__ __forceinline__ void trace_deferred(const SceneDev& s, const InitSoA& soa, float* __restrict__ srgb,
                                                float* __restrict__ rcross, Counters* __restrict__ ctr, long long D,
                                                unsigned long long& n_rays, unsigned long long& n_steps,
-                                               unsigned long long& n_f64, unsigned long long& n_evals) {
+                                               unsigned long long& n_f64, unsigned long long& n_evals,
+                                               unsigned long long& n_cf) {
     const unsigned FULL = 0xffffffffu;
     WarpQueue q{0, 0};
     bool drained = false, have = false;
@@ -462,22 +517,38 @@ __device__ __forceinline__ void trace_deferred(const SceneDev& s, const InitSoA&
         if (need && !drained) {
             long long idx = warp_take(q, need, &ctr->work2, D, 4);
             drained = q.base >= D;
-            if (!have && idx >= 0 && soa.flag[soa.list[idx]] == 1) {
+            if (!have && idx >= 0) {
                 item = soa.list[idx];
                 int x, y; uint32_t sid;
                 ray_coords(s, item, p, sl, x, y, sid);
                 float4 a = soa.a[item], b = soa.b[item];
                 cam_y = soa.cy[item];
-                if constexpr (FAM == kFam78df)
-                    dray78df_start(R, s, HiLo{b.x, b.y}, HiLo{b.z, b.w}, HiLo{a.x, a.y}, HiLo{a.z, a.w});
-                else if constexpr (FAM == kFam78)
-                    dray78_start(R, s, (double)b.x + (double)b.y, (double)b.z + (double)b.w,
-                                 (double)a.x + (double)a.y, (double)a.z + (double)a.w);
-                else
-                    dray_start(R, s, (double)b.x + (double)b.y, (double)b.z + (double)b.w,
-                               (double)a.x + (double)a.y, (double)a.z + (double)a.w);
-                have = true;
                 n_rays++;
+                bool solved = false;
+                if (s.crit_cf) {
+                    // the Mino-time solution in closed form; the ray is
+                    // integrated only when it is outside the closed forms
+                    const CamDir dir = camera_dir(s, x, y, sid, false, 0.0, 0.0);
+                    CritCF o;
+                    solved = crit_cf_solve(s, camera_momentum(s, dir), o);
+                    if (solved) {
+                        float col[3];
+                        sample_colour(s, o.status == 1, o.orders, o.disk, (float)o.min_r, cam_y, col);
+                        write_sample(s, srgb, rcross, p, sl, col, o.first_r);
+                        n_cf++;
+                    }
+                }
+                if (!solved) {
+                    if constexpr (FAM == kFam78df)
+                        dray78df_start(R, s, HiLo{b.x, b.y}, HiLo{b.z, b.w}, HiLo{a.x, a.y}, HiLo{a.z, a.w});
+                    else if constexpr (FAM == kFam78)
+                        dray78_start(R, s, (double)b.x + (double)b.y, (double)b.z + (double)b.w,
+                                     (double)a.x + (double)a.y, (double)a.z + (double)a.w);
+                    else
+                        dray_start(R, s, (double)b.x + (double)b.y, (double)b.z + (double)b.w,
+                                   (double)a.x + (double)a.y, (double)a.z + (double)a.w);
+                    have = true;
+                }
             }
         }
         if (!__any_sync(FULL, have)) break;
@@ -507,89 +578,13 @@ __device__ __forceinline__ void trace_deferred(const SceneDev& s, const InitSoA&
     }
 }
 
-// A near-critical ray in closed form (equator_cf.cuh): Carter's constants of
-// the camera momentum in the units E = M = 1, the disk crossings of the
-// Mino-time solution (radii in [rin, rout], at most max_orders), capture or
-// escape, and the closest approach.  false when the ray is outside the
-// closed forms (it is then integrated).
-struct CritCF {
-    int status, orders;
-    float disk[3];
-    double first_r, min_r;
-};
-
-__device__ __forceinline__ bool crit_constants(const SceneDev& s, const Momentum& m, double& l, double& q2,
-                                               double& su, double& sm) {
-    const double E = -m.pt, L = m.pph;
-    const double Q = m.pth * m.pth + s.cos_cam * s.cos_cam * (L * L / (s.sin_cam * s.sin_cam) - s.a * s.a * E * E);
-    l = L / (E * s.M);
-    q2 = Q / (E * E * s.M * s.M);
-    su = m.pr < 0.0 ? 1.0 : -1.0;
-    sm = m.pth > 0.0 ? -1.0 : 1.0;
-    return E > 0.0;
-}
-
-__device__ __forceinline__ bool crit_cf_solve(const SceneDev& s, const Momentum& m, CritCF& o) {
-    double l, q2, su, sm;
-    if (!crit_constants(s, m, l, q2, su, sm)) return false;
-    double xu[8];
-    const int kmax = s.disk_on ? min(s.max_orders, 8) : 0;
-    const gkcf::EqX x = gkcf::equator_crossings(s.a / s.M, l, q2, s.M / s.r_cam, s.cos_cam, su, sm, s.M / s.r_far,
-                                                s.M / s.rout, s.M / s.rin, kmax, xu, nullptr, nullptr);
-    if (x.status < 0) return false;
-    o.status = x.status;
-    o.orders = 0;
-    o.disk[0] = o.disk[1] = o.disk[2] = 0.0f;
-    o.first_r = 0.0;
-    for (int k = 0; k < x.n; ++k) {
-        const double rc = s.M / xu[k];
-        const float g = (float)doppler_g(rc, m.pt, m.pph, s.M, s.a);
-        shade_disk((float)rc, g, s.qf, s.gain, o.disk);
-        if (o.orders == 0) o.first_r = rc;
-        o.orders++;
-    }
-    o.min_r = x.status == 1 ? s.r_plus : (x.u_turn > 0.0 ? s.M / x.u_turn : s.r_cam);
-    return true;
-}
-
-// Near-critical rays of the deferred list in closed form, one ray per thread
-// (the FP64 work of a ray is a few hundred operations and a few Carlson
-// integrals, against thousands of FP64 integration steps).  A solved ray
-// gets flag 2 and is passed over by the tracer's FP64 warps; a ray outside
-// the closed forms keeps flag 1 and is integrated there.
-__global__ void __launch_bounds__(128)
-critical_cf_kernel(const SceneDev s, InitSoA soa, float* __restrict__ srgb, float* __restrict__ rcross,
-                   Counters* __restrict__ ctr, unsigned long long list_cap) {
-    const long long D = (long long)min(ctr->deferred, list_cap);
-    unsigned long long solved = 0;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < D;
-         i += (long long)gridDim.x * blockDim.x) {
-        const long long item = soa.list[i];
-        long long p; int sl, x, y; uint32_t sid;
-        ray_coords(s, item, p, sl, x, y, sid);
-        const CamDir dir = camera_dir(s, x, y, sid, false, 0.0, 0.0);
-        CritCF o;
-        if (!crit_cf_solve(s, camera_momentum(s, dir), o)) continue;
-        float col[3];
-        sample_colour(s, o.status == 1, o.orders, o.disk, (float)o.min_r, dir.cam_y, col);
-        write_sample(s, srgb, rcross, p, sl, col, o.first_r);
-        soa.flag[item] = 2;
-        solved++;
-    }
-    for (int o = 16; o > 0; o >>= 1) solved += __shfl_down_sync(0xffffffffu, solved, o);
-    if ((threadIdx.x & 31) == 0 && solved) {
-        atomicAdd(&ctr->closed_form, solved);
-        atomicAdd(&ctr->rays, solved);
-    }
-}
-
 template <int MINB, int FAM>
 __global__ void __launch_bounds__(kBlock, MINB)
 render_mixed_kernel(const SceneDev s, const InitSoA soa, float* __restrict__ srgb, float* __restrict__ rcross,
                     float* __restrict__ inv3, Counters* __restrict__ ctr, int chunk) {
     const unsigned FULL = 0xffffffffu;
     const SpaceK k{(float)s.a, (float)(s.a * s.a), (float)s.M, (float)s.r_plus, (float)s.r_minus};
-    unsigned long long n_rays = 0, n_steps = 0, n_f64 = 0, n_evals = 0;
+    unsigned long long n_rays = 0, n_steps = 0, n_f64 = 0, n_evals = 0, n_cf = 0;
 
     // ---- FP64 warps: near-critical rays.  Warp 0 of the first blocks starts
     // on them; every other warp joins once the FP32 queue is drained, so the
@@ -597,7 +592,7 @@ render_mixed_kernel(const SceneDev s, const InitSoA soa, float* __restrict__ srg
     const long long D = (long long)ctr->deferred;
     const int nd = D > 0 ? (int)min((long long)gridDim.x, (D + 3) / 4) : 0;
     if ((threadIdx.x >> 5) == 0 && (int)blockIdx.x < nd)
-        trace_deferred<FAM>(s, soa, srgb, rcross, ctr, D, n_rays, n_steps, n_f64, n_evals);
+        trace_deferred<FAM>(s, soa, srgb, rcross, ctr, D, n_rays, n_steps, n_f64, n_evals, n_cf);
 
     // ---- FP32 rays
     WarpQueue q{0, 0};
@@ -672,8 +667,8 @@ render_mixed_kernel(const SceneDev s, const InitSoA soa, float* __restrict__ srg
             have = false;
         }
     }
-    if (D > 0) trace_deferred<FAM>(s, soa, srgb, rcross, ctr, D, n_rays, n_steps, n_f64, n_evals);
-    flush_counters(ctr, n_rays, n_steps, n_f64, n_evals);
+    if (D > 0) trace_deferred<FAM>(s, soa, srgb, rcross, ctr, D, n_rays, n_steps, n_f64, n_evals, n_cf);
+    flush_counters(ctr, n_rays, n_steps, n_f64, n_evals, n_cf);
 }
 
 // rgb[c][p] (+)= sum_s srgb[s][c][p], summed in sample order.
@@ -937,14 +932,6 @@ void launch_mixed(int minb, const SceneDev& s, const InitSoA& soa, float* srgb, 
     }
 }
 
-// The near-critical rays listed by ray_init_kernel, in closed form (a fixed
-// grid over the device-side list length).
-void launch_critical(const SceneDev& s, const InitSoA& soa, float* srgb, float* rc, Counters* ctr,
-                     unsigned long long list_cap, cudaStream_t st) {
-    if (!(s.islands & kIslandCritical) || !s.crit_cf) return;
-    critical_cf_kernel<<<np_device_sms() * 4, 128, 0, st>>>(s, soa, srgb, rc, ctr, list_cap);
-}
-
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -1075,8 +1062,6 @@ int np_render_device(const np_scene_t* scene, int precision, float* d_rgb, float
         InitSoA soa{sc->soa_a, sc->soa_b, sc->soa_cy, sc->soa_flag, sc->list};
         int ib = (int)std::min<long long>((s.total + 255) / 256, (long long)np_device_sms() * 8);
         ray_init_kernel<<<ib, 256, 0, st>>>(s, soa, sc->ctr);
-        NP_CU(cudaGetLastError(), NP_ERR_KERNEL);
-        launch_critical(s, soa, sc->srgb, d_rcross, sc->ctr, (unsigned long long)s.total, st);
         NP_CU(cudaGetLastError(), NP_ERR_KERNEL);
         if (stats) NP_CU(cudaEventRecord(sc->ev1, st), NP_ERR_KERNEL);
         launch_mixed(g_tune.min_blocks, s, soa, sc->srgb, d_rcross, d_inv3, sc->ctr, g_tune.chunk, st);
@@ -1302,8 +1287,6 @@ extern "C" int np_render_device_noalloc(const np_scene_t* scene, int precision, 
         int ib = (int)std::min<long long>((s.total + 255) / 256, (long long)np_device_sms() * 8);
         ray_init_kernel<<<ib, 256, 0, st>>>(s, soa, ctr);
         NP_CU(cudaGetLastError(), NP_ERR_KERNEL);
-        launch_critical(s, soa, srgb, d_rcross, ctr, (unsigned long long)s.total, st);
-        NP_CU(cudaGetLastError(), NP_ERR_KERNEL);
         launch_mixed(g_tune.min_blocks, s, soa, srgb, d_rcross, nullptr, ctr, g_tune.chunk, st);
     }
     NP_CU(cudaGetLastError(), NP_ERR_KERNEL);
@@ -1380,7 +1363,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) batch_mixed_kernel(const BatchDev
     const unsigned FULL = 0xffffffffu;
     Counters* ctr = B.ctr;
     const InitSoA& soa = B.soa;
-    unsigned long long n_rays = 0, n_steps = 0, n_f64 = 0, n_evals = 0;
+    unsigned long long n_rays = 0, n_steps = 0, n_f64 = 0, n_evals = 0, n_cf = 0;
 
     // ---- FP64 warps: near-critical rays of every scene
     const long long D = (long long)min(ctr->deferred, B.list_cap);
@@ -1407,10 +1390,24 @@ __global__ void __launch_bounds__(BLOCK, MINB) batch_mixed_kernel(const BatchDev
                     ray_coords(*sp, item - B.ray_off[sc], p, sl, x, y, sid);
                     float4 a = soa.a[item], b = soa.b[item];
                     cam_y = soa.cy[item];
-                    dray_start(R, *sp, (double)b.x + (double)b.y, (double)b.z + (double)b.w,
-                               (double)a.x + (double)a.y, (double)a.z + (double)a.w);
-                    have = true;
                     n_rays++;
+                    bool solved = false;
+                    if (sp->crit_cf) {
+                        const CamDir dir = camera_dir(*sp, x, y, sid, false, 0.0, 0.0);
+                        CritCF o;
+                        solved = crit_cf_solve(*sp, camera_momentum(*sp, dir), o);
+                        if (solved) {
+                            float col[3];
+                            sample_colour(*sp, o.status == 1, o.orders, o.disk, (float)o.min_r, cam_y, col);
+                            batch_write(B, sc, *sp, p, sl, col, o.first_r);
+                            n_cf++;
+                        }
+                    }
+                    if (!solved) {
+                        dray_start(R, *sp, (double)b.x + (double)b.y, (double)b.z + (double)b.w,
+                                   (double)a.x + (double)a.y, (double)a.z + (double)a.w);
+                        have = true;
+                    }
                 }
             }
             if (!__any_sync(FULL, have)) break;
@@ -1485,7 +1482,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) batch_mixed_kernel(const BatchDev
             have = false;
         }
     }
-    flush_counters(ctr, n_rays, n_steps, n_f64, n_evals);
+    flush_counters(ctr, n_rays, n_steps, n_f64, n_evals, n_cf);
 }
 
 __global__ void batch_resolve_kernel(const BatchDev B) {
@@ -1610,6 +1607,8 @@ np_batch_t* np_batch_create(const np_scene_t* scenes, int n, int precision, void
     b->pix_off.assign((size_t)n + 1, 0);
     for (int i = 0; i < n; ++i) {
         int rc = check_path(scenes[i], NP_PREC_MIXED);
+        if (rc == NP_OK && scenes[i].integrator == NP_INTEG_RKF78)
+            rc = fail(NP_ERR_INVALID, "the 7(8) integrator runs one scene per launch (np_render_device)");
         if (rc == NP_OK) rc = prepare_scene(scenes[i], byidx[(size_t)i]);
         if (rc != NP_OK) {
             std::string msg = g_last_error;
@@ -1748,6 +1747,7 @@ int np_batch_run(np_batch_t* b, int use_graph, np_batch_stats_t* stats) {
         stats->steps = b->h_ctr->steps;
         stats->fp64_steps = b->h_ctr->fp64_steps;
         stats->deferred_rays = std::min<unsigned long long>(b->h_ctr->deferred, b->B.list_cap);
+        stats->closed_form_rays = b->h_ctr->closed_form;
         stats->total_ms = ms;
         stats->scene_ms_p50 = q(0.5);
         stats->scene_ms_p99 = q(0.99);

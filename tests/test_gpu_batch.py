@@ -34,6 +34,28 @@ def test_batch_matches_single_scene_renders(cuda):
     b.close()
 
 
+def test_batch_near_critical_closed_form(cuda):
+    """Critical-curve sampled scenes at a = 0.9 and 0.998 (RK4 mixed path):
+    the batch solves every near-critical ray in closed form, and each scene
+    matches its single-scene render bit for bit; a scene that integrates its
+    near-critical rays (NP_CRITICAL_INTEGRATE) keeps them on the FP64 warps."""
+    import torch
+    scenes = [npx.benchmark_scene(width=96, height=64, spp=4, spin=a).replace(jitter=npx.NP_JITTER_CRITICAL)
+              for a in (0.9, 0.998)]
+    scenes.append(scenes[0].replace(critical_solver=npx.NP_CRITICAL_INTEGRATE, seed=3))
+    b = batch.Batch(scenes)
+    st = b.run(graph=False, stats=True)
+    singles = [npx.render(sc, "mixed", stats=True) for sc in scenes]
+    assert st.deferred_rays == sum(s[2].deferred_rays for s in singles) > 0
+    assert st.closed_form_rays == singles[0][2].closed_form_rays + singles[1][2].closed_form_rays > 0
+    assert singles[2][2].closed_form_rays == 0
+    for i in range(len(scenes)):
+        rgb, rc = b.image(i)
+        torch.cuda.synchronize()
+        assert torch.equal(rgb, singles[i][0]) and torch.equal(rc, singles[i][1]), i
+    b.close()
+
+
 def test_graph_replay_and_tuning_are_deterministic(cuda):
     """Replays of one launch setting are bit-identical.  Chunk size and
     island batch never change a ray's arithmetic; the launch shapes are
@@ -83,5 +105,10 @@ def test_autotuner_installs_a_valid_setting(cuda):
 def test_batch_rejects_bad_scene(cuda):
     scenes = _small_scenes(3)
     scenes[1] = scenes[1].replace(spin=1.2)
+    with pytest.raises(npx.NullPathError):
+        batch.Batch(scenes)
+    # the embedded 7(8) tracer is not batched: refused, not silently run as RK4
+    scenes = _small_scenes(3)
+    scenes[2] = npx.accurate_scene(scenes[2])
     with pytest.raises(npx.NullPathError):
         batch.Batch(scenes)
