@@ -551,7 +551,12 @@ __device__ __forceinline__ void trace_deferred(const SceneDev& s, const InitSoA&
                 }
             }
         }
-        if (!__any_sync(FULL, have)) break;
+        // rays solved in closed form leave their lanes free at once: the
+        // warp stops only when its queue is drained as well
+        if (!__any_sync(FULL, have)) {
+            if (drained) break;
+            continue;
+        }
         if (have) {
             bool done;
             if constexpr (FAM == kFam78df) {
@@ -1410,7 +1415,10 @@ __global__ void __launch_bounds__(BLOCK, MINB) batch_mixed_kernel(const BatchDev
                     }
                 }
             }
-            if (!__any_sync(FULL, have)) break;
+            if (!__any_sync(FULL, have)) {
+                if (drained) break;
+                continue;
+            }
             if (have) {
                 bool done = dray_step(R, *sp);
                 n_steps++; n_f64++; n_evals += 4;

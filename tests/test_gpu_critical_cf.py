@@ -1,5 +1,6 @@
-"""Near-critical rays of the mixed path in closed form (critical_cf_kernel,
-np_scene_t.critical_solver = NP_CRITICAL_CLOSED_FORM) and the crossings
+"""Near-critical rays of the mixed path in closed form (crit_cf_solve on the
+tracer's FP64 warps, np_scene_t.critical_solver = NP_CRITICAL_CLOSED_FORM)
+and the crossings
 entry point np_geokerr_disk_crossings_* on the GPU: the same bits as the
 host build, the renderer's near-critical crossings against the Mino-time
 (Taylor) solver, and frames against the same frames with the near-critical
@@ -95,6 +96,23 @@ def test_render_closed_form_against_integrated(cuda, spin):
     assert ((rc > 0) == (rc2 > 0)).mean() >= 0.999
     both = (rc > 0) & (rc2 > 0)
     assert (np.abs(rc[both] - rc2[both]) <= 1e-5).mean() >= 0.999
+    assert np.isclose(rgb.cpu().numpy(), rgb2.cpu().numpy(), rtol=1e-3, atol=1e-6).all(axis=0).mean() >= 0.999
+
+
+def test_render_many_near_critical_rays(cuda):
+    """A 2048x1024x8 critical-sampled frame at a = 0.998 (about 190k
+    near-critical rays, more than the tracer's warps take in one round):
+    every ray is traced and every near-critical ray solved, and the frame
+    matches the one with the near-critical rays integrated."""
+    sc = npx.accurate_scene(npx.benchmark_scene(width=2048, height=1024, spp=8, spin=0.998)).replace(
+        jitter=npx.NP_JITTER_CRITICAL)
+    rgb, rc, st = npx.render(sc, "mixed", stats=True)
+    assert st.rays == 2048 * 1024 * 8
+    assert st.deferred_rays > 120000 and st.closed_form_rays == st.deferred_rays, (st.deferred_rays, st.closed_form_rays)
+    rgb2, rc2, st2 = npx.render(sc.replace(critical_solver=npx.NP_CRITICAL_INTEGRATE), "mixed", stats=True)
+    assert st2.rays == st.rays
+    rc, rc2 = rc.cpu().numpy(), rc2.cpu().numpy()
+    assert ((rc > 0) == (rc2 > 0)).mean() >= 0.999
     assert np.isclose(rgb.cpu().numpy(), rgb2.cpu().numpy(), rtol=1e-3, atol=1e-6).all(axis=0).mean() >= 0.999
 
 
