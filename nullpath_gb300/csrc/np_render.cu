@@ -495,6 +495,44 @@ __device__ __noinline__ bool crit_cf_solve(const SceneDev& s, const Momentum& m,
     return true;
 }
 
+// Long near-critical lists in a kernel of their own, one ray per thread.
+// Inside the tracer the closed form runs under the FP32 loop's register cap
+// (128), where its spills slowed it about fifty-fold; a few dozen rays
+// (a 1280x720x4 frame has 43) still go there, since the tracer's first
+// warps take them while the FP32 rays run, but a list of kCritKernelMin or
+// more (critical-curve sampling: about 1 % of the rays) is solved here
+// first.  The length is read on the device, so the launch needs no host
+// synchronisation; solved rays get flag 2 and the tracer passes them over.
+constexpr unsigned long long kCritKernelMin = 8192;
+
+__global__ void __launch_bounds__(128)
+critical_cf_kernel(const SceneDev s, InitSoA soa, float* __restrict__ srgb, float* __restrict__ rcross,
+                   Counters* __restrict__ ctr, unsigned long long list_cap) {
+    const unsigned long long Dl = min(ctr->deferred, list_cap);
+    if (Dl < kCritKernelMin) return;
+    const long long D = (long long)Dl;
+    unsigned long long solved = 0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < D;
+         i += (long long)gridDim.x * blockDim.x) {
+        const long long item = soa.list[i];
+        long long p; int sl, x, y; uint32_t sid;
+        ray_coords(s, item, p, sl, x, y, sid);
+        const CamDir dir = camera_dir(s, x, y, sid, false, 0.0, 0.0);
+        CritCF o;
+        if (!crit_cf_solve(s, camera_momentum(s, dir), o)) continue;
+        float col[3];
+        sample_colour(s, o.status == 1, o.orders, o.disk, (float)o.min_r, dir.cam_y, col);
+        write_sample(s, srgb, rcross, p, sl, col, o.first_r);
+        soa.flag[item] = 2;
+        solved++;
+    }
+    for (int o = 16; o > 0; o >>= 1) solved += __shfl_down_sync(0xffffffffu, solved, o);
+    if ((threadIdx.x & 31) == 0 && solved) {
+        atomicAdd(&ctr->closed_form, solved);
+        atomicAdd(&ctr->rays, solved);
+    }
+}
+
 // Near-critical rays from the deferred list, one per lane until the list is
 // drained (rays taken four at a time from work2): solved in closed form
 // (crit_cf_solve) when the scene asks for it and the ray is inside the
@@ -517,7 +555,7 @@ __device__ __forceinline__ void trace_deferred(const SceneDev& s, const InitSoA&
         if (need && !drained) {
             long long idx = warp_take(q, need, &ctr->work2, D, 4);
             drained = q.base >= D;
-            if (!have && idx >= 0) {
+            if (!have && idx >= 0 && soa.flag[soa.list[idx]] == 1) {
                 item = soa.list[idx];
                 int x, y; uint32_t sid;
                 ray_coords(s, item, p, sl, x, y, sid);
@@ -937,6 +975,14 @@ void launch_mixed(int minb, const SceneDev& s, const InitSoA& soa, float* srgb, 
     }
 }
 
+// Long near-critical lists of a pass, in closed form before the tracer runs
+// (the kernel returns at once for a short list).
+void launch_critical(const SceneDev& s, const InitSoA& soa, float* srgb, float* rc, Counters* ctr,
+                     unsigned long long list_cap, cudaStream_t st) {
+    if (!(s.islands & kIslandCritical) || !s.crit_cf) return;
+    critical_cf_kernel<<<np_device_sms() * 3, 128, 0, st>>>(s, soa, srgb, rc, ctr, list_cap);
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -1069,6 +1115,8 @@ int np_render_device(const np_scene_t* scene, int precision, float* d_rgb, float
         ray_init_kernel<<<ib, 256, 0, st>>>(s, soa, sc->ctr);
         NP_CU(cudaGetLastError(), NP_ERR_KERNEL);
         if (stats) NP_CU(cudaEventRecord(sc->ev1, st), NP_ERR_KERNEL);
+        launch_critical(s, soa, sc->srgb, d_rcross, sc->ctr, (unsigned long long)s.total, st);
+        NP_CU(cudaGetLastError(), NP_ERR_KERNEL);
         launch_mixed(g_tune.min_blocks, s, soa, sc->srgb, d_rcross, d_inv3, sc->ctr, g_tune.chunk, st);
         NP_CU(cudaGetLastError(), NP_ERR_KERNEL);
     }
@@ -1291,6 +1339,8 @@ extern "C" int np_render_device_noalloc(const np_scene_t* scene, int precision, 
                     (unsigned char*)(base + kNaFlag), (long long*)(base + kNaList)};
         int ib = (int)std::min<long long>((s.total + 255) / 256, (long long)np_device_sms() * 8);
         ray_init_kernel<<<ib, 256, 0, st>>>(s, soa, ctr);
+        NP_CU(cudaGetLastError(), NP_ERR_KERNEL);
+        launch_critical(s, soa, srgb, d_rcross, ctr, (unsigned long long)s.total, st);
         NP_CU(cudaGetLastError(), NP_ERR_KERNEL);
         launch_mixed(g_tune.min_blocks, s, soa, srgb, d_rcross, nullptr, ctr, g_tune.chunk, st);
     }
