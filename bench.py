@@ -263,6 +263,7 @@ def critical_leg(W=2048, spp=16, spin=0.998, n_acc=8000):
         leg = {"rays_per_s": rays / ((st.kernel_ms + st.init_ms) * 1e-3), "kernel_ms": st.kernel_ms + st.init_ms,
                "mean_steps_per_ray": st.steps / max(1, st.rays), "fp64_steps_frac": st.fp64_steps / max(1, st.steps),
                "deferred_rays": int(st.deferred_rays), "closed_form_rays": int(st.closed_form_rays),
+               "band_rays": int(st.band_rays),
                "error_vs_geokerr": accuracy.crossing_error(scn, n=n_acc, precision="mixed", seed=3, critical=True,
                                                            cache=cache)}
         out[name] = leg
@@ -509,8 +510,9 @@ def run_ours(args):
                        "fp64_islands": ("horizon band 0.1 M (certified capture, FP64 steps otherwise)" if
                                         args.path == "rkf78" else
                                         "horizon band 0.1 M, radial/polar turning points"),
-                       "near_critical": "|b-b_crit| < 1e-3 M: FP64 closed form (Mino-time solution, "
-                                        "crossings by Jacobi amplitude, Carlson R_F)",
+                       "near_critical": "|b-b_crit| < 1e-3 M, and rays entering the horizon band without a "
+                                        "capture certificate: FP64 closed form (Mino-time solution, crossings by "
+                                        "Jacobi amplitude, Carlson R_F)",
                        "l2": "256 MiB buffer written between timed steps (outside the step events)",
                        "parallelism": "replicas" if ws > 1 else "single"},
             "steps_per_s": ws * st.steps / (ms * 1e-3),
@@ -519,6 +521,7 @@ def run_ours(args):
             "fp64_island_steps_frac": st.fp64_steps / max(1, st.steps),
             "deferred_rays": st.deferred_rays,
             "closed_form_rays": st.closed_form_rays,
+            "band_rays": st.band_rays,
             "kernel_ms": {"tracer": kern_ms, "ray_init": statistics.mean(s.init_ms for s in stats)},
             "roofline": {"bound": "fp32" if args.precision == "mixed" else "fp64", "achieved": achieved,
                          "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
@@ -532,7 +535,7 @@ def run_ours(args):
             "e2e": {"value": replicas.aggregate_rays_per_s(rays_per_step, e2e, ws), "unit": "rays/s",
                     "h2d_bytes_per_step": C.sizeof(sc),
                     "d2h_bytes_per_step": 4 * H * W * 4},
-            "gpu_launches": (4 if args.precision == "mixed" else 2) * args.steps,
+            "gpu_launches": (5 if args.precision == "mixed" else 2) * args.steps,
             "clocks": clocks,
             "wall_s": wall,
         }
@@ -549,7 +552,7 @@ def run_ours(args):
                     "mean_steps_per_ray": best.steps / max(1, best.rays),
                     "rhs_evals_per_ray": best.rhs_evals / max(1, best.rays),
                     "fp64_island_steps_frac": best.fp64_steps / max(1, best.steps),
-                    "closed_form_rays": best.closed_form_rays}
+                    "closed_form_rays": best.closed_form_rays, "band_rays": best.band_rays}
         if args.precision == "mixed" and args.path == "rkf78":
             out["islands_all"] = timed(sc.replace(islands=npx.NP_ISLANDS_ALL))
             out["islands_all"]["islands"] = "horizon band, turning points (FP64 7(8) steps), near-critical"

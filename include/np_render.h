@@ -114,7 +114,12 @@ typedef enum np_island_arith { NP_ISLAND_ARITH_FP64 = 0, NP_ISLAND_ARITH_DF = 1 
  *                            integration steps.  Rays outside the closed
  *                            forms (a = 0, Carter's Q = 0, a camera inside
  *                            the photon region or beyond the escape radius)
- *                            are integrated as below.
+ *                            are integrated as below.  On the 7(8) path
+ *                            with NP_ISLAND_HORIZON (and the disk outside
+ *                            the horizon band), a ray that enters the band
+ *                            without a certificate of capture is solved the
+ *                            same way, whole, instead of taking FP64 island
+ *                            steps there.
  *   NP_CRITICAL_INTEGRATE    traced whole in FP64 (island_arith) by the
  *                            integrator family of the scene: 7(8) at
  *                            rtol_fp64, RK4 with the reference step law. */
@@ -180,6 +185,7 @@ typedef struct np_render_stats {
     double kernel_ms;             /* device time of the tracer kernel */
     double init_ms;               /* device time of the ray-generation kernel (mixed path) */
     uint64_t closed_form_rays;    /* near-critical rays solved in closed form (mixed path) */
+    uint64_t band_rays;           /* 7(8) rays handed from the horizon band to the closed form */
 } np_render_stats_t;
 
 /* ABI version compiled into the library. */

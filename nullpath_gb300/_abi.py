@@ -67,7 +67,7 @@ class RenderStats(C.Structure):
     _fields_ = [
         ("rays", C.c_uint64), ("steps", C.c_uint64), ("fp64_steps", C.c_uint64),
         ("rhs_evals", C.c_uint64), ("deferred_rays", C.c_uint64),
-        ("kernel_ms", C.c_double), ("init_ms", C.c_double), ("closed_form_rays", C.c_uint64),
+        ("kernel_ms", C.c_double), ("init_ms", C.c_double), ("closed_form_rays", C.c_uint64), ("band_rays", C.c_uint64),
     ]
 
 

@@ -69,6 +69,8 @@ struct SceneDev {
     int cert_capture;          // 7(8) path: rays certified to fall in end at the horizon band (disk outside it)
     int island_df;             // 7(8) path: FP64-class steps in double-float arithmetic
     int crit_cf;               // mixed path: near-critical rays in closed form (Mino-time solution)
+    int band_cf;               // 7(8) mixed path: rays entering the horizon band (not certified to fall
+                               // in) end there and are solved whole in closed form instead of FP64 steps
     float a_hl[2], M_hl[2], rp_hl[2], rm_hl[2];   // a, M, r_+, r_- as double-float pairs
     float rtol64_f, atol64_f;  // tolerances of the near-critical rays (double-float arithmetic)
     int island_batch;

@@ -92,6 +92,7 @@ struct Counters {
     unsigned long long deferred;    // deferred-list length
     unsigned long long rays, steps, fp64_steps, evals;
     unsigned long long closed_form;  // near-critical rays solved in closed form
+    unsigned long long band;         // rays handed from the horizon band to the closed form
 };
 
 // ---------------------------------------------------------------------------
@@ -224,6 +225,8 @@ int prepare_scene(const np_scene_t& sc, SceneDev& d) {
         d.cert_capture = !d.disk_on || d.rin > d.r_plus + kHorizonBand * d.M;
         d.island_df = sc.island_arith == NP_ISLAND_ARITH_DF;
         d.crit_cf = sc.critical_solver == NP_CRITICAL_CLOSED_FORM;
+        d.band_cf = d.crit_cf && (sc.islands & NP_ISLAND_HORIZON) && sc.integrator == NP_INTEG_RKF78 &&
+                    d.a != 0.0 && d.cert_capture;
         auto split = [](double x, float* o) { o[0] = (float)x; o[1] = (float)(x - (double)o[0]); };
         split(d.a, d.a_hl); split(d.M, d.M_hl); split(d.r_plus, d.rp_hl); split(d.r_minus, d.rm_hl);
         d.rtol64_f = (float)d.rtol64; d.atol64_f = (float)std::fmax(d.atol, 1e-14 * d.M);
@@ -533,6 +536,46 @@ critical_cf_kernel(const SceneDev s, InitSoA soa, float* __restrict__ srgb, floa
     }
 }
 
+// Rays of the 7(8) path that entered the horizon band without a certificate
+// of capture (status 3; listed after the near-critical rays): solved whole
+// in closed form, one ray per thread, after the tracer.  At a = 0.998 the
+// prograde photon orbit lies inside the band, and rays that wind there took
+// hundreds of FP64 island steps each.  A ray outside the closed forms is
+// traced whole in FP64 7(8) here instead.
+__global__ void __launch_bounds__(128)
+band_cf_kernel(const SceneDev s, InitSoA soa, float* __restrict__ srgb, float* __restrict__ rcross,
+               Counters* __restrict__ ctr) {
+    const long long D = (long long)ctr->deferred;
+    const long long nb = (long long)ctr->band;
+    unsigned long long steps = 0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nb;
+         i += (long long)gridDim.x * blockDim.x) {
+        const long long item = soa.list[D + i];
+        long long p; int sl, x, y; uint32_t sid;
+        ray_coords(s, item, p, sl, x, y, sid);
+        const CamDir dir = camera_dir(s, x, y, sid, false, 0.0, 0.0);
+        const Momentum m = camera_momentum(s, dir);
+        float col[3];
+        CritCF o;
+        if (crit_cf_solve(s, m, o)) {
+            sample_colour(s, o.status == 1, o.orders, o.disk, (float)o.min_r, dir.cam_y, col);
+            write_sample(s, srgb, rcross, p, sl, col, o.first_r);
+        } else {
+            DRay78<false> R;
+            dray78_start(R, s, -m.pt, m.pph, m.pr, m.pth);
+            bool acc;
+            while (!dray78_step(R, s, acc)) steps += acc ? 1 : 0;
+            sample_colour(s, R.status == 1, R.orders, R.disk, (float)R.min_r, dir.cam_y, col);
+            write_sample(s, srgb, rcross, p, sl, col, R.first_r);
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) steps += __shfl_down_sync(0xffffffffu, steps, o);
+    if ((threadIdx.x & 31) == 0 && steps) {
+        atomicAdd(&ctr->steps, steps);
+        atomicAdd(&ctr->fp64_steps, steps);
+    }
+}
+
 // Near-critical rays from the deferred list, one per lane until the list is
 // drained (rays taken four at a time from work2): solved in closed form
 // (crit_cf_solve) when the scene asks for it and the ray is inside the
@@ -704,9 +747,15 @@ render_mixed_kernel(const SceneDev s, const InitSoA soa, float* __restrict__ srg
             }
         }
         if (done) {
-            float col[3];
-            sample_colour(s, R.status == 1, R.orders, R.disk, R.min_r, cam_y, col);
-            write_sample(s, srgb, rcross, p, sl, col, R.first_r);
+            if (FAM != kFamRk4 && R.status == 3) {
+                // entered the horizon band: solved whole by band_cf_kernel
+                const unsigned long long slot = atomicAdd(&ctr->band, 1ull);
+                soa.list[D + (long long)slot] = (long long)sl * s.npix + p;
+            } else {
+                float col[3];
+                sample_colour(s, R.status == 1, R.orders, R.disk, R.min_r, cam_y, col);
+                write_sample(s, srgb, rcross, p, sl, col, R.first_r);
+            }
             have = false;
         }
     }
@@ -815,6 +864,19 @@ __global__ void trace_rays_kernel(const SceneDev s, int precision, int n, const 
         }
         for (int j = 0; j < 4; ++j) { xr[j] = R.xr_d[j]; xphi[j] = R.xphi[j]; }
         ncross = R.crossings; st = R.status;
+        if (st == 3) {
+            // entered the horizon band: the whole ray in closed form, as the
+            // renderer's band_cf_kernel (FP64 7(8) outside the closed forms)
+            for (int j = 0; j < 4; ++j) { xr[j] = 0.0; xphi[j] = 0.0; }
+            if (!crit_cf_cross(s, m, xr, xphi, ncross, st)) {
+                DRay78<true> D;
+                dray78_start(D, s, E, L, m.pr, m.pth);
+                bool acc;
+                while (!dray78_step(D, s, acc)) {}
+                for (int j = 0; j < 4; ++j) { xr[j] = D.xr[j]; xphi[j] = D.xphi[j]; }
+                ncross = D.crossings; st = D.status;
+            }
+        }
     } else {
         const SpaceK k{(float)s.a, (float)(s.a * s.a), (float)s.M, (float)s.r_plus, (float)s.r_minus};
         MRay<true> R;
@@ -983,6 +1045,12 @@ void launch_critical(const SceneDev& s, const InitSoA& soa, float* srgb, float* 
     critical_cf_kernel<<<np_device_sms() * 3, 128, 0, st>>>(s, soa, srgb, rc, ctr, list_cap);
 }
 
+// The horizon-band rays of a 7(8) pass, after the tracer.
+void launch_band(const SceneDev& s, const InitSoA& soa, float* srgb, float* rc, Counters* ctr, cudaStream_t st) {
+    if (!s.band_cf) return;
+    band_cf_kernel<<<np_device_sms() * 3, 128, 0, st>>>(s, soa, srgb, rc, ctr);
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -1119,6 +1187,8 @@ int np_render_device(const np_scene_t* scene, int precision, float* d_rgb, float
         NP_CU(cudaGetLastError(), NP_ERR_KERNEL);
         launch_mixed(g_tune.min_blocks, s, soa, sc->srgb, d_rcross, d_inv3, sc->ctr, g_tune.chunk, st);
         NP_CU(cudaGetLastError(), NP_ERR_KERNEL);
+        launch_band(s, soa, sc->srgb, d_rcross, sc->ctr, st);
+        NP_CU(cudaGetLastError(), NP_ERR_KERNEL);
     }
     if (stats) NP_CU(cudaEventRecord(sc->ev2, st), NP_ERR_KERNEL);
     {
@@ -1143,6 +1213,7 @@ int np_render_device(const np_scene_t* scene, int precision, float* d_rgb, float
         stats->rhs_evals = sc->h_ctr->evals;
         stats->deferred_rays = precision == NP_PREC_MIXED ? sc->h_ctr->deferred : 0;
         stats->closed_form_rays = sc->h_ctr->closed_form;
+        stats->band_rays = sc->h_ctr->band;
         stats->kernel_ms = ms;
         stats->init_ms = ms2;
     }
@@ -1343,6 +1414,8 @@ extern "C" int np_render_device_noalloc(const np_scene_t* scene, int precision, 
         launch_critical(s, soa, srgb, d_rcross, ctr, (unsigned long long)s.total, st);
         NP_CU(cudaGetLastError(), NP_ERR_KERNEL);
         launch_mixed(g_tune.min_blocks, s, soa, srgb, d_rcross, nullptr, ctr, g_tune.chunk, st);
+        NP_CU(cudaGetLastError(), NP_ERR_KERNEL);
+        launch_band(s, soa, srgb, d_rcross, ctr, st);
     }
     NP_CU(cudaGetLastError(), NP_ERR_KERNEL);
     long long n = 3 * s.npix;

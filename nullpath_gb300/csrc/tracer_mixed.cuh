@@ -1125,6 +1125,8 @@ __device__ __forceinline__ int mray_step78(MRay<PHI>& R, const SceneDev& s, cons
             R.step++; R.status = 1; R.min_r = s.r_plus_f;
             return STEP_DONE;
         }
+        // or the whole ray is handed to the FP64 closed form (status 3)
+        if (s.band_cf) { R.status = 3; return STEP_DONE; }
         R.pending = true; R.h_pend = h;
         return STEP_PARK;
     }

@@ -109,11 +109,39 @@ def test_render_many_near_critical_rays(cuda):
     rgb, rc, st = npx.render(sc, "mixed", stats=True)
     assert st.rays == 2048 * 1024 * 8
     assert st.deferred_rays > 120000 and st.closed_form_rays == st.deferred_rays, (st.deferred_rays, st.closed_form_rays)
+    # at a = 0.998 the prograde photon orbit lies inside the horizon band:
+    # rays that wind there are solved whole in closed form too
+    assert st.band_rays > 1000
     rgb2, rc2, st2 = npx.render(sc.replace(critical_solver=npx.NP_CRITICAL_INTEGRATE), "mixed", stats=True)
-    assert st2.rays == st.rays
+    assert st2.rays == st.rays and st2.band_rays == 0
     rc, rc2 = rc.cpu().numpy(), rc2.cpu().numpy()
     assert ((rc > 0) == (rc2 > 0)).mean() >= 0.999
     assert np.isclose(rgb.cpu().numpy(), rgb2.cpu().numpy(), rtol=1e-3, atol=1e-6).all(axis=0).mean() >= 0.999
+
+
+@pytest.mark.parametrize("spin", [0.9, 0.998])
+def test_trace_rays_band_rays_match_mino_solver(cuda, spin):
+    """Rays of the 7(8) mixed path that enter the horizon band (random image
+    positions of a critical-sampled camera): their crossings, from the
+    closed form, against the Mino-time solver to 1e-8 relative, and the
+    crossing error of the whole sample within the spec bar."""
+    sc = npx.accurate_scene(npx.benchmark_scene(spin=spin))
+    px, py = accuracy.critical_positions(sc, 8000, seed=5)
+    a = npx.trace_rays(sc, px, py, "mixed")
+    b = npx.trace_rays(sc.replace(critical_solver=npx.NP_CRITICAL_INTEGRATE), px, py, "mixed")
+    sel = np.abs(a["cross"].cpu().numpy() - b["cross"].cpu().numpy()).max(axis=(1, 2)) > 0
+    assert sel.sum() >= 20
+    cross = a["cross"].cpu().numpy()[sel]
+    u0, mu0, l, q2, su, sm = gk.render_ray_constants(a["consts"].cpu().numpy()[sel], sc)
+    xu, xphi, nx = gk.equator_crossings(sc.spin, u0, mu0, l, q2, su, sm, 1.0 / sc.escape_r, 4)
+    xu, nx = xu.cpu().numpy(), nx.cpu().numpy()
+    for i in range(sel.sum()):
+        k = min(int(nx[i]), 4)
+        if k:
+            r_ref = 1.0 / xu[i, :k]
+            assert np.max(np.abs(cross[i, :k, 0] - r_ref) / r_ref) <= 1e-8, i
+    r = accuracy.crossing_error(sc, n=20000, precision="mixed", seed=7, critical=True)
+    assert r["order1"]["r_err_p99"] <= 1e-5 and r["order1"]["disagree"] == 0, r["order1"]
 
 
 def test_render_outside_closed_forms_falls_back(cuda):
