@@ -500,12 +500,15 @@ __device__ __noinline__ bool crit_cf_solve(const SceneDev& s, const Momentum& m,
 
 // Long near-critical lists in a kernel of their own, one ray per thread.
 // Inside the tracer the closed form runs under the FP32 loop's register cap
-// (128), where its spills slowed it about fifty-fold; a few dozen rays
-// (a 1280x720x4 frame has 43) still go there, since the tracer's first
-// warps take them while the FP32 rays run, but a list of kCritKernelMin or
-// more (critical-curve sampling: about 1 % of the rays) is solved here
-// first.  The length is read on the device, so the launch needs no host
-// synchronisation; solved rays get flag 2 and the tracer passes them over.
+// (128) and spills, on the FP64 warps that the FP32 rays leave it; here it
+// has its own budget (158 registers, no spills) and every warp of the GPU.
+// A few dozen rays (a 1280x720x4 frame has 43) still go to the tracer,
+// whose first warps take them while the FP32 rays run, so that one
+// thread's latency (about 5 ms when this kernel ran them in front of the
+// tracer) is hidden; a list of kCritKernelMin or more (critical-curve
+// sampling: about 1 % of the rays) is solved here first.  The length is
+// read on the device, so the launch needs no host synchronisation; solved
+// rays get flag 2 and the tracer passes them over.
 constexpr unsigned long long kCritKernelMin = 8192;
 
 __global__ void __launch_bounds__(128)
