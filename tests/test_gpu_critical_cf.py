@@ -59,7 +59,7 @@ def test_trace_rays_near_critical_match_mino_solver(cuda, spin):
     against the Mino-time solver's (np_geokerr_equator_crossings, FP64
     Taylor) to 1e-8 relative in r and 1e-8 rad in phi, counts equal."""
     sc = npx.accurate_scene(npx.benchmark_scene(spin=spin))
-    px, py = accuracy.critical_positions(sc, 8000, seed=3)
+    px, py = accuracy.critical_positions(sc, 4000, seed=3)
     out, sel = _near_critical(sc, px, py)
     assert sel.sum() >= 20, sel.sum()
     consts = out["consts"].cpu().numpy()[sel]
@@ -119,14 +119,15 @@ def test_render_many_near_critical_rays(cuda):
     assert np.isclose(rgb.cpu().numpy(), rgb2.cpu().numpy(), rtol=1e-3, atol=1e-6).all(axis=0).mean() >= 0.999
 
 
-@pytest.mark.parametrize("spin", [0.9, 0.998])
+@pytest.mark.parametrize("spin", [0.998])
 def test_trace_rays_band_rays_match_mino_solver(cuda, spin):
-    """Rays of the 7(8) mixed path that enter the horizon band (random image
-    positions of a critical-sampled camera): their crossings, from the
+    """Rays of the 7(8) mixed path that enter the horizon band (critical-curve
+    samples at a = 0.998, where the band holds the prograde photon orbit):
+    their crossings, from the
     closed form, against the Mino-time solver to 1e-8 relative, and the
     crossing error of the whole sample within the spec bar."""
     sc = npx.accurate_scene(npx.benchmark_scene(spin=spin))
-    px, py = accuracy.critical_positions(sc, 8000, seed=5)
+    px, py = accuracy.critical_positions(sc, 4000, seed=5)
     a = npx.trace_rays(sc, px, py, "mixed")
     b = npx.trace_rays(sc.replace(critical_solver=npx.NP_CRITICAL_INTEGRATE), px, py, "mixed")
     sel = np.abs(a["cross"].cpu().numpy() - b["cross"].cpu().numpy()).max(axis=(1, 2)) > 0
@@ -140,7 +141,7 @@ def test_trace_rays_band_rays_match_mino_solver(cuda, spin):
         if k:
             r_ref = 1.0 / xu[i, :k]
             assert np.max(np.abs(cross[i, :k, 0] - r_ref) / r_ref) <= 1e-8, i
-    r = accuracy.crossing_error(sc, n=20000, precision="mixed", seed=7, critical=True)
+    r = accuracy.crossing_error(sc, n=8000, precision="mixed", seed=7, critical=True)
     assert r["order1"]["r_err_p99"] <= 1e-5 and r["order1"]["disagree"] == 0, r["order1"]
 
 
