@@ -66,10 +66,12 @@ typedef enum np_camera { NP_CAMERA_STATIC = 0, NP_CAMERA_ZAMO = 1 } np_camera;
  *   NP_PREC_MIXED  the Carter-form system in compensated FP32, error control
  *                  on (r, theta, p_r, p_theta) with rtol and atol (atol at
  *                  least 1e-9 M); FP64 islands take 7(8) steps at rtol,
- *                  near-critical rays are traced whole in FP64 at
- *                  rtol_fp64, and a ray inside the horizon band that
- *                  provably falls in (no radial turning point left) ends
- *                  there.  inv_gate is not used.  With NP_CROSS_ROOT a
+ *                  near-critical rays are solved in FP64 closed form (or
+ *                  traced whole in FP64 at rtol_fp64, critical_solver),
+ *                  and a ray inside the horizon band that provably falls
+ *                  in (no radial turning point left) ends there; any other
+ *                  ray that enters the band is solved in closed form too.
+ *                  inv_gate is not used.  With NP_CROSS_ROOT a
  *                  crossing is landed on the equator by one more 7(8) step
  *                  in theta (Henon's method). */
 typedef enum np_integrator { NP_INTEG_RK4 = 0, NP_INTEG_ADAPTIVE = 1, NP_INTEG_RKF78 = 2 } np_integrator;
@@ -169,7 +171,7 @@ typedef struct np_scene {
     int32_t islands;              /* NP_ISLAND_* mask of the mixed path */
     double inv_gate;              /* NP_INTEG_RKF78 invariant gate; <= 0 disables */
     double rtol_fp64;             /* rtol of the near-critical rays the mixed 7(8) path traces
-                                     whole in FP64; <= 0 means rtol (as its island steps) */
+                                     whole in FP64 (NP_CRITICAL_INTEGRATE); <= 0 means rtol */
     int32_t island_arith;         /* np_island_arith: arithmetic of the FP64-class steps of the
                                      mixed 7(8) path */
     int32_t critical_solver;      /* np_critical_solver: near-critical rays of the mixed path */

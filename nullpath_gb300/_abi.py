@@ -112,7 +112,8 @@ def benchmark_scene(width=1280, height=720, spp=4, spin=0.9, seed=0):
 def accurate_scene(scene, rtol=1e-8, atol=1e-9, islands=None):
     """`scene` on the mixed path's embedded 7(8) integrator: compensated FP32
     steps under error control at `rtol` / `atol`, crossings landed on the
-    equator by a Henon step, FP64 islands at rtol.  At the
+    equator by a Henon step, FP64 islands at rtol, near-critical and
+    horizon-band rays in FP64 closed form.  At the
     defaults the first disk crossing of the 1280x720x4, a = 0.9 benchmark
     frame is within 1e-5 M of the Mino-time solver's (p99).  Render it with
     precision "mixed"."""
