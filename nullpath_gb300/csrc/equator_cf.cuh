@@ -100,6 +100,7 @@ GKCF_HD EqX equator_crossings(double a, double l, double q2, double u0, double m
         return o;
     }
     CfRay R;
+    if (c[4] < 0.0 && (nr == 4 || (nr == 2 && sigma > 0.0))) polish_roots(a, l, q2, nr, rr, rho, sigma);
     if (nr == 4 && c[4] < 0.0) {
         if (!reduce_r4(rr, c[4], u0, R)) return o;
     } else if (nr == 2 && sigma > 0.0 && c[4] < 0.0) {

@@ -458,6 +458,105 @@ GKCF_HD void complex_poles(CfRay& R) {
     }
 }
 
+// Roots of U polished against its exact coefficients.  U(u) = 1 + c2 u^2 +
+// c3 u^3 + c4 u^4 with c2 = a^2 - l^2 - q2, c3 = 2 ((l - a)^2 + q2) and
+// c4 = -a^2 q2 is formed in double-double arithmetic from the double inputs
+// (Dekker's exact product by fma, Knuth's two-sum) and evaluated by a
+// compensated Horner scheme; Newton steps on that value move each root to
+// the root of the exact polynomial.  The double coefficients alone are
+// rounded by ~1e-16 relative, which moves a pair of nearly double roots
+// (a ray near the critical curve) by ~1e-16 / (U'' (u3 - u2)): 1e-13 at
+// u3 - u2 = 5e-5, and the crossings past the photon orbit inherit it times
+// the orbit's growth factor.  A step larger than a quarter of the distance
+// to the nearest other root is not taken.
+struct DD { double hi, lo; };
+GKCF_HD DD dd_fast(double a, double b) { const double s = a + b; return DD{s, b - (s - a)}; }
+GKCF_HD DD dd_two_sum(double a, double b) {
+    const double s = a + b, bb = s - a;
+    return DD{s, (a - (s - bb)) + (b - bb)};
+}
+GKCF_HD DD dd_two_prod(double a, double b) { const double p = a * b; return DD{p, std::fma(a, b, -p)}; }
+GKCF_HD DD dd_add(DD x, DD y) { const DD t = dd_two_sum(x.hi, y.hi); return dd_fast(t.hi, t.lo + x.lo + y.lo); }
+GKCF_HD DD dd_mul(DD x, double y) { const DD p = dd_two_prod(x.hi, y); return dd_fast(p.hi, p.lo + x.lo * y); }
+
+struct UExact { DD c2, c3, c4; };
+GKCF_HD UExact u_exact(double a, double l, double q2) {
+    UExact c;
+    const DD a2 = dd_two_prod(a, a), l2 = dd_two_prod(l, l);
+    c.c2 = dd_add(dd_add(a2, DD{-l2.hi, -l2.lo}), DD{-q2, 0.0});
+    const DD d = dd_two_sum(l, -a);
+    const DD d2 = dd_two_prod(d.hi, d.hi);
+    const DD k = dd_add(dd_fast(d2.hi, d2.lo + 2.0 * d.hi * d.lo), DD{q2, 0.0});
+    c.c3 = DD{2.0 * k.hi, 2.0 * k.lo};
+    c.c4 = dd_mul(a2, -q2);
+    return c;
+}
+
+GKCF_HD double polish_real(const UExact& c, double x, double gap) {
+    for (int it = 0; it < 3; ++it) {
+        DD t = dd_add(dd_mul(c.c4, x), c.c3);
+        t = dd_add(dd_mul(t, x), c.c2);
+        t = dd_mul(dd_mul(t, x), x);
+        t = dd_add(t, DD{1.0, 0.0});
+        const double d = x * (2.0 * c.c2.hi + x * (3.0 * c.c3.hi + 4.0 * x * c.c4.hi));
+        if (!(d != 0.0)) break;
+        const double dx = (t.hi + t.lo) / d;
+        if (!(std::fabs(dx) <= 0.25 * gap)) break;
+        x -= dx;
+        if (std::fabs(dx) <= 4e-16 * std::fabs(x)) break;     // the next step is below the last bit
+    }
+    return x;
+}
+
+// the complex root rho + i sigma (sigma > 0), by complex Newton steps
+GKCF_HD void polish_pair(const UExact& c, double& rho, double& sigma) {
+    double x = rho, y = sigma;
+    for (int it = 0; it < 3; ++it) {
+        // U(z) by Horner in double-double complex arithmetic
+        DD re = c.c4, im = DD{0.0, 0.0};
+        for (int k = 0; k < 4; ++k) {
+            const DD nre = dd_add(dd_mul(re, x), dd_mul(im, -y));
+            const DD nim = dd_add(dd_mul(re, y), dd_mul(im, x));
+            re = nre; im = nim;
+            if (k == 0) re = dd_add(re, c.c3);
+            else if (k == 1) re = dd_add(re, c.c2);
+            else if (k == 3) re = dd_add(re, DD{1.0, 0.0});
+        }
+        // U'(z) = z (2 c2 + z (3 c3 + 4 c4 z)) in double
+        const double c2 = c.c2.hi, c3 = c.c3.hi, c4 = c.c4.hi;
+        double pr = 3.0 * c3 + 4.0 * c4 * x, pi = 4.0 * c4 * y;
+        double qr = 2.0 * c2 + (pr * x - pi * y), qi = pr * y + pi * x;
+        const double dr = qr * x - qi * y, di = qr * y + qi * x;
+        const double den = dr * dr + di * di;
+        if (!(den > 0.0)) break;
+        const double ur = re.hi + re.lo, ui = im.hi + im.lo;
+        const double sr = (ur * dr + ui * di) / den, si = (ui * dr - ur * di) / den;
+        if (!(std::fabs(sr) + std::fabs(si) <= 0.25 * y)) break;
+        x -= sr; y -= si;
+        if (std::fabs(sr) + std::fabs(si) <= 4e-16 * (std::fabs(x) + y)) break;
+    }
+    rho = x; sigma = y;
+}
+
+// Polishes the roots of a q2 > 0 potential as found (nr real roots sorted,
+// a complex pair when nr = 2).
+GKCF_HD void polish_roots(double a, double l, double q2, int nr, double* rr, double& rho, double& sigma) {
+    const UExact c = u_exact(a, l, q2);
+    double out[4];
+    for (int i = 0; i < nr; ++i) {
+        double gap = nr == 2 ? std::fabs(rr[1] - rr[0]) : INFINITY;
+        for (int j = 0; j < nr; ++j)
+            if (j != i) gap = std::fmin(gap, std::fabs(rr[j] - rr[i]));
+        if (nr == 2 && sigma > 0.0) {
+            const double dz = std::sqrt((rr[i] - rho) * (rr[i] - rho) + sigma * sigma);
+            gap = std::fmin(gap, dz);
+        }
+        out[i] = polish_real(c, rr[i], gap);
+    }
+    for (int i = 0; i < nr; ++i) rr[i] = out[i];
+    if (nr == 2 && sigma > 0.0) polish_pair(c, rho, sigma);
+}
+
 // Radial reductions of q2 > 0 (c4 = -a^2 q2 < 0), motion in [u1, u2] holding
 // u0 with the turning point u2 ahead of an ingoing ray: kind, roots, m, mc
 // and g of R; false when u0 is outside that interval.
@@ -527,6 +626,7 @@ GKCF_HD void setup(double a, double l, double q2, double u0, double uf, double m
     const double c[5] = {1.0, 0.0, B, 2.0 * Kc, -a * a * q2};
     double rr[4], rho = 0.0, sigma = 0.0;
     const int nr = ::np::mino::real_roots(c, 4, rr, &rho, &sigma);
+    if (c[4] < 0.0 && (nr == 4 || (nr == 2 && sigma > 0.0))) polish_roots(a, l, q2, nr, rr, rho, sigma);
     const double sq = std::sqrt(1.0 - a * a);
     R.rp = 1.0 + sq;
     R.rm = a * a / R.rp;

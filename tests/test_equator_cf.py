@@ -22,11 +22,13 @@ def _truth():
 
 # Per crossing order: a near-critical ray's later crossings follow half
 # orbits near the photon orbit, each of which multiplies a perturbation of
-# the ray (here the double rounding of U's coefficients and roots) by about
-# 20; the Taylor restatement's errors against the same truth grow the same
-# way (1e-16, 1e-14, 3e-13, 6e-12, 1e-10, 3e-9 on the worst ray).
-BAR_U = (1e-11, 1e-11, 1e-11, 2e-11, 5e-10, 1e-8)
-BAR_PHI = (1e-11, 1e-11, 3e-11, 5e-11, 2e-10, 5e-9)
+# the ray by about 20.  The roots of U are polished against its exact
+# (double-double) coefficients, so u carries no such growth (2e-14 at the
+# sixth crossing, against 2.5e-9 with the double coefficients' roots and
+# 3e-9 for the Taylor restatement); phi, summed from the pole terms, keeps
+# some (2e-11 at the sixth).
+BAR_U = (5e-14, 5e-14, 5e-14, 5e-14, 1e-13, 1e-13)
+BAR_PHI = (5e-14, 2e-13, 5e-12, 3e-11, 3e-11, 1e-10)
 
 
 def test_crossings_match_quadrature_truth():
