@@ -125,7 +125,7 @@ def test_trace_rays_band_rays_match_mino_solver(cuda, spin):
     samples at a = 0.998, where the band holds the prograde photon orbit):
     their crossings, from the
     closed form, against the Mino-time solver to 1e-8 relative, and the
-    crossing error of the whole sample within the spec bar."""
+    order-1 crossing error of the whole sample within 1e-5 M (p99)."""
     sc = npx.accurate_scene(npx.benchmark_scene(spin=spin))
     px, py = accuracy.critical_positions(sc, 4000, seed=5)
     a = npx.trace_rays(sc, px, py, "mixed")
