@@ -71,8 +71,10 @@ GKCF_HD double radial_u(const CfRay& R, double S, double C, double D2) {
 // xu, and (when non-null) the Mino time in xl and the branch in xb (0
 // before the radial turning point, 1 after).  Crossings outside the window
 // are passed over; the ray is followed until it ends.  a = 0, q2 = 0, a
-// start inside the photon region or outside the escape radius, and q2 < 0
-// radial motions other than those named above return status -1.
+// start inside the photon region or outside the escape radius, a ray so
+// near the critical curve (~1e-12 relative) that its pair of roots is not
+// resolved, and q2 < 0 radial motions other than those named above return
+// status -1.
 GKCF_HD EqX equator_crossings(double a, double l, double q2, double u0, double mu0, double su, double sm,
                               double u_far, double u_lo, double u_hi, int kmax, double* xu, double* xl,
                               int32_t* xb) {
@@ -100,7 +102,8 @@ GKCF_HD EqX equator_crossings(double a, double l, double q2, double u0, double m
         return o;
     }
     CfRay R;
-    if (c[4] < 0.0 && (nr == 4 || (nr == 2 && sigma > 0.0))) polish_roots(a, l, q2, nr, rr, rho, sigma);
+    if (c[4] < 0.0 && (nr == 4 || (nr == 2 && sigma > 0.0)) && !polish_roots(a, l, q2, nr, rr, rho, sigma))
+        return o;
     if (nr == 4 && c[4] < 0.0) {
         if (!reduce_r4(rr, c[4], u0, R)) return o;
     } else if (nr == 2 && sigma > 0.0 && c[4] < 0.0) {

@@ -492,24 +492,29 @@ GKCF_HD UExact u_exact(double a, double l, double q2) {
     return c;
 }
 
-GKCF_HD double polish_real(const UExact& c, double x, double gap) {
+// Returns false when the root is not resolved: a step would move it by more
+// than a quarter of the distance to its neighbour (the iteration that found
+// the roots could not separate a nearly double pair), or the steps do not
+// settle to the last bits.
+GKCF_HD bool polish_real(const UExact& c, double& x, double gap) {
     for (int it = 0; it < 3; ++it) {
         DD t = dd_add(dd_mul(c.c4, x), c.c3);
         t = dd_add(dd_mul(t, x), c.c2);
         t = dd_mul(dd_mul(t, x), x);
         t = dd_add(t, DD{1.0, 0.0});
         const double d = x * (2.0 * c.c2.hi + x * (3.0 * c.c3.hi + 4.0 * x * c.c4.hi));
-        if (!(d != 0.0)) break;
+        if (!(d != 0.0)) return false;
         const double dx = (t.hi + t.lo) / d;
-        if (!(std::fabs(dx) <= 0.25 * gap)) break;
+        if (!(std::fabs(dx) <= 0.25 * gap)) return false;
         x -= dx;
-        if (std::fabs(dx) <= 4e-16 * std::fabs(x)) break;     // the next step is below the last bit
+        if (std::fabs(dx) <= 4e-16 * std::fabs(x)) return true;   // the next step is below the last bit
     }
-    return x;
+    return false;
 }
 
-// the complex root rho + i sigma (sigma > 0), by complex Newton steps
-GKCF_HD void polish_pair(const UExact& c, double& rho, double& sigma) {
+// the complex root rho + i sigma (sigma > 0), by complex Newton steps;
+// false as for polish_real (the conjugate is 2 sigma away)
+GKCF_HD bool polish_pair(const UExact& c, double& rho, double& sigma) {
     double x = rho, y = sigma;
     for (int it = 0; it < 3; ++it) {
         // U(z) by Horner in double-double complex arithmetic
@@ -528,21 +533,28 @@ GKCF_HD void polish_pair(const UExact& c, double& rho, double& sigma) {
         double qr = 2.0 * c2 + (pr * x - pi * y), qi = pr * y + pi * x;
         const double dr = qr * x - qi * y, di = qr * y + qi * x;
         const double den = dr * dr + di * di;
-        if (!(den > 0.0)) break;
+        if (!(den > 0.0)) return false;
         const double ur = re.hi + re.lo, ui = im.hi + im.lo;
         const double sr = (ur * dr + ui * di) / den, si = (ui * dr - ur * di) / den;
-        if (!(std::fabs(sr) + std::fabs(si) <= 0.25 * y)) break;
+        if (!(std::fabs(sr) + std::fabs(si) <= 0.25 * y)) return false;
         x -= sr; y -= si;
-        if (std::fabs(sr) + std::fabs(si) <= 4e-16 * (std::fabs(x) + y)) break;
+        if (std::fabs(sr) + std::fabs(si) <= 4e-16 * (std::fabs(x) + y)) {
+            rho = x; sigma = y;
+            return true;
+        }
     }
-    rho = x; sigma = y;
+    return false;
 }
 
 // Polishes the roots of a q2 > 0 potential as found (nr real roots sorted,
-// a complex pair when nr = 2).
-GKCF_HD void polish_roots(double a, double l, double q2, int nr, double* rr, double& rho, double& sigma) {
+// a complex pair when nr = 2).  false when a root is not resolved: such a
+// ray (within ~1e-12 relative of the critical curve, where the pair's
+// separation is below what the root iteration resolves) is left to the
+// integrators.
+GKCF_HD bool polish_roots(double a, double l, double q2, int nr, double* rr, double& rho, double& sigma) {
     const UExact c = u_exact(a, l, q2);
     double out[4];
+    bool ok = true;
     for (int i = 0; i < nr; ++i) {
         double gap = nr == 2 ? std::fabs(rr[1] - rr[0]) : INFINITY;
         for (int j = 0; j < nr; ++j)
@@ -551,10 +563,12 @@ GKCF_HD void polish_roots(double a, double l, double q2, int nr, double* rr, dou
             const double dz = std::sqrt((rr[i] - rho) * (rr[i] - rho) + sigma * sigma);
             gap = std::fmin(gap, dz);
         }
-        out[i] = polish_real(c, rr[i], gap);
+        out[i] = rr[i];
+        ok = polish_real(c, out[i], gap) && ok;
     }
     for (int i = 0; i < nr; ++i) rr[i] = out[i];
-    if (nr == 2 && sigma > 0.0) polish_pair(c, rho, sigma);
+    if (nr == 2 && sigma > 0.0) ok = polish_pair(c, rho, sigma) && ok;
+    return ok;
 }
 
 // Radial reductions of q2 > 0 (c4 = -a^2 q2 < 0), motion in [u1, u2] holding
@@ -626,7 +640,7 @@ GKCF_HD void setup(double a, double l, double q2, double u0, double uf, double m
     const double c[5] = {1.0, 0.0, B, 2.0 * Kc, -a * a * q2};
     double rr[4], rho = 0.0, sigma = 0.0;
     const int nr = ::np::mino::real_roots(c, 4, rr, &rho, &sigma);
-    if (c[4] < 0.0 && (nr == 4 || (nr == 2 && sigma > 0.0))) polish_roots(a, l, q2, nr, rr, rho, sigma);
+    if (c[4] < 0.0 && (nr == 4 || (nr == 2 && sigma > 0.0)) && !polish_roots(a, l, q2, nr, rr, rho, sigma)) return;
     const double sq = std::sqrt(1.0 - a * a);
     R.rp = 1.0 + sq;
     R.rm = a * a / R.rp;

@@ -50,6 +50,38 @@ def test_crossings_match_quadrature_truth():
         assert (du <= np.array(BAR_U[:n])).all() and (dphi <= np.array(BAR_PHI[:n])).all(), (i, du, dphi)
 
 
+def test_unresolved_pairs_are_left_to_the_integrators():
+    """Rays within 1e-15 .. 1e-11 (relative, in l) of the critical curve:
+    the pair of radial roots near the photon orbit is then closer than the
+    root iteration resolves, and such a ray must come back with status -1
+    (integrated by the renderer, Taylor-solved by GEOKERR) rather than with
+    wrong crossings.  Rays it does solve keep the Taylor restatement's
+    first two crossings (before any winding) to 1e-10."""
+    rng = np.random.default_rng(3)
+    mu0 = math.cos(math.radians(80.0))
+    left = solved = 0
+    for a in (0.9, 0.998, 0.5):
+        r_pro = 2 * (1 + math.cos(2 / 3 * math.acos(-a)))
+        r_ret = 2 * (1 + math.cos(2 / 3 * math.acos(a)))
+        for _ in range(40):
+            r = rng.uniform(r_pro, r_ret)
+            l = -(r ** 3 - 3 * r * r + a * a * r + a * a) / (a * (r - 1))
+            q2 = r ** 3 * (4 * a * a - r * (r - 3) ** 2) / (a * a * (r - 1) ** 2)
+            l *= 1 + 10.0 ** rng.uniform(-15, -11) * rng.choice([-1, 1])
+            if q2 <= 0 or q2 + (a * a - l * l - q2) * mu0 * mu0 - a * a * mu0 ** 4 < 0:
+                continue
+            sm = float(rng.choice([-1.0, 1.0]))
+            h = gk.disk_crossings(a, 0.02, mu0, np.array([l]), np.array([q2]), 1.0, sm, 1e-3, K=2)
+            if h["status"][0] < 0:
+                left += 1
+                continue
+            n, xu, _ = oracle.geokerr_crossings(0.02, mu0, a, l, q2, 1.0, sm, 1e-3, 2)
+            assert h["nx"][0] == n
+            assert np.max(np.abs(h["xu"][0, :n] - xu[:n]) / xu[:n]) <= 1e-10
+            solved += 1
+    assert left > 10 and solved > 10, (left, solved)
+
+
 @pytest.mark.parametrize("a", [0.9, 0.998, 0.5])
 def test_grid_crossings_match_taylor(a):
     """A 24 x 24 camera grid from r = 50 M (every q2 > 0 ray, ingoing): the
