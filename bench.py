@@ -535,7 +535,9 @@ def run_ours(args):
             "e2e": {"value": replicas.aggregate_rays_per_s(rays_per_step, e2e, ws), "unit": "rays/s",
                     "h2d_bytes_per_step": C.sizeof(sc),
                     "d2h_bytes_per_step": 4 * H * W * 4},
-            "gpu_launches": (5 if args.precision == "mixed" else 2) * args.steps,
+            # ray init, near-critical closed form, tracer, horizon-band closed
+            # form (7(8) path), resolve; FP64: tracer, resolve
+            "gpu_launches": ((5 if args.path == "rkf78" else 4) if args.precision == "mixed" else 2) * args.steps,
             "clocks": clocks,
             "wall_s": wall,
         }
