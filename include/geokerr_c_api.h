@@ -230,7 +230,7 @@ int np_geokerr_equator_crossings_cf_host(int n, double a, const double* u0, cons
  * pole with l != 0), the count in nx[i] and in status[i] (NULL to skip) 0
  * (leaves through u_far), 1 (falls into the horizon) or -1 (outside the
  * closed forms: a = 0, q2 = 0, a start inside the photon region or inside
- * u_far, or a ray within ~1e-12 relative of the critical curve, whose pair
+ * u_far, or a ray within ~1e-9 relative of the critical curve whose pair
  * of radial roots is not resolved).  q2 < 0 rays have no crossing.
  * np_status. */
 int np_geokerr_disk_crossings_device(int n, double a, const double* d_u0, const double* d_mu0, const double* d_l,

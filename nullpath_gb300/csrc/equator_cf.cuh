@@ -72,7 +72,7 @@ GKCF_HD double radial_u(const CfRay& R, double S, double C, double D2) {
 // before the radial turning point, 1 after).  Crossings outside the window
 // are passed over; the ray is followed until it ends.  a = 0, q2 = 0, a
 // start inside the photon region or outside the escape radius, a ray so
-// near the critical curve (~1e-12 relative) that its pair of roots is not
+// near the critical curve (~1e-9 relative) that its pair of roots is not
 // resolved, and q2 < 0 radial motions other than those named above return
 // status -1.
 GKCF_HD EqX equator_crossings(double a, double l, double q2, double u0, double mu0, double su, double sm,

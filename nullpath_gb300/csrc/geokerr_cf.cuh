@@ -548,7 +548,7 @@ GKCF_HD bool polish_pair(const UExact& c, double& rho, double& sigma) {
 
 // Polishes the roots of a q2 > 0 potential as found (nr real roots sorted,
 // a complex pair when nr = 2).  false when a root is not resolved: such a
-// ray (within ~1e-12 relative of the critical curve, where the pair's
+// ray (within ~1e-9 relative of the critical curve, where the pair's
 // separation is below what the root iteration resolves) is left to the
 // integrators.
 GKCF_HD bool polish_roots(double a, double l, double q2, int nr, double* rr, double& rho, double& sigma) {
