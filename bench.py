@@ -507,8 +507,8 @@ def run_ours(args):
                        "integrator": "compensated FP32 Fehlberg 7(8), rtol %g, atol %g, Henon crossings" % (
                            sc.rtol, sc.atol) if args.path == "rkf78" else "RK4, h = 0.01 clamp(r, 1, 100), Hermite",
                        "rays_per_step": rays_per_step,
-                       "fp64_islands": ("horizon band 0.1 M (certified capture, FP64 steps otherwise)" if
-                                        args.path == "rkf78" else
+                       "fp64_islands": ("horizon band 0.1 M: certified capture, else the whole ray in FP64 "
+                                        "closed form" if args.path == "rkf78" else
                                         "horizon band 0.1 M, radial/polar turning points"),
                        "near_critical": "|b-b_crit| < 1e-3 M, and rays entering the horizon band without a "
                                         "capture certificate: FP64 closed form (Mino-time solution, crossings by "
